@@ -1,0 +1,528 @@
+"""formoniq_gb300: the Galerkin assembly and Krylov solve path of formoniq on GB300.
+
+The compute lives in the native library ``_lib/libformoniq_gb300.so`` (CUDA
+sm_103a kernels behind the C ABI declared in ``include/formoniq_gpu.h``). This
+module binds that ABI with ctypes and mirrors the reference's Rust API on the
+path, so calling code reads like formoniq:
+
+    mesh = Mesh.kuhn_cube(ctx, 3, 32)            # CartesianGrid::new_unit(3, 32).triangulate()
+    mesh.kuhn_lengths(jitter=0.1, seed=7)         # MeshCoords::to_edge_lengths_sq
+    wc = WhitneyComplex(mesh)                     # WhitneyComplex::new
+    m1 = wc.mass(1)                               # HilbertComplex::mass
+    sigma, u, p, rep = solve_source(wc, f, 1)     # elliptic::solve_source
+
+There is no CPU fallback: importing succeeds without the library, but every
+entry point raises ``FqUnavailable`` when it is missing, and every compute call
+needs a CUDA device.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+__all__ = [
+    "FQ_MASS", "FQ_DIF_TRIAL", "FQ_DIF_TEST", "FQ_DIF_BOTH", "FQ_ABSOLUTE", "FQ_RELATIVE", "FQ_FP64", "FQ_FP32",
+    "FqError", "FqUnavailable", "Context", "Mesh", "Matrix", "WhitneyComplex", "MixedProblem", "SolveOpts",
+    "Report", "solve_source", "solve_dirac_source", "dirac_system", "minres", "cg", "lib_path", "load",
+    "exported_symbols",
+]
+
+FQ_MASS, FQ_DIF_TRIAL, FQ_DIF_TEST, FQ_DIF_BOTH = 0, 1, 2, 3
+FQ_ABSOLUTE, FQ_RELATIVE = 0, 1
+FQ_FP64, FQ_FP32 = 0, 1
+
+_STATUS = {
+    0: "FQ_OK", 1: "FQ_INVALID_ARG", 2: "FQ_DEGENERATE_CELL", 3: "FQ_NOT_CONVERGED", 4: "FQ_BREAKDOWN",
+    5: "FQ_OOM_BUDGET", 6: "FQ_TIMEOUT", 7: "FQ_CUDA_ERROR", 8: "FQ_NO_DEVICE", 9: "FQ_UNSUPPORTED",
+}
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def lib_path() -> str:
+    return os.path.join(_HERE, "_lib", "libformoniq_gb300.so")
+
+
+class FqUnavailable(RuntimeError):
+    """The native library is missing: build it with ``__graft_entry__.build()``."""
+
+
+class FqError(RuntimeError):
+    def __init__(self, status: int, message: str = ""):
+        self.status = status
+        self.name = _STATUS.get(status, f"status {status}")
+        super().__init__(f"{self.name}: {message}" if message else self.name)
+
+
+class SolveOpts(ctypes.Structure):
+    """StopCriterion (iterative/src/lib.rs:193-208) plus refinement knobs."""
+
+    _fields_ = [("rtol", ctypes.c_double), ("max_iters", ctypes.c_int64), ("precision", ctypes.c_int),
+                ("refine_rtol", ctypes.c_double), ("max_refinements", ctypes.c_int64)]
+
+    @staticmethod
+    def default(**kw) -> "SolveOpts":
+        o = SolveOpts(1e-10, 10_000, FQ_FP64, 1e-12, 6)
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+
+class _Report(ctypes.Structure):
+    _fields_ = [("iters", ctypes.c_int64), ("residual", ctypes.c_double), ("converged", ctypes.c_int32),
+                ("refinements", ctypes.c_int32), ("true_residual", ctypes.c_double)]
+
+
+@dataclass
+class Report:
+    """Report (iterative/src/lib.rs:212-219)."""
+
+    iters: int
+    residual: float
+    converged: bool
+    refinements: int = 0
+    true_residual: float = 0.0
+
+    @staticmethod
+    def of(r: _Report) -> "Report":
+        return Report(int(r.iters), float(r.residual), bool(r.converged), int(r.refinements),
+                      float(r.true_residual))
+
+
+_lib = None
+
+_P = ctypes.c_void_p
+_I32P = ctypes.POINTER(ctypes.c_int32)
+_I64P = ctypes.POINTER(ctypes.c_int64)
+_DP = ctypes.POINTER(ctypes.c_double)
+
+# name -> (restype, argtypes); every function declared in include/formoniq_gpu.h
+_SIGNATURES = {
+    "fq_ctx_create": (ctypes.c_int, [ctypes.c_int, _P, ctypes.c_uint64, ctypes.POINTER(_P)]),
+    "fq_ctx_destroy": (None, [_P]),
+    "fq_status_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "fq_ctx_last_error": (ctypes.c_char_p, [_P]),
+    "fq_ctx_synchronize": (ctypes.c_int, [_P]),
+    "fq_ctx_bytes_in_use": (ctypes.c_uint64, [_P]),
+    "fq_ctx_kernel_launches": (ctypes.c_uint64, [_P]),
+    "fq_default_solve_opts": (None, [ctypes.POINTER(SolveOpts)]),
+    "fq_mesh_from_cells": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64, _I32P, ctypes.POINTER(_P)]),
+    "fq_mesh_kuhn_cube": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
+    "fq_mesh_destroy": (None, [_P]),
+    "fq_mesh_dim": (ctypes.c_int, [_P]),
+    "fq_mesh_nsimplices": (ctypes.c_int64, [_P, ctypes.c_int]),
+    "fq_mesh_ndofs": (ctypes.c_int64, [_P, ctypes.c_int, ctypes.c_int]),
+    "fq_mesh_simplices": (ctypes.c_int, [_P, ctypes.c_int, _I32P]),
+    "fq_mesh_interior": (ctypes.c_int, [_P, ctypes.c_int, _I64P]),
+    "fq_mesh_orientation": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int8)]),
+    "fq_mesh_set_lengths_sq": (ctypes.c_int, [_P, _DP, ctypes.c_int]),
+    "fq_mesh_get_lengths_sq": (ctypes.c_int, [_P, _DP]),
+    "fq_mesh_lengths_from_coords": (ctypes.c_int, [_P, _DP, ctypes.c_int, _DP]),
+    "fq_mesh_kuhn_lengths": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_double, ctypes.c_uint64]),
+    "fq_cell_metrics": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "fq_element_matrices": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P,
+                                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "fq_assemble": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(_P)]),
+    "fq_reassemble": (ctypes.c_int, [_P, _P, _P]),
+    "fq_hdif_gram": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
+    "fq_coboundary": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
+    "fq_assemble_host": (ctypes.c_int, [_P, _P, _P, _DP, _P]),
+    "fq_matrix_info": (ctypes.c_int, [_P, _I64P, _I64P, _I64P, ctypes.POINTER(ctypes.c_int)]),
+    "fq_matrix_device_arrays": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+    "fq_matrix_copy_to_host": (ctypes.c_int, [_P, _P, _I32P, _I32P, _P]),
+    "fq_matrix_destroy": (None, [_P]),
+    "fq_spmv": (ctypes.c_int, [_P, _P, _P, _P]),
+    "fq_minres": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
+    "fq_cg": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
+    "fq_mixed_create": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
+    "fq_mixed_reassemble": (ctypes.c_int, [_P]),
+    "fq_mixed_solve": (ctypes.c_int, [_P, _DP, _DP, _DP, _DP, ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
+    "fq_mixed_solve_device": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.POINTER(SolveOpts),
+                                             ctypes.POINTER(_Report)]),
+    "fq_mixed_info": (ctypes.c_int, [_P, _I64P, _I64P, _I64P, _I64P]),
+    "fq_mixed_system": (_P, [_P]),
+    "fq_mixed_destroy": (None, [_P]),
+    "fq_solve_source": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _DP, _DP, _DP, _DP,
+                                       ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
+    "fq_solve_dirac_source": (ctypes.c_int, [_P, _P, ctypes.c_double, _DP, _DP, _DP, ctypes.POINTER(SolveOpts),
+                                             ctypes.POINTER(_Report)]),
+    "fq_dirac_system": (ctypes.c_int, [_P, _P, ctypes.c_double, ctypes.POINTER(_P)]),
+}
+
+
+def exported_symbols():
+    return list(_SIGNATURES)
+
+
+def load():
+    """Load the native library (raises FqUnavailable when it is not built)."""
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            raise FqUnavailable(f"{path} is missing; build it with __graft_entry__.build()")
+        L = ctypes.CDLL(path)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+class Context:
+    """fq_ctx: a device, a CUDA stream and an HBM budget (0 = unlimited)."""
+
+    def __init__(self, device: int = 0, stream: int = 0, budget_bytes: int = 0):
+        L = load()
+        h = _P()
+        s = L.fq_ctx_create(device, _P(stream) if stream else None, budget_bytes, ctypes.byref(h))
+        if s != 0:
+            raise FqError(s, "fq_ctx_create")
+        self.h = h
+        self.L = L
+
+    def check(self, status: int, what: str = ""):
+        if status != 0:
+            msg = self.L.fq_ctx_last_error(self.h)
+            raise FqError(status, f"{what}: {msg.decode() if msg else ''}")
+
+    def synchronize(self):
+        self.check(self.L.fq_ctx_synchronize(self.h), "synchronize")
+
+    @property
+    def bytes_in_use(self) -> int:
+        return int(self.L.fq_ctx_bytes_in_use(self.h))
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.L.fq_ctx_kernel_launches(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fq_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Matrix:
+    """An assembled Galerkin matrix resident on the device (GalerkinMatrix = CsrMatrix)."""
+
+    def __init__(self, ctx: Context, h, owned: bool = True):
+        self.ctx, self.h, self.owned = ctx, h, owned
+
+    def info(self):
+        nr, nc, nnz, pr = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
+        self.ctx.check(self.ctx.L.fq_matrix_info(self.h, ctypes.byref(nr), ctypes.byref(nc), ctypes.byref(nnz),
+                                                 ctypes.byref(pr)))
+        return nr.value, nc.value, nnz.value, pr.value
+
+    @property
+    def shape(self):
+        nr, nc, _, _ = self.info()
+        return (nr, nc)
+
+    @property
+    def nnz(self) -> int:
+        return self.info()[2]
+
+    def host_arrays(self):
+        nr, nc, nnz, pr = self.info()
+        rp = np.zeros(nr + 1, np.int32)
+        ci = np.zeros(max(nnz, 1), np.int32)
+        vv = np.zeros(max(nnz, 1), np.float32 if pr == FQ_FP32 else np.float64)
+        self.ctx.check(self.ctx.L.fq_matrix_copy_to_host(self.ctx.h, self.h, rp.ctypes.data_as(_I32P),
+                                                         ci.ctypes.data_as(_I32P), vv.ctypes.data_as(_P)))
+        return rp, ci[:nnz], vv[:nnz]
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+
+        nr, nc, _, _ = self.info()
+        rp, ci, vv = self.host_arrays()
+        m = sp.csr_matrix((vv, ci, rp), shape=(nr, nc))
+        m.has_sorted_indices = True
+        return m
+
+    def device_arrays(self):
+        rp, ci, vv = _P(), _P(), _P()
+        self.ctx.check(self.ctx.L.fq_matrix_device_arrays(self.h, ctypes.byref(rp), ctypes.byref(ci),
+                                                          ctypes.byref(vv)))
+        return rp.value, ci.value, vv.value
+
+    def reassemble(self, mesh: "Mesh"):
+        self.ctx.check(self.ctx.L.fq_reassemble(self.ctx.h, mesh.h, self.h), "fq_reassemble")
+
+    def close(self):
+        if self.owned and getattr(self, "h", None):
+            self.ctx.L.fq_matrix_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Mesh:
+    """A simplicial complex with Regge geometry: Complex + MeshLengthsSq."""
+
+    def __init__(self, ctx: Context, h):
+        self.ctx, self.h = ctx, h
+
+    @staticmethod
+    def from_cells(ctx: Context, cells: np.ndarray) -> "Mesh":
+        cells = np.ascontiguousarray(cells, np.int32)
+        h = _P()
+        ctx.check(ctx.L.fq_mesh_from_cells(ctx.h, cells.shape[1] - 1, cells.shape[0], cells.ctypes.data_as(_I32P),
+                                           ctypes.byref(h)), "fq_mesh_from_cells")
+        return Mesh(ctx, h)
+
+    @staticmethod
+    def kuhn_cube(ctx: Context, dim: int, nboxes: int) -> "Mesh":
+        h = _P()
+        ctx.check(ctx.L.fq_mesh_kuhn_cube(ctx.h, dim, nboxes, ctypes.byref(h)), "fq_mesh_kuhn_cube")
+        return Mesh(ctx, h)
+
+    @property
+    def dim(self) -> int:
+        return self.ctx.L.fq_mesh_dim(self.h)
+
+    def nsimplices(self, k: int) -> int:
+        return int(self.ctx.L.fq_mesh_nsimplices(self.h, k))
+
+    def ncells(self) -> int:
+        return self.nsimplices(self.dim)
+
+    def ndofs(self, k: int, bc: int = FQ_ABSOLUTE) -> int:
+        return int(self.ctx.L.fq_mesh_ndofs(self.h, k, bc))
+
+    def simplices(self, k: int) -> np.ndarray:
+        out = np.zeros((self.nsimplices(k), k + 1), np.int32)
+        self.ctx.check(self.ctx.L.fq_mesh_simplices(self.h, k, out.ctypes.data_as(_I32P)))
+        return out
+
+    def interior(self, k: int) -> np.ndarray:
+        out = np.zeros(max(self.ndofs(k, FQ_RELATIVE), 1), np.int64)
+        self.ctx.check(self.ctx.L.fq_mesh_interior(self.h, k, out.ctypes.data_as(_I64P)))
+        return out[: self.ndofs(k, FQ_RELATIVE)]
+
+    def orientation(self) -> np.ndarray:
+        out = np.zeros(self.ncells(), np.int8)
+        self.ctx.check(self.ctx.L.fq_mesh_orientation(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))))
+        return out
+
+    def set_lengths_sq(self, lengths: np.ndarray):
+        lengths = np.ascontiguousarray(lengths, np.float64)
+        self.ctx.check(self.ctx.L.fq_mesh_set_lengths_sq(self.h, _dp(lengths), 0), "fq_mesh_set_lengths_sq")
+
+    def lengths_sq(self) -> np.ndarray:
+        out = np.zeros(max(self.nsimplices(1), 1))
+        self.ctx.check(self.ctx.L.fq_mesh_get_lengths_sq(self.h, _dp(out)))
+        return out[: self.nsimplices(1)]
+
+    def lengths_from_coords(self, coords: np.ndarray, ambient_signs=None):
+        coords = np.ascontiguousarray(coords, np.float64)
+        signs = None if ambient_signs is None else np.ascontiguousarray(ambient_signs, np.float64)
+        self.ctx.check(self.ctx.L.fq_mesh_lengths_from_coords(self.h, _dp(coords), coords.shape[1],
+                                                              _dp(signs) if signs is not None else None))
+
+    def kuhn_lengths(self, side=None, ambient_signs=None, jitter: float = 0.0, seed: int = 0):
+        side = None if side is None else np.ascontiguousarray(side, np.float64)
+        signs = None if ambient_signs is None else np.ascontiguousarray(ambient_signs, np.float64)
+        self.ctx.check(self.ctx.L.fq_mesh_kuhn_lengths(self.h, _dp(side) if side is not None else None,
+                                                       _dp(signs) if signs is not None else None, float(jitter),
+                                                       int(seed)), "fq_mesh_kuhn_lengths")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.fq_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class WhitneyComplex:
+    """HilbertComplex (whitney_complex.rs:55-277) on the device: the full
+    complex, or the relative one (``relative=True``, essential BC)."""
+
+    def __init__(self, mesh: Mesh, relative: bool = False, precision: int = FQ_FP64):
+        self.mesh = mesh
+        self.ctx = mesh.ctx
+        self.bc = FQ_RELATIVE if relative else FQ_ABSOLUTE
+        self.precision = precision
+
+    @property
+    def dim(self) -> int:
+        return self.mesh.dim
+
+    def relative(self) -> "WhitneyComplex":
+        return WhitneyComplex(self.mesh, True, self.precision)
+
+    def ndofs(self, k: int) -> int:
+        return self.mesh.ndofs(k, self.bc)
+
+    def _assemble(self, form: int, k: int) -> Matrix:
+        h = _P()
+        self.ctx.check(self.ctx.L.fq_assemble(self.ctx.h, self.mesh.h, form, k, self.bc, self.precision,
+                                              ctypes.byref(h)), "fq_assemble")
+        return Matrix(self.ctx, h)
+
+    def mass(self, k: int) -> Matrix:
+        return self._assemble(FQ_MASS, k)
+
+    def dif_trial(self, k: int) -> Matrix:
+        return self._assemble(FQ_DIF_TRIAL, k)
+
+    def dif_test(self, k: int) -> Matrix:
+        return self._assemble(FQ_DIF_TEST, k)
+
+    def dif_both(self, k: int) -> Matrix:
+        return self._assemble(FQ_DIF_BOTH, k)
+
+    def hdif_gram(self, k: int) -> Matrix:
+        h = _P()
+        self.ctx.check(self.ctx.L.fq_hdif_gram(self.ctx.h, self.mesh.h, k, self.bc, ctypes.byref(h)), "fq_hdif_gram")
+        return Matrix(self.ctx, h)
+
+    def dif(self, k: int) -> Matrix:
+        h = _P()
+        self.ctx.check(self.ctx.L.fq_coboundary(self.ctx.h, self.mesh.h, k, self.bc, ctypes.byref(h)),
+                       "fq_coboundary")
+        return Matrix(self.ctx, h)
+
+
+class MixedProblem:
+    """The resident mixed Hodge-Laplace system of elliptic::solve_source."""
+
+    def __init__(self, mesh: Mesh, grade: int, bc: int = FQ_ABSOLUTE, precision: int = FQ_FP64):
+        self.mesh, self.ctx, self.grade, self.bc = mesh, mesh.ctx, grade, bc
+        h = _P()
+        self.ctx.check(self.ctx.L.fq_mixed_create(self.ctx.h, mesh.h, grade, bc, precision, ctypes.byref(h)),
+                       "fq_mixed_create")
+        self.h = h
+
+    def info(self):
+        a, b, c, d = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self.ctx.check(self.ctx.L.fq_mixed_info(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                                ctypes.byref(d)))
+        return a.value, b.value, c.value, d.value
+
+    def system(self) -> Matrix:
+        return Matrix(self.ctx, self.ctx.L.fq_mixed_system(self.h), owned=False)
+
+    def reassemble(self):
+        self.ctx.check(self.ctx.L.fq_mixed_reassemble(self.h), "fq_mixed_reassemble")
+
+    def solve(self, source: np.ndarray, opts: Optional[SolveOpts] = None, allow_unconverged=False):
+        m = self.mesh
+        source = np.ascontiguousarray(source, np.float64)
+        nk = m.nsimplices(self.grade)
+        nkm = m.nsimplices(self.grade - 1) if self.grade >= 1 else 0
+        ns, nu, nh, _ = self.info()
+        sigma = np.zeros(max(nkm, 1))
+        u = np.zeros(max(nk, 1))
+        p = np.zeros(max(nh, 1))
+        rep = _Report()
+        opts = opts or SolveOpts.default()
+        s = self.ctx.L.fq_mixed_solve(self.h, _dp(source), _dp(sigma), _dp(u), _dp(p), ctypes.byref(opts),
+                                      ctypes.byref(rep))
+        if not (s == 0 or (s == 3 and allow_unconverged)):
+            self.ctx.check(s, "fq_mixed_solve")
+        return sigma[:nkm], u[:nk], p[:nh], Report.of(rep)
+
+    def solve_device(self, src_ptr: int, sigma_ptr: int, u_ptr: int, p_ptr: int, opts: Optional[SolveOpts] = None):
+        rep = _Report()
+        opts = opts or SolveOpts.default()
+        s = self.ctx.L.fq_mixed_solve_device(self.h, _P(src_ptr), _P(sigma_ptr) if sigma_ptr else None,
+                                             _P(u_ptr) if u_ptr else None, _P(p_ptr) if p_ptr else None,
+                                             ctypes.byref(opts), ctypes.byref(rep))
+        if s not in (0, 3):
+            self.ctx.check(s, "fq_mixed_solve_device")
+        return Report.of(rep)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.fq_mixed_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve_source(complex_: WhitneyComplex, source: np.ndarray, grade: int, opts: Optional[SolveOpts] = None,
+                 precision: int = FQ_FP64):
+    """elliptic::solve_source (problems/elliptic.rs:132-182): (sigma, u, p, report)."""
+    prob = MixedProblem(complex_.mesh, grade, complex_.bc, precision)
+    try:
+        o = opts or SolveOpts.default(precision=precision)
+        return prob.solve(source, o)
+    finally:
+        prob.close()
+
+
+def solve_dirac_source(mesh: Mesh, mass_term: float, load_: np.ndarray, lift: Optional[np.ndarray] = None,
+                       opts: Optional[SolveOpts] = None):
+    """dirac::solve_dirac_source (problems/dirac.rs:473-531) by MINRES."""
+    ctx = mesh.ctx
+    load_ = np.ascontiguousarray(load_, np.float64)
+    lift_a = None if lift is None else np.ascontiguousarray(lift, np.float64)
+    x = np.zeros_like(load_)
+    rep = _Report()
+    opts = opts or SolveOpts.default()
+    s = ctx.L.fq_solve_dirac_source(ctx.h, mesh.h, float(mass_term), _dp(load_),
+                                    _dp(lift_a) if lift_a is not None else None, _dp(x), ctypes.byref(opts),
+                                    ctypes.byref(rep))
+    if s not in (0, 3):
+        ctx.check(s, "fq_solve_dirac_source")
+    return x, Report.of(rep)
+
+
+def dirac_system(mesh: Mesh, mass_term: float) -> Matrix:
+    h = _P()
+    mesh.ctx.check(mesh.ctx.L.fq_dirac_system(mesh.ctx.h, mesh.h, float(mass_term), ctypes.byref(h)),
+                   "fq_dirac_system")
+    return Matrix(mesh.ctx, h)
+
+
+def _krylov(fn: str, a: Matrix, b_ptr: int, x_ptr: int, inv_diag_ptr: int = 0, opts=None) -> Report:
+    rep = _Report()
+    opts = opts or SolveOpts.default()
+    L = a.ctx.L
+    s = getattr(L, fn)(a.ctx.h, a.h, _P(inv_diag_ptr) if inv_diag_ptr else None, _P(b_ptr), _P(x_ptr),
+                       ctypes.byref(opts), ctypes.byref(rep))
+    if s not in (0, 3):
+        a.ctx.check(s, fn)
+    return Report.of(rep)
+
+
+def minres(a: Matrix, b_ptr: int, x_ptr: int, inv_diag_ptr: int = 0, opts=None) -> Report:
+    """krylov::minres on device pointers (FP64)."""
+    return _krylov("fq_minres", a, b_ptr, x_ptr, inv_diag_ptr, opts)
+
+
+def cg(a: Matrix, b_ptr: int, x_ptr: int, inv_diag_ptr: int = 0, opts=None) -> Report:
+    """krylov::cg on device pointers (FP64)."""
+    return _krylov("fq_cg", a, b_ptr, x_ptr, inv_diag_ptr, opts)

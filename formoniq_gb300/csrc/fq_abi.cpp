@@ -1,0 +1,1127 @@
+// The extern "C" boundary (include/formoniq_gpu.h) and the host drivers behind
+// it. Every entry point catches every C++ exception and converts CUDA errors to
+// fq_status; nothing unwinds across the ABI.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "fq_internal.h"
+
+namespace fq {
+
+fq_status build_topology(fq_ctx* ctx, fq_mesh* m, int dim, int64_t ncells, const int32_t* cells);
+std::vector<int32_t> kuhn_cells(int dim, int nbox);
+double uniform_pm1(uint64_t seed, uint64_t counter);
+void compute_orientation(fq_mesh* m, const std::vector<int32_t>& facet_of_cell);
+
+template <typename VT>
+fq_status minres_run(fq_ctx*, const int32_t*, const int32_t*, const VT*, int64_t, int64_t, const VT*, const VT*, VT*,
+                     double, int64_t, fq_report*);
+template <typename VT>
+fq_status cg_run(fq_ctx*, const int32_t*, const int32_t*, const VT*, int64_t, int64_t, const VT*, const VT*, VT*,
+                 double, int64_t, fq_report*);
+fq_status residual64(fq_ctx*, const int32_t*, const int32_t*, const double*, int64_t, const double*, const double*,
+                     double*, double*, double*);
+void launch_to_float(const double* a, float* o, int64_t n, cudaStream_t st);
+void launch_to_float_scaled(const double* a, float* o, double s, int64_t n, cudaStream_t st);
+void launch_axpy_from_float(double* x, const float* d, double s, int64_t n, cudaStream_t st);
+void vec_diag(const fq_matrix* a, double* d, cudaStream_t st);
+void vec_recip(const double* d, double* inv, float* inv32, int64_t n, int absval, cudaStream_t st);
+void vec_gather(const double* in, const int32_t* map, double* out, int64_t n, cudaStream_t st);
+void vec_scatter_map(const double* in, const int32_t* map, double* out, int64_t n, cudaStream_t st);
+void vec_sub(double* a, const double* b, int64_t n, cudaStream_t st);
+void vec_add(double* a, const double* b, int64_t n, cudaStream_t st);
+void vec_fill(double* a, double v, int64_t n, cudaStream_t st);
+void vec_scale(double* a, double s, int64_t n, cudaStream_t st);
+fq_status border_csr(fq_ctx* ctx, const fq_matrix* a, const double* mh, int64_t ns, int64_t nu, DevBuf& nrp,
+                     DevBuf& nci, DevBuf& nval);
+
+// ---- DevBuf -----------------------------------------------------------------
+DevBuf& DevBuf::operator=(DevBuf&& o) noexcept {
+  if (this != &o) {
+    release();
+    ctx = o.ctx;
+    p = o.p;
+    bytes = o.bytes;
+    o.ctx = nullptr;
+    o.p = nullptr;
+    o.bytes = 0;
+  }
+  return *this;
+}
+
+fq_status DevBuf::alloc(fq_ctx* c, size_t nbytes) {
+  release();
+  if (nbytes == 0) nbytes = 16;
+  if (c->budget && c->in_use + nbytes > c->budget)
+    return set_error(c, FQ_OOM_BUDGET, "HBM budget exceeded: " + std::to_string(c->in_use + nbytes) + " > " +
+                                           std::to_string(c->budget) + " bytes");
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, nbytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(c, e == cudaErrorMemoryAllocation ? FQ_OOM_BUDGET : FQ_CUDA_ERROR,
+                     std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  ctx = c;
+  p = q;
+  bytes = nbytes;
+  c->in_use += nbytes;
+  return FQ_OK;
+}
+
+void DevBuf::release() {
+  if (p) {
+    cudaFree(p);
+    if (ctx) ctx->in_use -= bytes;
+  }
+  p = nullptr;
+  bytes = 0;
+  ctx = nullptr;
+}
+
+fq_status dev_alloc(fq_ctx* ctx, DevBuf& b, size_t bytes) { return b.alloc(ctx, bytes); }
+
+fq_status set_error(fq_ctx* ctx, fq_status s, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return s;
+}
+
+fq_status cuda_check(fq_ctx* ctx, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  return set_error(ctx, FQ_CUDA_ERROR, m);
+}
+
+fq_status make_matrix(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int bc, int precision, double param,
+                      fq_matrix** out) {
+  Plan* plan = nullptr;
+  FQ_TRY(get_plan(ctx, mesh, kind, grade, bc, bc, &plan));
+  auto* m = new fq_matrix();
+  m->ctx = ctx;
+  m->mesh = mesh;
+  m->plan = plan;
+  m->kind = kind;
+  m->grade = grade;
+  m->bc = bc;
+  m->precision = precision;
+  m->param = param;
+  m->nrows = plan->nrows;
+  m->ncols = plan->ncols;
+  fq_status s = assemble_into(ctx, m);
+  if (s != FQ_OK) {
+    delete m;
+    return s;
+  }
+  *out = m;
+  return FQ_OK;
+}
+
+// Relative -> ambient index list of grade k (device), built on demand.
+static fq_status interior_list(fq_ctx* ctx, fq_mesh* m, int k, DevBuf& out) {
+  std::vector<int32_t> lst;
+  for (int64_t i = 0; i < m->nsimp[k]; ++i)
+    if (!m->boundary[k][i]) lst.push_back(int32_t(i));
+  FQ_TRY(out.alloc(ctx, std::max<size_t>(lst.size(), 1) * 4));
+  if (!lst.empty())
+    FQ_CUDA(ctx, cudaMemcpyAsync(out.p, lst.data(), lst.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return FQ_OK;
+}
+
+static int64_t ndofs(const fq_mesh* m, int k, int bc) {
+  if (k < 0 || k > m->dim) return 0;
+  return bc == FQ_RELATIVE ? m->ninterior[k] : m->nsimp[k];
+}
+
+static bool valid_form_shape(const fq_mesh* m, int form, int grade, int bc, int64_t* rows, int64_t* cols) {
+  const int tg = (form == FQ_DIF_TEST || form == FQ_DIF_BOTH) ? grade - 1 : grade;
+  const int sg = (form == FQ_DIF_TRIAL || form == FQ_DIF_BOTH) ? grade - 1 : grade;
+  *rows = ndofs(m, tg, bc);
+  *cols = ndofs(m, sg, bc);
+  return *rows > 0 && *cols > 0;
+}
+
+static fq_status empty_matrix(fq_ctx* ctx, fq_mesh* mesh, int64_t rows, int64_t cols, int precision,
+                              fq_matrix** out) {
+  auto* m = new fq_matrix();
+  m->ctx = ctx;
+  m->mesh = mesh;
+  m->nrows = rows;
+  m->ncols = cols;
+  m->nnz = 0;
+  m->precision = precision;
+  fq_status s = m->row_ptr.alloc(ctx, (rows + 1) * 4);
+  if (s == FQ_OK) s = m->col_idx.alloc(ctx, 4);
+  if (s == FQ_OK) s = m->values.alloc(ctx, 8);
+  if (s != FQ_OK) {
+    delete m;
+    return s;
+  }
+  cudaMemsetAsync(m->row_ptr.p, 0, (rows + 1) * 4, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  m->rp = m->row_ptr.as<int32_t>();
+  m->ci = m->col_idx.as<int32_t>();
+  *out = m;
+  return FQ_OK;
+}
+
+}  // namespace fq
+
+using namespace fq;
+
+// ============================================================================
+// The mixed Hodge-Laplace problem
+// ============================================================================
+struct fq_mixed {
+  fq_ctx* ctx = nullptr;
+  fq_mesh* mesh = nullptr;
+  int grade = 0, bc = 0, precision = 0;
+  int64_t ns = 0, nu = 0, nh = 0, n = 0;
+  fq_matrix* kkt = nullptr;    // FP64, unbordered
+  fq_matrix* kkt32 = nullptr;  // FP32 element values (FQ_FP32)
+  DevBuf diag, dinv;           // FP64 preconditioner diagonal / reciprocal (size n)
+  DevBuf dinv32;
+  DevBuf mh;                   // border M_k h (size nu) when nh = 1
+  DevBuf brp, bci, bval, brp32, bci32, bval32;  // bordered systems
+  DevBuf list_sigma, list_u;   // relative -> ambient maps
+  // system actually solved
+  const int32_t* rp = nullptr;
+  const int32_t* ci = nullptr;
+  const double* val = nullptr;
+  int64_t nnz = 0;
+  const int32_t* rp32 = nullptr;
+  const int32_t* ci32 = nullptr;
+  const float* val32 = nullptr;
+  int64_t nnz32 = 0;
+  fq_matrix sysview;  // non-owning view handed out by fq_mixed_system
+  ~fq_mixed() {
+    delete kkt;
+    delete kkt32;
+  }
+};
+
+namespace fq {
+
+// Harmonic border of the contractible case: b_0 = 1 on the full complex
+// (constants), b_n = 1 on the relative complex (M_n^{-1} z, z the coherent
+// orientation); every other Betti number of a contractible mesh is zero.
+static fq_status mixed_harmonic(fq_mixed* P) {
+  fq_ctx* ctx = P->ctx;
+  fq_mesh* m = P->mesh;
+  const int n = m->dim, k = P->grade;
+  P->nh = 0;
+  if (P->bc == FQ_ABSOLUTE && k == 0) P->nh = 1;
+  if (P->bc == FQ_RELATIVE && k == n) P->nh = 1;
+  if (!P->nh) return FQ_OK;
+  FQ_TRY(P->mh.alloc(ctx, std::max<int64_t>(P->nu, 1) * 8));
+  fq_matrix* mass = nullptr;
+  FQ_TRY(make_matrix(ctx, m, EK_MASS, k, P->bc, FQ_FP64, 0.0, &mass));
+  std::unique_ptr<fq_matrix> guard(mass);
+  const int64_t nu = P->nu;
+  DevBuf tmp, g;
+  FQ_TRY(tmp.alloc(ctx, nu * 8));
+  FQ_TRY(g.alloc(ctx, nu * 8));
+  std::vector<double> host(nu);
+  if (k == 0 && P->bc == FQ_ABSOLUTE) {
+    vec_fill(tmp.as<double>(), 1.0, nu, ctx->stream);
+    launch_spmv(mass, tmp.p, P->mh.p, ctx->stream);  // M 1
+    FQ_CUDA(ctx, cudaMemcpyAsync(host.data(), P->mh.p, nu * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double s = 0.0;
+    for (double v : host) s += v;  // 1^T M 1
+    vec_scale(P->mh.as<double>(), 1.0 / std::sqrt(s), nu, ctx->stream);
+  } else {
+    if (m->orientation.empty()) {
+      if (n == 0) {
+        m->orientation.assign(size_t(m->ncells), 1);
+      } else {
+        compute_orientation(m, m->cell_faces_host[n - 1]);
+      }
+    }
+    std::vector<double> z(nu);
+    for (int64_t i = 0; i < nu; ++i) z[i] = m->orientation[i];
+    FQ_CUDA(ctx, cudaMemcpyAsync(tmp.p, z.data(), nu * 8, cudaMemcpyHostToDevice, ctx->stream));
+    DevBuf d, dinv;
+    FQ_TRY(d.alloc(ctx, nu * 8));
+    FQ_TRY(dinv.alloc(ctx, nu * 8));
+    vec_diag(mass, d.as<double>(), ctx->stream);
+    vec_recip(d.as<double>(), dinv.as<double>(), nullptr, nu, 0, ctx->stream);
+    fq_report rep{};
+    FQ_TRY(cg_run<double>(ctx, mass->rp, mass->ci, mass->values.as<double>(), nu, mass->nnz, dinv.as<double>(),
+                          tmp.as<double>(), g.as<double>(), 1e-14, 10000, &rep));
+    std::vector<double> gh(nu);
+    FQ_CUDA(ctx, cudaMemcpyAsync(gh.data(), g.p, nu * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double s = 0.0;
+    for (int64_t i = 0; i < nu; ++i) s += gh[i] * z[i];  // z^T M^{-1} z
+    // M h = z / sqrt(z^T M^{-1} z)
+    FQ_CUDA(ctx, cudaMemcpyAsync(P->mh.p, tmp.p, nu * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    vec_scale(P->mh.as<double>(), 1.0 / std::sqrt(s), nu, ctx->stream);
+  }
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return FQ_OK;
+}
+
+static fq_status mixed_assemble(fq_mixed* P) {
+  fq_ctx* ctx = P->ctx;
+  fq_mesh* m = P->mesh;
+  if (P->kkt) {
+    FQ_TRY(assemble_into(ctx, P->kkt));
+  } else {
+    FQ_TRY(make_matrix(ctx, m, EK_KKT, P->grade, P->bc, FQ_FP64, 0.0, &P->kkt));
+  }
+  // preconditioner diagonal from the same element pass (mesh->elem still holds it)
+  const int64_t n0 = P->ns + P->nu;
+  FQ_TRY(P->diag.alloc(ctx, std::max<int64_t>(P->n, 1) * 8));
+  FQ_TRY(P->dinv.alloc(ctx, std::max<int64_t>(P->n, 1) * 8));
+  launch_scatter_diag(*P->kkt->plan, m->elem.p, P->diag.as<double>(), 0, ctx->stream);
+  ctx->launches++;
+  if (P->nh) vec_fill(P->diag.as<double>() + n0, 1.0, P->nh, ctx->stream);
+  FQ_TRY(mixed_harmonic(P));
+  if (P->precision == FQ_FP32) {
+    FQ_TRY(P->dinv32.alloc(ctx, std::max<int64_t>(P->n, 1) * 4));
+    vec_recip(P->diag.as<double>(), P->dinv.as<double>(), P->dinv32.as<float>(), P->n, 0, ctx->stream);
+    if (P->kkt32) {
+      FQ_TRY(assemble_into(ctx, P->kkt32));
+    } else {
+      FQ_TRY(make_matrix(ctx, m, EK_KKT, P->grade, P->bc, FQ_FP32, 0.0, &P->kkt32));
+    }
+  } else {
+    vec_recip(P->diag.as<double>(), P->dinv.as<double>(), nullptr, P->n, 0, ctx->stream);
+  }
+  if (P->nh) {
+    FQ_TRY(border_csr(ctx, P->kkt, P->mh.as<double>(), P->ns, P->nu, P->brp, P->bci, P->bval));
+    P->rp = P->brp.as<int32_t>();
+    P->ci = P->bci.as<int32_t>();
+    P->val = P->bval.as<double>();
+    P->nnz = P->kkt->nnz + 2 * P->nu;
+    if (P->kkt32) {
+      FQ_TRY(border_csr(ctx, P->kkt32, P->mh.as<double>(), P->ns, P->nu, P->brp32, P->bci32, P->bval32));
+      P->rp32 = P->brp32.as<int32_t>();
+      P->ci32 = P->bci32.as<int32_t>();
+      P->val32 = P->bval32.as<float>();
+      P->nnz32 = P->kkt32->nnz + 2 * P->nu;
+    }
+  } else {
+    P->rp = P->kkt->rp;
+    P->ci = P->kkt->ci;
+    P->val = P->kkt->values.as<double>();
+    P->nnz = P->kkt->nnz;
+    if (P->kkt32) {
+      P->rp32 = P->kkt32->rp;
+      P->ci32 = P->kkt32->ci;
+      P->val32 = P->kkt32->values.as<float>();
+      P->nnz32 = P->kkt32->nnz;
+    }
+  }
+  P->sysview.ctx = ctx;
+  P->sysview.mesh = m;
+  P->sysview.nrows = P->sysview.ncols = P->n;
+  P->sysview.nnz = P->nnz;
+  P->sysview.precision = FQ_FP64;
+  P->sysview.rp = P->rp;
+  P->sysview.ci = P->ci;
+  P->sysview.values.p = const_cast<double*>(P->val);  // non-owning
+  P->sysview.values.ctx = nullptr;
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return FQ_OK;
+}
+
+// Solve the assembled (bordered) system for rhs (device, size n) into x (device).
+static fq_status mixed_krylov(fq_mixed* P, const double* rhs, double* x, const fq_solve_opts* o, fq_report* rep) {
+  fq_ctx* ctx = P->ctx;
+  const int64_t n = P->n;
+  rep->refinements = 0;
+  if (P->precision != FQ_FP32 || !P->kkt32) {
+    FQ_TRY(minres_run<double>(ctx, P->rp, P->ci, P->val, n, P->nnz, P->dinv.as<double>(), rhs, x, o->rtol,
+                              o->max_iters, rep));
+  } else {
+    // FP64 residual and update around an FP32 MINRES (iterative refinement).
+    DevBuf r, r32, d32;
+    FQ_TRY(r.alloc(ctx, std::max<int64_t>(n, 1) * 8));
+    FQ_TRY(r32.alloc(ctx, std::max<int64_t>(n, 1) * 4));
+    FQ_TRY(d32.alloc(ctx, std::max<int64_t>(n, 1) * 4));
+    FQ_CUDA(ctx, cudaMemsetAsync(x, 0, std::max<int64_t>(n, 1) * 8, ctx->stream));
+    int64_t total = 0;
+    fq_report inner{};
+    for (int64_t ref = 0; ref <= o->max_refinements; ++ref) {
+      double rn = 0, bn = 0;
+      FQ_TRY(residual64(ctx, P->rp, P->ci, P->val, n, x, rhs, r.as<double>(), &rn, &bn));
+      if (bn == 0.0 || rn <= o->refine_rtol * bn || ref == o->max_refinements) break;
+      launch_to_float_scaled(r.as<double>(), r32.as<float>(), 1.0 / rn, n, ctx->stream);
+      FQ_TRY(minres_run<float>(ctx, P->rp32, P->ci32, P->val32, n, P->nnz32, P->dinv32.as<float>(),
+                               r32.as<float>(), d32.as<float>(), o->rtol, o->max_iters, &inner));
+      launch_axpy_from_float(x, d32.as<float>(), rn, n, ctx->stream);
+      total += inner.iters;
+      rep->refinements++;
+    }
+    rep->iters = total;
+    rep->residual = inner.residual;
+    rep->converged = inner.converged;
+  }
+  // true FP64 residual
+  DevBuf r;
+  FQ_TRY(r.alloc(ctx, std::max<int64_t>(n, 1) * 8));
+  double rn = 0, bn = 0;
+  FQ_TRY(residual64(ctx, P->rp, P->ci, P->val, n, x, rhs, r.as<double>(), &rn, &bn));
+  rep->true_residual = bn > 0 ? rn / bn : 0.0;
+  if (P->precision == FQ_FP32) rep->converged = rep->true_residual <= o->refine_rtol;
+  return FQ_OK;
+}
+
+}  // namespace fq
+
+// ============================================================================
+// extern "C"
+// ============================================================================
+#define FQ_GUARD_BEGIN try {
+#define FQ_GUARD_END(ctx)                                                  \
+  }                                                                        \
+  catch (const std::bad_alloc&) {                                          \
+    return fq::set_error(ctx, FQ_OOM_BUDGET, "host allocation failed");    \
+  }                                                                        \
+  catch (const std::exception& e) {                                        \
+    return fq::set_error(ctx, FQ_INVALID_ARG, e.what());                   \
+  }                                                                        \
+  catch (...) {                                                            \
+    return fq::set_error(ctx, FQ_INVALID_ARG, "unknown error");            \
+  }
+
+extern "C" {
+
+const char* fq_status_name(fq_status s) {
+  switch (s) {
+    case FQ_OK:
+      return "FQ_OK";
+    case FQ_INVALID_ARG:
+      return "FQ_INVALID_ARG";
+    case FQ_DEGENERATE_CELL:
+      return "FQ_DEGENERATE_CELL";
+    case FQ_NOT_CONVERGED:
+      return "FQ_NOT_CONVERGED";
+    case FQ_BREAKDOWN:
+      return "FQ_BREAKDOWN";
+    case FQ_OOM_BUDGET:
+      return "FQ_OOM_BUDGET";
+    case FQ_TIMEOUT:
+      return "FQ_TIMEOUT";
+    case FQ_CUDA_ERROR:
+      return "FQ_CUDA_ERROR";
+    case FQ_NO_DEVICE:
+      return "FQ_NO_DEVICE";
+    case FQ_UNSUPPORTED:
+      return "FQ_UNSUPPORTED";
+  }
+  return "FQ_UNKNOWN";
+}
+
+void fq_default_solve_opts(fq_solve_opts* o) {
+  if (!o) return;
+  o->rtol = 1e-10;
+  o->max_iters = 10000;
+  o->precision = FQ_FP64;
+  o->refine_rtol = 1e-12;
+  o->max_refinements = 6;
+}
+
+fq_status fq_ctx_create(int device, void* stream, uint64_t budget, fq_ctx** out) {
+  if (!out) return FQ_INVALID_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return FQ_NO_DEVICE;
+  }
+  if (device < 0 || device >= ndev) return FQ_INVALID_ARG;
+  auto* ctx = new (std::nothrow) fq_ctx();
+  if (!ctx) return FQ_OOM_BUDGET;
+  ctx->device = device;
+  ctx->budget = budget;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    delete ctx;
+    return FQ_CUDA_ERROR;
+  }
+  if (stream) {
+    ctx->stream = static_cast<cudaStream_t>(stream);
+  } else {
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete ctx;
+      return FQ_CUDA_ERROR;
+    }
+    ctx->owns_stream = true;
+  }
+  if (ctx->status.alloc(ctx, 8 * sizeof(int)) != FQ_OK ||
+      cudaMallocHost(reinterpret_cast<void**>(&ctx->host_status), 8 * sizeof(int)) != cudaSuccess) {
+    fq_ctx_destroy(ctx);
+    return FQ_CUDA_ERROR;
+  }
+  cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream);
+  *out = ctx;
+  return FQ_OK;
+}
+
+void fq_ctx_destroy(fq_ctx* ctx) {
+  if (!ctx) return;
+  cudaStreamSynchronize(ctx->stream);
+  ctx->status.release();
+  ctx->scratch.release();
+  if (ctx->host_status) cudaFreeHost(ctx->host_status);
+  if (ctx->owns_stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* fq_ctx_last_error(const fq_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+fq_status fq_ctx_synchronize(fq_ctx* ctx) {
+  if (!ctx) return FQ_INVALID_ARG;
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return FQ_OK;
+}
+
+uint64_t fq_ctx_bytes_in_use(const fq_ctx* ctx) { return ctx ? ctx->in_use : 0; }
+uint64_t fq_ctx_kernel_launches(const fq_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+// ---- meshes -----------------------------------------------------------------
+fq_status fq_mesh_from_cells(fq_ctx* ctx, int dim, int64_t ncells, const int32_t* cells, fq_mesh** out) {
+  if (!ctx || !out) return FQ_INVALID_ARG;
+  *out = nullptr;
+  if (dim < 0 || dim > 4) return set_error(ctx, FQ_UNSUPPORTED, "dimension outside 0..4");
+  if (ncells <= 0 || !cells) return set_error(ctx, FQ_INVALID_ARG, "a mesh needs at least one cell");
+  FQ_GUARD_BEGIN
+  auto* m = new fq_mesh();
+  m->ctx = ctx;
+  fq_status s = build_topology(ctx, m, dim, ncells, cells);
+  if (s != FQ_OK) {
+    delete m;
+    return s;
+  }
+  *out = m;
+  return FQ_OK;
+  FQ_GUARD_END(ctx)
+}
+
+fq_status fq_mesh_kuhn_cube(fq_ctx* ctx, int dim, int nbox, fq_mesh** out) {
+  if (!ctx || !out) return FQ_INVALID_ARG;
+  if (dim < 1 || dim > 4 || nbox < 1) return set_error(ctx, FQ_INVALID_ARG, "kuhn cube needs dim 1..4, n >= 1");
+  FQ_GUARD_BEGIN
+  auto cells = kuhn_cells(dim, nbox);
+  fq_status s = fq_mesh_from_cells(ctx, dim, int64_t(cells.size()) / (dim + 1), cells.data(), out);
+  if (s == FQ_OK) (*out)->kuhn_nbox = nbox;
+  return s;
+  FQ_GUARD_END(ctx)
+}
+
+void fq_mesh_destroy(fq_mesh* m) {
+  if (!m) return;
+  cudaStreamSynchronize(m->ctx->stream);
+  delete m;
+}
+
+int fq_mesh_dim(const fq_mesh* m) { return m ? m->dim : -1; }
+
+int64_t fq_mesh_nsimplices(const fq_mesh* m, int k) {
+  if (!m || k < 0 || k > m->dim) return 0;
+  return m->nsimp[k];
+}
+
+int64_t fq_mesh_ndofs(const fq_mesh* m, int k, fq_bc bc) { return m ? ndofs(m, k, bc) : 0; }
+
+fq_status fq_mesh_simplices(const fq_mesh* m, int k, int32_t* out) {
+  if (!m || !out || k < 0 || k > m->dim) return FQ_INVALID_ARG;
+  std::memcpy(out, m->skel[k].data(), m->skel[k].size() * sizeof(int32_t));
+  return FQ_OK;
+}
+
+fq_status fq_mesh_interior(const fq_mesh* m, int k, int64_t* out) {
+  if (!m || !out || k < 0 || k > m->dim) return FQ_INVALID_ARG;
+  int64_t c = 0;
+  for (int64_t i = 0; i < m->nsimp[k]; ++i)
+    if (!m->boundary[k][i]) out[c++] = i;
+  return FQ_OK;
+}
+
+fq_status fq_mesh_orientation(const fq_mesh* mc, int8_t* out) {
+  auto* m = const_cast<fq_mesh*>(mc);
+  if (!m || !out) return FQ_INVALID_ARG;
+  FQ_GUARD_BEGIN
+  if (m->orientation.empty()) {
+    if (m->dim == 0)
+      m->orientation.assign(size_t(m->ncells), 1);
+    else
+      compute_orientation(m, m->cell_faces_host[m->dim - 1]);
+  }
+  std::memcpy(out, m->orientation.data(), m->orientation.size());
+  return FQ_OK;
+  FQ_GUARD_END(m->ctx)
+}
+
+fq_status fq_mesh_set_lengths_sq(fq_mesh* m, const double* l, int on_device) {
+  if (!m || (!l && m->nsimp[1] > 0)) return FQ_INVALID_ARG;
+  fq_ctx* ctx = m->ctx;
+  const int64_t ne = m->dim >= 1 ? m->nsimp[1] : 0;
+  if (m->lengths.bytes < size_t(std::max<int64_t>(ne, 1)) * 8) FQ_TRY(m->lengths.alloc(ctx, std::max<int64_t>(ne, 1) * 8));
+  if (ne > 0)
+    FQ_CUDA(ctx, cudaMemcpyAsync(m->lengths.p, l, ne * 8, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  m->has_lengths = true;
+  return FQ_OK;
+}
+
+fq_status fq_mesh_get_lengths_sq(const fq_mesh* m, double* out) {
+  if (!m || !out || !m->has_lengths) return FQ_INVALID_ARG;
+  const int64_t ne = m->dim >= 1 ? m->nsimp[1] : 0;
+  if (ne > 0) FQ_CUDA(m->ctx, cudaMemcpyAsync(out, m->lengths.p, ne * 8, cudaMemcpyDeviceToHost, m->ctx->stream));
+  FQ_CUDA(m->ctx, cudaStreamSynchronize(m->ctx->stream));
+  return FQ_OK;
+}
+
+fq_status fq_mesh_lengths_from_coords(fq_mesh* m, const double* coords, int adim, const double* signs) {
+  if (!m || !coords || adim <= 0) return FQ_INVALID_ARG;
+  FQ_GUARD_BEGIN
+  const int64_t ne = m->dim >= 1 ? m->nsimp[1] : 0;
+  std::vector<double> l(size_t(std::max<int64_t>(ne, 1)));
+  for (int64_t e = 0; e < ne; ++e) {
+    const int32_t vi = m->skel[1][e * 2], vj = m->skel[1][e * 2 + 1];
+    double acc = 0.0;
+    for (int a = 0; a < adim; ++a) {
+      const double d = coords[int64_t(vj) * adim + a] - coords[int64_t(vi) * adim + a];
+      acc += d * ((signs ? signs[a] : 1.0) * d);
+    }
+    l[e] = acc;
+  }
+  return fq_mesh_set_lengths_sq(m, l.data(), 0);
+  FQ_GUARD_END(m->ctx)
+}
+
+fq_status fq_mesh_kuhn_lengths(fq_mesh* m, const double* side, const double* signs, double jitter, uint64_t seed) {
+  if (!m || m->kuhn_nbox <= 0) return m ? set_error(m->ctx, FQ_INVALID_ARG, "not a kuhn cube mesh") : FQ_INVALID_ARG;
+  FQ_GUARD_BEGIN
+  const int d = m->dim, nb = m->kuhn_nbox;
+  int64_t nv = 1;
+  for (int a = 0; a < d; ++a) nv *= (nb + 1);
+  std::vector<double> x(size_t(nv * d));
+  for (int64_t v = 0; v < nv; ++v) {
+    int64_t rem = v;
+    for (int a = 0; a < d; ++a) {
+      const int64_t c = rem % (nb + 1);
+      rem /= (nb + 1);
+      const double sa = side ? side[a] : 1.0;
+      double pos = (double(c) / double(nb)) * sa;
+      if (jitter != 0.0) {
+        const double u = uniform_pm1(seed, uint64_t(v) * uint64_t(d) + uint64_t(a));
+        pos = pos + jitter * (sa / nb) * u;
+      }
+      x[v * d + a] = pos;
+    }
+  }
+  return fq_mesh_lengths_from_coords(m, x.data(), d, signs);
+  FQ_GUARD_END(m->ctx)
+}
+
+// ---- kernels (a), (b) -----------------------------------------------------------
+fq_status fq_cell_metrics(fq_ctx* ctx, fq_mesh* m, double* ginv, double* det, double* vol) {
+  if (!ctx || !m) return FQ_INVALID_ARG;
+  if (!m->has_lengths) return set_error(ctx, FQ_INVALID_ARG, "mesh has no edge lengths");
+  FQ_GUARD_BEGIN
+  ElemArgs a;
+  a.ncells = m->ncells;
+  a.lengths = m->lengths.as<double>();
+  a.cell_edges = m->dim >= 1 ? m->cell_faces[1].as<int32_t>() : nullptr;
+  a.out = nullptr;
+  a.ginv_out = ginv;
+  a.det_out = det;
+  a.vol_out = vol;
+  a.param = 0.0;
+  a.status = ctx->status.as<int>();
+  FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
+  if (launch_element(m->dim, 0, EK_METRIC, 0, a, ctx->stream) != 0) return set_error(ctx, FQ_UNSUPPORTED, "dim");
+  ctx->launches++;
+  FQ_CUDA(ctx, cudaGetLastError());
+  FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
+  return FQ_OK;
+  FQ_GUARD_END(ctx)
+}
+
+fq_status fq_element_matrices(fq_ctx* ctx, fq_mesh* m, fq_form form, int grade, fq_precision prec, void* out,
+                              int* rows, int* cols) {
+  if (!ctx || !m || !out) return FQ_INVALID_ARG;
+  if (!m->has_lengths) return set_error(ctx, FQ_INVALID_ARG, "mesh has no edge lengths");
+  FQ_GUARD_BEGIN
+  const int n = m->dim;
+  const int tg = (form == FQ_DIF_TEST || form == FQ_DIF_BOTH) ? grade - 1 : grade;
+  const int sg = (form == FQ_DIF_TRIAL || form == FQ_DIF_BOTH) ? grade - 1 : grade;
+  const int lr = (tg >= 0 && tg <= n) ? cbinom(n + 1, tg + 1) : 0;
+  const int lc = (sg >= 0 && sg <= n) ? cbinom(n + 1, sg + 1) : 0;
+  if (rows) *rows = lr;
+  if (cols) *cols = lc;
+  if (lr == 0 || lc == 0 || grade > n) return FQ_OK;
+  const int kind = int(form);
+  Layout lay = make_layout(n, kind, grade);
+  const int fp32 = prec == FQ_FP32;
+  FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
+  FQ_TRY(element_pass(ctx, m, kind, grade, fp32, 0.0, m->elem, lay.nent));
+  // expand packed/full entries into row-major [lr*lc][ncells]
+  const size_t w = fp32 ? 4 : 8;
+  for (int i = 0; i < lr; ++i)
+    for (int j = 0; j < lc; ++j) {
+      const int e = lay.entry[size_t(i) * lc + j];
+      char* dst = static_cast<char*>(out) + (size_t(i) * lc + j) * m->ncells * w;
+      if (e < 0)
+        FQ_CUDA(ctx, cudaMemsetAsync(dst, 0, m->ncells * w, ctx->stream));
+      else
+        FQ_CUDA(ctx, cudaMemcpyAsync(dst, m->elem.as<char>() + size_t(e) * m->ncells * w, m->ncells * w,
+                                     cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+  FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
+  return FQ_OK;
+  FQ_GUARD_END(ctx)
+}
+
+// ---- assembly ---------------------------------------------------------------------
+fq_status fq_assemble(fq_ctx* ctx, fq_mesh* m, fq_form form, int grade, fq_bc bc, fq_precision prec,
+                      fq_matrix** out) {
+  if (!ctx || !m || !out) return FQ_INVALID_ARG;
+  *out = nullptr;
+  if (int(form) < 0 || int(form) > 3) return set_error(ctx, FQ_INVALID_ARG, "unknown form");
+  FQ_GUARD_BEGIN
+  int64_t rows = 0, cols = 0;
+  if (!valid_form_shape(m, form, grade, bc, &rows, &cols) || grade > m->dim)
+    return empty_matrix(ctx, m, rows, cols, prec, out);
+  return make_matrix(ctx, m, int(form), grade, int(bc), int(prec), 0.0, out);
+  FQ_GUARD_END(ctx)
+}
+
+fq_status fq_reassemble(fq_ctx* ctx, fq_mesh* m, fq_matrix* mat) {
+  if (!ctx || !m || !mat || mat->mesh != m) return FQ_INVALID_ARG;
+  if (!mat->plan) return FQ_OK;
+  FQ_GUARD_BEGIN
+  return assemble_into(ctx, mat);
+  FQ_GUARD_END(ctx)
+}
+
+fq_status fq_hdif_gram(fq_ctx* ctx, fq_mesh* m, int grade, fq_bc bc, fq_matrix** out) {
+  if (!ctx || !m || !out) return FQ_INVALID_ARG;
+  FQ_GUARD_BEGIN
+  const int64_t nk = ndofs(m, grade, bc);
+  if (nk == 0) return empty_matrix(ctx, m, nk, nk, FQ_FP64, out);
+  return make_matrix(ctx, m, EK_HDIF, grade, int(bc), FQ_FP64, 0.0, out);
+  FQ_GUARD_END(ctx)
+}
+
+fq_status fq_coboundary(fq_ctx* ctx, fq_mesh* m, int k, fq_bc bc, fq_matrix** out) {
+  if (!ctx || !m || !out) return FQ_INVALID_ARG;
+  FQ_GUARD_BEGIN
+  const int64_t nr = ndofs(m, k + 1, bc), nc = ndofs(m, k, bc);
+  if (k < 0 || k >= m->dim || nr == 0 || nc == 0) return empty_matrix(ctx, m, nr, nc, FQ_FP64, out);
+  // rows: (k+1)-simplices; entries (-1)^p at the face omitting position p.
+  const int w = k + 2;
+  std::vector<int32_t> rp(1, 0), ci;
+  std::vector<double> val;
+  const auto& sk = m->skel[k + 1];
+  const auto& low = m->skel[k];
+  const int fw = w - 1;
+  for (int64_t r = 0; r < m->nsimp[k + 1]; ++r) {
+    if (bc == FQ_RELATIVE && m->boundary[k + 1][r]) continue;
+    std::vector<std::pair<int32_t, double>> ent;
+    for (int p = 0; p < w; ++p) {
+      int32_t tup[5];
+      int q = 0;
+      for (int i = 0; i < w; ++i)
+        if (i != p) tup[q++] = sk[r * w + i];
+      int64_t lo = 0, hi = m->nsimp[k] - 1, found = -1;
+      while (lo <= hi) {
+        const int64_t mid = (lo + hi) / 2;
+        int cmp = 0;
+        for (int i = fw - 1; i >= 0; --i)
+          if (low[mid * fw + i] != tup[i]) {
+            cmp = low[mid * fw + i] < tup[i] ? -1 : 1;
+            break;
+          }
+        if (cmp == 0) {
+          found = mid;
+          break;
+        }
+        if (cmp < 0)
+          lo = mid + 1;
+        else
+          hi = mid - 1;
+      }
+      int64_t c = found;
+      if (bc == FQ_RELATIVE) c = m->interior_map[k][found];
+      if (c < 0) continue;
+      ent.emplace_back(int32_t(c), (p % 2) ? -1.0 : 1.0);
+    }
+    std::sort(ent.begin(), ent.end());
+    for (auto& e : ent) {
+      ci.push_back(e.first);
+      val.push_back(e.second);
+    }
+    rp.push_back(int32_t(ci.size()));
+  }
+  auto* mat = new fq_matrix();
+  mat->ctx = ctx;
+  mat->mesh = m;
+  mat->nrows = nr;
+  mat->ncols = nc;
+  mat->nnz = int64_t(ci.size());
+  mat->precision = FQ_FP64;
+  fq_status s = mat->row_ptr.alloc(ctx, rp.size() * 4);
+  if (s == FQ_OK) s = mat->col_idx.alloc(ctx, std::max<size_t>(ci.size(), 1) * 4);
+  if (s == FQ_OK) s = mat->values.alloc(ctx, std::max<size_t>(val.size(), 1) * 8);
+  if (s != FQ_OK) {
+    delete mat;
+    return s;
+  }
+  cudaMemcpyAsync(mat->row_ptr.p, rp.data(), rp.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+  if (!ci.empty()) {
+    cudaMemcpyAsync(mat->col_idx.p, ci.data(), ci.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(mat->values.p, val.data(), val.size() * 8, cudaMemcpyHostToDevice, ctx->stream);
+  }
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  mat->rp = mat->row_ptr.as<int32_t>();
+  mat->ci = mat->col_idx.as<int32_t>();
+  *out = mat;
+  return FQ_OK;
+  FQ_GUARD_END(ctx)
+}
+
+fq_status fq_assemble_host(fq_ctx* ctx, fq_mesh* m, fq_matrix* mat, const double* lengths, void* values_out) {
+  if (!ctx || !m || !mat || !lengths || !values_out) return FQ_INVALID_ARG;
+  FQ_GUARD_BEGIN
+  FQ_TRY(fq_mesh_set_lengths_sq(m, lengths, 0));
+  if (mat->plan) FQ_TRY(assemble_into(ctx, mat));
+  const size_t w = mat->precision == FQ_FP32 ? 4 : 8;
+  if (mat->nnz > 0)
+    FQ_CUDA(ctx, cudaMemcpyAsync(values_out, mat->values.p, mat->nnz * w, cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return FQ_OK;
+  FQ_GUARD_END(ctx)
+}
+
+fq_status fq_matrix_info(const fq_matrix* a, int64_t* nrows, int64_t* ncols, int64_t* nnz, int* precision) {
+  if (!a) return FQ_INVALID_ARG;
+  if (nrows) *nrows = a->nrows;
+  if (ncols) *ncols = a->ncols;
+  if (nnz) *nnz = a->nnz;
+  if (precision) *precision = a->precision;
+  return FQ_OK;
+}
+
+fq_status fq_matrix_device_arrays(const fq_matrix* a, const int32_t** rp, const int32_t** ci, const void** val) {
+  if (!a) return FQ_INVALID_ARG;
+  if (rp) *rp = a->rp;
+  if (ci) *ci = a->ci;
+  if (val) *val = a->values.p;
+  return FQ_OK;
+}
+
+fq_status fq_matrix_copy_to_host(fq_ctx* ctx, const fq_matrix* a, int32_t* rp, int32_t* ci, void* val) {
+  if (!ctx || !a) return FQ_INVALID_ARG;
+  const size_t w = a->precision == FQ_FP32 ? 4 : 8;
+  if (rp) FQ_CUDA(ctx, cudaMemcpyAsync(rp, a->rp, (a->nrows + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (a->nnz > 0) {
+    if (ci) FQ_CUDA(ctx, cudaMemcpyAsync(ci, a->ci, a->nnz * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (val) FQ_CUDA(ctx, cudaMemcpyAsync(val, a->values.p, a->nnz * w, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return FQ_OK;
+}
+
+void fq_matrix_destroy(fq_matrix* a) {
+  if (!a) return;
+  if (a->ctx) cudaStreamSynchronize(a->ctx->stream);
+  delete a;
+}
+
+// ---- solvers --------------------------------------------------------------------------
+fq_status fq_spmv(fq_ctx* ctx, const fq_matrix* a, const void* x, void* y) {
+  if (!ctx || !a || (a->nrows && (!x || !y))) return FQ_INVALID_ARG;
+  launch_spmv(a, x, y, ctx->stream);
+  ctx->launches++;
+  FQ_CUDA(ctx, cudaGetLastError());
+  return FQ_OK;
+}
+
+static fq_status check_square(fq_ctx* ctx, const fq_matrix* a) {
+  if (a->nrows != a->ncols) return set_error(ctx, FQ_INVALID_ARG, "operator must be square");
+  if (a->precision != FQ_FP64) return set_error(ctx, FQ_INVALID_ARG, "solver takes an FP64 operator");
+  return FQ_OK;
+}
+
+fq_status fq_minres(fq_ctx* ctx, const fq_matrix* a, const double* dinv, const double* b, double* x,
+                    const fq_solve_opts* o, fq_report* rep) {
+  if (!ctx || !a || !b || !x) return FQ_INVALID_ARG;
+  FQ_TRY(check_square(ctx, a));
+  FQ_GUARD_BEGIN
+  fq_solve_opts d;
+  fq_default_solve_opts(&d);
+  if (!o) o = &d;
+  fq_report r{};
+  FQ_TRY(minres_run<double>(ctx, a->rp, a->ci, a->values.as<double>(), a->nrows, a->nnz, dinv, b, x, o->rtol,
+                            o->max_iters, &r));
+  if (rep) *rep = r;
+  return r.converged ? FQ_OK : FQ_NOT_CONVERGED;
+  FQ_GUARD_END(ctx)
+}
+
+fq_status fq_cg(fq_ctx* ctx, const fq_matrix* a, const double* dinv, const double* b, double* x,
+                const fq_solve_opts* o, fq_report* rep) {
+  if (!ctx || !a || !b || !x) return FQ_INVALID_ARG;
+  FQ_TRY(check_square(ctx, a));
+  FQ_GUARD_BEGIN
+  fq_solve_opts d;
+  fq_default_solve_opts(&d);
+  if (!o) o = &d;
+  fq_report r{};
+  FQ_TRY(cg_run<double>(ctx, a->rp, a->ci, a->values.as<double>(), a->nrows, a->nnz, dinv, b, x, o->rtol,
+                        o->max_iters, &r));
+  if (rep) *rep = r;
+  return r.converged ? FQ_OK : FQ_NOT_CONVERGED;
+  FQ_GUARD_END(ctx)
+}
+
+// ---- mixed problem ----------------------------------------------------------------
+fq_status fq_mixed_create(fq_ctx* ctx, fq_mesh* m, int grade, fq_bc bc, int precision, fq_mixed** out) {
+  if (!ctx || !m || !out) return FQ_INVALID_ARG;
+  *out = nullptr;
+  if (grade < 0 || grade > m->dim) return set_error(ctx, FQ_INVALID_ARG, "grade outside 0..dim");
+  FQ_GUARD_BEGIN
+  // The closed-form harmonic border needs the cohomology of a ball.
+  int64_t chi = 0;
+  for (int k = 0; k <= m->dim; ++k) chi += (k % 2 ? -1 : 1) * m->nsimp[k];
+  if (chi != 1)
+    return set_error(ctx, FQ_UNSUPPORTED, "mixed solve supports meshes with the cohomology of a ball (Euler characteristic 1)");
+  auto* P = new fq_mixed();
+  P->ctx = ctx;
+  P->mesh = m;
+  P->grade = grade;
+  P->bc = bc;
+  P->precision = precision;
+  P->ns = ndofs(m, grade - 1, bc);
+  P->nu = ndofs(m, grade, bc);
+  P->nh = ((bc == FQ_ABSOLUTE && grade == 0) || (bc == FQ_RELATIVE && grade == m->dim)) ? 1 : 0;
+  P->n = P->ns + P->nu + P->nh;
+  fq_status s = FQ_OK;
+  if (grade >= 1) s = interior_list(ctx, m, grade - 1, P->list_sigma);
+  if (s == FQ_OK) s = interior_list(ctx, m, grade, P->list_u);
+  if (s == FQ_OK) s = mixed_assemble(P);
+  if (s != FQ_OK) {
+    delete P;
+    return s;
+  }
+  *out = P;
+  return FQ_OK;
+  FQ_GUARD_END(ctx)
+}
+
+fq_status fq_mixed_reassemble(fq_mixed* P) {
+  if (!P) return FQ_INVALID_ARG;
+  FQ_GUARD_BEGIN
+  return mixed_assemble(P);
+  FQ_GUARD_END(P->ctx)
+}
+
+fq_status fq_mixed_info(const fq_mixed* P, int64_t* ns, int64_t* nu, int64_t* nh, int64_t* nnz) {
+  if (!P) return FQ_INVALID_ARG;
+  if (ns) *ns = P->ns;
+  if (nu) *nu = P->nu;
+  if (nh) *nh = P->nh;
+  if (nnz) *nnz = P->nnz;
+  return FQ_OK;
+}
+
+const fq_matrix* fq_mixed_system(const fq_mixed* P) { return P ? &P->sysview : nullptr; }
+
+void fq_mixed_destroy(fq_mixed* P) {
+  if (!P) return;
+  cudaStreamSynchronize(P->ctx->stream);
+  P->sysview.values.p = nullptr;
+  delete P;
+}
+
+fq_status fq_mixed_solve_device(fq_mixed* P, const double* src, double* sigma, double* u, double* p,
+                                const fq_solve_opts* o, fq_report* rep) {
+  if (!P || !src) return FQ_INVALID_ARG;
+  FQ_GUARD_BEGIN
+  fq_ctx* ctx = P->ctx;
+  fq_mesh* m = P->mesh;
+  fq_solve_opts d;
+  fq_default_solve_opts(&d);
+  if (!o) o = &d;
+  const int64_t n = P->n;
+  DevBuf rhs, x;
+  FQ_TRY(rhs.alloc(ctx, std::max<int64_t>(n, 1) * 8));
+  FQ_TRY(x.alloc(ctx, std::max<int64_t>(n, 1) * 8));
+  FQ_CUDA(ctx, cudaMemsetAsync(rhs.p, 0, std::max<int64_t>(n, 1) * 8, ctx->stream));
+  // rhs = [0; E^T f; 0]
+  vec_gather(src, P->bc == FQ_RELATIVE ? P->list_u.as<int32_t>() : nullptr, rhs.as<double>() + P->ns, P->nu,
+             ctx->stream);
+  fq_report r{};
+  FQ_TRY(mixed_krylov(P, rhs.as<double>(), x.as<double>(), o, &r));
+  // split and extend by E
+  if (sigma && P->grade >= 1) {
+    const int64_t amb = m->nsimp[P->grade - 1];
+    FQ_CUDA(ctx, cudaMemsetAsync(sigma, 0, std::max<int64_t>(amb, 1) * 8, ctx->stream));
+    vec_scatter_map(x.as<double>(), P->bc == FQ_RELATIVE ? P->list_sigma.as<int32_t>() : nullptr, sigma, P->ns,
+                    ctx->stream);
+  }
+  if (u) {
+    const int64_t amb = m->nsimp[P->grade];
+    FQ_CUDA(ctx, cudaMemsetAsync(u, 0, std::max<int64_t>(amb, 1) * 8, ctx->stream));
+    vec_scatter_map(x.as<double>() + P->ns, P->bc == FQ_RELATIVE ? P->list_u.as<int32_t>() : nullptr, u, P->nu,
+                    ctx->stream);
+  }
+  if (p && P->nh)
+    FQ_CUDA(ctx, cudaMemcpyAsync(p, x.as<double>() + P->ns + P->nu, P->nh * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (rep) *rep = r;
+  return r.converged ? FQ_OK : FQ_NOT_CONVERGED;
+  FQ_GUARD_END(P->ctx)
+}
+
+fq_status fq_mixed_solve(fq_mixed* P, const double* src_h, double* sigma_h, double* u_h, double* p_h,
+                         const fq_solve_opts* o, fq_report* rep) {
+  if (!P || !src_h) return FQ_INVALID_ARG;
+  FQ_GUARD_BEGIN
+  fq_ctx* ctx = P->ctx;
+  fq_mesh* m = P->mesh;
+  const int64_t nk = m->nsimp[P->grade];
+  const int64_t nkm = P->grade >= 1 ? m->nsimp[P->grade - 1] : 0;
+  DevBuf src, sg, uu, pp;
+  FQ_TRY(src.alloc(ctx, std::max<int64_t>(nk, 1) * 8));
+  FQ_TRY(sg.alloc(ctx, std::max<int64_t>(nkm, 1) * 8));
+  FQ_TRY(uu.alloc(ctx, std::max<int64_t>(nk, 1) * 8));
+  FQ_TRY(pp.alloc(ctx, 16));
+  FQ_CUDA(ctx, cudaMemcpyAsync(src.p, src_h, nk * 8, cudaMemcpyHostToDevice, ctx->stream));
+  fq_status s = fq_mixed_solve_device(P, src.as<double>(), sg.as<double>(), uu.as<double>(), pp.as<double>(), o, rep);
+  if (s != FQ_OK && s != FQ_NOT_CONVERGED) return s;
+  if (sigma_h && nkm > 0) FQ_CUDA(ctx, cudaMemcpyAsync(sigma_h, sg.p, nkm * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  if (u_h) FQ_CUDA(ctx, cudaMemcpyAsync(u_h, uu.p, nk * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  if (p_h && P->nh) FQ_CUDA(ctx, cudaMemcpyAsync(p_h, pp.p, P->nh * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return s;
+  FQ_GUARD_END(P->ctx)
+}
+
+fq_status fq_solve_source(fq_ctx* ctx, fq_mesh* m, int grade, fq_bc bc, const double* src, double* sigma, double* u,
+                          double* p, const fq_solve_opts* o, fq_report* rep) {
+  if (!ctx || !m || !src) return FQ_INVALID_ARG;
+  fq_mixed* P = nullptr;
+  fq_solve_opts d;
+  fq_default_solve_opts(&d);
+  if (!o) o = &d;
+  FQ_TRY(fq_mixed_create(ctx, m, grade, bc, o->precision, &P));
+  fq_status s = fq_mixed_solve(P, src, sigma, u, p, o, rep);
+  fq_mixed_destroy(P);
+  return s;
+}
+
+// ---- Dirac ----------------------------------------------------------------------------
+fq_status fq_dirac_system(fq_ctx* ctx, fq_mesh* m, double mass_term, fq_matrix** out) {
+  if (!ctx || !m || !out) return FQ_INVALID_ARG;
+  FQ_GUARD_BEGIN
+  return make_matrix(ctx, m, EK_DIRAC, 0, FQ_RELATIVE, FQ_FP64, mass_term, out);
+  FQ_GUARD_END(ctx)
+}
+
+fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* m, double mass_term, const double* load_h,
+                                const double* lift_h, double* x_h, const fq_solve_opts* o, fq_report* rep) {
+  if (!ctx || !m || !load_h || !x_h) return FQ_INVALID_ARG;
+  if (mass_term == 0.0)
+    return set_error(ctx, FQ_UNSUPPORTED, "massless Dirac needs the bordered direct solve; pass a nonzero mass term");
+  FQ_GUARD_BEGIN
+  fq_solve_opts d;
+  fq_default_solve_opts(&d);
+  if (!o) o = &d;
+  const int n = m->dim;
+  int64_t nfull = 0, nrel = 0;
+  for (int k = 0; k <= n; ++k) {
+    nfull += m->nsimp[k];
+    nrel += m->ninterior[k];
+  }
+  // S_II (solve) and S_IB (rhs lift term) from the same element program
+  fq_matrix* sii = nullptr;
+  FQ_TRY(make_matrix(ctx, m, EK_DIRAC, 0, FQ_RELATIVE, FQ_FP64, mass_term, &sii));
+  std::unique_ptr<fq_matrix> g1(sii);
+  Plan* pib = nullptr;
+  FQ_TRY(get_plan(ctx, m, EK_DIRAC, 0, FQ_RELATIVE, FQ_ABSOLUTE, &pib));
+  auto sib = std::make_unique<fq_matrix>();
+  sib->ctx = ctx;
+  sib->mesh = m;
+  sib->plan = pib;
+  sib->kind = EK_DIRAC;
+  sib->bc = FQ_RELATIVE;
+  sib->precision = FQ_FP64;
+  sib->param = mass_term;
+  sib->nrows = pib->nrows;
+  sib->ncols = pib->ncols;
+  FQ_TRY(assemble_into(ctx, sib.get()));
+  // relative -> ambient flattened map
+  std::vector<int32_t> map;
+  {
+    int64_t off = 0;
+    for (int k = 0; k <= n; ++k) {
+      for (int64_t i = 0; i < m->nsimp[k]; ++i)
+        if (!m->boundary[k][i]) map.push_back(int32_t(off + i));
+      off += m->nsimp[k];
+    }
+  }
+  DevBuf dmap, load, lift, rhs, tmp, x, diag, dinv;
+  FQ_TRY(dmap.alloc(ctx, std::max<size_t>(map.size(), 1) * 4));
+  FQ_TRY(load.alloc(ctx, std::max<int64_t>(nfull, 1) * 8));
+  FQ_TRY(lift.alloc(ctx, std::max<int64_t>(nfull, 1) * 8));
+  FQ_TRY(rhs.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));
+  FQ_TRY(tmp.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));
+  FQ_TRY(x.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));
+  FQ_TRY(diag.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));
+  FQ_TRY(dinv.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));
+  cudaStream_t st = ctx->stream;
+  if (!map.empty()) FQ_CUDA(ctx, cudaMemcpyAsync(dmap.p, map.data(), map.size() * 4, cudaMemcpyHostToDevice, st));
+  FQ_CUDA(ctx, cudaMemcpyAsync(load.p, load_h, nfull * 8, cudaMemcpyHostToDevice, st));
+  if (lift_h)
+    FQ_CUDA(ctx, cudaMemcpyAsync(lift.p, lift_h, nfull * 8, cudaMemcpyHostToDevice, st));
+  else
+    FQ_CUDA(ctx, cudaMemsetAsync(lift.p, 0, nfull * 8, st));
+  // rhs = E^T load - S_IB lift
+  vec_gather(load.as<double>(), dmap.as<int32_t>(), rhs.as<double>(), nrel, st);
+  launch_spmv(sib.get(), lift.p, tmp.p, st);
+  vec_sub(rhs.as<double>(), tmp.as<double>(), nrel, st);
+  vec_diag(sii, diag.as<double>(), st);
+  vec_recip(diag.as<double>(), dinv.as<double>(), nullptr, nrel, 1, st);
+  ctx->launches += 5;
+  fq_report r{};
+  FQ_TRY(minres_run<double>(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, sii->nnz, dinv.as<double>(),
+                            rhs.as<double>(), x.as<double>(), o->rtol, o->max_iters, &r));
+  {
+    DevBuf rr;
+    FQ_TRY(rr.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));
+    double rn = 0, bn = 0;
+    FQ_TRY(residual64(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, x.as<double>(), rhs.as<double>(),
+                      rr.as<double>(), &rn, &bn));
+    r.true_residual = bn > 0 ? rn / bn : 0.0;
+  }
+  // x = lift + E x_int
+  DevBuf ext;
+  FQ_TRY(ext.alloc(ctx, std::max<int64_t>(nfull, 1) * 8));
+  FQ_CUDA(ctx, cudaMemsetAsync(ext.p, 0, nfull * 8, st));
+  vec_scatter_map(x.as<double>(), dmap.as<int32_t>(), ext.as<double>(), nrel, st);
+  vec_add(ext.as<double>(), lift.as<double>(), nfull, st);
+  FQ_CUDA(ctx, cudaMemcpyAsync(x_h, ext.p, nfull * 8, cudaMemcpyDeviceToHost, st));
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  if (rep) *rep = r;
+  return r.converged ? FQ_OK : FQ_NOT_CONVERGED;
+  FQ_GUARD_END(ctx)
+}
+
+}  // extern "C"

@@ -1,0 +1,638 @@
+// Kernel (c) and its set-up: the scatter of per-cell element entries into a
+// precomputed CSR pattern, atomic-free.
+//
+// The reference assembles by pushing every nonzero element entry as a COO
+// triplet in cell order and letting the COO -> CSR conversion sum duplicates
+// (formoniq/src/galerkin.rs:138-188). Here the (row, col) of every element entry
+// is known before any value exists, so the set-up sorts the contributions once
+// by (row, col) -- a stable radix sort, so within a slot they stay in cell order,
+// the reference's summation order -- and the hot loop is then
+//   element kernel:  values of every cell, entry-major (coalesced stores)
+//   scatter kernel:  one thread per CSR slot sums its run of contributions
+// with no atomics and a deterministic summation order. A slot whose every
+// contribution is exactly 0.0 does not exist in the reference (the `val != 0.0`
+// rule, galerkin.rs:173); such slots are flagged and compacted away.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "fq_element_kernel.cuh"
+#include "fq_internal.h"
+
+namespace fq {
+
+// ---------------------------------------------------------------------------
+// Local layouts
+// ---------------------------------------------------------------------------
+Layout make_layout(int n, int kind, int K) {
+  Layout L;
+  auto push_grade = [&](int grade, int block, bool row, bool col) {
+    const int cnt = (grade >= 0 && grade <= n) ? cbinom(n + 1, grade + 1) : 0;
+    for (int l = 0; l < cnt; ++l) {
+      if (row) {
+        L.row_grade.push_back(grade);
+        L.row_face.push_back(l);
+        L.row_block.push_back(block);
+      }
+      if (col) {
+        L.col_grade.push_back(grade);
+        L.col_face.push_back(l);
+        L.col_block.push_back(block);
+      }
+    }
+  };
+  bool sym = true;
+  switch (kind) {
+    case EK_MASS:
+    case EK_HDIF:
+      push_grade(K, 0, true, true);
+      L.block_grade = {K};
+      break;
+    case EK_DIF_BOTH:
+      push_grade(K - 1, 0, true, true);
+      L.block_grade = {K - 1};
+      break;
+    case EK_DIF_TEST:
+      push_grade(K - 1, 0, true, false);
+      push_grade(K, 0, false, true);
+      L.block_grade = {K - 1};
+      sym = false;
+      break;
+    case EK_DIF_TRIAL:
+      push_grade(K, 0, true, false);
+      push_grade(K - 1, 0, false, true);
+      L.block_grade = {K};
+      sym = false;
+      break;
+    case EK_KKT:
+      push_grade(K - 1, 0, true, true);
+      push_grade(K, 1, true, true);
+      L.block_grade = {K - 1, K};
+      break;
+    case EK_DIRAC:
+      for (int j = 0; j <= n; ++j) push_grade(j, j, true, true);
+      for (int j = 0; j <= n; ++j) L.block_grade.push_back(j);
+      break;
+    default:
+      break;
+  }
+  L.nblocks = int(L.block_grade.size());
+  L.nrow_local = int(L.row_grade.size());
+  L.ncol_local = int(L.col_grade.size());
+  L.entry.assign(size_t(L.nrow_local) * L.ncol_local, -1);
+  if (sym) {
+    const int Lc = L.nrow_local;
+    for (int i = 0; i < Lc; ++i)
+      for (int j = 0; j < Lc; ++j) {
+        const int a = std::min(i, j), b = std::max(i, j);
+        bool zero = false;
+        if (kind == EK_KKT && L.row_block[i] == 1 && L.row_block[j] == 1 && K == n) zero = true;  // dif_both(n+1)=0
+        if (kind == EK_DIF_BOTH && K > n) zero = true;
+        if (kind == EK_DIRAC && std::abs(L.row_grade[i] - L.row_grade[j]) >= 2) zero = true;
+        if (!zero) L.entry[size_t(i) * Lc + j] = packed_index(a, b, Lc);
+      }
+    L.nent = (Lc * (Lc + 1)) / 2;
+    if (kind == EK_KKT) {
+      for (int i = 0; i < Lc; ++i) L.diag_entry.push_back(L.nent + i);
+      L.nent += Lc;
+    }
+  } else {
+    for (int i = 0; i < L.nrow_local; ++i)
+      for (int j = 0; j < L.ncol_local; ++j) L.entry[size_t(i) * L.ncol_local + j] = i * L.ncol_local + j;
+    L.nent = L.nrow_local * L.ncol_local;
+  }
+  return L;
+}
+
+// ---------------------------------------------------------------------------
+// Plan construction (set-up, once per mesh and program)
+// ---------------------------------------------------------------------------
+struct KeyArgs {
+  int64_t ncells;
+  int lr, lc;
+  const int32_t* entry;       // [lr*lc]
+  const int32_t* row_src;     // per local row: pointer index into faces table
+  const int32_t* col_src;
+  const int64_t* row_off;     // per local row: global offset of its block
+  const int64_t* col_off;
+  const int32_t* const* faces;  // per (local row/col) : cell_faces[grade] + face*ncells
+  const int32_t* const* rmaps;  // per local row: interior map or null
+  const int32_t* const* cmaps;
+  int64_t ncols;
+  uint64_t sentinel;
+  uint64_t* keys;
+  int32_t* vals;
+};
+
+__global__ void plan_keys_kernel(KeyArgs a) {
+  const int64_t per = int64_t(a.lr) * a.lc;
+  const int64_t total = a.ncells * per;
+  for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t c = t / per;
+    const int rem = int(t - c * per);
+    const int i = rem / a.lc, j = rem - (rem / a.lc) * a.lc;
+    const int e = a.entry[rem];
+    uint64_t key = a.sentinel;
+    int32_t val = 0;
+    if (e >= 0) {
+      int64_t gi = a.faces[a.row_src[i]][c];
+      int64_t gj = a.faces[a.col_src[j]][c];
+      if (a.rmaps[i]) gi = a.rmaps[i][gi];
+      if (a.cmaps[j]) gj = a.cmaps[j][gj];
+      if (gi >= 0 && gj >= 0) {
+        key = uint64_t(gi + a.row_off[i]) * uint64_t(a.ncols) + uint64_t(gj + a.col_off[j]);
+        val = int32_t(int64_t(e) * a.ncells + c);
+      }
+    }
+    a.keys[t] = key;
+    a.vals[t] = val;
+  }
+}
+
+__global__ void plan_diag_keys_kernel(KeyArgs a, const int32_t* diag_entry) {
+  const int64_t total = a.ncells * a.lr;
+  for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t c = t / a.lr;
+    const int i = int(t - c * a.lr);
+    int64_t gi = a.faces[a.row_src[i]][c];
+    if (a.rmaps[i]) gi = a.rmaps[i][gi];
+    uint64_t key = a.sentinel;
+    int32_t val = 0;
+    if (gi >= 0) {
+      key = uint64_t(gi + a.row_off[i]);
+      val = int32_t(int64_t(diag_entry[i]) * a.ncells + c);
+    }
+    a.keys[t] = key;
+    a.vals[t] = val;
+  }
+}
+
+// ptr[r] = first position p in sorted keys with key[p] >= r * stride, r in [0, nrows].
+__global__ void lower_bound_rows_kernel(const uint64_t* keys, int64_t nkeys, int64_t nrows, uint64_t stride,
+                                        int32_t* ptr) {
+  for (int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; r <= nrows; r += int64_t(gridDim.x) * blockDim.x) {
+    const uint64_t target = uint64_t(r) * stride;
+    int64_t lo = 0, hi = nkeys;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (keys[mid] < target)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    ptr[r] = int32_t(lo);
+  }
+}
+
+__global__ void col_from_key_kernel(const uint64_t* ukeys, int64_t n, uint64_t ncols, int32_t* col) {
+  for (int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; s < n; s += int64_t(gridDim.x) * blockDim.x)
+    col[s] = int32_t(ukeys[s] % ncols);
+}
+
+static int grid_for(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  return int(std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32)));
+}
+
+static int bits_needed(uint64_t v) {
+  int b = 1;
+  while (b < 64 && (v >> b)) ++b;
+  return b;
+}
+
+// Global block sizes and offsets for a layout under a boundary condition.
+static std::vector<int64_t> block_offsets(const fq_mesh* m, const Layout& lay, int bc, int64_t* total) {
+  std::vector<int64_t> off;
+  int64_t acc = 0;
+  for (int b = 0; b < lay.nblocks; ++b) {
+    off.push_back(acc);
+    const int g = lay.block_grade[b];
+    int64_t sz = 0;
+    if (g >= 0 && g <= m->dim) sz = bc == FQ_RELATIVE ? m->ninterior[g] : m->nsimp[g];
+    acc += sz;
+  }
+  *total = acc;
+  return off;
+}
+
+fq_status build_plan(fq_ctx* ctx, fq_mesh* m, Plan& plan, const Layout& lay) {
+  cudaStream_t st = ctx->stream;
+  const int64_t nc = m->ncells;
+  // Row / column spaces. Column blocks follow the column grades.
+  Layout colview = lay;
+  int64_t nrows = 0, ncols = 0;
+  auto roff = block_offsets(m, lay, plan.row_bc, &nrows);
+  // Column blocks: same block structure, own grades (DIF_TEST/TRIAL have one
+  // block each side with different grades).
+  std::vector<int64_t> coff;
+  {
+    std::vector<int> cgrades;
+    // distinct column blocks in order of appearance
+    for (size_t j = 0; j < lay.col_block.size(); ++j) {
+      const int b = lay.col_block[j];
+      if (int(cgrades.size()) <= b) cgrades.resize(b + 1, -99);
+      cgrades[b] = lay.col_grade[j];
+    }
+    int64_t acc = 0;
+    for (size_t b = 0; b < cgrades.size(); ++b) {
+      coff.push_back(acc);
+      const int g = cgrades[b];
+      int64_t sz = 0;
+      if (g >= 0 && g <= m->dim) sz = plan.col_bc == FQ_RELATIVE ? m->ninterior[g] : m->nsimp[g];
+      acc += sz;
+    }
+    ncols = acc;
+  }
+  plan.nrows = nrows;
+  plan.ncols = ncols;
+  plan.nent = lay.nent;
+  const int lr = lay.nrow_local, lc = lay.ncol_local;
+
+  // small device tables
+  std::vector<const int32_t*> faces;
+  std::vector<const int32_t*> rmaps(lr), cmaps(lc);
+  std::vector<int32_t> row_src(lr), col_src(lc);
+  std::vector<int64_t> row_off(lr), col_off(lc);
+  for (int i = 0; i < lr; ++i) {
+    const int g = lay.row_grade[i];
+    row_src[i] = int32_t(faces.size());
+    faces.push_back(m->cell_faces[g].as<int32_t>() + int64_t(lay.row_face[i]) * nc);
+    rmaps[i] = plan.row_bc == FQ_RELATIVE ? m->interior_dev[g].as<int32_t>() : nullptr;
+    row_off[i] = roff[lay.row_block[i]];
+  }
+  for (int j = 0; j < lc; ++j) {
+    const int g = lay.col_grade[j];
+    col_src[j] = int32_t(faces.size());
+    faces.push_back(m->cell_faces[g].as<int32_t>() + int64_t(lay.col_face[j]) * nc);
+    cmaps[j] = plan.col_bc == FQ_RELATIVE ? m->interior_dev[g].as<int32_t>() : nullptr;
+    col_off[j] = coff[lay.col_block[j]];
+  }
+  // pack tables into one device buffer
+  std::vector<char> blob;
+  auto put = [&](const void* src, size_t bytes) {
+    size_t o = (blob.size() + 15) & ~size_t(15);
+    blob.resize(o + bytes);
+    memcpy(blob.data() + o, src, bytes);
+    return o;
+  };
+  std::vector<int32_t> entry32(lay.entry.begin(), lay.entry.end());
+  std::vector<int32_t> diag32(lay.diag_entry.begin(), lay.diag_entry.end());
+  const size_t o_entry = put(entry32.data(), entry32.size() * 4 + 4);
+  const size_t o_rsrc = put(row_src.data(), row_src.size() * 4 + 4);
+  const size_t o_csrc = put(col_src.data(), col_src.size() * 4 + 4);
+  const size_t o_roff = put(row_off.data(), row_off.size() * 8 + 8);
+  const size_t o_coff = put(col_off.data(), col_off.size() * 8 + 8);
+  const size_t o_faces = put(faces.data(), faces.size() * sizeof(void*) + 8);
+  const size_t o_rmaps = put(rmaps.data(), rmaps.size() * sizeof(void*) + 8);
+  const size_t o_cmaps = put(cmaps.data(), cmaps.size() * sizeof(void*) + 8);
+  const size_t o_diag = put(diag32.data(), diag32.size() * 4 + 4);
+  DevBuf tables;
+  FQ_TRY(tables.alloc(ctx, blob.size()));
+  FQ_CUDA(ctx, cudaMemcpyAsync(tables.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, st));
+  char* tb = tables.as<char>();
+
+  KeyArgs ka;
+  ka.ncells = nc;
+  ka.lr = lr;
+  ka.lc = lc;
+  ka.entry = reinterpret_cast<const int32_t*>(tb + o_entry);
+  ka.row_src = reinterpret_cast<const int32_t*>(tb + o_rsrc);
+  ka.col_src = reinterpret_cast<const int32_t*>(tb + o_csrc);
+  ka.row_off = reinterpret_cast<const int64_t*>(tb + o_roff);
+  ka.col_off = reinterpret_cast<const int64_t*>(tb + o_coff);
+  ka.faces = reinterpret_cast<const int32_t* const*>(tb + o_faces);
+  ka.rmaps = reinterpret_cast<const int32_t* const*>(tb + o_rmaps);
+  ka.cmaps = reinterpret_cast<const int32_t* const*>(tb + o_cmaps);
+  ka.ncols = std::max<int64_t>(ncols, 1);
+  ka.sentinel = uint64_t(std::max<int64_t>(nrows, 1)) * uint64_t(std::max<int64_t>(ncols, 1));
+  const int end_bit = bits_needed(ka.sentinel);
+
+  const int64_t total = nc * int64_t(lr) * lc;
+  if (total >= (int64_t(1) << 31) || int64_t(lay.nent) * nc >= (int64_t(1) << 31))
+    return set_error(ctx, FQ_UNSUPPORTED, "mesh too large for 32-bit scatter indices");
+  DevBuf keys, keys2, vals, vals2;
+  FQ_TRY(keys.alloc(ctx, std::max<int64_t>(total, 1) * 8));
+  FQ_TRY(keys2.alloc(ctx, std::max<int64_t>(total, 1) * 8));
+  FQ_TRY(vals.alloc(ctx, std::max<int64_t>(total, 1) * 4));
+  FQ_TRY(vals2.alloc(ctx, std::max<int64_t>(total, 1) * 4));
+  if (total > 0) {
+    ka.keys = keys.as<uint64_t>();
+    ka.vals = vals.as<int32_t>();
+    plan_keys_kernel<<<grid_for(total, 256), 256, 0, st>>>(ka);
+    ctx->launches++;
+    size_t tmp_bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.as<uint64_t>(), keys2.as<uint64_t>(),
+                                    vals.as<int32_t>(), vals2.as<int32_t>(), int(total), 0, end_bit, st);
+    DevBuf tmp;
+    FQ_TRY(tmp.alloc(ctx, std::max<size_t>(tmp_bytes, 16)));
+    FQ_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.as<uint64_t>(), keys2.as<uint64_t>(),
+                                                 vals.as<int32_t>(), vals2.as<int32_t>(), int(total), 0,
+                                                 end_bit, st));
+  }
+  // run-length encode the sorted keys -> unique keys and counts
+  DevBuf ukeys, counts, nruns;
+  FQ_TRY(ukeys.alloc(ctx, std::max<int64_t>(total, 1) * 8));
+  FQ_TRY(counts.alloc(ctx, (std::max<int64_t>(total, 1) + 1) * 4));
+  FQ_TRY(nruns.alloc(ctx, 8));
+  int64_t nruns_h = 0;
+  if (total > 0) {
+    size_t tmp_bytes = 0;
+    cub::DeviceRunLengthEncode::Encode(nullptr, tmp_bytes, keys2.as<uint64_t>(), ukeys.as<uint64_t>(),
+                                       counts.as<int32_t>(), nruns.as<int32_t>(), int(total), st);
+    DevBuf tmp;
+    FQ_TRY(tmp.alloc(ctx, std::max<size_t>(tmp_bytes, 16)));
+    FQ_CUDA(ctx, cub::DeviceRunLengthEncode::Encode(tmp.p, tmp_bytes, keys2.as<uint64_t>(), ukeys.as<uint64_t>(),
+                                                    counts.as<int32_t>(), nruns.as<int32_t>(), int(total), st));
+    int32_t nr = 0;
+    FQ_CUDA(ctx, cudaMemcpyAsync(&nr, nruns.p, 4, cudaMemcpyDeviceToHost, st));
+    FQ_CUDA(ctx, cudaStreamSynchronize(st));
+    nruns_h = nr;
+    uint64_t lastkey = 0;
+    if (nruns_h > 0) {
+      FQ_CUDA(ctx, cudaMemcpyAsync(&lastkey, ukeys.as<uint64_t>() + (nruns_h - 1), 8, cudaMemcpyDeviceToHost, st));
+      FQ_CUDA(ctx, cudaStreamSynchronize(st));
+      if (lastkey == ka.sentinel) --nruns_h;
+    }
+  }
+  plan.nslots = nruns_h;
+  FQ_TRY(plan.slot_ptr.alloc(ctx, (nruns_h + 1) * 4));
+  FQ_TRY(plan.col_idx.alloc(ctx, std::max<int64_t>(nruns_h, 1) * 4));
+  FQ_TRY(plan.row_ptr.alloc(ctx, (nrows + 1) * 4));
+  FQ_CUDA(ctx, cudaMemsetAsync(plan.slot_ptr.p, 0, 4, st));
+  if (nruns_h > 0) {
+    size_t tmp_bytes = 0;
+    cub::DeviceScan::InclusiveSum(nullptr, tmp_bytes, counts.as<int32_t>(), plan.slot_ptr.as<int32_t>() + 1,
+                                  int(nruns_h), st);
+    DevBuf tmp;
+    FQ_TRY(tmp.alloc(ctx, std::max<size_t>(tmp_bytes, 16)));
+    FQ_CUDA(ctx, cub::DeviceScan::InclusiveSum(tmp.p, tmp_bytes, counts.as<int32_t>(),
+                                               plan.slot_ptr.as<int32_t>() + 1, int(nruns_h), st));
+    col_from_key_kernel<<<grid_for(nruns_h, 256), 256, 0, st>>>(ukeys.as<uint64_t>(), nruns_h, ka.ncols,
+                                                                plan.col_idx.as<int32_t>());
+    ctx->launches++;
+  }
+  lower_bound_rows_kernel<<<grid_for(nrows + 1, 256), 256, 0, st>>>(ukeys.as<uint64_t>(), nruns_h, nrows,
+                                                                     uint64_t(ka.ncols), plan.row_ptr.as<int32_t>());
+  ctx->launches++;
+  int32_t ntrip = 0;
+  FQ_CUDA(ctx, cudaMemcpyAsync(&ntrip, plan.slot_ptr.as<int32_t>() + nruns_h, 4, cudaMemcpyDeviceToHost, st));
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  plan.ntrip = ntrip;
+  FQ_TRY(plan.perm.alloc(ctx, std::max<int64_t>(ntrip, 1) * 4));
+  if (ntrip > 0)
+    FQ_CUDA(ctx, cudaMemcpyAsync(plan.perm.p, vals2.p, size_t(ntrip) * 4, cudaMemcpyDeviceToDevice, st));
+
+  // diagonal plan (preconditioner of the mixed system)
+  if (!lay.diag_entry.empty()) {
+    const int64_t dtotal = nc * lr;
+    ka.sentinel = uint64_t(std::max<int64_t>(nrows, 1));
+    ka.keys = keys.as<uint64_t>();
+    ka.vals = vals.as<int32_t>();
+    plan_diag_keys_kernel<<<grid_for(dtotal, 256), 256, 0, st>>>(ka, reinterpret_cast<const int32_t*>(tb + o_diag));
+    ctx->launches++;
+    size_t tmp_bytes = 0;
+    const int dbits = bits_needed(ka.sentinel);
+    cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.as<uint64_t>(), keys2.as<uint64_t>(),
+                                    vals.as<int32_t>(), vals2.as<int32_t>(), int(dtotal), 0, dbits, st);
+    DevBuf tmp;
+    FQ_TRY(tmp.alloc(ctx, std::max<size_t>(tmp_bytes, 16)));
+    FQ_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.as<uint64_t>(), keys2.as<uint64_t>(),
+                                                 vals.as<int32_t>(), vals2.as<int32_t>(), int(dtotal), 0, dbits,
+                                                 st));
+    FQ_TRY(plan.diag_ptr.alloc(ctx, (nrows + 1) * 4));
+    lower_bound_rows_kernel<<<grid_for(nrows + 1, 256), 256, 0, st>>>(keys2.as<uint64_t>(), dtotal, nrows, 1,
+                                                                       plan.diag_ptr.as<int32_t>());
+    ctx->launches++;
+    int32_t nd = 0;
+    FQ_CUDA(ctx, cudaMemcpyAsync(&nd, plan.diag_ptr.as<int32_t>() + nrows, 4, cudaMemcpyDeviceToHost, st));
+    FQ_CUDA(ctx, cudaStreamSynchronize(st));
+    plan.ndiag_trip = nd;
+    FQ_TRY(plan.diag_perm.alloc(ctx, std::max<int64_t>(nd, 1) * 4));
+    if (nd > 0)
+      FQ_CUDA(ctx, cudaMemcpyAsync(plan.diag_perm.p, vals2.p, size_t(nd) * 4, cudaMemcpyDeviceToDevice, st));
+  }
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  FQ_CUDA(ctx, cudaGetLastError());
+  return FQ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Hot loop: scatter
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) scatter_kernel(const int32_t* __restrict__ slot_ptr,
+                                                      const int32_t* __restrict__ perm, const T* __restrict__ elem,
+                                                      T* __restrict__ values, uint8_t* __restrict__ zflag,
+                                                      int* zero_count, int64_t nslots) {
+  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= nslots) return;
+  const int b = __ldg(slot_ptr + s), e = __ldg(slot_ptr + s + 1);
+  T acc = T(0);
+  bool nz = false;
+  for (int t = b; t < e; ++t) {
+    const T v = __ldg(elem + __ldg(perm + t));
+    acc += v;
+    nz |= (v != T(0));
+  }
+  values[s] = acc;
+  zflag[s] = nz ? 0 : 1;
+  if (!nz) atomicAdd(zero_count, 1);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) scatter_diag_kernel(const int32_t* __restrict__ ptr,
+                                                           const int32_t* __restrict__ perm,
+                                                           const T* __restrict__ elem, double* __restrict__ out,
+                                                           int64_t n) {
+  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int b = __ldg(ptr + s), e = __ldg(ptr + s + 1);
+  T acc = T(0);
+  for (int t = b; t < e; ++t) acc += __ldg(elem + __ldg(perm + t));
+  out[s] = double(acc);
+}
+
+void launch_scatter(const Plan& plan, const void* elem, void* values, uint8_t* zero_flags, int* zero_count,
+                    int fp32, cudaStream_t st) {
+  if (plan.nslots == 0) return;
+  const int threads = 256;
+  const unsigned blocks = unsigned((plan.nslots + threads - 1) / threads);
+  if (fp32)
+    scatter_kernel<float><<<blocks, threads, 0, st>>>(plan.slot_ptr.as<int32_t>(), plan.perm.as<int32_t>(),
+                                                      static_cast<const float*>(elem), static_cast<float*>(values),
+                                                      zero_flags, zero_count, plan.nslots);
+  else
+    scatter_kernel<double><<<blocks, threads, 0, st>>>(plan.slot_ptr.as<int32_t>(), plan.perm.as<int32_t>(),
+                                                       static_cast<const double*>(elem),
+                                                       static_cast<double*>(values), zero_flags, zero_count,
+                                                       plan.nslots);
+}
+
+void launch_scatter_diag(const Plan& plan, const void* elem, double* out, int fp32, cudaStream_t st) {
+  if (plan.nrows == 0) return;
+  const int threads = 256;
+  const unsigned blocks = unsigned((plan.nrows + threads - 1) / threads);
+  if (fp32)
+    scatter_diag_kernel<float><<<blocks, threads, 0, st>>>(plan.diag_ptr.as<int32_t>(), plan.diag_perm.as<int32_t>(),
+                                                           static_cast<const float*>(elem), out, plan.nrows);
+  else
+    scatter_diag_kernel<double><<<blocks, threads, 0, st>>>(plan.diag_ptr.as<int32_t>(),
+                                                            plan.diag_perm.as<int32_t>(),
+                                                            static_cast<const double*>(elem), out, plan.nrows);
+}
+
+// ---------------------------------------------------------------------------
+// Compaction of exact-zero slots (rare: unjittered meshes only)
+// ---------------------------------------------------------------------------
+__global__ void keep_kernel(const uint8_t* zflag, int64_t n, int32_t* keep) {
+  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s < n) keep[s] = zflag[s] ? 0 : 1;
+  if (s == n) keep[s] = 0;
+}
+
+template <typename T>
+__global__ void compact_kernel(const int32_t* pos, const uint8_t* zflag, const int32_t* col, const T* val,
+                               int64_t n, int32_t* ncol, T* nval) {
+  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= n || zflag[s]) return;
+  ncol[pos[s]] = col[s];
+  nval[pos[s]] = val[s];
+}
+
+__global__ void compact_rows_kernel(const int32_t* pos, const int32_t* row_ptr, int64_t nrows, int32_t* nrow_ptr) {
+  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r <= nrows) nrow_ptr[r] = pos[row_ptr[r]];
+}
+
+fq_status compact_csr(fq_ctx* ctx, fq_matrix* m, int64_t nzero) {
+  cudaStream_t st = ctx->stream;
+  const Plan& p = *m->plan;
+  const int64_t n = p.nslots;
+  const size_t w = m->precision == FQ_FP32 ? 4 : 8;
+  DevBuf keep, pos;
+  FQ_TRY(keep.alloc(ctx, (n + 1) * 4));
+  FQ_TRY(pos.alloc(ctx, (n + 1) * 4));
+  keep_kernel<<<unsigned((n + 256) / 256), 256, 0, st>>>(m->zero_flags.as<uint8_t>(), n, keep.as<int32_t>());
+  size_t tmp_bytes = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, keep.as<int32_t>(), pos.as<int32_t>(), int(n + 1), st);
+  DevBuf tmp;
+  FQ_TRY(tmp.alloc(ctx, std::max<size_t>(tmp_bytes, 16)));
+  FQ_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp.p, tmp_bytes, keep.as<int32_t>(), pos.as<int32_t>(), int(n + 1), st));
+  const int64_t nnz = n - nzero;
+  if (m->col_idx.bytes < size_t(std::max<int64_t>(nnz, 1)) * 4) FQ_TRY(m->col_idx.alloc(ctx, std::max<int64_t>(nnz, 1) * 4));
+  if (m->row_ptr.bytes < size_t(p.nrows + 1) * 4) FQ_TRY(m->row_ptr.alloc(ctx, (p.nrows + 1) * 4));
+  if (m->values.bytes < size_t(std::max<int64_t>(nnz, 1)) * w) FQ_TRY(m->values.alloc(ctx, std::max<int64_t>(nnz, 1) * w));
+  if (w == 4)
+    compact_kernel<float><<<unsigned((n + 255) / 256), 256, 0, st>>>(
+        pos.as<int32_t>(), m->zero_flags.as<uint8_t>(), p.col_idx.as<int32_t>(), m->full_values.as<float>(), n,
+        m->col_idx.as<int32_t>(), m->values.as<float>());
+  else
+    compact_kernel<double><<<unsigned((n + 255) / 256), 256, 0, st>>>(
+        pos.as<int32_t>(), m->zero_flags.as<uint8_t>(), p.col_idx.as<int32_t>(), m->full_values.as<double>(), n,
+        m->col_idx.as<int32_t>(), m->values.as<double>());
+  compact_rows_kernel<<<unsigned((p.nrows + 256) / 256), 256, 0, st>>>(pos.as<int32_t>(), p.row_ptr.as<int32_t>(),
+                                                                      p.nrows, m->row_ptr.as<int32_t>());
+  ctx->launches += 3;
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  m->nnz = nnz;
+  m->rp = m->row_ptr.as<int32_t>();
+  m->ci = m->col_idx.as<int32_t>();
+  m->compacted = true;
+  return FQ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Element pass and assembly driver
+// ---------------------------------------------------------------------------
+int launch_element(int n, int grade, int kind, int fp32, const ElemArgs& a, cudaStream_t st) {
+  switch (n) {
+    case 0:
+      return launch_element_dim<0>(grade, kind, fp32, a, st);
+    case 1:
+      return launch_element_dim<1>(grade, kind, fp32, a, st);
+    case 2:
+      return launch_element_dim<2>(grade, kind, fp32, a, st);
+    case 3:
+      return launch_element_dim<3>(grade, kind, fp32, a, st);
+    case 4:
+      return launch_element_dim<4>(grade, kind, fp32, a, st);
+    default:
+      return -1;
+  }
+}
+
+fq_status element_pass(fq_ctx* ctx, fq_mesh* m, int kind, int grade, int fp32, double param, DevBuf& buf,
+                       int nent) {
+  if (!m->has_lengths) return set_error(ctx, FQ_INVALID_ARG, "mesh has no edge lengths");
+  const size_t need = size_t(std::max(nent, 1)) * size_t(std::max<int64_t>(m->ncells, 1)) * (fp32 ? 4 : 8);
+  if (buf.bytes < need) FQ_TRY(buf.alloc(ctx, need));
+  ElemArgs a;
+  a.ncells = m->ncells;
+  a.lengths = m->lengths.as<double>();
+  a.cell_edges = m->dim >= 1 ? m->cell_faces[1].as<int32_t>() : nullptr;
+  a.out = buf.p;
+  a.ginv_out = a.det_out = a.vol_out = nullptr;
+  a.param = param;
+  a.status = ctx->status.as<int>();
+  if (launch_element(m->dim, grade, kind, fp32, a, ctx->stream) != 0)
+    return set_error(ctx, FQ_UNSUPPORTED, "no element program for this dimension/grade");
+  ctx->launches++;
+  FQ_CUDA(ctx, cudaGetLastError());
+  return FQ_OK;
+}
+
+fq_status get_plan(fq_ctx* ctx, fq_mesh* m, int kind, int grade, int row_bc, int col_bc, Plan** out) {
+  auto key = std::make_tuple(kind, grade, row_bc, col_bc);
+  auto it = m->plans.find(key);
+  if (it != m->plans.end()) {
+    *out = it->second.get();
+    return FQ_OK;
+  }
+  auto plan = std::make_unique<Plan>();
+  plan->kind = kind;
+  plan->grade = grade;
+  plan->row_bc = row_bc;
+  plan->col_bc = col_bc;
+  Layout lay = make_layout(m->dim, kind, grade);
+  FQ_TRY(build_plan(ctx, m, *plan, lay));
+  *out = plan.get();
+  m->plans[key] = std::move(plan);
+  return FQ_OK;
+}
+
+// Element pass + scatter (+ compaction when needed) into m.
+fq_status assemble_into(fq_ctx* ctx, fq_matrix* m) {
+  fq_mesh* mesh = m->mesh;
+  Plan& p = *m->plan;
+  const int fp32 = m->precision == FQ_FP32;
+  const size_t w = fp32 ? 4 : 8;
+  if (m->full_values.bytes < size_t(std::max<int64_t>(p.nslots, 1)) * w)
+    FQ_TRY(m->full_values.alloc(ctx, std::max<int64_t>(p.nslots, 1) * w));
+  if (m->zero_flags.bytes < size_t(std::max<int64_t>(p.nslots, 1)))
+    FQ_TRY(m->zero_flags.alloc(ctx, std::max<int64_t>(p.nslots, 1)));
+  int* zc = ctx->status.as<int>() + 1;
+  FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
+  if (p.nslots > 0 || p.ndiag_trip > 0) FQ_TRY(element_pass(ctx, mesh, m->kind, m->grade, fp32, m->param, mesh->elem, p.nent));
+  launch_scatter(p, mesh->elem.p, m->full_values.p, m->zero_flags.as<uint8_t>(), zc, fp32, ctx->stream);
+  if (p.nslots > 0) ctx->launches++;
+  FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
+  const int nzero = ctx->host_status[1];
+  if (nzero > 0) {
+    FQ_TRY(compact_csr(ctx, m, nzero));
+  } else {
+    m->nnz = p.nslots;
+    m->rp = p.row_ptr.as<int32_t>();
+    m->ci = p.col_idx.as<int32_t>();
+    m->compacted = false;
+    // values live in full_values: swap roles to avoid a copy
+    std::swap(m->values, m->full_values);
+  }
+  return FQ_OK;
+}
+
+}  // namespace fq

@@ -1,0 +1,171 @@
+// Host-side internals of the library: context, device buffers, meshes, scatter
+// plans and assembled matrices.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/formoniq_gpu.h"
+#include "fq_kinds.h"
+
+struct fq_ctx;
+
+namespace fq {
+
+// Owned device allocation, charged against the context's HBM budget.
+struct DevBuf {
+  fq_ctx* ctx = nullptr;
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept { *this = std::move(o); }
+  DevBuf& operator=(DevBuf&& o) noexcept;
+  ~DevBuf() { release(); }
+  fq_status alloc(fq_ctx* c, size_t nbytes);
+  void release();
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+// The scatter plan of one element program on one mesh: the CSR pattern and the
+// contributions of every slot, sorted by (row, col) and, within a slot, by cell
+// (the reference's summation order: per-thread triplets concatenated in cell
+// order, galerkin.rs:150-188).
+struct Plan {
+  int kind = 0, grade = 0, row_bc = 0, col_bc = 0;
+  int64_t nrows = 0, ncols = 0;
+  int64_t nslots = 0;   // topological nnz
+  int64_t ntrip = 0;    // contributions
+  int nent = 0;         // element entries per cell of the program
+  DevBuf row_ptr;       // int32 [nrows+1]
+  DevBuf col_idx;       // int32 [nslots]
+  DevBuf slot_ptr;      // int32 [nslots+1]
+  DevBuf perm;          // int32 [ntrip]: element buffer index entry*ncells + cell
+  // Diagonal plan (EK_KKT preconditioner): slots = rows.
+  int64_t ndiag_trip = 0;
+  DevBuf diag_ptr;      // int32 [nrows+1]
+  DevBuf diag_perm;     // int32 [ndiag_trip]
+};
+
+// Local degree-of-freedom layout of an element program (host mirror of the
+// entry numbering in fq_element_kernel.cuh).
+struct Layout {
+  int nrow_local = 0, ncol_local = 0;
+  std::vector<int> row_grade, row_face, row_block;  // per local row
+  std::vector<int> col_grade, col_face, col_block;
+  std::vector<int> entry;  // [nrow_local * ncol_local], -1 = structurally zero
+  int nent = 0;            // entries written per cell
+  std::vector<int> diag_entry;  // EK_KKT: preconditioner diagonal entry per local dof
+  int nblocks = 0;
+  std::vector<int> block_grade;  // grade of each block
+};
+Layout make_layout(int n, int kind, int grade);
+
+}  // namespace fq
+
+struct fq_mesh {
+  fq_ctx* ctx = nullptr;
+  int dim = 0;
+  int64_t ncells = 0;
+  int64_t nsimp[6] = {0, 0, 0, 0, 0, 0};
+  int kuhn_nbox = 0;  // > 0 when made by fq_mesh_kuhn_cube
+  // host topology
+  std::vector<int32_t> skel[5];        // colex skeletons [N_k][k+1]
+  std::vector<uint8_t> boundary[5];    // per simplex: on the boundary subcomplex
+  std::vector<int32_t> interior_map[5];  // kidx -> relative index or -1
+  int64_t ninterior[5] = {0, 0, 0, 0, 0};
+  std::vector<int8_t> orientation;     // lazily computed
+  std::vector<int32_t> cell_faces_host[5];  // cell-major [ncells][C(n+1,k+1)]
+  // device topology: cell -> face kidx, entry-major [C(n+1,k+1)][ncells]
+  fq::DevBuf cell_faces[5];
+  fq::DevBuf interior_dev[5];  // int32 relative map
+  // geometry
+  fq::DevBuf lengths;  // double [N_1]
+  bool has_lengths = false;
+  // cached scatter plans
+  std::map<std::tuple<int, int, int, int>, std::unique_ptr<fq::Plan>> plans;
+  // element buffer reused across assemblies
+  fq::DevBuf elem;
+};
+
+struct fq_matrix {
+  fq_ctx* ctx = nullptr;
+  fq_mesh* mesh = nullptr;
+  fq::Plan* plan = nullptr;  // owned by the mesh; null for coboundaries
+  int kind = 0, grade = 0, bc = 0, precision = 0;
+  double param = 0.0;
+  int64_t nrows = 0, ncols = 0, nnz = 0;
+  bool compacted = false;  // some topological slot summed exact zeros only
+  const int32_t* rp = nullptr;  // row_ptr in use (plan's or own)
+  const int32_t* ci = nullptr;  // col_idx in use
+  fq::DevBuf row_ptr, col_idx, values;
+  // topological-pattern values and flags before compaction
+  fq::DevBuf full_values, zero_flags;
+};
+
+struct fq_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool owns_stream = false;
+  uint64_t budget = 0;
+  uint64_t in_use = 0;
+  uint64_t launches = 0;
+  std::string last_error;
+  fq::DevBuf status;       // int [8] device status words
+  int* host_status = nullptr;  // pinned mirror
+  fq::DevBuf scratch;      // reusable temporary storage
+};
+
+namespace fq {
+
+fq_status set_error(fq_ctx* ctx, fq_status s, const std::string& msg);
+fq_status cuda_check(fq_ctx* ctx, cudaError_t e, const char* what);
+#define FQ_CUDA(ctx, call)                                        \
+  do {                                                            \
+    cudaError_t _e = (call);                                      \
+    if (_e != cudaSuccess) return ::fq::cuda_check(ctx, _e, #call); \
+  } while (0)
+#define FQ_TRY(expr)                  \
+  do {                                \
+    fq_status _s = (expr);            \
+    if (_s != FQ_OK) return _s;       \
+  } while (0)
+
+// ---- device entry points (implemented in .cu files) ----
+struct ElemArgs;
+int launch_element(int n, int grade, int kind, int fp32, const ElemArgs& a, cudaStream_t st);
+
+// Build the scatter plan on the device (sort with CUB).
+fq_status build_plan(fq_ctx* ctx, fq_mesh* mesh, Plan& plan, const Layout& lay);
+
+// values[s] = sum of elem[perm[t]] over the slot's contributions; zero_flags[s]
+// = 1 when every contribution was exactly 0.0; *zero_count += count.
+void launch_scatter(const Plan& plan, const void* elem, void* values, uint8_t* zero_flags, int* zero_count,
+                    int fp32, cudaStream_t st);
+void launch_scatter_diag(const Plan& plan, const void* elem, double* out, int fp32, cudaStream_t st);
+
+// Compaction: drop slots whose flag is set.
+fq_status compact_csr(fq_ctx* ctx, fq_matrix* m, int64_t nzero);
+
+fq_status element_pass(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int fp32, double param, DevBuf& buf,
+                       int nent);
+fq_status get_plan(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int row_bc, int col_bc, Plan** out);
+fq_status assemble_into(fq_ctx* ctx, fq_matrix* m);
+fq_status make_matrix(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int bc, int precision, double param,
+                      fq_matrix** out);
+
+// SpMV and vector kernels
+void launch_spmv(const fq_matrix* a, const void* x, void* y, cudaStream_t st);
+fq_status dev_alloc(fq_ctx* ctx, DevBuf& b, size_t bytes);
+
+}  // namespace fq

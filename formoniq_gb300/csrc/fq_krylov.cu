@@ -1,0 +1,690 @@
+// Kernel (d): the operator apply and the Krylov solvers, device resident.
+//
+// krylov::minres (iterative/src/krylov.rs:113-211) and krylov::cg (:48-95) are
+// restated with their recurrences unchanged; only the data movement is new.
+// Each iteration is three kernels:
+//   A: the SpMV, fused with the Lanczos/CG vector update that consumes it,
+//      and a per-block partial of the first inner product;
+//   B: the remaining vector updates, the diagonal preconditioner, and the
+//      partials of the second inner product;
+//   C: the scalar recurrence (Givens rotation / step lengths), recomputed
+//      identically by every block from the partials, and the solution update.
+// Inner products are reduced in two fixed-order levels (block partials, then a
+// per-block re-reduction of all partials), so results are deterministic and no
+// scalar ever travels to the host inside the loop. The scalar state lives in
+// two device slots written alternately, so a block never reads a slot that
+// another block of the same kernel writes. The host only polls for convergence
+// every few iterations.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <vector>
+
+#include "fq_internal.h"
+
+namespace fq {
+
+constexpr int KT = 256;          // threads per block of the vector kernels
+constexpr int KBLOCKS = 152 * 4; // grid of the vector kernels: 4 blocks per SM
+
+struct SolverState {
+  double beta1, beta, oldb, dbar, epsln, phibar, cs, sn;  // MINRES
+  double alfa;
+  double rz, bnorm;                                       // CG
+  double residual;
+  long long iters;
+  int done, converged, breakdown, pad;
+};
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = (l < int(blockDim.x >> 5)) ? sh[l] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    if (l == 0) sh[0] = r;
+  }
+  __syncthreads();
+  r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// Every block reduces the same partial array in the same order.
+__device__ __forceinline__ double reduce_partials(const double* part, int np, double* sh) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) v += part[i];
+  return block_sum(v, sh);
+}
+
+// Sub-warp CSR row product: W lanes per row, fixed lane order.
+template <int W, typename VT>
+__device__ __forceinline__ VT row_dot(const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                      const VT* __restrict__ val, const VT* __restrict__ x, int64_t row, bool valid,
+                                      int lane) {
+  VT acc = VT(0);
+  if (valid) {
+    const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
+    for (int t = b + lane; t < e; t += W) acc += __ldg(val + t) * __ldg(x + __ldg(ci + t));
+  }
+#pragma unroll
+  for (int o = W / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, W);
+  return acc;
+}
+
+// ---------------------------------------------------------------------------
+// plain SpMV (LinearOperator::apply)
+// ---------------------------------------------------------------------------
+template <int W, typename VT>
+__global__ void __launch_bounds__(KT) spmv_kernel(const int32_t* rp, const int32_t* ci, const VT* val, const VT* x,
+                                                  VT* y, int64_t nrows) {
+  const int lane = threadIdx.x % W;
+  const int64_t rows_per_grid = int64_t(gridDim.x) * (blockDim.x / W);
+  for (int64_t base = int64_t(blockIdx.x) * (blockDim.x / W); base < nrows; base += rows_per_grid) {
+    const int64_t row = base + threadIdx.x / W;
+    const bool valid = row < nrows;
+    const VT acc = row_dot<W, VT>(rp, ci, val, x, row, valid, lane);
+    if (valid && lane == 0) y[row] = acc;
+  }
+}
+
+template <typename VT>
+static int pick_w(int64_t nnz, int64_t nrows) {
+  const double avg = nrows > 0 ? double(nnz) / double(nrows) : 0.0;
+  if (avg <= 6) return 4;
+  if (avg <= 14) return 8;
+  if (avg <= 40) return 16;
+  return 32;
+}
+
+static int spmv_blocks(int64_t nrows, int W) {
+  const int64_t rows_per_block = KT / W;
+  return int(std::max<int64_t>(1, std::min<int64_t>((nrows + rows_per_block - 1) / rows_per_block, 152 * 16)));
+}
+
+template <typename VT>
+static void spmv_dispatch(const int32_t* rp, const int32_t* ci, const VT* val, const VT* x, VT* y, int64_t nrows,
+                          int64_t nnz, cudaStream_t st) {
+  const int W = pick_w<VT>(nnz, nrows);
+  const int g = spmv_blocks(nrows, W);
+  switch (W) {
+    case 4:
+      spmv_kernel<4, VT><<<g, KT, 0, st>>>(rp, ci, val, x, y, nrows);
+      break;
+    case 8:
+      spmv_kernel<8, VT><<<g, KT, 0, st>>>(rp, ci, val, x, y, nrows);
+      break;
+    case 16:
+      spmv_kernel<16, VT><<<g, KT, 0, st>>>(rp, ci, val, x, y, nrows);
+      break;
+    default:
+      spmv_kernel<32, VT><<<g, KT, 0, st>>>(rp, ci, val, x, y, nrows);
+      break;
+  }
+}
+
+void launch_spmv(const fq_matrix* a, const void* x, void* y, cudaStream_t st) {
+  if (a->nrows == 0) return;
+  if (a->precision == FQ_FP32)
+    spmv_dispatch<float>(a->rp, a->ci, a->values.as<float>(), static_cast<const float*>(x), static_cast<float*>(y),
+                         a->nrows, a->nnz, st);
+  else
+    spmv_dispatch<double>(a->rp, a->ci, a->values.as<double>(), static_cast<const double*>(x),
+                          static_cast<double*>(y), a->nrows, a->nnz, st);
+}
+
+// ---------------------------------------------------------------------------
+// MINRES
+// ---------------------------------------------------------------------------
+template <typename VT>
+struct MinresVecs {
+  VT *x, *r1, *r2, *y, *v, *z, *w, *w2;
+  const VT* dinv;  // may be null: identity preconditioner
+  const VT* b;
+  double *partA, *partB;
+};
+
+template <typename VT>
+__global__ void __launch_bounds__(KT) minres_init(MinresVecs<VT> m, int64_t n) {
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const VT bi = m.b[i];
+    const VT yi = m.dinv ? bi * m.dinv[i] : bi;
+    m.r1[i] = bi;
+    m.r2[i] = bi;
+    m.y[i] = yi;
+    m.x[i] = VT(0);
+    m.w[i] = VT(0);
+    m.w2[i] = VT(0);
+    acc += double(bi) * double(yi);
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) m.partB[blockIdx.x] = acc;
+}
+
+__global__ void minres_init_state(SolverState* s0, SolverState* s1, const double* partB, int np, double rtol,
+                                  long long max_iters) {
+  __shared__ double sh[32];
+  const double beta1_sq = reduce_partials(partB, np, sh);
+  if (threadIdx.x == 0) {
+    SolverState s{};
+    s.iters = 0;
+    if (!(beta1_sq > 0.0)) {
+      // b = 0 (trivial solve) or a non-positive preconditioner product.
+      s.done = 1;
+      s.converged = beta1_sq == 0.0 ? 1 : 0;
+      s.breakdown = beta1_sq == 0.0 ? 0 : 1;
+      s.residual = 0.0;
+    } else {
+      const double beta1 = sqrt(beta1_sq);
+      s.beta1 = beta1;
+      s.beta = beta1;
+      s.oldb = 0.0;
+      s.dbar = 0.0;
+      s.epsln = 0.0;
+      s.phibar = beta1;
+      s.cs = -1.0;
+      s.sn = 0.0;
+      s.residual = 1.0;
+      s.done = max_iters <= 0 ? 1 : 0;
+    }
+    (void)rtol;
+    *s0 = s;
+    *s1 = s;
+  }
+}
+
+// A: v = y / beta, z = A v - (beta/oldb) r1, partial v.z
+template <int W, typename VT>
+__global__ void __launch_bounds__(KT) minres_a(const int32_t* rp, const int32_t* ci, const VT* val, MinresVecs<VT> m,
+                                               const SolverState* __restrict__ S, int64_t n) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  const double rb = 1.0 / S->beta;
+  const double c1 = S->iters >= 1 ? (-S->beta / S->oldb) : 0.0;
+  const VT rbt = VT(rb), c1t = VT(c1);
+  const int lane = threadIdx.x % W;
+  double acc = 0.0;
+  const int64_t rows_per_grid = int64_t(gridDim.x) * (blockDim.x / W);
+  for (int64_t base = int64_t(blockIdx.x) * (blockDim.x / W); base < n; base += rows_per_grid) {
+    const int64_t row = base + threadIdx.x / W;
+    const bool valid = row < n;
+    const VT av = row_dot<W, VT>(rp, ci, val, m.y, row, valid, lane);
+    if (valid && lane == 0) {
+      const VT vi = m.y[row] * rbt;
+      const VT zi = av * rbt + c1t * m.r1[row];
+      m.v[row] = vi;
+      m.z[row] = zi;
+      acc += double(vi) * double(zi);
+    }
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) m.partA[blockIdx.x] = acc;
+}
+
+// B: alfa; z -= (alfa/beta) r2; r1 = r2; r2 = z; y = P r2; partial r2.y
+template <typename VT>
+__global__ void __launch_bounds__(KT) minres_b(MinresVecs<VT> m, SolverState* __restrict__ S, int npa, int64_t n) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  const double alfa = reduce_partials(m.partA, npa, sh);
+  const VT c2 = VT(-alfa / S->beta);
+  double acc = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const VT r2 = m.r2[i];
+    const VT zi = m.z[i] + c2 * r2;
+    const VT yi = m.dinv ? zi * m.dinv[i] : zi;
+    m.r1[i] = r2;
+    m.r2[i] = zi;
+    m.y[i] = yi;
+    acc += double(zi) * double(yi);
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) m.partB[blockIdx.x] = acc;
+}
+
+// C: rotation (identical in every block), w/x update, state -> the other slot
+template <typename VT>
+__global__ void __launch_bounds__(KT) minres_c(MinresVecs<VT> m, const SolverState* __restrict__ Sin,
+                                               SolverState* __restrict__ Sout, int npa, int npb, double rtol,
+                                               long long max_iters, int64_t n) {
+  __shared__ double sh[32];
+  if (Sin->done) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *Sout = *Sin;
+    return;
+  }
+  const double alfa = reduce_partials(m.partA, npa, sh);
+  const double beta_sq = reduce_partials(m.partB, npb, sh);
+  SolverState s = *Sin;
+  const double eps = DBL_EPSILON;
+  const double oldb = s.beta;
+  const double beta = sqrt(fmax(beta_sq, 0.0));
+  const double oldeps = s.epsln;
+  const double delta = s.cs * s.dbar + s.sn * alfa;
+  const double gbar = s.sn * s.dbar - s.cs * alfa;
+  const double epsln = s.sn * beta;
+  const double dbar = -s.cs * beta;
+  const double gamma = fmax(sqrt(gbar * gbar + beta * beta), eps);
+  const double cs = gbar / gamma;
+  const double sn = beta / gamma;
+  const double phi = cs * s.phibar;
+  const double phibar = s.phibar * sn;
+  const VT ce = VT(-oldeps), cd = VT(-delta), cg = VT(1.0 / gamma), cp = VT(phi);
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const VT w = m.w[i];
+    VT wn = m.v[i] + ce * m.w2[i];
+    wn = wn + cd * w;
+    wn = wn * cg;
+    m.w2[i] = w;
+    m.w[i] = wn;
+    m.x[i] = m.x[i] + cp * wn;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    s.oldb = oldb;
+    s.beta = beta;
+    s.epsln = epsln;
+    s.dbar = dbar;
+    s.cs = cs;
+    s.sn = sn;
+    s.phibar = phibar;
+    s.alfa = alfa;
+    s.iters += 1;
+    s.residual = phibar / s.beta1;
+    if (!isfinite(s.residual)) {
+      s.breakdown = 1;
+      s.done = 1;
+    }
+    if (s.residual <= rtol) {
+      s.converged = 1;
+      s.done = 1;
+    }
+    if (s.iters >= max_iters) s.done = 1;
+    *Sout = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// CG
+// ---------------------------------------------------------------------------
+template <typename VT>
+struct CgVecs {
+  VT *x, *r, *z, *p, *ap;
+  const VT* dinv;
+  const VT* b;
+  double *partA, *partB, *partC;
+};
+
+template <typename VT>
+__global__ void __launch_bounds__(KT) cg_init(CgVecs<VT> c, int64_t n) {
+  __shared__ double sh[32];
+  double rz = 0.0, bb = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const VT bi = c.b[i];
+    const VT zi = c.dinv ? bi * c.dinv[i] : bi;
+    c.x[i] = VT(0);
+    c.r[i] = bi;
+    c.z[i] = zi;
+    c.p[i] = zi;
+    rz += double(bi) * double(zi);
+    bb += double(bi) * double(bi);
+  }
+  rz = block_sum(rz, sh);
+  bb = block_sum(bb, sh);
+  if (threadIdx.x == 0) {
+    c.partB[blockIdx.x] = rz;
+    c.partC[blockIdx.x] = bb;
+  }
+}
+
+__global__ void cg_init_state(SolverState* s0, SolverState* s1, const double* partB, const double* partC, int np,
+                              double rtol, long long max_iters) {
+  __shared__ double sh[32];
+  const double rz = reduce_partials(partB, np, sh);
+  const double bb = reduce_partials(partC, np, sh);
+  if (threadIdx.x == 0) {
+    SolverState s{};
+    s.bnorm = sqrt(bb);
+    s.rz = rz;
+    s.iters = 0;
+    if (s.bnorm == 0.0) {
+      s.done = 1;
+      s.converged = 1;
+      s.residual = 0.0;
+    } else {
+      s.residual = 1.0;
+      s.converged = s.residual <= rtol;
+      s.done = s.converged || max_iters <= 0;
+    }
+    *s0 = s;
+    *s1 = s;
+  }
+}
+
+// A: ap = A p, partial p.ap
+template <int W, typename VT>
+__global__ void __launch_bounds__(KT) cg_a(const int32_t* rp, const int32_t* ci, const VT* val, CgVecs<VT> c,
+                                           const SolverState* __restrict__ S, int64_t n) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  const int lane = threadIdx.x % W;
+  double acc = 0.0;
+  const int64_t rows_per_grid = int64_t(gridDim.x) * (blockDim.x / W);
+  for (int64_t base = int64_t(blockIdx.x) * (blockDim.x / W); base < n; base += rows_per_grid) {
+    const int64_t row = base + threadIdx.x / W;
+    const bool valid = row < n;
+    const VT av = row_dot<W, VT>(rp, ci, val, c.p, row, valid, lane);
+    if (valid && lane == 0) {
+      c.ap[row] = av;
+      acc += double(c.p[row]) * double(av);
+    }
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) c.partA[blockIdx.x] = acc;
+}
+
+// B: alpha = rz / p.ap; x += alpha p; r -= alpha ap; z = P r; partials r.z, r.r
+template <typename VT>
+__global__ void __launch_bounds__(KT) cg_b(CgVecs<VT> c, const SolverState* __restrict__ S, int npa, int64_t n) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  const double pap = reduce_partials(c.partA, npa, sh);
+  const double alpha = S->rz / pap;
+  const VT at = VT(alpha), mat = VT(-alpha);
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    c.x[i] = c.x[i] + at * c.p[i];
+    const VT ri = c.r[i] + mat * c.ap[i];
+    const VT zi = c.dinv ? ri * c.dinv[i] : ri;
+    c.r[i] = ri;
+    c.z[i] = zi;
+    rz += double(ri) * double(zi);
+    rr += double(ri) * double(ri);
+  }
+  rz = block_sum(rz, sh);
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    c.partB[blockIdx.x] = rz;
+    c.partC[blockIdx.x] = rr;
+  }
+}
+
+// C: beta = rz_next / rz; p = beta p + z; state
+template <typename VT>
+__global__ void __launch_bounds__(KT) cg_c(CgVecs<VT> c, const SolverState* __restrict__ Sin,
+                                           SolverState* __restrict__ Sout, int npb, double rtol, long long max_iters,
+                                           int64_t n) {
+  __shared__ double sh[32];
+  if (Sin->done) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *Sout = *Sin;
+    return;
+  }
+  const double rz_next = reduce_partials(c.partB, npb, sh);
+  const double rr = reduce_partials(c.partC, npb, sh);
+  const double beta = rz_next / Sin->rz;
+  const VT bt = VT(beta);
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    c.p[i] = c.p[i] * bt + c.z[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    SolverState s = *Sin;
+    s.rz = rz_next;
+    s.iters += 1;
+    s.residual = sqrt(rr) / s.bnorm;
+    if (!isfinite(s.residual)) {
+      s.breakdown = 1;
+      s.done = 1;
+    }
+    if (s.residual <= rtol) {
+      s.converged = 1;
+      s.done = 1;
+    }
+    if (s.iters >= max_iters) s.done = 1;
+    *Sout = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host drivers
+// ---------------------------------------------------------------------------
+struct Workspace {
+  DevBuf vecs, parts, state;
+  SolverState* host_state = nullptr;
+};
+
+static fq_status poll_state(fq_ctx* ctx, const SolverState* dev, SolverState* host) {
+  FQ_CUDA(ctx, cudaMemcpyAsync(host, dev, sizeof(SolverState), cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return FQ_OK;
+}
+
+template <typename VT>
+fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* val, int64_t n, int64_t nnz,
+                     const VT* dinv, const VT* b, VT* x, double rtol, int64_t max_iters, fq_report* rep) {
+  cudaStream_t st = ctx->stream;
+  DevBuf vecs, parts, state;
+  const size_t vb = size_t(std::max<int64_t>(n, 1)) * sizeof(VT);
+  FQ_TRY(vecs.alloc(ctx, vb * 7));
+  FQ_TRY(parts.alloc(ctx, 2 * KBLOCKS * sizeof(double)));
+  FQ_TRY(state.alloc(ctx, 2 * sizeof(SolverState)));
+  MinresVecs<VT> m;
+  char* base = vecs.as<char>();
+  m.x = x;
+  m.r1 = reinterpret_cast<VT*>(base + 0 * vb);
+  m.r2 = reinterpret_cast<VT*>(base + 1 * vb);
+  m.y = reinterpret_cast<VT*>(base + 2 * vb);
+  m.v = reinterpret_cast<VT*>(base + 3 * vb);
+  m.z = reinterpret_cast<VT*>(base + 4 * vb);
+  m.w = reinterpret_cast<VT*>(base + 5 * vb);
+  m.w2 = reinterpret_cast<VT*>(base + 6 * vb);
+  m.dinv = dinv;
+  m.b = b;
+  m.partA = parts.as<double>();
+  m.partB = parts.as<double>() + KBLOCKS;
+  SolverState* S = state.as<SolverState>();
+  const int W = pick_w<VT>(nnz, n);
+  const int ga = std::min(spmv_blocks(n, W), KBLOCKS);
+  const int gv = int(std::max<int64_t>(1, std::min<int64_t>((n + KT - 1) / KT, KBLOCKS)));
+  minres_init<VT><<<gv, KT, 0, st>>>(m, n);
+  minres_init_state<<<1, KT, 0, st>>>(S, S + 1, m.partB, gv, rtol, (long long)max_iters);
+  ctx->launches += 2;
+  SolverState hs{};
+  int cur = 0;
+  int64_t launched = 0;
+  int64_t poll_every = 8;
+  for (;;) {
+    FQ_TRY(poll_state(ctx, S + cur, &hs));
+    if (hs.done || launched >= max_iters) break;
+    const int64_t batch = std::min<int64_t>(poll_every, max_iters - launched);
+    for (int64_t it = 0; it < batch; ++it) {
+      switch (W) {
+        case 4:
+          minres_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+          break;
+        case 8:
+          minres_a<8, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+          break;
+        case 16:
+          minres_a<16, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+          break;
+        default:
+          minres_a<32, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+          break;
+      }
+      minres_b<VT><<<gv, KT, 0, st>>>(m, S + cur, ga, n);
+      minres_c<VT><<<gv, KT, 0, st>>>(m, S + cur, S + (1 - cur), ga, gv, rtol, (long long)max_iters, n);
+      cur = 1 - cur;
+      ctx->launches += 3;
+    }
+    launched += batch;
+    poll_every = std::min<int64_t>(poll_every * 2, 64);
+    FQ_CUDA(ctx, cudaGetLastError());
+  }
+  rep->iters = hs.iters;
+  rep->residual = hs.residual;
+  rep->converged = hs.converged;
+  if (hs.breakdown) return set_error(ctx, FQ_BREAKDOWN, "MINRES breakdown (non-positive preconditioner product or NaN)");
+  return FQ_OK;
+}
+
+template <typename VT>
+fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* val, int64_t n, int64_t nnz,
+                 const VT* dinv, const VT* b, VT* x, double rtol, int64_t max_iters, fq_report* rep) {
+  cudaStream_t st = ctx->stream;
+  DevBuf vecs, parts, state;
+  const size_t vb = size_t(std::max<int64_t>(n, 1)) * sizeof(VT);
+  FQ_TRY(vecs.alloc(ctx, vb * 4));
+  FQ_TRY(parts.alloc(ctx, 3 * KBLOCKS * sizeof(double)));
+  FQ_TRY(state.alloc(ctx, 2 * sizeof(SolverState)));
+  CgVecs<VT> c;
+  char* base = vecs.as<char>();
+  c.x = x;
+  c.r = reinterpret_cast<VT*>(base + 0 * vb);
+  c.z = reinterpret_cast<VT*>(base + 1 * vb);
+  c.p = reinterpret_cast<VT*>(base + 2 * vb);
+  c.ap = reinterpret_cast<VT*>(base + 3 * vb);
+  c.dinv = dinv;
+  c.b = b;
+  c.partA = parts.as<double>();
+  c.partB = parts.as<double>() + KBLOCKS;
+  c.partC = parts.as<double>() + 2 * KBLOCKS;
+  SolverState* S = state.as<SolverState>();
+  const int W = pick_w<VT>(nnz, n);
+  const int ga = std::min(spmv_blocks(n, W), KBLOCKS);
+  const int gv = int(std::max<int64_t>(1, std::min<int64_t>((n + KT - 1) / KT, KBLOCKS)));
+  cg_init<VT><<<gv, KT, 0, st>>>(c, n);
+  cg_init_state<<<1, KT, 0, st>>>(S, S + 1, c.partB, c.partC, gv, rtol, (long long)max_iters);
+  ctx->launches += 2;
+  SolverState hs{};
+  int cur = 0;
+  int64_t launched = 0, poll_every = 8;
+  for (;;) {
+    FQ_TRY(poll_state(ctx, S + cur, &hs));
+    if (hs.done || launched >= max_iters) break;
+    const int64_t batch = std::min<int64_t>(poll_every, max_iters - launched);
+    for (int64_t it = 0; it < batch; ++it) {
+      switch (W) {
+        case 4:
+          cg_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
+          break;
+        case 8:
+          cg_a<8, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
+          break;
+        case 16:
+          cg_a<16, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
+          break;
+        default:
+          cg_a<32, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
+          break;
+      }
+      cg_b<VT><<<gv, KT, 0, st>>>(c, S + cur, ga, n);
+      cg_c<VT><<<gv, KT, 0, st>>>(c, S + cur, S + (1 - cur), gv, rtol, (long long)max_iters, n);
+      cur = 1 - cur;
+      ctx->launches += 3;
+    }
+    launched += batch;
+    poll_every = std::min<int64_t>(poll_every * 2, 64);
+    FQ_CUDA(ctx, cudaGetLastError());
+  }
+  rep->iters = hs.iters;
+  rep->residual = hs.residual;
+  rep->converged = hs.converged;
+  if (hs.breakdown) return set_error(ctx, FQ_BREAKDOWN, "CG breakdown (NaN)");
+  return FQ_OK;
+}
+
+template fq_status minres_run<double>(fq_ctx*, const int32_t*, const int32_t*, const double*, int64_t, int64_t,
+                                      const double*, const double*, double*, double, int64_t, fq_report*);
+template fq_status minres_run<float>(fq_ctx*, const int32_t*, const int32_t*, const float*, int64_t, int64_t,
+                                     const float*, const float*, float*, double, int64_t, fq_report*);
+template fq_status cg_run<double>(fq_ctx*, const int32_t*, const int32_t*, const double*, int64_t, int64_t,
+                                  const double*, const double*, double*, double, int64_t, fq_report*);
+template fq_status cg_run<float>(fq_ctx*, const int32_t*, const int32_t*, const float*, int64_t, int64_t,
+                                 const float*, const float*, float*, double, int64_t, fq_report*);
+
+// ---------------------------------------------------------------------------
+// Small vector kernels used by the problem drivers
+// ---------------------------------------------------------------------------
+// r = b - A x (FP64), partial ||r||^2 and ||b||^2
+__global__ void __launch_bounds__(KT) residual64_kernel(const int32_t* rp, const int32_t* ci, const double* val,
+                                                        const double* x, const double* b, double* r, double* part,
+                                                        int64_t n) {
+  __shared__ double sh[32];
+  constexpr int W = 8;
+  const int lane = threadIdx.x % W;
+  double rr = 0.0, bb = 0.0;
+  const int64_t rows_per_grid = int64_t(gridDim.x) * (blockDim.x / W);
+  for (int64_t base = int64_t(blockIdx.x) * (blockDim.x / W); base < n; base += rows_per_grid) {
+    const int64_t row = base + threadIdx.x / W;
+    const bool valid = row < n;
+    const double ax = row_dot<W, double>(rp, ci, val, x, row, valid, lane);
+    if (valid && lane == 0) {
+      const double ri = b[row] - ax;
+      r[row] = ri;
+      rr += ri * ri;
+      bb += b[row] * b[row];
+    }
+  }
+  rr = block_sum(rr, sh);
+  bb = block_sum(bb, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = rr;
+    part[KBLOCKS + blockIdx.x] = bb;
+  }
+}
+
+__global__ void to_float_scaled(const double* a, float* o, double s, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    o[i] = float(a[i] * s);
+}
+__global__ void axpy_from_float(double* x, const float* d, double s, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    x[i] += s * double(d[i]);
+}
+__global__ void to_float_kernel(const double* a, float* o, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    o[i] = float(a[i]);
+}
+
+static int vgrid(int64_t n) { return int(std::max<int64_t>(1, std::min<int64_t>((n + KT - 1) / KT, KBLOCKS))); }
+
+// ||b - A x|| and ||b|| in FP64 (r receives the residual).
+fq_status residual64(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const double* val, int64_t n,
+                     const double* x, const double* b, double* r, double* rnorm, double* bnorm) {
+  DevBuf part;
+  FQ_TRY(part.alloc(ctx, 2 * KBLOCKS * sizeof(double)));
+  FQ_CUDA(ctx, cudaMemsetAsync(part.p, 0, 2 * KBLOCKS * sizeof(double), ctx->stream));
+  const int g = std::min(spmv_blocks(n, 8), KBLOCKS);
+  residual64_kernel<<<g, KT, 0, ctx->stream>>>(rp, ci, val, x, b, r, part.as<double>(), n);
+  ctx->launches++;
+  std::vector<double> h(2 * KBLOCKS);
+  FQ_CUDA(ctx, cudaMemcpyAsync(h.data(), part.p, 2 * KBLOCKS * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  double rr = 0, bb = 0;
+  for (int i = 0; i < KBLOCKS; ++i) {
+    rr += h[i];
+    bb += h[KBLOCKS + i];
+  }
+  *rnorm = std::sqrt(rr);
+  *bnorm = std::sqrt(bb);
+  return FQ_OK;
+}
+
+void launch_to_float(const double* a, float* o, int64_t n, cudaStream_t st) {
+  if (n > 0) to_float_kernel<<<vgrid(n), KT, 0, st>>>(a, o, n);
+}
+void launch_to_float_scaled(const double* a, float* o, double s, int64_t n, cudaStream_t st) {
+  if (n > 0) to_float_scaled<<<vgrid(n), KT, 0, st>>>(a, o, s, n);
+}
+void launch_axpy_from_float(double* x, const float* d, double s, int64_t n, cudaStream_t st) {
+  if (n > 0) axpy_from_float<<<vgrid(n), KT, 0, st>>>(x, d, s, n);
+}
+
+}  // namespace fq

@@ -1,0 +1,234 @@
+/*
+ * formoniq_gpu.h -- C ABI of the GB300-native Galerkin assembly and Krylov solve
+ * path of formoniq (Finite Element Exterior Calculus on Regge meshes).
+ *
+ * The entry points replace the reference's Rust API on that path; each one cites
+ * the reference item it stands in for (paths relative to the formoniq workspace).
+ * Conventions of the reference kept here:
+ *   - a form's grade argument is the grade of the inner product (WhitneyPairing,
+ *     crates/formoniq/src/operators.rs:118-192): mass(k) is N_k x N_k,
+ *     dif_test(k) is N_{k-1} x N_k, dif_trial(k) is N_k x N_{k-1},
+ *     dif_both(k) is N_{k-1} x N_{k-1};
+ *   - simplices of every grade are numbered by colex order of their sorted vertex
+ *     tuples (crates/simplicial/src/topology/skeleton.rs:50-83), cells included;
+ *   - an assembled entry exists iff some cell contributes an element value that
+ *     is not exactly 0.0 (crates/formoniq/src/galerkin.rs:170-177);
+ *   - operators are total in the grade: out-of-range grades give correctly
+ *     shaped empty matrices (crates/formoniq/src/whitney_complex.rs:113-122).
+ *
+ * Error behaviour: the reference panics on contract violations and returns
+ * Option/Result elsewhere; here every call returns an fq_status, no exception or
+ * abort crosses the ABI, and fq_ctx_last_error() holds a message. All device work
+ * is ordered on the context's CUDA stream. A context is not thread-safe; use one
+ * per host thread.
+ */
+#ifndef FORMONIQ_GPU_H
+#define FORMONIQ_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum fq_status {
+  FQ_OK = 0,
+  FQ_INVALID_ARG = 1,      /* reference: assert!/panic on a contract violation */
+  FQ_DEGENERATE_CELL = 2,  /* a cell metric is singular (Metric::dual .expect) */
+  FQ_NOT_CONVERGED = 3,    /* Report{converged: false} (iterative/src/lib.rs:212-219) */
+  FQ_BREAKDOWN = 4,        /* non-positive preconditioner inner product / NaN */
+  FQ_OOM_BUDGET = 5,       /* the context's HBM budget would be exceeded */
+  FQ_TIMEOUT = 6,          /* a bounded device wait ran out */
+  FQ_CUDA_ERROR = 7,       /* a CUDA runtime call failed */
+  FQ_NO_DEVICE = 8,        /* no CUDA device / the library was built without one */
+  FQ_UNSUPPORTED = 9       /* dimension or grade outside 0..4 */
+} fq_status;
+
+typedef enum fq_form {
+  FQ_MASS = 0,      /* WhitneyPairing::mass       operators.rs:169-171 */
+  FQ_DIF_TRIAL = 1, /* WhitneyPairing::dif_trial  operators.rs:175-177 */
+  FQ_DIF_TEST = 2,  /* WhitneyPairing::dif_test   operators.rs:182-184 */
+  FQ_DIF_BOTH = 3   /* WhitneyPairing::dif_both   operators.rs:189-191 */
+} fq_form;
+
+typedef enum fq_bc {
+  FQ_ABSOLUTE = 0, /* WhitneyComplex: natural BC           whitney_complex.rs:322-465 */
+  FQ_RELATIVE = 1  /* RelativeWhitneyComplex: essential BC whitney_complex.rs:523-714 */
+} fq_bc;
+
+typedef enum fq_precision {
+  FQ_FP64 = 0, /* everything in FP64 */
+  FQ_FP32 = 1  /* FP64 Gram inverse/determinant, FP32 element matrices and values */
+} fq_precision;
+
+typedef struct fq_ctx fq_ctx;
+typedef struct fq_mesh fq_mesh;
+typedef struct fq_matrix fq_matrix;
+typedef struct fq_mixed fq_mixed;
+
+/* StopCriterion (iterative/src/lib.rs:193-208) plus solver knobs. */
+typedef struct fq_solve_opts {
+  double rtol;             /* relative residual target; reference default 1e-10 */
+  int64_t max_iters;       /* reference default 10_000 */
+  int precision;           /* fq_precision of the inner Krylov solve */
+  double refine_rtol;      /* FQ_FP32: outer FP64 refinement target (relative residual) */
+  int64_t max_refinements; /* FQ_FP32: cap on outer refinement steps */
+} fq_solve_opts;
+
+/* Report (iterative/src/lib.rs:212-219) plus refinement telemetry. */
+typedef struct fq_report {
+  int64_t iters;        /* total inner Krylov iterations */
+  double residual;      /* final relative residual of the last Krylov solve */
+  int32_t converged;    /* 1 when rtol was met */
+  int32_t refinements;  /* outer FP64 refinement steps taken (0 in FQ_FP64) */
+  double true_residual; /* ||b - A x|| / ||b|| recomputed in FP64 at the end */
+} fq_report;
+
+/* ---- context ------------------------------------------------------------ */
+fq_status fq_ctx_create(int device, void* cuda_stream, uint64_t hbm_budget_bytes, fq_ctx** out);
+void fq_ctx_destroy(fq_ctx* ctx);
+const char* fq_status_name(fq_status s);
+const char* fq_ctx_last_error(const fq_ctx* ctx);
+fq_status fq_ctx_synchronize(fq_ctx* ctx);
+uint64_t fq_ctx_bytes_in_use(const fq_ctx* ctx);
+/* Number of this library's kernels launched on the context so far. */
+uint64_t fq_ctx_kernel_launches(const fq_ctx* ctx);
+void fq_default_solve_opts(fq_solve_opts* opts);
+
+/* ---- topology: Complex -------------------------------------------------- */
+/* Complex::from_cells (crates/simplicial/src/topology/complex.rs:278-336):
+ * cells is host int32 [ncells][dim+1], each row strictly increasing; the cells
+ * are renumbered in colex order, every skeleton derived. dim in 0..4. */
+fq_status fq_mesh_from_cells(fq_ctx* ctx, int dim, int64_t ncells, const int32_t* cells, fq_mesh** out);
+/* CartesianGrid::new_unit(dim, n).triangulate() topology
+ * (crates/regge/src/mesher/cartesian.rs:210-213, simplicial/src/mesher/grid.rs:77-98). */
+fq_status fq_mesh_kuhn_cube(fq_ctx* ctx, int dim, int nboxes_per_axis, fq_mesh** out);
+void fq_mesh_destroy(fq_mesh* mesh);
+int fq_mesh_dim(const fq_mesh* mesh);
+/* Complex::nsimplices; 0 off 0..dim. */
+int64_t fq_mesh_nsimplices(const fq_mesh* mesh, int grade);
+/* HilbertComplex::ndofs (whitney_complex.rs:376-383 / :588-595). */
+int64_t fq_mesh_ndofs(const fq_mesh* mesh, int grade, fq_bc bc);
+/* The grade-k skeleton, host int32 [N_k][k+1], colex order. */
+fq_status fq_mesh_simplices(const fq_mesh* mesh, int grade, int32_t* out);
+/* Kept (interior) kidx of the relative complex, increasing (whitney_complex.rs:548-566). */
+fq_status fq_mesh_interior(const fq_mesh* mesh, int grade, int64_t* out);
+/* A coherent orientation of the cells, +-1 (simplicial topology/orientation.rs). */
+fq_status fq_mesh_orientation(const fq_mesh* mesh, int8_t* out);
+
+/* ---- geometry: MeshLengthsSq ------------------------------------------- */
+/* MeshLengthsSq::new (crates/regge/src/lengths/mesh.rs:34-36): one signed
+ * squared length per edge in colex edge order. `on_device` != 0 means the pointer
+ * is device memory on the context's device. */
+fq_status fq_mesh_set_lengths_sq(fq_mesh* mesh, const double* lengths_sq, int on_device);
+fq_status fq_mesh_get_lengths_sq(const fq_mesh* mesh, double* out_host);
+/* MeshCoords::to_edge_lengths_sq (crates/regge/src/coord/mesh.rs:208-216):
+ * s_e = (x_j - x_i)^T diag(ambient_signs) (x_j - x_i); coords host [nverts][adim]. */
+fq_status fq_mesh_lengths_from_coords(fq_mesh* mesh, const double* coords, int adim, const double* ambient_signs);
+/* Input generator for the Kuhn configs: CartesianGrid vertex placement
+ * (cartesian.rs:158-169) on [0,side_a] per axis, seeded uniform +-jitter*h
+ * jitter of every coordinate of every vertex, then the squared lengths
+ * under diag(ambient_signs). Requires a mesh made by fq_mesh_kuhn_cube. */
+fq_status fq_mesh_kuhn_lengths(fq_mesh* mesh, const double* side, const double* ambient_signs, double jitter,
+                               uint64_t seed);
+
+/* ---- kernel (a): per-cell Regge metric ---------------------------------- */
+/* SimplexLengthsSq::metric (regge/src/lengths/simplex.rs:308-326),
+ * Metric::dual (metric/src/lib.rs:250-257), cell_volume (regge/src/lib.rs:26-28),
+ * for every cell. Device outputs: ginv [n*n][ncells] (entry-major), det [ncells],
+ * vol [ncells]; any may be NULL. */
+fq_status fq_cell_metrics(fq_ctx* ctx, fq_mesh* mesh, double* ginv, double* det, double* vol);
+
+/* ---- kernel (b): element matrices --------------------------------------- */
+/* BilinearForm::element for a WhitneyPairing (operators.rs:201-211), every cell.
+ * Device output, entry-major [rows*cols][ncells] (row-major local entries),
+ * double for FQ_FP64, float for FQ_FP32. rows/cols receive the local shape. */
+fq_status fq_element_matrices(fq_ctx* ctx, fq_mesh* mesh, fq_form form, int grade, fq_precision prec,
+                              void* out, int* rows, int* cols);
+
+/* ---- assembly ----------------------------------------------------------- */
+/* BilinearForm::assemble (galerkin.rs:52-57 -> assemble_matrix :138-188) through
+ * HilbertComplex::{mass,dif_trial,dif_test,dif_both} (whitney_complex.rs:130-170),
+ * on the full or the relative complex (E^T A E, whitney_complex.rs:620-624).
+ * The pattern and the sorted scatter permutation are built on the first call per
+ * (form, grade, bc) and cached on the mesh. */
+fq_status fq_assemble(fq_ctx* ctx, fq_mesh* mesh, fq_form form, int grade, fq_bc bc, fq_precision prec,
+                      fq_matrix** out);
+/* Re-assemble into an existing matrix (same mesh, form, grade, bc, precision)
+ * after new lengths: the hot loop of a geometry sweep. */
+fq_status fq_reassemble(fq_ctx* ctx, fq_mesh* mesh, fq_matrix* mat);
+/* HilbertComplex::hdif_gram (whitney_complex.rs:180-183): M_k + dif_both(k+1). */
+fq_status fq_hdif_gram(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, fq_matrix** out);
+/* HilbertComplex::dif (whitney_complex.rs:417-423, relative :640-643): the
+ * coboundary N_{k+1} x N_k, entries +-1. */
+fq_status fq_coboundary(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, fq_matrix** out);
+/* The end-to-end assembly call with host buffers: uploads lengths_sq (N_1
+ * doubles), assembles, downloads the CSR values (nnz doubles or floats) into
+ * values_out. The pattern comes from fq_matrix_copy_to_host of a prior fq_assemble. */
+fq_status fq_assemble_host(fq_ctx* ctx, fq_mesh* mesh, fq_matrix* mat, const double* lengths_sq_host,
+                           void* values_out_host);
+
+fq_status fq_matrix_info(const fq_matrix* m, int64_t* nrows, int64_t* ncols, int64_t* nnz, int* precision);
+fq_status fq_matrix_device_arrays(const fq_matrix* m, const int32_t** row_ptr, const int32_t** col_idx,
+                                  const void** values);
+/* Host copies: row_ptr [nrows+1], col_idx [nnz], values [nnz] (double or float). */
+fq_status fq_matrix_copy_to_host(fq_ctx* ctx, const fq_matrix* m, int32_t* row_ptr, int32_t* col_idx,
+                                 void* values);
+void fq_matrix_destroy(fq_matrix* m);
+
+/* ---- kernel (d): operator, Krylov, preconditioner ------------------------ */
+/* LinearOperator::apply for CsrMatrix (iterative/src/operator.rs:5-13):
+ * y = A x, device vectors of the matrix's precision. */
+fq_status fq_spmv(fq_ctx* ctx, const fq_matrix* a, const void* x, void* y);
+/* krylov::minres (iterative/src/krylov.rs:113-211), device-resident, FP64, with
+ * the SPD diagonal preconditioner y = inv_diag .* r (NULL = identity). b, x,
+ * inv_diag are device pointers; x is overwritten (start from zero). */
+fq_status fq_minres(fq_ctx* ctx, const fq_matrix* a, const double* inv_diag, const double* b, double* x,
+                    const fq_solve_opts* opts, fq_report* report);
+/* krylov::cg (iterative/src/krylov.rs:48-95), same conventions. */
+fq_status fq_cg(fq_ctx* ctx, const fq_matrix* a, const double* inv_diag, const double* b, double* x,
+                const fq_solve_opts* opts, fq_report* report);
+
+/* ---- the mixed Hodge-Laplace source problem ------------------------------ */
+/* The resident form of elliptic::solve_source (problems/elliptic.rs:132-182):
+ * assembles the symmetrised KKT system of assemble_mixed_kkt (:54-114) with the
+ * harmonic border, and the diagonal of mixed_block_preconditioner (:29-47), once;
+ * later solves reuse it. */
+fq_status fq_mixed_create(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, int precision, fq_mixed** out);
+/* Re-assemble the KKT system after new lengths on the same mesh. */
+fq_status fq_mixed_reassemble(fq_mixed* prob);
+/* Solve with a host source GalerkinVector (ambient N_k doubles); outputs host
+ * sigma (ambient N_{k-1}), u (ambient N_k), p (harmonic_dim); any may be NULL. */
+fq_status fq_mixed_solve(fq_mixed* prob, const double* source_host, double* sigma_host, double* u_host,
+                         double* p_host, const fq_solve_opts* opts, fq_report* report);
+/* Same on device pointers (source ambient N_k; outputs in the same layouts). */
+fq_status fq_mixed_solve_device(fq_mixed* prob, const double* source, double* sigma, double* u, double* p,
+                                const fq_solve_opts* opts, fq_report* report);
+/* Sizes: n_sigma, n_u, n_harmonic (relative-DOF counts), system nnz. */
+fq_status fq_mixed_info(const fq_mixed* prob, int64_t* n_sigma, int64_t* n_u, int64_t* n_harmonic,
+                        int64_t* nnz);
+/* The assembled KKT matrix (owned by the problem; do not destroy). */
+const fq_matrix* fq_mixed_system(const fq_mixed* prob);
+void fq_mixed_destroy(fq_mixed* prob);
+/* One-shot elliptic::solve_source with host buffers. */
+fq_status fq_solve_source(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, const double* source_host,
+                          double* sigma_host, double* u_host, double* p_host, const fq_solve_opts* opts,
+                          fq_report* report);
+
+/* ---- the covariant Hodge-Dirac source problem ---------------------------- */
+/* dirac::solve_dirac_source (problems/dirac.rs:473-531) with MINRES in place of
+ * the reference's sparse LU: S = A + m M of HodgeDirac::assemble_selfadjoint
+ * (:205-260) on the relative complex, rhs = E^T (load - S lift), |diag(S)|
+ * Jacobi preconditioner. load/lift/x are host, flattened by grade (ambient
+ * offsets of HodgeDirac, :181-200). mass_term must be nonzero. */
+fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* mesh, double mass_term, const double* load_host,
+                                const double* lift_host, double* x_host, const fq_solve_opts* opts,
+                                fq_report* report);
+/* The assembled relative Dirac system S (for parity tests); caller destroys. */
+fq_status fq_dirac_system(fq_ctx* ctx, fq_mesh* mesh, double mass_term, fq_matrix** out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FORMONIQ_GPU_H */

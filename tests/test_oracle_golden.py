@@ -1,0 +1,422 @@
+"""Pin the oracle (the CPU restatement) against the reference's own known-answer
+tests and laws. CPU only: these run without a GPU.
+
+Each test names the reference test it ports.
+"""
+import itertools
+import math
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from golden import reference_known_answers as KA
+
+MASS, DIF_TRIAL, DIF_TEST, DIF_BOTH = 0, 1, 2, 3
+
+
+def rel_frob(a, b):
+    a = a.toarray() if sp.issparse(a) else np.asarray(a)
+    b = b.toarray() if sp.issparse(b) else np.asarray(b)
+    den = max(np.linalg.norm(b), 1e-300)
+    return np.linalg.norm(a - b) / den
+
+
+# ---- element matrices on the reference cell (operators.rs, tests/unit_elmat.rs) ----
+
+def test_hodge_mass_dim2_grade1(oracle):
+    m = oracle.element_matrix(2, MASS, 1, oracle.unit_lengths(2))
+    np.testing.assert_allclose(m, KA.HODGE_MASS_DIM2_GRADE1, atol=1e-15)
+
+
+def test_dif_trial_and_dif_test_n2_k1(oracle):
+    np.testing.assert_allclose(oracle.element_matrix(2, DIF_TRIAL, 1, oracle.unit_lengths(2)), KA.DIF_TRIAL_N2_K1,
+                               atol=1e-15)
+    np.testing.assert_allclose(oracle.element_matrix(2, DIF_TEST, 1, oracle.unit_lengths(2)), KA.DIF_TEST_N2_K1,
+                               atol=1e-15)
+
+
+@pytest.mark.parametrize("dim", [0, 1, 2, 3])
+def test_unit_mass_and_mass0_is_scalar_mass(oracle, dim):
+    m = oracle.element_matrix(dim, MASS, 0, oracle.unit_lengths(dim))
+    np.testing.assert_allclose(m, KA.UNIT_MASS[dim], atol=1e-15)
+    # hodge_mass0_is_scalar_mass (operators.rs:920-929): vol * Q
+    nv = dim + 1
+    q = (np.ones((nv, nv)) + np.eye(nv)) / (nv * (nv + 1))
+    np.testing.assert_allclose(m, q / math.factorial(dim), atol=1e-15)
+
+
+@pytest.mark.parametrize("dim", list(range(1, 11)))
+def test_unit_laplacian(oracle, dim):
+    m = oracle.element_matrix(dim, DIF_BOTH, 1, oracle.unit_lengths(dim))
+    np.testing.assert_allclose(m, KA.unit_laplacian(dim), rtol=1e-13, atol=1e-15)
+
+
+def _compound(b, k):
+    n = b.shape[0]
+    subs = [c for c in itertools.combinations(range(n), k)]
+    subs.sort(key=lambda c: sum(1 << v for v in c))  # colex
+    out = np.zeros((len(subs), len(subs)))
+    for i, r in enumerate(subs):
+        for j, c in enumerate(subs):
+            out[i, j] = np.linalg.det(b[np.ix_(r, c)]) if k else 1.0
+    return out
+
+
+def _random_cell_lengths(n, rng):
+    x = np.vstack([np.zeros(n), np.eye(n) + 0.2 * rng.standard_normal((n, n))])
+    edges = [(a, b) for b in range(n + 1) for a in range(b)]
+    return np.array([np.sum((x[b] - x[a]) ** 2) for a, b in edges]), x
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3, 4])
+def test_dif_both_is_gramian_of_difwhitneys(oracle, dim):
+    """operators.rs:977-997: dif_both(k+1) = vol (k+1)!^2 <dlambda_I, dlambda_J>."""
+    rng = np.random.default_rng(dim)
+    lengths, x = _random_cell_lengths(dim, rng)
+    e = (x[1:] - x[0])
+    g = e @ e.T
+    gi = np.linalg.inv(g)
+    L = np.vstack([-np.ones(dim), np.eye(dim)])
+    B = L @ gi @ L.T
+    vol = math.sqrt(abs(np.linalg.det(g))) / math.factorial(dim)
+    for grade in range(dim):
+        k = grade + 1
+        d = oracle.element_matrix(dim, DIF_BOTH, k, lengths)
+        expect = vol * math.factorial(k) ** 2 * _compound(B, k)
+        assert rel_frob(d, expect) < 1e-12
+
+
+# ---- meshes (regge/src/mesher/cartesian.rs, simplicial/src/mesher/grid.rs) ----
+
+def test_unit_cube_mesh(oracle):
+    cx, coords = oracle.cartesian_unit(3, 1)
+    np.testing.assert_array_equal(cx.simplices(3), KA.UNIT_CUBE_CELLS)
+    np.testing.assert_array_equal(coords, KA.UNIT_CUBE_COORDS)
+
+
+def test_unit_square_mesh(oracle):
+    cx, coords = oracle.cartesian_unit(2, 2)
+    np.testing.assert_array_equal(cx.simplices(2), KA.UNIT_SQUARE_CELLS)
+    np.testing.assert_array_equal(coords, KA.UNIT_SQUARE_COORDS)
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3, 4])
+@pytest.mark.parametrize("n", [1, 2, 3])
+def test_the_counts_hold_at_every_size(oracle, dim, n):
+    """grid.rs:143-154."""
+    cx = oracle.Complex.from_cells(oracle.kuhn_cells(dim, n))
+    assert cx.ncells() == math.factorial(dim) * n ** dim
+    assert cx.nsimplices(0) == (n + 1) ** dim
+
+
+def test_skeletons_are_colex_sorted(oracle):
+    cx = oracle.Complex.from_cells(oracle.kuhn_cells(3, 2))
+    for k in range(4):
+        s = cx.simplices(k)
+        keys = [tuple(reversed(r)) for r in s.tolist()]
+        assert keys == sorted(keys) and len(set(keys)) == len(keys)
+
+
+# ---- geometry (regge/src/lengths/simplex.rs:350-436) ----
+
+@pytest.mark.parametrize("dim", [1, 2, 3, 4])
+def test_metric_tensor_roundtrip(oracle, dim):
+    for q in range(dim + 1):
+        j = np.eye(dim)
+        for i in range(dim):
+            for jj in range(i):
+                j[i, jj] = ((2 * i + 3 * jj) % 4) / 8
+        eta = np.diag([1.0] * (dim - q) + [-1.0] * q)
+        g = j.T @ eta @ j
+        edges = [(a, b) for b in range(dim + 1) for a in range(b)]
+        lengths = np.array([g[b - 1, b - 1] if a == 0 else g[a - 1, a - 1] + g[b - 1, b - 1] - 2 * g[a - 1, b - 1]
+                            for a, b in edges])
+        cx = oracle.Complex.from_cells(np.arange(dim + 1, dtype=np.int32)[None, :])
+        G, Gi, det, vol, bad = cx.cell_metrics(lengths)
+        assert bad == 0
+        np.testing.assert_allclose(G[0], g, atol=1e-12)
+        np.testing.assert_allclose(Gi[0] @ g, np.eye(dim), atol=1e-10)
+        assert np.sign(det[0]) == (-1) ** q
+
+
+@pytest.mark.parametrize("dim", [2, 3, 4])
+def test_minkowski_regge_volume(oracle, dim):
+    """simplex.rs:414-431: the Minkowski reference cell has the unit volume."""
+    eta = np.diag([-1.0] + [1.0] * (dim - 1))
+    edges = [(a, b) for b in range(dim + 1) for a in range(b)]
+    lengths = np.array([eta[b - 1, b - 1] if a == 0 else eta[a - 1, a - 1] + eta[b - 1, b - 1] - 2 * eta[a - 1, b - 1]
+                        for a, b in edges])
+    cx = oracle.Complex.from_cells(np.arange(dim + 1, dtype=np.int32)[None, :])
+    _, _, _, vol, _ = cx.cell_metrics(lengths)
+    assert abs(vol[0] - 1 / math.factorial(dim)) < 1e-12
+
+
+# ---- global operators (tests/fem3d.rs, tests/fdm.rs, whitney_complex.rs tests) ----
+
+def _fem3d(n):
+    """The reference's hand-written 3D P1 stiffness (tests/fem3d.rs:18-104)."""
+    nvd = n + 1
+    nv = nvd ** 3
+    h = 1.0 / n
+    coords = np.zeros((nv, 3))
+    for z in range(nvd):
+        for y in range(nvd):
+            for x in range(nvd):
+                coords[x + nvd * (y + nvd * z)] = (h * x, h * y, h * z)
+    tet_vol = h ** 3 / 6
+    gal = np.zeros((nv, nv))
+    for zb in range(n):
+        for yb in range(n):
+            for xb in range(n):
+                box = [0] * 8
+                for k in range(2):
+                    for j in range(2):
+                        for i in range(2):
+                            box[i + 2 * (j + 2 * k)] = (xb + i) + nvd * ((yb + j) + nvd * (zb + k))
+                for tet in KA.FEM3D_TETS:
+                    gv = [box[i] for i in tet]
+                    pts = coords[gv]
+                    ns = []
+                    for i in range(4):
+                        face = np.delete(pts, i, axis=0)
+                        sign = 1.0 if i % 2 == 0 else -1.0
+                        ns.append(sign * np.cross(face[1] - face[0], face[2] - face[0]))
+                    el = np.array([[ns[i] @ ns[j] for j in range(4)] for i in range(4)]) / (36 * tet_vol)
+                    for a in range(4):
+                        for b in range(4):
+                            gal[gv[a], gv[b]] += el[a, b]
+    return gal
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4])
+def test_feec_vs_fem3d(oracle, n):
+    cx, coords = oracle.cartesian_unit(3, n)
+    wc = oracle.WhitneyComplex(cx, cx.edge_lengths_sq(coords))
+    np.testing.assert_allclose(wc.dif_both(1).toarray(), _fem3d(n), atol=1e-12, rtol=1e-12)
+
+
+def _kron_sum(mats):
+    out = 0
+    sizes = [m.shape[0] for m in mats]
+    for d, m in enumerate(mats):
+        before = np.eye(int(np.prod(sizes[:d]))) if d else np.eye(1)
+        after = np.eye(int(np.prod(sizes[d + 1:]))) if d + 1 < len(sizes) else np.eye(1)
+        out = out + np.kron(np.kron(before, m), after)
+    return out
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_fdm_vs_handchecked_interior(dim):
+    lap1 = np.array([[2, -1], [-1, 2]])
+    np.testing.assert_array_equal(_kron_sum([lap1] * dim), KA.LAPLACE_MATRICES_INTERIOR[dim])
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3, 4])
+@pytest.mark.parametrize("nb", [1, 2, 3])
+def test_feec_vs_fdm_interior(oracle, dim, nb):
+    """tests/fdm.rs:166-206."""
+    if dim == 4 and nb == 3:
+        pytest.skip("covered at smaller sizes")
+    n = nb + 2
+    cx = oracle.Complex.from_cells(oracle.kuhn_cells(dim, n))
+    coords = oracle.grid_coords(dim, n, side=np.full(dim, float(n)))
+    wc = oracle.WhitneyComplex(cx, cx.edge_lengths_sq(coords))
+    gal = wc.dif_both(1).toarray()
+    galvec = wc.mass(0) @ np.ones(cx.nsimplices(0))
+    gal = gal / galvec[:, None]
+    cart = np.array([[(v // (n + 1) ** a) % (n + 1) for a in range(dim)] for v in range(cx.nsimplices(0))])
+    interior = np.all((cart != 0) & (cart != n), axis=1)
+    sub = gal[np.ix_(interior, interior)]
+    assert np.all(np.abs(sub - np.round(sub)) <= 1e-11)
+    lap1 = np.diag(2 * np.ones(nb + 1)) - np.diag(np.ones(nb), 1) - np.diag(np.ones(nb), -1)
+    np.testing.assert_array_equal(np.round(sub).astype(int), _kron_sum([lap1] * dim).astype(int))
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_dif_both_and_dif_test_local_and_global_routes_agree(oracle, dim):
+    """whitney_complex.rs:733-815."""
+    cx, coords = oracle.cartesian_unit(dim, 2)
+    wc = oracle.WhitneyComplex(cx, cx.edge_lengths_sq(coords))
+    for grade in range(dim + 1):
+        local = wc.dif_both(grade + 1)
+        d = wc.dif(grade)
+        glob = d.T @ wc.mass(grade + 1) @ d
+        scale = max(np.abs(local.toarray()).max() if local.nnz else 0.0, 1.0)
+        assert local.shape == glob.shape
+        assert np.abs((local - glob).toarray()).max() <= 1e-12 * scale
+        lt = wc.dif_test(grade)
+        gt = wc.dif(grade - 1).T @ wc.mass(grade)
+        assert lt.shape == gt.shape
+        if lt.shape[0] and lt.shape[1]:
+            assert np.abs((lt - gt).toarray()).max() <= 1e-12 * max(np.abs(lt.toarray()).max(), 1.0)
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_the_relative_stiffness_is_the_restriction_of_the_full_one(oracle, dim):
+    """whitney_complex.rs:825-861."""
+    cx, coords = oracle.cartesian_unit(dim, 2)
+    rel = oracle.WhitneyComplex(cx, cx.edge_lengths_sq(coords), relative=True)
+    for grade in range(dim + 1):
+        if grade < dim:
+            assert rel.ndofs(grade) < cx.nsimplices(grade)
+        r = rel.dif_both(grade + 1)
+        d = rel.dif(grade)
+        by_def = d.T @ rel.mass(grade + 1) @ d
+        assert np.abs((r - by_def).toarray()).max() <= 1e-12 * max(np.abs(r.toarray()).max() if r.nnz else 0, 1.0)
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_operators_are_total_at_the_trivial_ends(oracle, dim):
+    """whitney_complex.rs:989-1027."""
+    cx, coords = oracle.cartesian_unit(dim, 2)
+    wc = oracle.WhitneyComplex(cx, cx.edge_lengths_sq(coords))
+    for ghost in (-1, dim + 1):
+        assert wc.ndofs(ghost) == 0
+        assert wc.mass(ghost).shape == (0, 0)
+        assert wc.dif_both(ghost + 1).shape == (0, 0)
+    assert wc.dif(-1).shape == (wc.ndofs(0), 0)
+    assert wc.dif(dim).shape == (0, wc.ndofs(dim))
+    top = wc.dif_both(dim + 1)
+    assert top.shape == (wc.ndofs(dim), wc.ndofs(dim)) and top.nnz == 0
+
+
+# ---- Krylov (iterative/src/krylov.rs:224-320) ----
+
+def _sym_from_spectrum(eigs, seed=0):
+    n = len(eigs)
+    if n == 0:
+        return np.zeros((0, 0))
+    q, _ = np.linalg.qr(np.random.default_rng(seed).standard_normal((n, n)))
+    return q @ np.diag(eigs) @ q.T
+
+
+@pytest.mark.parametrize("n", list(range(0, 9)))
+def test_cg_terminates_in_at_most_n_steps(oracle, n):
+    a = _sym_from_spectrum([1.0 + k for k in range(n)])
+    x_true = np.log(np.arange(1, n + 1, dtype=float))
+    b = a @ x_true
+    x, rep = oracle.cg(sp.csr_matrix(a), lambda r: r, b, rtol=1e-10, max_iters=max(n, 1))
+    assert rep.converged and rep.iters <= n
+    if n:
+        assert np.linalg.norm(x - x_true) < 1e-7
+
+
+@pytest.mark.parametrize("n", list(range(0, 9)))
+def test_minres_solves_symmetric_indefinite_systems(oracle, n):
+    eigs = [(k // 2 + 1) * (1 if k % 2 == 0 else -1) for k in range(n)]
+    a = _sym_from_spectrum(eigs)
+    b = np.sqrt(np.arange(1, n + 1, dtype=float))
+    x, rep = oracle.minres(sp.csr_matrix(a), lambda r: r, b, rtol=1e-11)
+    assert rep.converged
+    if n:
+        assert np.linalg.norm(x - np.linalg.solve(a, b)) < 1e-7
+
+
+def test_minres_agrees_with_cg_on_spd(oracle):
+    n = 25
+    a = sp.diags([np.ones(n - 1), 4 * np.ones(n), np.ones(n - 1)], [-1, 0, 1]).tocsr()
+    x_true = np.sin(np.arange(n, dtype=float))
+    b = a @ x_true
+    jac = oracle.jacobi(a.diagonal())
+    xm, rm = oracle.minres(a, jac, b, rtol=1e-12)
+    xc, _ = oracle.cg(a, jac, b, rtol=1e-12)
+    assert rm.converged
+    assert np.linalg.norm(xm - x_true) < 1e-8
+    assert np.linalg.norm(xm - xc) < 1e-7
+
+
+# ---- the mixed problem (problems/elliptic.rs:259-367) ----
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_block_minres_matches_direct_on_the_mixed_system(oracle, dim):
+    cx, coords = oracle.cartesian_unit(dim, 2)
+    rel = oracle.WhitneyComplex(cx, cx.edge_lengths_sq(coords), relative=True)
+    for grade in range(dim + 1):
+        harm = oracle.harmonics(rel, grade)
+        src = (np.arange(cx.nsimplices(grade)) % 7) - 3.0
+        a, b, ns, nu = oracle.assemble_mixed_kkt(rel, src, grade, harm)
+        assert abs(a - a.T).max() <= 1e-14 * max(abs(a).max(), 1.0)  # symmetrised saddle point
+        blocks = []
+        if grade > 0:
+            blocks.append(rel.hdif_gram(grade - 1))
+        blocks.append(rel.hdif_gram(grade))
+        if harm.shape[1]:
+            blocks.append(sp.identity(harm.shape[1], format="csr"))
+        x, rep = oracle.minres(a, oracle.BlockDiagonal(blocks), b, rtol=1e-11)
+        assert rep.converged
+        x_lu = oracle.direct_solve(a, b)
+        err = np.linalg.norm(x - x_lu) / max(np.linalg.norm(x_lu), 1.0)
+        assert err < KA.BLOCK_MINRES_VS_LU_TOL
+
+
+def test_block_minres_iteration_count_is_mesh_independent(oracle):
+    def iters(nb):
+        cx, coords = oracle.cartesian_unit(2, nb)
+        rel = oracle.WhitneyComplex(cx, cx.edge_lengths_sq(coords), relative=True)
+        src = ((np.arange(cx.nsimplices(1)) % 5) - 2.0) * 0.3
+        _, _, _, rep = oracle.solve_source(rel, src, 1, rtol=1e-10)
+        assert rep.converged
+        return rep.iters
+
+    assert iters(8) <= iters(4) + KA.MINRES_ITER_SLACK
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_harmonics_are_harmonic(oracle, dim):
+    """harmonic.rs tests: dh = 0, D^T M h = 0, M-orthonormal (closed forms)."""
+    cx, coords = oracle.cartesian_unit(dim, 2)
+    for relative in (False, True):
+        wc = oracle.WhitneyComplex(cx, cx.edge_lengths_sq(coords), relative=relative)
+        for grade in range(dim + 1):
+            h = oracle.harmonics(wc, grade)
+            m = wc.mass(grade)
+            for col in h.T:
+                assert np.linalg.norm(wc.dif(grade) @ col) <= 1e-8 * max(np.linalg.norm(col), 1)
+                assert np.linalg.norm(wc.dif(grade - 1).T @ (m @ col)) <= 1e-8 * max(np.linalg.norm(col), 1)
+                assert abs(col @ (m @ col) - 1.0) < 1e-8
+
+
+# ---- Hodge-Dirac (problems/dirac.rs:632-947) ----
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_selfadjoint_operator_is_symmetric(oracle, dim):
+    for mink in (False, True):
+        if mink:
+            cx, coords, signs = oracle.minkowski(dim, 2)
+        else:
+            (cx, coords), signs = oracle.cartesian_unit(dim, 2), None
+        full = oracle.WhitneyComplex(cx, cx.edge_lengths_sq(coords, signs))
+        _, _, a = oracle.dirac_selfadjoint(full)
+        assert abs(a - a.T).max() == 0.0
+
+
+def derham_constant(cx, coords, k):
+    """de Rham coefficients of the constant k-form with every component 1:
+    sum_I det((x_j - x_0)_I) / k! over the simplex (derham/src/project.rs)."""
+    s = cx.simplices(k)
+    dim = coords.shape[1]
+    if k == 0:
+        return np.ones(len(s))
+    out = np.zeros(len(s))
+    subs = list(itertools.combinations(range(dim), k))
+    for i, simp in enumerate(s):
+        e = (coords[simp[1:]] - coords[simp[0]]).T  # dim x k
+        out[i] = sum(np.linalg.det(e[list(I), :]) for I in subs) / math.factorial(k)
+    return out
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_dirac_source_reproduces_constant_field(oracle, dim):
+    for mink in (False, True):
+        if mink:
+            cx, coords, signs = oracle.minkowski(dim, 2)
+        else:
+            (cx, coords), signs = oracle.cartesian_unit(dim, 2), None
+        lengths = cx.edge_lengths_sq(coords, signs)
+        exact = np.concatenate([derham_constant(cx, coords, k) for k in range(dim + 1)])
+        full = oracle.WhitneyComplex(cx, lengths)
+        _, mb, _ = oracle.dirac_selfadjoint(full)
+        load = mb @ exact
+        sol = oracle.dirac_solve_source(cx, lengths, 1.0, load, exact)
+        np.testing.assert_allclose(sol, exact, atol=1e-9)
