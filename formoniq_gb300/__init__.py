@@ -110,6 +110,9 @@ _SIGNATURES = {
     "fq_ctx_bytes_in_use": (ctypes.c_uint64, [_P]),
     "fq_ctx_kernel_launches": (ctypes.c_uint64, [_P]),
     "fq_default_solve_opts": (None, [ctypes.POINTER(SolveOpts)]),
+    "fq_ctx_set_profiling": (ctypes.c_int, [_P, ctypes.c_int]),
+    "fq_ctx_profile": (ctypes.c_int, [_P, _DP, _I64P, ctypes.c_int, ctypes.c_int]),
+    "fq_measure_fma_peak": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
     "fq_mesh_from_cells": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64, _I32P, ctypes.POINTER(_P)]),
     "fq_mesh_kuhn_cube": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
     "fq_mesh_destroy": (None, [_P]),
@@ -206,6 +209,21 @@ class Context:
     @property
     def kernel_launches(self) -> int:
         return int(self.L.fq_ctx_kernel_launches(self.h))
+
+    def set_profiling(self, enable: bool):
+        self.check(self.L.fq_ctx_set_profiling(self.h, int(enable)), "fq_ctx_set_profiling")
+
+    def profile(self, reset: bool = False):
+        """(element_ms, scatter_ms), (element_launches, scatter_launches)."""
+        ms = (ctypes.c_double * 4)()
+        n = (ctypes.c_int64 * 4)()
+        self.check(self.L.fq_ctx_profile(self.h, ms, n, 4, int(reset)))
+        return list(ms)[:2], list(n)[:2]
+
+    def fma_peak_tflops(self, fp64: bool = True) -> float:
+        t = ctypes.c_double()
+        self.check(self.L.fq_measure_fma_peak(self.h, int(fp64), ctypes.byref(t)), "fq_measure_fma_peak")
+        return t.value
 
     def close(self):
         if getattr(self, "h", None):

@@ -470,6 +470,8 @@ fq_status fq_ctx_create(int device, void* stream, uint64_t budget, fq_ctx** out)
 void fq_ctx_destroy(fq_ctx* ctx) {
   if (!ctx) return;
   cudaStreamSynchronize(ctx->stream);
+  for (auto& e : ctx->ev)
+    if (e) cudaEventDestroy(e);
   ctx->status.release();
   ctx->scratch.release();
   if (ctx->host_status) cudaFreeHost(ctx->host_status);
@@ -486,6 +488,29 @@ fq_status fq_ctx_synchronize(fq_ctx* ctx) {
 }
 
 uint64_t fq_ctx_bytes_in_use(const fq_ctx* ctx) { return ctx ? ctx->in_use : 0; }
+
+fq_status fq_ctx_set_profiling(fq_ctx* ctx, int enable) {
+  if (!ctx) return FQ_INVALID_ARG;
+  if (enable && !ctx->ev[0]) {
+    for (auto& e : ctx->ev) FQ_CUDA(ctx, cudaEventCreate(&e));
+  }
+  ctx->profiling = enable != 0;
+  return FQ_OK;
+}
+
+fq_status fq_ctx_profile(fq_ctx* ctx, double* ms, int64_t* launches, int nslots, int reset) {
+  if (!ctx) return FQ_INVALID_ARG;
+  for (int i = 0; i < nslots && i < 4; ++i) {
+    if (ms) ms[i] = ctx->prof_ms[i];
+    if (launches) launches[i] = ctx->prof_n[i];
+  }
+  if (reset)
+    for (int i = 0; i < 4; ++i) {
+      ctx->prof_ms[i] = 0.0;
+      ctx->prof_n[i] = 0;
+    }
+  return FQ_OK;
+}
 uint64_t fq_ctx_kernel_launches(const fq_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 // ---- meshes -----------------------------------------------------------------

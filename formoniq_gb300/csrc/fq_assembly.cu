@@ -271,23 +271,25 @@ fq_status build_plan(fq_ctx* ctx, fq_mesh* m, Plan& plan, const Layout& lay) {
   }
   // pack tables into one device buffer
   std::vector<char> blob;
+  // Each table is copied with its exact size into a 16-byte aligned, zero-padded
+  // slot; an empty table reads nothing.
   auto put = [&](const void* src, size_t bytes) {
-    size_t o = (blob.size() + 15) & ~size_t(15);
-    blob.resize(o + bytes);
-    memcpy(blob.data() + o, src, bytes);
+    const size_t o = (blob.size() + 15) & ~size_t(15);
+    blob.resize(o + bytes + 16, 0);
+    if (bytes) memcpy(blob.data() + o, src, bytes);
     return o;
   };
   std::vector<int32_t> entry32(lay.entry.begin(), lay.entry.end());
   std::vector<int32_t> diag32(lay.diag_entry.begin(), lay.diag_entry.end());
-  const size_t o_entry = put(entry32.data(), entry32.size() * 4 + 4);
-  const size_t o_rsrc = put(row_src.data(), row_src.size() * 4 + 4);
-  const size_t o_csrc = put(col_src.data(), col_src.size() * 4 + 4);
-  const size_t o_roff = put(row_off.data(), row_off.size() * 8 + 8);
-  const size_t o_coff = put(col_off.data(), col_off.size() * 8 + 8);
-  const size_t o_faces = put(faces.data(), faces.size() * sizeof(void*) + 8);
-  const size_t o_rmaps = put(rmaps.data(), rmaps.size() * sizeof(void*) + 8);
-  const size_t o_cmaps = put(cmaps.data(), cmaps.size() * sizeof(void*) + 8);
-  const size_t o_diag = put(diag32.data(), diag32.size() * 4 + 4);
+  const size_t o_entry = put(entry32.data(), entry32.size() * 4);
+  const size_t o_rsrc = put(row_src.data(), row_src.size() * 4);
+  const size_t o_csrc = put(col_src.data(), col_src.size() * 4);
+  const size_t o_roff = put(row_off.data(), row_off.size() * 8);
+  const size_t o_coff = put(col_off.data(), col_off.size() * 8);
+  const size_t o_faces = put(faces.data(), faces.size() * sizeof(void*));
+  const size_t o_rmaps = put(rmaps.data(), rmaps.size() * sizeof(void*));
+  const size_t o_cmaps = put(cmaps.data(), cmaps.size() * sizeof(void*));
+  const size_t o_diag = put(diag32.data(), diag32.size() * 4);
   DevBuf tables;
   FQ_TRY(tables.alloc(ctx, blob.size()));
   FQ_CUDA(ctx, cudaMemcpyAsync(tables.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, st));
@@ -614,12 +616,26 @@ fq_status assemble_into(fq_ctx* ctx, fq_matrix* m) {
     FQ_TRY(m->zero_flags.alloc(ctx, std::max<int64_t>(p.nslots, 1)));
   int* zc = ctx->status.as<int>() + 1;
   FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
+  const bool prof = ctx->profiling && ctx->ev[0];
+  if (prof) FQ_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
   if (p.nslots > 0 || p.ndiag_trip > 0) FQ_TRY(element_pass(ctx, mesh, m->kind, m->grade, fp32, m->param, mesh->elem, p.nent));
+  if (prof) FQ_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+  if (prof) FQ_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
   launch_scatter(p, mesh->elem.p, m->full_values.p, m->zero_flags.as<uint8_t>(), zc, fp32, ctx->stream);
+  if (prof) FQ_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
   if (p.nslots > 0) ctx->launches++;
   FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost,
                                ctx->stream));
   FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (prof) {
+    float a = 0.f, b = 0.f;
+    FQ_CUDA(ctx, cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]));
+    FQ_CUDA(ctx, cudaEventElapsedTime(&b, ctx->ev[2], ctx->ev[3]));
+    ctx->prof_ms[0] += a;
+    ctx->prof_ms[1] += b;
+    ctx->prof_n[0] += 1;
+    ctx->prof_n[1] += 1;
+  }
   if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
   const int nzero = ctx->host_status[1];
   if (nzero > 0) {

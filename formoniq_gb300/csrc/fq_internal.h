@@ -124,6 +124,12 @@ struct fq_ctx {
   fq::DevBuf status;       // int [8] device status words
   int* host_status = nullptr;  // pinned mirror
   fq::DevBuf scratch;      // reusable temporary storage
+  // instrumentation: CUDA events on `stream` around element passes (slot 0) and
+  // scatters (slot 1) of every assembly while `profiling` is set
+  bool profiling = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double prof_ms[4] = {0, 0, 0, 0};
+  int64_t prof_n[4] = {0, 0, 0, 0};
 };
 
 namespace fq {

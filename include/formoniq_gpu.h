@@ -95,6 +95,17 @@ uint64_t fq_ctx_bytes_in_use(const fq_ctx* ctx);
 /* Number of this library's kernels launched on the context so far. */
 uint64_t fq_ctx_kernel_launches(const fq_ctx* ctx);
 void fq_default_solve_opts(fq_solve_opts* opts);
+/* Instrumentation, no counterpart in the reference (which times with
+ * Instant::now() in ignored benches): while enabled, CUDA events recorded on the
+ * context's stream bracket the element-kernel pass (slot 0) and the scatter
+ * (slot 1) of every assembly; fq_ctx_profile returns the accumulated
+ * milliseconds and launch counts per slot and optionally resets them. */
+fq_status fq_ctx_set_profiling(fq_ctx* ctx, int enable);
+fq_status fq_ctx_profile(fq_ctx* ctx, double* ms, int64_t* launches, int nslots, int reset);
+/* Instrumentation, no counterpart in the reference: the sustained FMA rate of
+ * this device's FP64 (fp64 != 0) or FP32 pipe, in TFLOP/s (2 flops per FMA),
+ * from a register-resident FMA-chain kernel timed with CUDA events. */
+fq_status fq_measure_fma_peak(fq_ctx* ctx, int fp64, double* tflops);
 
 /* ---- topology: Complex -------------------------------------------------- */
 /* Complex::from_cells (crates/simplicial/src/topology/complex.rs:278-336):
