@@ -665,6 +665,7 @@ fq_status fq_cell_metrics(fq_ctx* ctx, fq_mesh* m, double* ginv, double* det, do
   a.vol_out = vol;
   a.param = 0.0;
   a.status = ctx->status.as<int>();
+  a.nent = 0;
   FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
   if (launch_element(m->dim, 0, EK_METRIC, 0, a, ctx->stream) != 0) return set_error(ctx, FQ_UNSUPPORTED, "dim");
   ctx->launches++;
@@ -708,6 +709,7 @@ fq_status fq_element_matrices(fq_ctx* ctx, fq_mesh* m, fq_form form, int grade, 
     }
   FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->host_status[0] & 2) return set_error(ctx, FQ_INVALID_ARG, "element program wrote outside its layout");
   if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
   return FQ_OK;
   FQ_GUARD_END(ctx)

@@ -67,7 +67,7 @@ Layout make_layout(int n, int kind, int K) {
       sym = false;
       break;
     case EK_KKT:
-      push_grade(K - 1, 0, true, true);
+      push_grade(K - 1, 0, true, true);  // kkt_sigma_local(n, K) dofs
       push_grade(K, 1, true, true);
       L.block_grade = {K - 1, K};
       break;
@@ -578,6 +578,7 @@ fq_status element_pass(fq_ctx* ctx, fq_mesh* m, int kind, int grade, int fp32, d
   a.ginv_out = a.det_out = a.vol_out = nullptr;
   a.param = param;
   a.status = ctx->status.as<int>();
+  a.nent = nent;
   if (launch_element(m->dim, grade, kind, fp32, a, ctx->stream) != 0)
     return set_error(ctx, FQ_UNSUPPORTED, "no element program for this dimension/grade");
   ctx->launches++;
@@ -636,6 +637,7 @@ fq_status assemble_into(fq_ctx* ctx, fq_matrix* m) {
     ctx->prof_n[0] += 1;
     ctx->prof_n[1] += 1;
   }
+  if (ctx->host_status[0] & 2) return set_error(ctx, FQ_INVALID_ARG, "element program wrote outside its layout");
   if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
   const int nzero = ctx->host_status[1];
   if (nzero > 0) {

@@ -42,7 +42,13 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs a) {
     Bary<N, T> B;
     bary_gramian<N, T>(ginv, B);
     T* out = static_cast<T*>(a.out);
-    auto put = [&](int e, T v) { out[int64_t(e) * nc + cell] = v; };
+    const int nent = a.nent;
+    auto put = [&](int e, T v) {
+      if (e < nent)
+        out[int64_t(e) * nc + cell] = v;
+      else
+        atomicOr(a.status, 2);
+    };
     // mass scale vol (k!)^2 / ((n+1)(n+2)); dif_test scale vol (k!)^2 / (n+1);
     // stiffness scale vol (k!)^2.
     auto mscale = [&](int k) { return T(vol * double(cfact(k)) * double(cfact(k)) / double((N + 1) * (N + 2))); };
@@ -102,7 +108,7 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs a) {
       });
     } else if constexpr (KIND == EK_KKT) {
       // Local composite: sigma = (k-1)-faces, then u = k-faces.
-      constexpr int LS = cbinom(N + 1, K);
+      constexpr int LS = kkt_sigma_local(N, K);
       constexpr int LU = cbinom(N + 1, K + 1);
       constexpr int L = LS + LU;
       constexpr int P = (L * (L + 1)) / 2;

@@ -26,6 +26,10 @@ FQ_HD constexpr int grade_offset(int n, int j) {
   return o;
 }
 
+// Local sigma-block size of the mixed system at grade k: the (k-1)-faces of a
+// cell, none at grade 0 (Lambda^{-1} = 0).
+FQ_HD constexpr int kkt_sigma_local(int n, int k) { return k > 0 ? cbinom(n + 1, k) : 0; }
+
 // Arguments of the per-cell kernel (device pointers).
 struct ElemArgs {
   int64_t ncells;
@@ -36,7 +40,9 @@ struct ElemArgs {
   double* det_out;           // optional [ncells]
   double* vol_out;           // optional [ncells]
   double param;              // mass term of the Dirac program
-  int* status;               // bit 0: a singular or non-finite cell metric
+  int* status;               // bit 0: a singular or non-finite cell metric;
+                             // bit 1: an element entry index outside [0, nent)
+  int nent;                  // entries per cell the output buffer holds
 };
 
 }  // namespace fq

@@ -464,11 +464,12 @@ def assemble_mixed_kkt(wc: WhitneyComplex, source: np.ndarray, k: int, harm: np.
     ntot = ns + nu + nh
     a = coo_to_csr(np.concatenate(rows) if rows else [], np.concatenate(cols) if cols else [],
                    np.concatenate(vals) if vals else [], (ntot, ntot))
-    # sign flip of the sigma rows (elliptic.rs:102-113)
+    # sign flip of the sigma rows (elliptic.rs:102-113): an exact negation of the
+    # stored values of rows < ns, pattern and column order unchanged
     sign = np.ones(ntot)
     sign[:ns] = -1.0
-    a = sp.diags(sign) @ a
-    a = sp.csr_matrix(a)
+    a = a.copy()
+    a.data = a.data * np.repeat(sign, np.diff(a.indptr))
     src = wc.inclusion(k).T @ source
     rhs = np.concatenate([np.zeros(ns), src, np.zeros(nh)])
     return a, sign * rhs, ns, nu
@@ -688,7 +689,12 @@ def dirac_source_system(cx: Complex, lengths: np.ndarray, mass_term: float, load
     keep = np.concatenate([cx.interior(k) + offsets[k] for k in range(cx.dim + 1)])
     e = sp.csr_matrix((np.ones(len(keep)), (keep, np.arange(len(keep)))), shape=(int(offsets[-1]), len(keep)))
     rhs = e.T @ (load - s @ lift)
-    s_rel = sp.csr_matrix(s[keep][:, keep])
+    # E^T S E: keep interior rows and columns, renumbered (explicit entries kept)
+    newidx = -np.ones(int(offsets[-1]), np.int64)
+    newidx[keep] = np.arange(len(keep))
+    c = s.tocoo()
+    sel = (newidx[c.row] >= 0) & (newidx[c.col] >= 0)
+    s_rel = coo_to_csr(newidx[c.row[sel]], newidx[c.col[sel]], c.data[sel], (len(keep), len(keep)))
     return s_rel, rhs, keep, offsets
 
 

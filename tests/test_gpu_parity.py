@@ -178,10 +178,26 @@ def test_assembly_fp32(oracle, ctx, dim, nb):
                 assert rel_frob(b, a) < FP32_TOL
 
 
+def pattern_difference_is_roundoff(gpu: sp.csr_matrix, ref: sp.csr_matrix, rel=1e-14):
+    """Slots present on one side only must hold values at roundoff level: the
+    `val != 0.0` rule (galerkin.rs:173) keeps a mathematically zero entry exactly
+    when its rounding happens to leave a nonzero, which depends on the order of
+    operations, not on the mathematics."""
+    g = gpu.tocoo()
+    r = ref.tocoo()
+    gs = {(i, j): v for i, j, v in zip(g.row, g.col, g.data)}
+    rs = {(i, j): v for i, j, v in zip(r.row, r.col, r.data)}
+    scale = max(np.abs(r.data).max() if r.nnz else 0.0, np.abs(g.data).max() if g.nnz else 0.0, 1e-300)
+    only = [abs(gs[k]) for k in gs.keys() - rs.keys()] + [abs(rs[k]) for k in rs.keys() - gs.keys()]
+    assert all(v <= rel * scale for v in only), max(only) / scale
+    return len(only)
+
+
 @pytest.mark.parametrize("dim", [1, 2, 3])
 def test_assembly_unjittered_pattern_follows_the_nonzero_rule(oracle, ctx, dim):
-    """N = 2 unit cube: dyadic lengths, so mathematically zero element entries are
-    exact zeros on both sides and the `val != 0.0` rule drops the same slots."""
+    """The reference's own unjittered N = 2 unit meshes, where mathematically
+    zero element entries occur: both sides drop exact zeros, and every slot that
+    one side keeps and the other drops holds a roundoff-level value."""
     cx, mesh, lengths, _ = make_pair(oracle, ctx, dim, 2, jitter=0.0)
     owc = oracle.WhitneyComplex(cx, lengths)
     gwc = fq.WhitneyComplex(mesh)
@@ -189,7 +205,8 @@ def test_assembly_unjittered_pattern_follows_the_nonzero_rule(oracle, ctx, dim):
         for name in ("mass", "dif_trial", "dif_test", "dif_both"):
             a = getattr(owc, name)(grade)
             b = getattr(gwc, name)(grade).to_scipy()
-            csr_equal_pattern(b, a)
+            assert a.shape == b.shape
+            pattern_difference_is_roundoff(b, a)
             if a.nnz:
                 assert rel_frob(b, a) < FP64_TOL
 
@@ -296,7 +313,7 @@ def test_solve_source_matches_direct(oracle, ctx, dim, nb, relative):
         x = oracle.direct_solve(a, rhs)
         sig_o = owc.inclusion(grade - 1) @ x[:ns] if grade > 0 else np.zeros(0)
         u_o = owc.inclusion(grade) @ x[ns:ns + nu]
-        sigma, u, p, rep = fq.solve_source(gwc, src, grade, fq.SolveOpts.default(rtol=1e-13))
+        sigma, u, p, rep = fq.solve_source(gwc, src, grade, fq.SolveOpts.default(rtol=1e-12))
         assert rep.converged, (grade, rep)
         scale = max(np.linalg.norm(x), 1.0)
         err = math.sqrt(np.linalg.norm(u - u_o) ** 2 + (np.linalg.norm(sigma - sig_o) ** 2 if grade else 0.0))
