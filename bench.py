@@ -181,7 +181,7 @@ def run_ours(args):
     ncells = mesh.ncells()
     wc = fq.WhitneyComplex(mesh)
     t0 = time.perf_counter()
-    mats = [getattr(wc, name)(k) for name, k in FORMS]  # plans built here (set-up)
+    mats = [getattr(wc, name)(k) for name, k in FORMS]  # patterns and permutations built here (set-up)
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t0
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -209,22 +209,52 @@ def run_ours(args):
             evs[i][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
-    ctx.set_profiling(False)
-    launches = ctx.kernel_launches - launches0
-    step_ms = [a.elapsed_time(b) for a, b in evs]
-    ms = sum(step_ms) / len(step_ms)
+        ctx.set_profiling(False)
+        launches = ctx.kernel_launches - launches0
+        step_ms = [a.elapsed_time(b) for a, b in evs]
+        ms = sum(step_ms) / len(step_ms)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        value = world * ncells / (ms * 1e-3)
+        (el_ms, sc_ms), (el_n, sc_n) = ctx.profile(reset=True)
+        solve = None if args.no_solve else solve_phase(fq, torch, mesh, stream, args)
+    roofline = roofline_record(ctx, mesh, mats, ncells, ms, el_ms, sc_ms, el_n, sc_n)
+    e2e = None if args.no_e2e else e2e_phase(ctx, mesh, mats, flush, args, ncells, world)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cnc, ct, cores = cpu_assembly(NBOX, 1)
+        cpu = {"value": cnc / ct[0], "unit": "cells/s", "cores": cores, "kind": "port",
+               "sample": f"one full step ({cnc} tets, 4 forms), oracle C++/OpenMP assembly"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"kuhn {DIM}D {NBOX}^3 ({ncells} tets), jitter 0.1h seed {SEED}; step = M_1, M_2, "
+                               f"dif_both(2), dif_both(3) assembled from resident lengths",
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
+                   "setup_s_pattern_and_permutation": round(setup_s, 3)},
+        "roofline": roofline,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "wall_s_timed": wall,
+        "solve": solve,
+    }
+    if rank == 0:
+        print(json.dumps(line))
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * ncells / (ms * 1e-3)
-    (el_ms, sc_ms), (el_n, sc_n) = ctx.profile(reset=True)
+        torch.distributed.destroy_process_group()
 
-    # algorithmic bytes per launch of each kernel (per form, summed over forms)
+
+def roofline_record(ctx, mesh, mats, ncells, ms, el_ms, sc_ms, el_n, sc_n):
+    """Algorithmic bytes per launch of each kernel (per form, summed over the
+    step's forms) over its CUDA-event time on the launching stream."""
     n = DIM
     n1 = mesh.nsimplices(1)
     el_bytes = sc_bytes = fused_bytes = 0
-    fp64_flops = 0
     for (name, k), m in zip(FORMS, mats):
         lr, lc, sym = local_shape(n, name, k)
         nent = lr * (lr + 1) // 2 if sym else lr * lc
@@ -234,41 +264,64 @@ def run_ours(args):
         sc_bytes += ntrip * (8 + 4) + (nnz + 1) * 4 + nnz * (8 + 1)
         tg = k - 1 if name == "dif_both" else k
         fused_bytes += n1 * 8 + ncells * (n + 1) * 4 + ncells * 2 * comb(n + 1, tg + 1) * 4 + nnz * 8
-    el_avg = el_ms / max(el_n, 1) * len(FORMS)   # per step, all four forms
+    el_avg = el_ms / max(el_n, 1) * len(FORMS)  # per step, all forms
     sc_avg = sc_ms / max(sc_n, 1) * len(FORMS)
     hbm_peak, peak_src = measured_peaks()
     dominant = "element" if el_avg >= sc_avg else "scatter"
     dom_bytes, dom_ms = (el_bytes, el_avg) if dominant == "element" else (sc_bytes, sc_avg)
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    fp64_peak = ctx.fma_peak_tflops(True)
-    fp32_peak = ctx.fma_peak_tflops(False)
+    return {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+            "algorithmic_bytes_per_step": dom_bytes, "kernel_ms_per_step": dom_ms,
+            "element_ms_per_step": el_avg, "scatter_ms_per_step": sc_avg,
+            "element_bytes_per_step": el_bytes, "scatter_bytes_per_step": sc_bytes,
+            "scatter_GBps": sc_bytes / (sc_avg * 1e-3) / 1e9,
+            "fp64_fma_peak_tflops_measured": ctx.fma_peak_tflops(True),
+            "fp32_fma_peak_tflops_measured": ctx.fma_peak_tflops(False),
+            "fused_assembly_bytes_per_step": fused_bytes,
+            "fused_assembly_GBps": fused_bytes / (ms * 1e-3) / 1e9}
 
-    # ---- solve: mixed k=1 Hodge-Laplace, MINRES to 1e-10, resident problem ----
+
+def solve_phase(fq, torch, mesh, stream, args):
+    """Mixed k=1 Hodge-Laplace, MINRES to 1e-10 on the resident problem."""
     prob = fq.MixedProblem(mesh, 1, fq.FQ_ABSOLUTE, fq.FQ_FP64)
     ns, nu, nh, sys_nnz = prob.info()
     rng = np.random.default_rng(SEED)
     src = torch.tensor(rng.standard_normal(mesh.nsimplices(1)), device="cuda")
     sig = torch.empty(mesh.nsimplices(0), dtype=torch.float64, device="cuda")
     u = torch.empty(mesh.nsimplices(1), dtype=torch.float64, device="cuda")
-    opts = fq.SolveOpts.default(rtol=1e-10)
+    opts = fq.SolveOpts.default(rtol=1e-10, max_iters=args.max_iters)
+    torch.cuda.synchronize()
     prob.solve_device(src.data_ptr(), sig.data_ptr(), u.data_ptr(), 0, opts)  # warm-up
-    lat = []
-    reps = []
-    for i in range(args.solves):
+    lat, reps = [], []
+    for _ in range(args.solves):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        rep = prob.solve_device(src.data_ptr(), sig.data_ptr(), u.data_ptr(), 0, opts)
+        reps.append(prob.solve_device(src.data_ptr(), sig.data_ptr(), u.data_ptr(), 0, opts))
         b.record(stream)
         torch.cuda.synchronize()
         lat.append(a.elapsed_time(b))
-        reps.append(rep)
+    prob.close()
+    if not lat:
+        return None
     lat_sorted = sorted(lat)
 
     def pct(p):
         return lat_sorted[min(len(lat_sorted) - 1, int(math.ceil(p / 100 * len(lat_sorted))) - 1)]
 
-    # ---- e2e: the C-ABI call with host buffers (H2D lengths, D2H values) ----
+    return {"problem": f"mixed k=1 Hodge-Laplace, {ns + nu + nh} DOFs, {sys_nnz} nnz, MINRES rtol 1e-10, "
+                       "Jacobi of the H(d) Gram blocks",
+            "solves_per_s": 1e3 / (sum(lat) / len(lat)), "p50_ms": pct(50), "p99_ms": pct(99),
+            "iters": reps[-1].iters, "ms_per_iter": (sum(lat) / len(lat)) / max(reps[-1].iters, 1),
+            "true_residual": reps[-1].true_residual, "converged": all(r.converged for r in reps), "n": len(lat)}
+
+
+def e2e_phase(ctx, mesh, mats, flush, args, ncells, world):
+    """The same metric through the C-ABI call with host buffers: every step
+    uploads the lengths (H2D) and downloads every matrix's values (D2H)."""
     import ctypes
+
+    import torch
 
     lengths_h = torch.from_numpy(mesh.lengths_sq()).pin_memory()
     outs = [torch.empty(m.nnz, dtype=torch.float64).pin_memory() for m in mats]
@@ -290,48 +343,9 @@ def run_ours(args):
         e2e_step()
         e_ms.append((time.perf_counter() - t) * 1e3)
     e2e_ms = sum(e_ms) / len(e_ms)
-    h2d = len(mats) * lengths_h.numel() * 8
-    d2h = sum(o.numel() * 8 for o in outs)
-
-    # ---- CPU baseline (rank 0, N=1 only): the oracle on a bounded sample ----
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        cnc, ct, cores = cpu_assembly(NBOX, 1)
-        cpu = {"value": cnc / ct[0], "unit": "cells/s", "cores": cores, "kind": "port",
-               "sample": f"one full step ({cnc} tets, 4 forms), oracle C++/OpenMP assembly"}
-
-    line = {
-        "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"kuhn {DIM}D {NBOX}^3 ({ncells} tets), jitter 0.1h seed {SEED}; step = M_1, M_2, "
-                               f"dif_both(2), dif_both(3) assembled from resident lengths",
-                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
-                   "setup_s_pattern_and_permutation": round(setup_s, 3)},
-        "roofline": {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
-                     "algorithmic_bytes_per_step": dom_bytes, "kernel_ms_per_step": dom_ms,
-                     "element_ms_per_step": el_avg, "scatter_ms_per_step": sc_avg,
-                     "fp64_fma_peak_tflops_measured": fp64_peak, "fp32_fma_peak_tflops_measured": fp32_peak,
-                     "fused_assembly_bytes_per_step": fused_bytes,
-                     "fused_assembly_GBps": fused_bytes / (ms * 1e-3) / 1e9},
-        "e2e": {"value": world * ncells / (e2e_ms * 1e-3), "unit": "cells/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-        "cpu_baseline": cpu,
-        "gpu_launches": launches,
-        "clocks": clocks.summary(),
-        "wall_s_timed": wall,
-        "solve": {"problem": f"mixed k=1 Hodge-Laplace, {ns + nu + nh} DOFs, {sys_nnz} nnz, MINRES rtol 1e-10, "
-                             "Jacobi of the H(d) Gram blocks",
-                  "solves_per_s": 1e3 / (sum(lat) / len(lat)), "p50_ms": pct(50), "p99_ms": pct(99),
-                  "iters": reps[-1].iters, "true_residual": reps[-1].true_residual,
-                  "converged": all(r.converged for r in reps), "n": len(lat)},
-    }
-    if rank == 0:
-        print(json.dumps(line))
-    prob.close()
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    return {"value": world * ncells / (e2e_ms * 1e-3), "unit": "cells/s",
+            "h2d_bytes_per_step": len(mats) * lengths_h.numel() * 8,
+            "d2h_bytes_per_step": sum(o.numel() * 8 for o in outs), "ms_per_step": e2e_ms}
 
 
 def main():
@@ -341,7 +355,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--solves", type=int, default=5)
+    ap.add_argument("--max-iters", type=int, default=10000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-solve", action="store_true", help="skip the solve phase (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer phase (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
