@@ -174,7 +174,8 @@ def run_ours(args):
 
         dist.init_process_group("nccl")
     torch.cuda.set_device(local_rank)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # a real stream: the library launches on it and the events time it
+    torch.cuda.set_stream(stream)
     ctx = fq.Context(local_rank, stream=stream.cuda_stream)
     mesh = fq.Mesh.kuhn_cube(ctx, DIM, NBOX)
     mesh.kuhn_lengths(jitter=JITTER, seed=SEED + rank)

@@ -459,9 +459,82 @@ struct Workspace {
   SolverState* host_state = nullptr;
 };
 
-static fq_status poll_state(fq_ctx* ctx, const SolverState* dev, SolverState* host) {
-  FQ_CUDA(ctx, cudaMemcpyAsync(host, dev, sizeof(SolverState), cudaMemcpyDeviceToHost, ctx->stream));
-  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+
+// Runs `one_iteration(parity)` (the three kernels of one iteration, reading
+// state slot `parity` and writing slot 1 - parity) as a CUDA graph of two
+// iterations, relaunched until the device state says done. Convergence is
+// polled through pinned memory one batch behind the launches, so the device
+// always has the next batch queued; iterations after convergence are no-ops.
+template <typename F>
+static fq_status run_graph_loop(fq_ctx* ctx, SolverState* S, int64_t max_iters, F&& one_iteration,
+                                SolverState* final_state) {
+  cudaStream_t st = ctx->stream;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  // A stream that cannot be captured (the legacy default stream) falls back to
+  // direct launches of the same kernels.
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    one_iteration(0);
+    one_iteration(1);
+    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    if (ce != cudaSuccess) return cuda_check(ctx, ce, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return cuda_check(ctx, ce, "cudaGraphInstantiate");
+  } else {
+    cudaGetLastError();
+  }
+  SolverState* pinned = nullptr;
+  cudaEvent_t ev[2];
+  FQ_CUDA(ctx, cudaMallocHost(reinterpret_cast<void**>(&pinned), 2 * sizeof(SolverState)));
+  cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+  fq_status status = FQ_OK;
+  int64_t launched = 0;  // iterations enqueued
+  int64_t batch = 4;     // graph launches (x2 iterations) per batch
+  int slot = 0;
+  bool have_prev = false;
+  for (;;) {
+    const int64_t nlaunch = std::min<int64_t>(batch, (max_iters - launched + 1) / 2 + 1);
+    for (int64_t i = 0; i < nlaunch; ++i) {
+      cudaError_t e = cudaSuccess;
+      if (exec) {
+        e = cudaGraphLaunch(exec, st);
+      } else {
+        one_iteration(0);
+        one_iteration(1);
+        e = cudaGetLastError();
+      }
+      if (e != cudaSuccess) {
+        status = cuda_check(ctx, e, "iteration launch");
+        break;
+      }
+    }
+    if (status != FQ_OK) break;
+    ctx->launches += uint64_t(6 * nlaunch);
+    launched += 2 * nlaunch;
+    cudaMemcpyAsync(pinned + slot, S, sizeof(SolverState), cudaMemcpyDeviceToHost, st);
+    cudaEventRecord(ev[slot], st);
+    if (have_prev) {
+      cudaEventSynchronize(ev[1 - slot]);
+      if (pinned[1 - slot].done) break;
+    }
+    have_prev = true;
+    slot = 1 - slot;
+    if (launched > max_iters + 2) {
+      cudaEventSynchronize(ev[1 - slot]);
+      break;
+    }
+    batch = std::min<int64_t>(batch * 2, 64);
+  }
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  cudaError_t e = cudaMemcpy(final_state, S, sizeof(SolverState), cudaMemcpyDeviceToHost);
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  cudaFreeHost(pinned);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (status != FQ_OK) return status;
+  if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMemcpy state");
   return FQ_OK;
 }
 
@@ -496,37 +569,25 @@ fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT
   minres_init_state<<<1, KT, 0, st>>>(S, S + 1, m.partB, gv, rtol, (long long)max_iters);
   ctx->launches += 2;
   SolverState hs{};
-  int cur = 0;
-  int64_t launched = 0;
-  int64_t poll_every = 8;
-  for (;;) {
-    FQ_TRY(poll_state(ctx, S + cur, &hs));
-    if (hs.done || launched >= max_iters) break;
-    const int64_t batch = std::min<int64_t>(poll_every, max_iters - launched);
-    for (int64_t it = 0; it < batch; ++it) {
-      switch (W) {
-        case 4:
-          minres_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
-          break;
-        case 8:
-          minres_a<8, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
-          break;
-        case 16:
-          minres_a<16, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
-          break;
-        default:
-          minres_a<32, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
-          break;
-      }
-      minres_b<VT><<<gv, KT, 0, st>>>(m, S + cur, ga, n);
-      minres_c<VT><<<gv, KT, 0, st>>>(m, S + cur, S + (1 - cur), ga, gv, rtol, (long long)max_iters, n);
-      cur = 1 - cur;
-      ctx->launches += 3;
+  auto iteration = [&](int cur) {
+    switch (W) {
+      case 4:
+        minres_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+        break;
+      case 8:
+        minres_a<8, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+        break;
+      case 16:
+        minres_a<16, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+        break;
+      default:
+        minres_a<32, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+        break;
     }
-    launched += batch;
-    poll_every = std::min<int64_t>(poll_every * 2, 64);
-    FQ_CUDA(ctx, cudaGetLastError());
-  }
+    minres_b<VT><<<gv, KT, 0, st>>>(m, S + cur, ga, n);
+    minres_c<VT><<<gv, KT, 0, st>>>(m, S + cur, S + (1 - cur), ga, gv, rtol, (long long)max_iters, n);
+  };
+  FQ_TRY(run_graph_loop(ctx, S, max_iters, iteration, &hs));
   rep->iters = hs.iters;
   rep->residual = hs.residual;
   rep->converged = hs.converged;
@@ -563,36 +624,25 @@ fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* va
   cg_init_state<<<1, KT, 0, st>>>(S, S + 1, c.partB, c.partC, gv, rtol, (long long)max_iters);
   ctx->launches += 2;
   SolverState hs{};
-  int cur = 0;
-  int64_t launched = 0, poll_every = 8;
-  for (;;) {
-    FQ_TRY(poll_state(ctx, S + cur, &hs));
-    if (hs.done || launched >= max_iters) break;
-    const int64_t batch = std::min<int64_t>(poll_every, max_iters - launched);
-    for (int64_t it = 0; it < batch; ++it) {
-      switch (W) {
-        case 4:
-          cg_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
-          break;
-        case 8:
-          cg_a<8, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
-          break;
-        case 16:
-          cg_a<16, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
-          break;
-        default:
-          cg_a<32, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
-          break;
-      }
-      cg_b<VT><<<gv, KT, 0, st>>>(c, S + cur, ga, n);
-      cg_c<VT><<<gv, KT, 0, st>>>(c, S + cur, S + (1 - cur), gv, rtol, (long long)max_iters, n);
-      cur = 1 - cur;
-      ctx->launches += 3;
+  auto iteration = [&](int cur) {
+    switch (W) {
+      case 4:
+        cg_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
+        break;
+      case 8:
+        cg_a<8, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
+        break;
+      case 16:
+        cg_a<16, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
+        break;
+      default:
+        cg_a<32, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
+        break;
     }
-    launched += batch;
-    poll_every = std::min<int64_t>(poll_every * 2, 64);
-    FQ_CUDA(ctx, cudaGetLastError());
-  }
+    cg_b<VT><<<gv, KT, 0, st>>>(c, S + cur, ga, n);
+    cg_c<VT><<<gv, KT, 0, st>>>(c, S + cur, S + (1 - cur), gv, rtol, (long long)max_iters, n);
+  };
+  FQ_TRY(run_graph_loop(ctx, S, max_iters, iteration, &hs));
   rep->iters = hs.iters;
   rep->residual = hs.residual;
   rep->converged = hs.converged;
