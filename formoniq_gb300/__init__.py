@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 from dataclasses import dataclass
 from typing import Optional
 
@@ -135,6 +136,7 @@ _SIGNATURES = {
     "fq_hdif_gram": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
     "fq_coboundary": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
     "fq_assemble_host": (ctypes.c_int, [_P, _P, _P, _DP, _P]),
+    "fq_reassemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P]),
     "fq_matrix_info": (ctypes.c_int, [_P, _I64P, _I64P, _I64P, ctypes.POINTER(ctypes.c_int)]),
     "fq_matrix_device_arrays": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     "fq_matrix_copy_to_host": (ctypes.c_int, [_P, _P, _I32P, _I32P, _P]),
@@ -193,6 +195,14 @@ class Context:
             raise FqError(s, "fq_ctx_create")
         self.h = h
         self.L = L
+        # native objects made on this context, closed before it (the C ABI needs
+        # meshes, matrices and problems destroyed before their context)
+        self._children = weakref.WeakSet()
+        self._meshes = weakref.WeakSet()
+
+    def _adopt(self, obj, mesh: bool = False):
+        (self._meshes if mesh else self._children).add(obj)
+        return obj
 
     def check(self, status: int, what: str = ""):
         if status != 0:
@@ -227,6 +237,12 @@ class Context:
 
     def close(self):
         if getattr(self, "h", None):
+            for group in (self._children, self._meshes):
+                for obj in list(group):
+                    try:
+                        obj.close()
+                    except Exception:
+                        pass
             self.L.fq_ctx_destroy(self.h)
             self.h = None
 
@@ -242,6 +258,8 @@ class Matrix:
 
     def __init__(self, ctx: Context, h, owned: bool = True):
         self.ctx, self.h, self.owned = ctx, h, owned
+        if owned:
+            ctx._adopt(self)
 
     def info(self):
         nr, nc, nnz, pr = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
@@ -285,6 +303,12 @@ class Matrix:
     def reassemble(self, mesh: "Mesh"):
         self.ctx.check(self.ctx.L.fq_reassemble(self.ctx.h, mesh.h, self.h), "fq_reassemble")
 
+    def reassemble_noalloc(self, mesh: "Mesh", values_ptr: int):
+        """Values of this matrix's pattern into a caller-owned device buffer,
+        with no device allocation (see fq_reassemble_noalloc)."""
+        self.ctx.check(self.ctx.L.fq_reassemble_noalloc(self.ctx.h, mesh.h, self.h, _P(values_ptr)),
+                       "fq_reassemble_noalloc")
+
     def close(self):
         if self.owned and getattr(self, "h", None):
             self.ctx.L.fq_matrix_destroy(self.h)
@@ -302,6 +326,7 @@ class Mesh:
 
     def __init__(self, ctx: Context, h):
         self.ctx, self.h = ctx, h
+        ctx._adopt(self, mesh=True)
 
     @staticmethod
     def from_cells(ctx: Context, cells: np.ndarray) -> "Mesh":
@@ -438,6 +463,7 @@ class MixedProblem:
         self.ctx.check(self.ctx.L.fq_mixed_create(self.ctx.h, mesh.h, grade, bc, precision, ctypes.byref(h)),
                        "fq_mixed_create")
         self.h = h
+        self.ctx._adopt(self)
 
     def info(self):
         a, b, c, d = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

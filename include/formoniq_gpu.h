@@ -87,6 +87,7 @@ typedef struct fq_report {
 
 /* ---- context ------------------------------------------------------------ */
 fq_status fq_ctx_create(int device, void* cuda_stream, uint64_t hbm_budget_bytes, fq_ctx** out);
+/* Destroy every mesh, matrix and mixed problem made on a context first. */
 void fq_ctx_destroy(fq_ctx* ctx);
 const char* fq_status_name(fq_status s);
 const char* fq_ctx_last_error(const fq_ctx* ctx);
@@ -179,6 +180,21 @@ fq_status fq_coboundary(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, fq_matr
  * values_out. The pattern comes from fq_matrix_copy_to_host of a prior fq_assemble. */
 fq_status fq_assemble_host(fq_ctx* ctx, fq_mesh* mesh, fq_matrix* mat, const double* lengths_sq_host,
                            void* values_out_host);
+
+/* Re-assembly that allocates no device memory. It has no counterpart in the
+ * reference. For callers that cannot let this library call cudaMalloc (a host
+ * that owns all device memory through its own arena, or a latency-critical loop
+ * where an allocation would synchronise the device): the per-cell element
+ * buffer lives in a static device array of 32 MiB that every GPU loading the
+ * library holds until exit, and the values (nnz of `pattern`, its precision)
+ * are written to the caller's device buffer `values_out` in the CSR order of
+ * `pattern`, a matrix fq_assemble made on this mesh. Rejects, with
+ * FQ_INVALID_ARG and a message, a mesh whose element buffer plus one byte per
+ * slot exceeds the array; returns FQ_UNSUPPORTED when the exact-zero rule
+ * would change the pattern. The first call on a device looks up the array's
+ * device address and should come before any stream capture. All calls share
+ * the array: calls whose work overlaps on the GPU race. */
+fq_status fq_reassemble_noalloc(fq_ctx* ctx, fq_mesh* mesh, const fq_matrix* pattern, void* values_out);
 
 fq_status fq_matrix_info(const fq_matrix* m, int64_t* nrows, int64_t* ncols, int64_t* nnz, int* precision);
 fq_status fq_matrix_device_arrays(const fq_matrix* m, const int32_t** row_ptr, const int32_t** col_idx,
