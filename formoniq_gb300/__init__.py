@@ -26,7 +26,7 @@ from typing import Optional
 import numpy as np
 
 __all__ = [
-    "FQ_MASS", "FQ_DIF_TRIAL", "FQ_DIF_TEST", "FQ_DIF_BOTH", "FQ_ABSOLUTE", "FQ_RELATIVE", "FQ_FP64", "FQ_FP32",
+    "FQ_MASS", "FQ_DIF_TRIAL", "FQ_DIF_TEST", "FQ_DIF_BOTH", "FQ_ABSOLUTE", "FQ_RELATIVE", "FQ_FP64", "FQ_FP32", "FQ_FP64_IEEE",
     "FqError", "FqUnavailable", "Context", "Mesh", "Matrix", "WhitneyComplex", "MixedProblem", "SolveOpts",
     "Report", "solve_source", "solve_dirac_source", "dirac_system", "minres", "cg", "lib_path", "load",
     "exported_symbols",
@@ -34,7 +34,7 @@ __all__ = [
 
 FQ_MASS, FQ_DIF_TRIAL, FQ_DIF_TEST, FQ_DIF_BOTH = 0, 1, 2, 3
 FQ_ABSOLUTE, FQ_RELATIVE = 0, 1
-FQ_FP64, FQ_FP32 = 0, 1
+FQ_FP64, FQ_FP32, FQ_FP64_IEEE = 0, 1, 2
 
 _STATUS = {
     0: "FQ_OK", 1: "FQ_INVALID_ARG", 2: "FQ_DEGENERATE_CELL", 3: "FQ_NOT_CONVERGED", 4: "FQ_BREAKDOWN",

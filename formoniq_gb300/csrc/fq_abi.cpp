@@ -281,7 +281,7 @@ static fq_status mixed_assemble(fq_mixed* P) {
   const int64_t n0 = P->ns + P->nu;
   FQ_TRY(P->diag.alloc(ctx, std::max<int64_t>(P->n, 1) * 8));
   FQ_TRY(P->dinv.alloc(ctx, std::max<int64_t>(P->n, 1) * 8));
-  launch_scatter_diag(*P->kkt->plan, m->elem.p, P->diag.as<double>(), 0, ctx->stream);
+  launch_scatter_diag(*P->kkt->plan, m->elem.p, P->diag.as<double>(), P->kkt->precision, ctx->stream);
   ctx->launches++;
   if (P->nh) vec_fill(P->diag.as<double>() + n0, 1.0, P->nh, ctx->stream);
   FQ_TRY(mixed_harmonic(P));
@@ -692,20 +692,22 @@ fq_status fq_element_matrices(fq_ctx* ctx, fq_mesh* m, fq_form form, int grade, 
   if (lr == 0 || lc == 0 || grade > n) return FQ_OK;
   const int kind = int(form);
   Layout lay = make_layout(n, kind, grade);
-  const int fp32 = prec == FQ_FP32;
+  const int mode = int(prec);
   FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
-  FQ_TRY(element_pass(ctx, m, kind, grade, fp32, 0.0, m->elem, lay.nent));
+  FQ_TRY(element_pass(ctx, m, kind, grade, mode, 0.0, m->elem, lay.nent));
   // expand packed/full entries into row-major [lr*lc][ncells]
-  const size_t w = fp32 ? 4 : 8;
+  const size_t w = mode == FQ_FP32 ? 4 : 8;
   for (int i = 0; i < lr; ++i)
     for (int j = 0; j < lc; ++j) {
       const int e = lay.entry[size_t(i) * lc + j];
       char* dst = static_cast<char*>(out) + (size_t(i) * lc + j) * m->ncells * w;
+      const char* src = m->elem.as<char>() + size_t(e) * m->ncells * w;
       if (e < 0)
         FQ_CUDA(ctx, cudaMemsetAsync(dst, 0, m->ncells * w, ctx->stream));
+      else if (mode == FQ_FP64)
+        launch_df64_to_double(src, reinterpret_cast<double*>(dst), m->ncells, ctx->stream);
       else
-        FQ_CUDA(ctx, cudaMemcpyAsync(dst, m->elem.as<char>() + size_t(e) * m->ncells * w, m->ncells * w,
-                                     cudaMemcpyDeviceToDevice, ctx->stream));
+        FQ_CUDA(ctx, cudaMemcpyAsync(dst, src, m->ncells * w, cudaMemcpyDeviceToDevice, ctx->stream));
     }
   FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -721,6 +723,7 @@ fq_status fq_assemble(fq_ctx* ctx, fq_mesh* m, fq_form form, int grade, fq_bc bc
   if (!ctx || !m || !out) return FQ_INVALID_ARG;
   *out = nullptr;
   if (int(form) < 0 || int(form) > 3) return set_error(ctx, FQ_INVALID_ARG, "unknown form");
+  if (int(prec) < 0 || int(prec) > 2) return set_error(ctx, FQ_INVALID_ARG, "unknown precision");
   FQ_GUARD_BEGIN
   int64_t rows = 0, cols = 0;
   if (!valid_form_shape(m, form, grade, bc, &rows, &cols) || grade > m->dim)
@@ -882,7 +885,7 @@ fq_status fq_spmv(fq_ctx* ctx, const fq_matrix* a, const void* x, void* y) {
 
 static fq_status check_square(fq_ctx* ctx, const fq_matrix* a) {
   if (a->nrows != a->ncols) return set_error(ctx, FQ_INVALID_ARG, "operator must be square");
-  if (a->precision != FQ_FP64) return set_error(ctx, FQ_INVALID_ARG, "solver takes an FP64 operator");
+  if (a->precision == FQ_FP32) return set_error(ctx, FQ_INVALID_ARG, "solver takes an FP64 operator");
   return FQ_OK;
 }
 

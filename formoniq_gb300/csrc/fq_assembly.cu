@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <vector>
 
+#include "fq_df64.cuh"
 #include "fq_element_kernel.cuh"
 #include "fq_internal.h"
 
@@ -423,66 +424,95 @@ fq_status build_plan(fq_ctx* ctx, fq_mesh* m, Plan& plan, const Layout& lay) {
 // ---------------------------------------------------------------------------
 // Hot loop: scatter
 // ---------------------------------------------------------------------------
-template <typename T>
+// The exact-zero test of the reference's `val != 0.0` rule on the bit pattern:
+// integer instructions instead of an FP64 compare, +0.0 and -0.0 both zero.
+__device__ __forceinline__ bool nonzero_bits(double v) { return (__double_as_longlong(v) << 1) != 0; }
+__device__ __forceinline__ bool nonzero_bits(float v) { return (__float_as_int(v) << 1) != 0; }
+__device__ __forceinline__ bool nonzero_bits(df64 v) { return nonzero_bits(v.hi) || nonzero_bits(v.lo); }
+__device__ __forceinline__ double store_value(double v) { return v; }
+__device__ __forceinline__ float store_value(float v) { return v; }
+__device__ __forceinline__ double store_value(df64 v) { return v.to_double(); }
+
+// One thread per CSR slot; contributions summed in cell order. E is the element
+// type (df64, float or double), V the stored value type.
+template <typename E, typename V>
 __global__ void __launch_bounds__(256) scatter_kernel(const int32_t* __restrict__ slot_ptr,
-                                                      const int32_t* __restrict__ perm, const T* __restrict__ elem,
-                                                      T* __restrict__ values, uint8_t* __restrict__ zflag,
+                                                      const int32_t* __restrict__ perm, const E* __restrict__ elem,
+                                                      V* __restrict__ values, uint8_t* __restrict__ zflag,
                                                       int* zero_count, int64_t nslots) {
   const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (s >= nslots) return;
   const int b = __ldg(slot_ptr + s), e = __ldg(slot_ptr + s + 1);
-  T acc = T(0);
+  E acc = E(0);
   bool nz = false;
   for (int t = b; t < e; ++t) {
-    const T v = __ldg(elem + __ldg(perm + t));
+    const E v = elem[__ldg(perm + t)];
     acc += v;
-    nz |= (v != T(0));
+    nz |= nonzero_bits(v);
   }
-  values[s] = acc;
+  values[s] = store_value(acc);
   zflag[s] = nz ? 0 : 1;
   if (!nz) atomicAdd(zero_count, 1);
 }
 
-template <typename T>
+template <typename E>
 __global__ void __launch_bounds__(256) scatter_diag_kernel(const int32_t* __restrict__ ptr,
                                                            const int32_t* __restrict__ perm,
-                                                           const T* __restrict__ elem, double* __restrict__ out,
+                                                           const E* __restrict__ elem, double* __restrict__ out,
                                                            int64_t n) {
   const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const int b = __ldg(ptr + s), e = __ldg(ptr + s + 1);
-  T acc = T(0);
-  for (int t = b; t < e; ++t) acc += __ldg(elem + __ldg(perm + t));
-  out[s] = double(acc);
+  E acc = E(0);
+  for (int t = b; t < e; ++t) acc += elem[__ldg(perm + t)];
+  out[s] = double(store_value(acc));
+}
+
+__global__ void df64_to_double_kernel(const df64* __restrict__ in, double* __restrict__ out, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    out[i] = in[i].to_double();
+}
+
+void launch_df64_to_double(const void* in, double* out, int64_t n, cudaStream_t st) {
+  if (n <= 0) return;
+  const int g = int(std::min<int64_t>((n + 255) / 256, 152 * 16));
+  df64_to_double_kernel<<<g, 256, 0, st>>>(static_cast<const df64*>(in), out, n);
 }
 
 void launch_scatter(const Plan& plan, const void* elem, void* values, uint8_t* zero_flags, int* zero_count,
-                    int fp32, cudaStream_t st) {
+                    int mode, cudaStream_t st) {
   if (plan.nslots == 0) return;
   const int threads = 256;
   const unsigned blocks = unsigned((plan.nslots + threads - 1) / threads);
-  if (fp32)
-    scatter_kernel<float><<<blocks, threads, 0, st>>>(plan.slot_ptr.as<int32_t>(), plan.perm.as<int32_t>(),
-                                                      static_cast<const float*>(elem), static_cast<float*>(values),
-                                                      zero_flags, zero_count, plan.nslots);
+  const int32_t* sp = plan.slot_ptr.as<int32_t>();
+  const int32_t* pm = plan.perm.as<int32_t>();
+  if (mode == 1)
+    scatter_kernel<float, float><<<blocks, threads, 0, st>>>(sp, pm, static_cast<const float*>(elem),
+                                                             static_cast<float*>(values), zero_flags, zero_count,
+                                                             plan.nslots);
+  else if (mode == 2)
+    scatter_kernel<double, double><<<blocks, threads, 0, st>>>(sp, pm, static_cast<const double*>(elem),
+                                                               static_cast<double*>(values), zero_flags, zero_count,
+                                                               plan.nslots);
   else
-    scatter_kernel<double><<<blocks, threads, 0, st>>>(plan.slot_ptr.as<int32_t>(), plan.perm.as<int32_t>(),
-                                                       static_cast<const double*>(elem),
-                                                       static_cast<double*>(values), zero_flags, zero_count,
-                                                       plan.nslots);
+    scatter_kernel<df64, double><<<blocks, threads, 0, st>>>(sp, pm, static_cast<const df64*>(elem),
+                                                             static_cast<double*>(values), zero_flags, zero_count,
+                                                             plan.nslots);
 }
 
-void launch_scatter_diag(const Plan& plan, const void* elem, double* out, int fp32, cudaStream_t st) {
+void launch_scatter_diag(const Plan& plan, const void* elem, double* out, int mode, cudaStream_t st) {
   if (plan.nrows == 0) return;
   const int threads = 256;
   const unsigned blocks = unsigned((plan.nrows + threads - 1) / threads);
-  if (fp32)
-    scatter_diag_kernel<float><<<blocks, threads, 0, st>>>(plan.diag_ptr.as<int32_t>(), plan.diag_perm.as<int32_t>(),
-                                                           static_cast<const float*>(elem), out, plan.nrows);
+  const int32_t* dp = plan.diag_ptr.as<int32_t>();
+  const int32_t* pm = plan.diag_perm.as<int32_t>();
+  if (mode == 1)
+    scatter_diag_kernel<float><<<blocks, threads, 0, st>>>(dp, pm, static_cast<const float*>(elem), out, plan.nrows);
+  else if (mode == 2)
+    scatter_diag_kernel<double><<<blocks, threads, 0, st>>>(dp, pm, static_cast<const double*>(elem), out,
+                                                            plan.nrows);
   else
-    scatter_diag_kernel<double><<<blocks, threads, 0, st>>>(plan.diag_ptr.as<int32_t>(),
-                                                            plan.diag_perm.as<int32_t>(),
-                                                            static_cast<const double*>(elem), out, plan.nrows);
+    scatter_diag_kernel<df64><<<blocks, threads, 0, st>>>(dp, pm, static_cast<const df64*>(elem), out, plan.nrows);
 }
 
 // ---------------------------------------------------------------------------
@@ -548,27 +578,36 @@ fq_status compact_csr(fq_ctx* ctx, fq_matrix* m, int64_t nzero) {
 // ---------------------------------------------------------------------------
 // Element pass and assembly driver
 // ---------------------------------------------------------------------------
-int launch_element(int n, int grade, int kind, int fp32, const ElemArgs& a, cudaStream_t st) {
+template <int N>
+static int launch_dim(int grade, int kind, int mode, const ElemArgs& a, cudaStream_t st) {
+  // The 4D Dirac program (all five grades coupled, 31 local dofs) runs in IEEE
+  // double: no configuration needs it fast and its float-float build is large.
+  if (kind == EK_METRIC || mode == 2 || (N == 4 && kind == EK_DIRAC)) return launch_typed<N, double>(grade, kind, a, st);
+  if (mode == 1) return launch_typed<N, float>(grade, kind, a, st);
+  return launch_typed<N, df64>(grade, kind, a, st);
+}
+
+int launch_element(int n, int grade, int kind, int mode, const ElemArgs& a, cudaStream_t st) {
   switch (n) {
     case 0:
-      return launch_element_dim<0>(grade, kind, fp32, a, st);
+      return launch_dim<0>(grade, kind, mode, a, st);
     case 1:
-      return launch_element_dim<1>(grade, kind, fp32, a, st);
+      return launch_dim<1>(grade, kind, mode, a, st);
     case 2:
-      return launch_element_dim<2>(grade, kind, fp32, a, st);
+      return launch_dim<2>(grade, kind, mode, a, st);
     case 3:
-      return launch_element_dim<3>(grade, kind, fp32, a, st);
+      return launch_dim<3>(grade, kind, mode, a, st);
     case 4:
-      return launch_element_dim<4>(grade, kind, fp32, a, st);
+      return launch_dim<4>(grade, kind, mode, a, st);
     default:
       return -1;
   }
 }
 
-fq_status element_pass(fq_ctx* ctx, fq_mesh* m, int kind, int grade, int fp32, double param, DevBuf& buf,
+fq_status element_pass(fq_ctx* ctx, fq_mesh* m, int kind, int grade, int mode, double param, DevBuf& buf,
                        int nent) {
   if (!m->has_lengths) return set_error(ctx, FQ_INVALID_ARG, "mesh has no edge lengths");
-  const size_t need = size_t(std::max(nent, 1)) * size_t(std::max<int64_t>(m->ncells, 1)) * (fp32 ? 4 : 8);
+  const size_t need = size_t(std::max(nent, 1)) * size_t(std::max<int64_t>(m->ncells, 1)) * (mode == 1 ? 4 : 8);
   if (buf.bytes < need) FQ_TRY(buf.alloc(ctx, need));
   ElemArgs a;
   a.ncells = m->ncells;
@@ -579,7 +618,7 @@ fq_status element_pass(fq_ctx* ctx, fq_mesh* m, int kind, int grade, int fp32, d
   a.param = param;
   a.status = ctx->status.as<int>();
   a.nent = nent;
-  if (launch_element(m->dim, grade, kind, fp32, a, ctx->stream) != 0)
+  if (launch_element(m->dim, grade, kind, mode, a, ctx->stream) != 0)
     return set_error(ctx, FQ_UNSUPPORTED, "no element program for this dimension/grade");
   ctx->launches++;
   FQ_CUDA(ctx, cudaGetLastError());
@@ -609,8 +648,8 @@ fq_status get_plan(fq_ctx* ctx, fq_mesh* m, int kind, int grade, int row_bc, int
 fq_status assemble_into(fq_ctx* ctx, fq_matrix* m) {
   fq_mesh* mesh = m->mesh;
   Plan& p = *m->plan;
-  const int fp32 = m->precision == FQ_FP32;
-  const size_t w = fp32 ? 4 : 8;
+  const int mode = m->precision;
+  const size_t w = mode == FQ_FP32 ? 4 : 8;
   if (m->full_values.bytes < size_t(std::max<int64_t>(p.nslots, 1)) * w)
     FQ_TRY(m->full_values.alloc(ctx, std::max<int64_t>(p.nslots, 1) * w));
   if (m->zero_flags.bytes < size_t(std::max<int64_t>(p.nslots, 1)))
@@ -619,10 +658,10 @@ fq_status assemble_into(fq_ctx* ctx, fq_matrix* m) {
   FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
   const bool prof = ctx->profiling && ctx->ev[0];
   if (prof) FQ_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
-  if (p.nslots > 0 || p.ndiag_trip > 0) FQ_TRY(element_pass(ctx, mesh, m->kind, m->grade, fp32, m->param, mesh->elem, p.nent));
+  if (p.nslots > 0 || p.ndiag_trip > 0) FQ_TRY(element_pass(ctx, mesh, m->kind, m->grade, mode, m->param, mesh->elem, p.nent));
   if (prof) FQ_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
   if (prof) FQ_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
-  launch_scatter(p, mesh->elem.p, m->full_values.p, m->zero_flags.as<uint8_t>(), zc, fp32, ctx->stream);
+  launch_scatter(p, mesh->elem.p, m->full_values.p, m->zero_flags.as<uint8_t>(), zc, mode, ctx->stream);
   if (prof) FQ_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
   if (p.nslots > 0) ctx->launches++;
   FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost,

@@ -6,6 +6,7 @@
 
 #include <cmath>
 
+#include "fq_df64.cuh"
 #include "fq_element.cuh"
 #include "fq_kinds.h"
 
@@ -193,8 +194,8 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs a) {
   }
 }
 
-// Launch helper for one dimension, every program and grade.
-template <int N>
-int launch_element_dim(int K, int kind, int fp32, const ElemArgs& a, cudaStream_t st);
+// Launch helper for one dimension and arithmetic type, every program and grade.
+template <int N, typename T>
+int launch_typed(int K, int kind, const ElemArgs& a, cudaStream_t st);
 
 }  // namespace fq

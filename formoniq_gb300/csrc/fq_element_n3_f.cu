@@ -1,0 +1,7 @@
+// Element programs for cell dimension 3 in float arithmetic.
+#define FQ_ELEM_T float
+#include "fq_element_dispatch.cuh"
+
+namespace fq {
+template int launch_typed<3, float>(int K, int kind, const ElemArgs& a, cudaStream_t st);
+}  // namespace fq

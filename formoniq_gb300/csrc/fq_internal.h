@@ -149,7 +149,8 @@ fq_status cuda_check(fq_ctx* ctx, cudaError_t e, const char* what);
 
 // ---- device entry points (implemented in .cu files) ----
 struct ElemArgs;
-int launch_element(int n, int grade, int kind, int fp32, const ElemArgs& a, cudaStream_t st);
+// mode = fq_precision: 0 float-float compute with FP64 values, 1 FP32, 2 IEEE FP64.
+int launch_element(int n, int grade, int kind, int mode, const ElemArgs& a, cudaStream_t st);
 
 // Build the scatter plan on the device (sort with CUB).
 fq_status build_plan(fq_ctx* ctx, fq_mesh* mesh, Plan& plan, const Layout& lay);
@@ -157,13 +158,14 @@ fq_status build_plan(fq_ctx* ctx, fq_mesh* mesh, Plan& plan, const Layout& lay);
 // values[s] = sum of elem[perm[t]] over the slot's contributions; zero_flags[s]
 // = 1 when every contribution was exactly 0.0; *zero_count += count.
 void launch_scatter(const Plan& plan, const void* elem, void* values, uint8_t* zero_flags, int* zero_count,
-                    int fp32, cudaStream_t st);
-void launch_scatter_diag(const Plan& plan, const void* elem, double* out, int fp32, cudaStream_t st);
+                    int mode, cudaStream_t st);
+void launch_scatter_diag(const Plan& plan, const void* elem, double* out, int mode, cudaStream_t st);
+void launch_df64_to_double(const void* in, double* out, int64_t n, cudaStream_t st);
 
 // Compaction: drop slots whose flag is set.
 fq_status compact_csr(fq_ctx* ctx, fq_matrix* m, int64_t nzero);
 
-fq_status element_pass(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int fp32, double param, DevBuf& buf,
+fq_status element_pass(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int mode, double param, DevBuf& buf,
                        int nent);
 fq_status get_plan(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int row_bc, int col_bc, Plan** out);
 fq_status assemble_into(fq_ctx* ctx, fq_matrix* m);

@@ -66,8 +66,8 @@ extern "C" fq_status fq_reassemble_noalloc(fq_ctx* ctx, fq_mesh* mesh, const fq_
     return set_error(ctx, FQ_UNSUPPORTED, "pattern was compacted (exact-zero slots); use fq_reassemble");
   if (!mesh->has_lengths) return set_error(ctx, FQ_INVALID_ARG, "mesh has no edge lengths");
   const Plan& p = *pattern->plan;
-  const int fp32 = pattern->precision == FQ_FP32;
-  const size_t w = fp32 ? 4 : 8;
+  const int mode = pattern->precision;
+  const size_t w = mode == FQ_FP32 ? 4 : 8;
   const size_t elem_bytes = (size_t(p.nent) * size_t(mesh->ncells) * w + 255) & ~size_t(255);
   const size_t need = elem_bytes + size_t(p.nslots);
   if (need > kNoAllocScratchBytes)
@@ -90,11 +90,11 @@ extern "C" fq_status fq_reassemble_noalloc(fq_ctx* ctx, fq_mesh* mesh, const fq_
     a.param = pattern->param;
     a.status = ctx->status.as<int>();
     a.nent = p.nent;
-    if (launch_element(mesh->dim, pattern->grade, pattern->kind, fp32, a, st) != 0)
+    if (launch_element(mesh->dim, pattern->grade, pattern->kind, mode, a, st) != 0)
       return set_error(ctx, FQ_UNSUPPORTED, "no element program for this dimension/grade");
     ctx->launches++;
     FQ_CUDA(ctx, cudaGetLastError());
-    launch_scatter(p, base, values_out, base + elem_bytes, ctx->status.as<int>() + 1, fp32, st);
+    launch_scatter(p, base, values_out, base + elem_bytes, ctx->status.as<int>() + 1, mode, st);
     ctx->launches++;
     FQ_CUDA(ctx, cudaGetLastError());
   }

@@ -58,8 +58,11 @@ typedef enum fq_bc {
 } fq_bc;
 
 typedef enum fq_precision {
-  FQ_FP64 = 0, /* everything in FP64 */
-  FQ_FP32 = 1  /* FP64 Gram inverse/determinant, FP32 element matrices and values */
+  FQ_FP64 = 0,      /* FP64 values; Gram inverse and determinant in IEEE double, element
+                       entries and scatter sums in float-float (48-bit significand) on
+                       the FP32 pipe, well inside the 1e-12 relative element tolerance */
+  FQ_FP32 = 1,      /* FP64 Gram inverse/determinant, FP32 element matrices and values */
+  FQ_FP64_IEEE = 2  /* FP64 values computed in IEEE double throughout */
 } fq_precision;
 
 typedef struct fq_ctx fq_ctx;

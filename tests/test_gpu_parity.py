@@ -142,10 +142,13 @@ def test_element_matrices(oracle, ctx, dim, prec):
 
 @pytest.mark.parametrize("dim,nb", [(1, 5), (2, 4), (3, 3), (4, 2)])
 @pytest.mark.parametrize("relative", [False, True])
-def test_assembly_parity_jittered(oracle, ctx, dim, nb, relative):
+@pytest.mark.parametrize("prec", [fq.FQ_FP64, fq.FQ_FP64_IEEE])
+def test_assembly_parity_jittered(oracle, ctx, dim, nb, relative, prec):
+    """FQ_FP64 computes element entries and scatter sums in float-float on the
+    FP32 pipe; FQ_FP64_IEEE in IEEE double. Both must meet the 1e-12 bar."""
     cx, mesh, lengths, _ = make_pair(oracle, ctx, dim, nb, jitter=0.1, seed=dim * 10 + nb)
     owc = oracle.WhitneyComplex(cx, lengths, relative=relative)
-    gwc = fq.WhitneyComplex(mesh, relative=relative)
+    gwc = fq.WhitneyComplex(mesh, relative=relative, precision=prec)
     for grade in range(-1, dim + 2):
         for name in ("mass", "dif_trial", "dif_test", "dif_both"):
             a = getattr(owc, name)(grade)
