@@ -1,14 +1,16 @@
-// Compile-time dispatch of the element programs for one dimension N.
+// Compile-time dispatch of the element programs for one dimension N and one
+// arithmetic type T. Every template here takes T explicitly, so the instances
+// made in different translation units (one per (N, T)) have distinct names.
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "fq_element_kernel.cuh"
 
 namespace fq {
 
-// One arithmetic type per translation unit: launch_typed<N, T> is defined by
-// instantiating this header in fq_element_n{N}_{df,f,d}.cu.
 template <int N, int K, int KIND, typename T>
 int launch_one_t(const ElemArgs& a, cudaStream_t st) {
   constexpr int threads = 128;
@@ -18,54 +20,46 @@ int launch_one_t(const ElemArgs& a, cudaStream_t st) {
   return 0;
 }
 
+// Programs of a (dimension, type) that live in their own translation unit to
+// bound compile time: the float-float 4D mixed-system and H(d) Gram programs.
+int launch_kkt_n4_df(int K, const ElemArgs& a, cudaStream_t st);
+int launch_hdif_n4_df(int K, const ElemArgs& a, cudaStream_t st);
+
 template <int N, typename T>
-int launch_typed(int K, int kind, const ElemArgs& a, cudaStream_t st);
-
-// mode: 0 float-float (df64), 1 float, 2 IEEE double; the metric kernel is double.
-template <int N, int K, int KIND>
-int launch_one(int mode, const ElemArgs& a, cudaStream_t st) {
-  (void)mode;
-  return launch_one_t<N, K, KIND, FQ_ELEM_T>(a, st);
+constexpr bool split_n4_df() {
+  return N == 4 && std::is_same<T, df64>::value;
 }
-#ifdef FQ_SPLIT_KKT
-// The mixed-system program of this (dimension, type) lives in its own
-// translation unit (compile time).
-int launch_kkt_split(int K, const ElemArgs& a, cudaStream_t st);
-int launch_hdif_split(int K, const ElemArgs& a, cudaStream_t st);
-#endif
 
-template <int N, int K>
-int launch_k(int kind, int mode, const ElemArgs& a, cudaStream_t st) {
+template <int N, int K, typename T>
+int launch_k_t(int kind, const ElemArgs& a, cudaStream_t st) {
   switch (kind) {
     case EK_MASS:
-      return launch_one<N, K, EK_MASS>(mode, a, st);
+      return launch_one_t<N, K, EK_MASS, T>(a, st);
     case EK_HDIF:
-#ifdef FQ_SPLIT_KKT
-      return launch_hdif_split(K, a, st);
-#else
-      return launch_one<N, K, EK_HDIF>(mode, a, st);
-#endif
+      if constexpr (split_n4_df<N, T>())
+        return launch_hdif_n4_df(K, a, st);
+      else
+        return launch_one_t<N, K, EK_HDIF, T>(a, st);
     case EK_KKT:
-#ifdef FQ_SPLIT_KKT
-      return launch_kkt_split(K, a, st);
-#else
-      return launch_one<N, K, EK_KKT>(mode, a, st);
-#endif
+      if constexpr (split_n4_df<N, T>())
+        return launch_kkt_n4_df(K, a, st);
+      else
+        return launch_one_t<N, K, EK_KKT, T>(a, st);
     case EK_DIF_BOTH:
-      if constexpr (K >= 1) return launch_one<N, K, EK_DIF_BOTH>(mode, a, st);
+      if constexpr (K >= 1) return launch_one_t<N, K, EK_DIF_BOTH, T>(a, st);
       break;
     case EK_DIF_TEST:
-      if constexpr (K >= 1) return launch_one<N, K, EK_DIF_TEST>(mode, a, st);
+      if constexpr (K >= 1) return launch_one_t<N, K, EK_DIF_TEST, T>(a, st);
       break;
     case EK_DIF_TRIAL:
-      if constexpr (K >= 1) return launch_one<N, K, EK_DIF_TRIAL>(mode, a, st);
+      if constexpr (K >= 1) return launch_one_t<N, K, EK_DIF_TRIAL, T>(a, st);
       break;
     case EK_DIRAC:
-      if constexpr (K == 0 && !(N == 4 && std::is_same<FQ_ELEM_T, df64>::value))
-        return launch_one<N, 0, EK_DIRAC>(mode, a, st);
+      // the 4D Dirac program is dispatched to IEEE double by the caller
+      if constexpr (K == 0 && !split_n4_df<N, T>()) return launch_one_t<N, 0, EK_DIRAC, T>(a, st);
       break;
     case EK_METRIC:
-      if constexpr (K == 0 && std::is_same<FQ_ELEM_T, double>::value) return launch_one<N, 0, EK_METRIC>(0, a, st);
+      if constexpr (K == 0 && std::is_same<T, double>::value) return launch_one_t<N, 0, EK_METRIC, T>(a, st);
       break;
     default:
       break;
@@ -76,11 +70,16 @@ int launch_k(int kind, int mode, const ElemArgs& a, cudaStream_t st) {
 template <int N, typename T>
 int launch_typed(int K, int kind, const ElemArgs& a, cudaStream_t st) {
   if (kind == EK_DIRAC || kind == EK_METRIC) K = 0;
-  if constexpr (N >= 0) if (K == 0) return launch_k<N, 0>(kind, 0, a, st);
-  if constexpr (N >= 1) if (K == 1) return launch_k<N, 1>(kind, 0, a, st);
-  if constexpr (N >= 2) if (K == 2) return launch_k<N, 2>(kind, 0, a, st);
-  if constexpr (N >= 3) if (K == 3) return launch_k<N, 3>(kind, 0, a, st);
-  if constexpr (N >= 4) if (K == 4) return launch_k<N, 4>(kind, 0, a, st);
+  if constexpr (N >= 0)
+    if (K == 0) return launch_k_t<N, 0, T>(kind, a, st);
+  if constexpr (N >= 1)
+    if (K == 1) return launch_k_t<N, 1, T>(kind, a, st);
+  if constexpr (N >= 2)
+    if (K == 2) return launch_k_t<N, 2, T>(kind, a, st);
+  if constexpr (N >= 3)
+    if (K == 3) return launch_k_t<N, 3, T>(kind, a, st);
+  if constexpr (N >= 4)
+    if (K == 4) return launch_k_t<N, 4, T>(kind, a, st);
   return -1;
 }
 

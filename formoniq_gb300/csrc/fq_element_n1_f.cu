@@ -1,5 +1,4 @@
 // Element programs for cell dimension 1 in float arithmetic.
-#define FQ_ELEM_T float
 #include "fq_element_dispatch.cuh"
 
 namespace fq {

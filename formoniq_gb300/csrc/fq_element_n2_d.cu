@@ -1,5 +1,4 @@
 // Element programs for cell dimension 2 in double arithmetic.
-#define FQ_ELEM_T double
 #include "fq_element_dispatch.cuh"
 
 namespace fq {

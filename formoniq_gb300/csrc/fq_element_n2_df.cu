@@ -1,5 +1,4 @@
 // Element programs for cell dimension 2 in df64 arithmetic.
-#define FQ_ELEM_T df64
 #include "fq_element_dispatch.cuh"
 
 namespace fq {

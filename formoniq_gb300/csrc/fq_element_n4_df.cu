@@ -1,7 +1,4 @@
-// Element programs for cell dimension 4 in float-float arithmetic (the
-// mixed-system and H(d) Gram programs are in fq_element_n4_df_{kkt,hdif}.cu).
-#define FQ_ELEM_T df64
-#define FQ_SPLIT_KKT
+// Element programs for cell dimension 4 in df64 arithmetic.
 #include "fq_element_dispatch.cuh"
 
 namespace fq {

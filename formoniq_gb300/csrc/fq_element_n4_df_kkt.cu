@@ -1,9 +1,9 @@
-// The mixed-system element program for cell dimension 4 in float-float arithmetic.
-#define FQ_ELEM_T df64
+// The float-float mixed-system element program for cell dimension 4 (its own
+// translation unit to bound compile time).
 #include "fq_element_dispatch.cuh"
 
 namespace fq {
-int launch_kkt_split(int K, const ElemArgs& a, cudaStream_t st) {
+int launch_kkt_n4_df(int K, const ElemArgs& a, cudaStream_t st) {
   switch (K) {
     case 0:
       return launch_one_t<4, 0, EK_KKT, df64>(a, st);
