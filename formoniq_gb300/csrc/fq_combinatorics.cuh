@@ -11,10 +11,14 @@
 // and no multiplications by +-1 reach the FP pipes.
 #pragma once
 
+// FQ_HD marks code that both the device kernels and host-side checks compile;
+// FQ_HDI is the same for small helpers that must inline.
 #if defined(__CUDACC__)
 #define FQ_HD __host__ __device__
+#define FQ_HDI __host__ __device__ __forceinline__
 #else
 #define FQ_HD
+#define FQ_HDI inline
 #endif
 
 namespace fq {

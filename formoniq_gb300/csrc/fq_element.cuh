@@ -31,11 +31,11 @@
 namespace fq {
 
 template <typename F, int... I>
-__device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int, I...>) {
+FQ_HDI void static_for_impl(F&& f, std::integer_sequence<int, I...>) {
   (f(std::integral_constant<int, I>{}), ...);
 }
 template <int N, typename F>
-__device__ __forceinline__ void static_for(F&& f) {
+FQ_HDI void static_for(F&& f) {
   static_for_impl(f, std::make_integer_sequence<int, N>{});
 }
 
@@ -58,7 +58,7 @@ struct Metric {
 };
 
 template <int N>
-__device__ __forceinline__ void regge_metric(const double* s, double (&g)[N > 0 ? N : 1][N > 0 ? N : 1]) {
+FQ_HDI void regge_metric(const double* s, double (&g)[N > 0 ? N : 1][N > 0 ? N : 1]) {
 #pragma unroll
   for (int i = 0; i < N; ++i) g[i][i] = s[edge_index(0, i + 1)];
 #pragma unroll
@@ -74,7 +74,7 @@ __device__ __forceinline__ void regge_metric(const double* s, double (&g)[N > 0 
 // Symmetric inverse by cofactors (N <= 3) and by the 2x2-minor Laplace
 // expansion (N = 4). Returns det.
 template <int N>
-__device__ __forceinline__ double sym_inverse(const double (&a)[N > 0 ? N : 1][N > 0 ? N : 1],
+FQ_HDI double sym_inverse(const double (&a)[N > 0 ? N : 1][N > 0 ? N : 1],
                                               double (&inv)[N > 0 ? N : 1][N > 0 ? N : 1]) {
   if constexpr (N == 0) {
     return 1.0;
@@ -149,7 +149,7 @@ struct Bary {
 };
 
 template <int N, typename T>
-__device__ __forceinline__ void bary_gramian(const double (&ginv)[N > 0 ? N : 1][N > 0 ? N : 1],
+FQ_HDI void bary_gramian(const double (&ginv)[N > 0 ? N : 1][N > 0 ? N : 1],
                                              Bary<N, T>& B) {
   // B[i+1][j+1] = ginv[i][j]; row/col 0 is minus the column sums (sum of dlambda = 0).
   double col[N > 0 ? N : 1];
@@ -187,7 +187,7 @@ struct MaskList {
 
 // det of B restricted to rows R, cols C (J x J, J <= 4), index sets compile-time.
 template <int N, int J, unsigned RM, unsigned CM, typename T>
-__device__ __forceinline__ T minor_det(const Bary<N, T>& B) {
+FQ_HDI T minor_det(const Bary<N, T>& B) {
   if constexpr (J == 0) {
     return T(1);
   } else {
@@ -232,7 +232,7 @@ struct Blades {
   static constexpr int P = (L * (L + 1)) / 2;
   T h[P > 0 ? P : 1];
   template <int I, int K>
-  __device__ __forceinline__ T at() const {
+  FQ_HDI T at() const {
     if constexpr (I <= K)
       return h[packed_index(I, K, L)];
     else
@@ -241,7 +241,7 @@ struct Blades {
 };
 
 template <int N, int J, typename T>
-__device__ __forceinline__ void compute_blades(const Bary<N, T>& B, Blades<N, J, T>& H) {
+FQ_HDI void compute_blades(const Bary<N, T>& B, Blades<N, J, T>& H) {
   constexpr int L = Blades<N, J, T>::L;
   if constexpr (J > N) {
     // Lambda^{n+1} B = det B = 0: the barycentric differentials sum to zero.
@@ -262,7 +262,7 @@ __device__ __forceinline__ void compute_blades(const Bary<N, T>& B, Blades<N, J,
 
 // Single H_J entry on the fly (no storage), for blocks read once.
 template <int N, int J, int I, int K, typename T>
-__device__ __forceinline__ T blade_entry(const Bary<N, T>& B) {
+FQ_HDI T blade_entry(const Bary<N, T>& B) {
   if constexpr (J > N) {
     return T(0);
   } else {
@@ -278,7 +278,7 @@ __device__ __forceinline__ T blade_entry(const Bary<N, T>& B) {
 // mass_k[s, t] / (vol (k!)^2 / ((n+1)(n+2))): s, t are the I-th and K-th
 // (k+1)-subsets of {0..n}.
 template <int N, int KG, int I, int K, typename T>
-__device__ __forceinline__ T mass_sum(const Blades<N, KG, T>& H) {
+FQ_HDI T mass_sum(const Blades<N, KG, T>& H) {
   constexpr unsigned ms = Tab<N + 1, KG + 1>::v.mask[I];
   constexpr unsigned mt = Tab<N + 1, KG + 1>::v.mask[K];
   T acc = T(0);
@@ -310,7 +310,7 @@ __device__ __forceinline__ T mass_sum(const Blades<N, KG, T>& H) {
 // dif_test_k[r, t] / (vol (k!)^2 / (n+1)): r the R-th k-subset, t the C-th
 // (k+1)-subset.
 template <int N, int KG, int R, int C, typename T>
-__device__ __forceinline__ T dif_test_sum(const Blades<N, KG, T>& H) {
+FQ_HDI T dif_test_sum(const Blades<N, KG, T>& H) {
   constexpr unsigned mt = Tab<N + 1, KG + 1>::v.mask[C];
   T acc = T(0);
   static_for<KG + 1>([&](auto Q) {

@@ -12,7 +12,157 @@
 
 namespace fq {
 
+// One cell's element program: the entries of element KIND at grade K from the
+// cell's inverse metric and volume, handed to put(entry, value) in the entry
+// numbering of the program (packed upper triangle, or row-major for the
+// rectangular dif_test/dif_trial). Shared by the device kernel and host checks.
+template <int N, int K, int KIND, typename T, typename Put>
+FQ_HD void element_entries(const double (&ginv)[N > 0 ? N : 1][N > 0 ? N : 1], double vol, double param, Put&& put) {
+  static_assert(KIND != EK_METRIC, "the metric program has no element entries");
+  Bary<N, T> B;
+  bary_gramian<N, T>(ginv, B);
+  // mass scale vol (k!)^2 / ((n+1)(n+2)); dif_test scale vol (k!)^2 / (n+1);
+  // stiffness scale vol (k!)^2.
+  auto mscale = [&](int k) { return T(vol * double(cfact(k)) * double(cfact(k)) / double((N + 1) * (N + 2))); };
+  auto tscale = [&](int k) { return T(vol * double(cfact(k)) * double(cfact(k)) / double(N + 1)); };
+  auto bscale = [&](int k) { return T(vol * double(cfact(k)) * double(cfact(k))); };
 
+  if constexpr (KIND == EK_MASS) {
+    constexpr int L = cbinom(N + 1, K + 1);
+    Blades<N, K, T> H;
+    compute_blades<N, K, T>(B, H);
+    const T sc = mscale(K);
+    static_for<L>([&](auto I) {
+      static_for<L>([&](auto J) {
+        constexpr int i = decltype(I)::value, j = decltype(J)::value;
+        if constexpr (i <= j) put(packed_index(i, j, L), sc * mass_sum<N, K, i, j, T>(H));
+      });
+    });
+  } else if constexpr (KIND == EK_DIF_BOTH) {
+    constexpr int L = cbinom(N + 1, K);
+    const T sc = bscale(K);
+    static_for<L>([&](auto I) {
+      static_for<L>([&](auto J) {
+        constexpr int i = decltype(I)::value, j = decltype(J)::value;
+        if constexpr (i <= j) put(packed_index(i, j, L), sc * blade_entry<N, K, i, j, T>(B));
+      });
+    });
+  } else if constexpr (KIND == EK_HDIF) {
+    constexpr int L = cbinom(N + 1, K + 1);
+    Blades<N, K, T> H;
+    compute_blades<N, K, T>(B, H);
+    const T sm = mscale(K), sb = bscale(K + 1);
+    static_for<L>([&](auto I) {
+      static_for<L>([&](auto J) {
+        constexpr int i = decltype(I)::value, j = decltype(J)::value;
+        if constexpr (i <= j) {
+          T v = sm * mass_sum<N, K, i, j, T>(H);
+          if constexpr (K + 1 <= N) v += sb * blade_entry<N, K + 1, i, j, T>(B);
+          put(packed_index(i, j, L), v);
+        }
+      });
+    });
+  } else if constexpr (KIND == EK_DIF_TEST || KIND == EK_DIF_TRIAL) {
+    constexpr int LR = cbinom(N + 1, K);      // (k-1)-faces
+    constexpr int LC = cbinom(N + 1, K + 1);  // k-faces
+    Blades<N, K, T> H;
+    compute_blades<N, K, T>(B, H);
+    const T sc = tscale(K);
+    static_for<LR>([&](auto R) {
+      static_for<LC>([&](auto C) {
+        constexpr int r = decltype(R)::value, c = decltype(C)::value;
+        const T v = sc * dif_test_sum<N, K, r, c, T>(H);
+        if constexpr (KIND == EK_DIF_TEST)
+          put(r * LC + c, v);
+        else
+          put(c * LR + r, v);
+      });
+    });
+  } else if constexpr (KIND == EK_KKT) {
+    // Local composite: sigma = (k-1)-faces, then u = k-faces.
+    constexpr int LS = kkt_sigma_local(N, K);
+    constexpr int LU = cbinom(N + 1, K + 1);
+    constexpr int L = LS + LU;
+    constexpr int P = (L * (L + 1)) / 2;
+    Blades<N, (K > 0 ? K - 1 : 0), T> Hs;
+    if constexpr (K > 0) compute_blades<N, K - 1, T>(B, Hs);
+    Blades<N, K, T> Hu;
+    compute_blades<N, K, T>(B, Hu);
+    const T sms = mscale(K > 0 ? K - 1 : 0), st = tscale(K), sbs = bscale(K);
+    const T smu = mscale(K), sbu = bscale(K + 1);
+    if constexpr (K > 0) {
+      static_for<LS>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        static_for<LS>([&](auto J) {
+          constexpr int j = decltype(J)::value;
+          if constexpr (i <= j) {
+            const T m = sms * mass_sum<N, K - 1, i, j, T>(Hs);
+            put(packed_index(i, j, L), -m);
+            if constexpr (i == j) put(P + i, m + sbs * Hu.template at<i, i>());
+          }
+        });
+        static_for<LU>([&](auto J) {
+          constexpr int j = decltype(J)::value;
+          put(packed_index(i, LS + j, L), st * dif_test_sum<N, K, i, j, T>(Hu));
+        });
+      });
+    }
+    static_for<LU>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      static_for<LU>([&](auto J) {
+        constexpr int j = decltype(J)::value;
+        if constexpr (i <= j) {
+          T st2 = T(0);
+          if constexpr (K + 1 <= N) st2 = sbu * blade_entry<N, K + 1, i, j, T>(B);
+          if constexpr (K + 1 <= N) put(packed_index(LS + i, LS + j, L), st2);
+          if constexpr (i == j) put(P + LS + i, smu * mass_sum<N, K, i, i, T>(Hu) + st2);
+        }
+      });
+    });
+  } else if constexpr (KIND == EK_DIRAC) {
+    // Local composite over every grade j = 0..n, block offsets o_j.
+    constexpr int L = (1 << (N + 1)) - 1;
+    const T mt = T(param);
+    Blades<N, 0, T> H0;
+    compute_blades<N, 0, T>(B, H0);
+    Blades<N, (N >= 1 ? 1 : 0), T> H1;
+    Blades<N, (N >= 2 ? 2 : 0), T> H2;
+    Blades<N, (N >= 3 ? 3 : 0), T> H3;
+    Blades<N, (N >= 4 ? 4 : 0), T> H4;
+    if constexpr (N >= 1) compute_blades<N, 1, T>(B, H1);
+    if constexpr (N >= 2) compute_blades<N, 2, T>(B, H2);
+    if constexpr (N >= 3) compute_blades<N, 3, T>(B, H3);
+    if constexpr (N >= 4) compute_blades<N, 4, T>(B, H4);
+    auto grade_block = [&](auto JG, const auto& HJ) {
+      constexpr int j = decltype(JG)::value;
+      constexpr int off = grade_offset(N, j);
+      constexpr int LJ = cbinom(N + 1, j + 1);
+      const T sm = mt * mscale(j);
+      static_for<LJ>([&](auto I) {
+        static_for<LJ>([&](auto J2) {
+          constexpr int a2 = decltype(I)::value, b2 = decltype(J2)::value;
+          if constexpr (a2 <= b2) put(packed_index(off + a2, off + b2, L), sm * mass_sum<N, j, a2, b2, T>(HJ));
+        });
+      });
+      if constexpr (j >= 1) {
+        constexpr int offm = off - cbinom(N + 1, j);
+        constexpr int LM = cbinom(N + 1, j);
+        const T st = tscale(j);
+        static_for<LM>([&](auto R) {
+          static_for<LJ>([&](auto C) {
+            constexpr int r = decltype(R)::value, c = decltype(C)::value;
+            put(packed_index(offm + r, off + c, L), st * dif_test_sum<N, j, r, c, T>(HJ));
+          });
+        });
+      }
+    };
+    grade_block(std::integral_constant<int, 0>{}, H0);
+    if constexpr (N >= 1) grade_block(std::integral_constant<int, 1>{}, H1);
+    if constexpr (N >= 2) grade_block(std::integral_constant<int, 2>{}, H2);
+    if constexpr (N >= 3) grade_block(std::integral_constant<int, 3>{}, H3);
+    if constexpr (N >= 4) grade_block(std::integral_constant<int, 4>{}, H4);
+  }
+}
 
 template <int N, int K, int KIND, typename T>
 __global__ void __launch_bounds__(128) element_kernel(ElemArgs a) {
@@ -38,159 +188,15 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs a) {
     }
     if (a.det_out) a.det_out[cell] = det;
     if (a.vol_out) a.vol_out[cell] = vol;
-    return;
   } else {
-    Bary<N, T> B;
-    bary_gramian<N, T>(ginv, B);
     T* out = static_cast<T*>(a.out);
     const int nent = a.nent;
-    auto put = [&](int e, T v) {
+    element_entries<N, K, KIND, T>(ginv, vol, a.param, [&](int e, T v) {
       if (e < nent)
         out[int64_t(e) * nc + cell] = v;
       else
         atomicOr(a.status, 2);
-    };
-    // mass scale vol (k!)^2 / ((n+1)(n+2)); dif_test scale vol (k!)^2 / (n+1);
-    // stiffness scale vol (k!)^2.
-    auto mscale = [&](int k) { return T(vol * double(cfact(k)) * double(cfact(k)) / double((N + 1) * (N + 2))); };
-    auto tscale = [&](int k) { return T(vol * double(cfact(k)) * double(cfact(k)) / double(N + 1)); };
-    auto bscale = [&](int k) { return T(vol * double(cfact(k)) * double(cfact(k))); };
-
-    if constexpr (KIND == EK_MASS) {
-      constexpr int L = cbinom(N + 1, K + 1);
-      Blades<N, K, T> H;
-      compute_blades<N, K, T>(B, H);
-      const T sc = mscale(K);
-      static_for<L>([&](auto I) {
-        static_for<L>([&](auto J) {
-          constexpr int i = decltype(I)::value, j = decltype(J)::value;
-          if constexpr (i <= j) put(packed_index(i, j, L), sc * mass_sum<N, K, i, j, T>(H));
-        });
-      });
-    } else if constexpr (KIND == EK_DIF_BOTH) {
-      constexpr int L = cbinom(N + 1, K);
-      const T sc = bscale(K);
-      static_for<L>([&](auto I) {
-        static_for<L>([&](auto J) {
-          constexpr int i = decltype(I)::value, j = decltype(J)::value;
-          if constexpr (i <= j) put(packed_index(i, j, L), sc * blade_entry<N, K, i, j, T>(B));
-        });
-      });
-    } else if constexpr (KIND == EK_HDIF) {
-      constexpr int L = cbinom(N + 1, K + 1);
-      Blades<N, K, T> H;
-      compute_blades<N, K, T>(B, H);
-      const T sm = mscale(K), sb = bscale(K + 1);
-      static_for<L>([&](auto I) {
-        static_for<L>([&](auto J) {
-          constexpr int i = decltype(I)::value, j = decltype(J)::value;
-          if constexpr (i <= j) {
-            T v = sm * mass_sum<N, K, i, j, T>(H);
-            if constexpr (K + 1 <= N) v += sb * blade_entry<N, K + 1, i, j, T>(B);
-            put(packed_index(i, j, L), v);
-          }
-        });
-      });
-    } else if constexpr (KIND == EK_DIF_TEST || KIND == EK_DIF_TRIAL) {
-      constexpr int LR = cbinom(N + 1, K);      // (k-1)-faces
-      constexpr int LC = cbinom(N + 1, K + 1);  // k-faces
-      Blades<N, K, T> H;
-      compute_blades<N, K, T>(B, H);
-      const T sc = tscale(K);
-      static_for<LR>([&](auto R) {
-        static_for<LC>([&](auto C) {
-          constexpr int r = decltype(R)::value, c = decltype(C)::value;
-          const T v = sc * dif_test_sum<N, K, r, c, T>(H);
-          if constexpr (KIND == EK_DIF_TEST)
-            put(r * LC + c, v);
-          else
-            put(c * LR + r, v);
-        });
-      });
-    } else if constexpr (KIND == EK_KKT) {
-      // Local composite: sigma = (k-1)-faces, then u = k-faces.
-      constexpr int LS = kkt_sigma_local(N, K);
-      constexpr int LU = cbinom(N + 1, K + 1);
-      constexpr int L = LS + LU;
-      constexpr int P = (L * (L + 1)) / 2;
-      Blades<N, (K > 0 ? K - 1 : 0), T> Hs;
-      if constexpr (K > 0) compute_blades<N, K - 1, T>(B, Hs);
-      Blades<N, K, T> Hu;
-      compute_blades<N, K, T>(B, Hu);
-      const T sms = mscale(K > 0 ? K - 1 : 0), st = tscale(K), sbs = bscale(K);
-      const T smu = mscale(K), sbu = bscale(K + 1);
-      if constexpr (K > 0) {
-        static_for<LS>([&](auto I) {
-          constexpr int i = decltype(I)::value;
-          static_for<LS>([&](auto J) {
-            constexpr int j = decltype(J)::value;
-            if constexpr (i <= j) {
-              const T m = sms * mass_sum<N, K - 1, i, j, T>(Hs);
-              put(packed_index(i, j, L), -m);
-              if constexpr (i == j) put(P + i, m + sbs * Hu.template at<i, i>());
-            }
-          });
-          static_for<LU>([&](auto J) {
-            constexpr int j = decltype(J)::value;
-            put(packed_index(i, LS + j, L), st * dif_test_sum<N, K, i, j, T>(Hu));
-          });
-        });
-      }
-      static_for<LU>([&](auto I) {
-        constexpr int i = decltype(I)::value;
-        static_for<LU>([&](auto J) {
-          constexpr int j = decltype(J)::value;
-          if constexpr (i <= j) {
-            T st2 = T(0);
-            if constexpr (K + 1 <= N) st2 = sbu * blade_entry<N, K + 1, i, j, T>(B);
-            if constexpr (K + 1 <= N) put(packed_index(LS + i, LS + j, L), st2);
-            if constexpr (i == j) put(P + LS + i, smu * mass_sum<N, K, i, i, T>(Hu) + st2);
-          }
-        });
-      });
-    } else if constexpr (KIND == EK_DIRAC) {
-      // Local composite over every grade j = 0..n, block offsets o_j.
-      constexpr int L = (1 << (N + 1)) - 1;
-      const T mt = T(a.param);
-      Blades<N, 0, T> H0;
-      compute_blades<N, 0, T>(B, H0);
-      Blades<N, (N >= 1 ? 1 : 0), T> H1;
-      Blades<N, (N >= 2 ? 2 : 0), T> H2;
-      Blades<N, (N >= 3 ? 3 : 0), T> H3;
-      Blades<N, (N >= 4 ? 4 : 0), T> H4;
-      if constexpr (N >= 1) compute_blades<N, 1, T>(B, H1);
-      if constexpr (N >= 2) compute_blades<N, 2, T>(B, H2);
-      if constexpr (N >= 3) compute_blades<N, 3, T>(B, H3);
-      if constexpr (N >= 4) compute_blades<N, 4, T>(B, H4);
-      auto grade_block = [&](auto JG, const auto& HJ) {
-        constexpr int j = decltype(JG)::value;
-        constexpr int off = grade_offset(N, j);
-        constexpr int LJ = cbinom(N + 1, j + 1);
-        const T sm = mt * mscale(j);
-        static_for<LJ>([&](auto I) {
-          static_for<LJ>([&](auto J2) {
-            constexpr int a2 = decltype(I)::value, b2 = decltype(J2)::value;
-            if constexpr (a2 <= b2) put(packed_index(off + a2, off + b2, L), sm * mass_sum<N, j, a2, b2, T>(HJ));
-          });
-        });
-        if constexpr (j >= 1) {
-          constexpr int offm = off - cbinom(N + 1, j);
-          constexpr int LM = cbinom(N + 1, j);
-          const T st = tscale(j);
-          static_for<LM>([&](auto R) {
-            static_for<LJ>([&](auto C) {
-              constexpr int r = decltype(R)::value, c = decltype(C)::value;
-              put(packed_index(offm + r, off + c, L), st * dif_test_sum<N, j, r, c, T>(HJ));
-            });
-          });
-        }
-      };
-      grade_block(std::integral_constant<int, 0>{}, H0);
-      if constexpr (N >= 1) grade_block(std::integral_constant<int, 1>{}, H1);
-      if constexpr (N >= 2) grade_block(std::integral_constant<int, 2>{}, H2);
-      if constexpr (N >= 3) grade_block(std::integral_constant<int, 3>{}, H3);
-      if constexpr (N >= 4) grade_block(std::integral_constant<int, 4>{}, H4);
-    }
+    });
   }
 }
 

@@ -1,0 +1,156 @@
+"""The element programs of the device kernels, compiled for the host, against the oracle.
+
+The per-cell code the element kernels run (metric, inverse, blade Gramians,
+mass/stiffness/coboundary sums) is host+device code; tests/element_host.cu
+compiles it with the host compiler, with contraction off, once per (dimension,
+arithmetic type). This checks the element algebra and the float-float arithmetic
+on CPU at the same tolerances as the GPU parity tests (operators.rs:58-212 via
+the oracle's element_matrix).
+"""
+
+import concurrent.futures as cf
+import ctypes
+import math
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "element_host.cu")
+CSRC = os.path.join(ROOT, "formoniq_gb300", "csrc")
+OUT = os.path.join(ROOT, "tests", "_build")
+LIB = os.path.join(OUT, "libelement_host.so")
+
+MASS, DIF_TRIAL, DIF_TEST, DIF_BOTH, HDIF = 0, 1, 2, 3, 4
+DF64, F32, F64 = 0, 1, 2
+TOL = {DF64: 1e-12, F64: 1e-12, F32: 1e-5}
+DIMS = (1, 2, 3, 4)
+
+
+def _inputs_newer_than(target):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    deps = [SRC] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _build():
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    if not _inputs_newer_than(LIB):
+        return LIB
+    os.makedirs(OUT, exist_ok=True)
+    jobs = [(t, n) for t in (DF64, F32, F64) for n in DIMS]
+
+    def one(job):
+        t, n = job
+        obj = os.path.join(OUT, f"element_host_t{t}_n{n}.o")
+        cmd = [nvcc, "-std=c++17", "-O1", "--expt-relaxed-constexpr", "-x", "cu", "-Xcompiler",
+               "-fPIC,-ffp-contract=off", f"-DEH_TYPE={t}", f"-DEH_DIM={n}", "-I", CSRC, "-c", SRC, "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"host element build failed ({t}, {n}):\n{r.stderr[-4000:]}")
+        return obj
+
+    # the 4D objects take longest: start them first
+    jobs.sort(key=lambda j: -j[1])
+    with cf.ThreadPoolExecutor(min(len(jobs), max(2, os.cpu_count() or 2))) as ex:
+        objs = list(ex.map(one, jobs))
+    tmp = LIB + ".tmp"
+    r = subprocess.run([nvcc, "-shared", "-o", tmp] + objs, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"host element link failed:\n{r.stderr[-4000:]}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+@pytest.fixture(scope="module")
+def host_lib():
+    lib = ctypes.CDLL(_build())
+    f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    fns = {}
+    for t in (DF64, F32, F64):
+        for n in DIMS:
+            fn = getattr(lib, f"eh_element_t{t}_n{n}")
+            fn.restype = ctypes.c_int
+            fn.argtypes = [ctypes.c_int, ctypes.c_int, f64p, ctypes.c_double, f64p, ctypes.c_int,
+                           ctypes.POINTER(ctypes.c_double)]
+            fns[(t, n)] = fn
+    return fns
+
+
+def run(host_lib, t, n, k, kind, lengths, param=0.0):
+    out = np.zeros(4096)
+    det = ctypes.c_double()
+    ne = host_lib[(t, n)](k, kind, np.ascontiguousarray(lengths, np.float64), param, out, out.size,
+                          ctypes.byref(det))
+    assert ne >= 0, (t, n, k, kind, ne)
+    return out[:ne], det.value
+
+
+def unpack_sym(v, L):
+    m = np.zeros((L, L))
+    iu = np.triu_indices(L)
+    m[iu] = v[: len(iu[0])]
+    return m + np.triu(m, 1).T
+
+
+def rel_frob(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def sample_cells(oracle, dim, seed=3, jitter=0.15):
+    cx, coords = oracle.cartesian_unit(dim, 2)
+    coords = oracle.jitter_coords(coords, 2, seed, jitter, side=np.ones(dim))
+    lengths = cx.edge_lengths_sq(coords)
+    edges = cx.cell_faces(1)
+    nc = cx.ncells()
+    return [lengths[edges[c]] for c in range(0, nc, max(1, nc // 7))]
+
+
+@pytest.mark.parametrize("dim", DIMS)
+@pytest.mark.parametrize("t", [DF64, F32, F64])
+def test_whitney_pairings(oracle, host_lib, dim, t):
+    for ll in sample_cells(oracle, dim):
+        for form in (MASS, DIF_TRIAL, DIF_TEST, DIF_BOTH):
+            for grade in range(dim + 1):
+                tg = grade - 1 if form in (DIF_TEST, DIF_BOTH) else grade
+                sg = grade - 1 if form in (DIF_TRIAL, DIF_BOTH) else grade
+                if tg < 0 or sg < 0:
+                    continue
+                lr, lc = math.comb(dim + 1, tg + 1), math.comb(dim + 1, sg + 1)
+                v, _ = run(host_lib, t, dim, grade, form, ll)
+                got = unpack_sym(v, lr) if form in (MASS, DIF_BOTH) else v[: lr * lc].reshape(lr, lc)
+                expect = oracle.element_matrix(dim, form, grade, ll)
+                assert rel_frob(got, expect) < TOL[t], (form, grade)
+
+
+@pytest.mark.parametrize("dim", DIMS)
+@pytest.mark.parametrize("t", [DF64, F64])
+def test_hdif_gram(oracle, host_lib, dim, t):
+    """hdif_gram(k) = M_k + dif_both(k+1) (whitney_complex.rs:180-183), per cell."""
+    for ll in sample_cells(oracle, dim, seed=5):
+        for grade in range(dim + 1):
+            L = math.comb(dim + 1, grade + 1)
+            v, _ = run(host_lib, t, dim, grade, HDIF, ll)
+            expect = oracle.element_matrix(dim, MASS, grade, ll)
+            if grade + 1 <= dim:
+                expect = expect + oracle.element_matrix(dim, DIF_BOTH, grade + 1, ll)
+            assert rel_frob(unpack_sym(v, L), expect) < TOL[t], grade
+
+
+@pytest.mark.parametrize("dim", DIMS)
+def test_float_float_beats_float(oracle, host_lib, dim):
+    """The float-float programs carry about 48 bits: far below FP32's error."""
+    for ll in sample_cells(oracle, dim, seed=9, jitter=0.3):
+        for grade in range(1, dim + 1):
+            expect = oracle.element_matrix(dim, DIF_BOTH, grade, ll)
+            L = expect.shape[0]
+            e_df = rel_frob(unpack_sym(run(host_lib, DF64, dim, grade, DIF_BOTH, ll)[0], L), expect)
+            e_f = rel_frob(unpack_sym(run(host_lib, F32, dim, grade, DIF_BOTH, ll)[0], L), expect)
+            assert e_df < TOL[DF64] and e_df < 1e-4 * e_f, (grade, e_df, e_f)
