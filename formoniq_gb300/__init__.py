@@ -28,13 +28,14 @@ import numpy as np
 __all__ = [
     "FQ_MASS", "FQ_DIF_TRIAL", "FQ_DIF_TEST", "FQ_DIF_BOTH", "FQ_ABSOLUTE", "FQ_RELATIVE", "FQ_FP64", "FQ_FP32", "FQ_FP64_IEEE",
     "FqError", "FqUnavailable", "Context", "Mesh", "Matrix", "WhitneyComplex", "MixedProblem", "SolveOpts",
-    "Report", "solve_source", "solve_dirac_source", "dirac_system", "minres", "cg", "lib_path", "load",
-    "exported_symbols",
+    "Report", "solve_source", "solve_dirac_source", "dirac_system", "minres", "cg", "hx_cg", "hx_apply", "lib_path",
+    "load", "exported_symbols", "FQ_PC_AUTO", "FQ_PC_JACOBI", "FQ_PC_HX",
 ]
 
 FQ_MASS, FQ_DIF_TRIAL, FQ_DIF_TEST, FQ_DIF_BOTH = 0, 1, 2, 3
 FQ_ABSOLUTE, FQ_RELATIVE = 0, 1
 FQ_FP64, FQ_FP32, FQ_FP64_IEEE = 0, 1, 2
+FQ_PC_AUTO, FQ_PC_JACOBI, FQ_PC_HX = 0, 1, 2
 
 _STATUS = {
     0: "FQ_OK", 1: "FQ_INVALID_ARG", 2: "FQ_DEGENERATE_CELL", 3: "FQ_NOT_CONVERGED", 4: "FQ_BREAKDOWN",
@@ -63,11 +64,12 @@ class SolveOpts(ctypes.Structure):
     """StopCriterion (iterative/src/lib.rs:193-208) plus refinement knobs."""
 
     _fields_ = [("rtol", ctypes.c_double), ("max_iters", ctypes.c_int64), ("precision", ctypes.c_int),
-                ("refine_rtol", ctypes.c_double), ("max_refinements", ctypes.c_int64)]
+                ("refine_rtol", ctypes.c_double), ("max_refinements", ctypes.c_int64),
+                ("preconditioner", ctypes.c_int)]
 
     @staticmethod
     def default(**kw) -> "SolveOpts":
-        o = SolveOpts(1e-10, 10_000, FQ_FP64, 1e-12, 6)
+        o = SolveOpts(1e-10, 10_000, FQ_FP64, 1e-12, 6, FQ_PC_AUTO)
         for k, v in kw.items():
             setattr(o, k, v)
         return o
@@ -144,6 +146,9 @@ _SIGNATURES = {
     "fq_spmv": (ctypes.c_int, [_P, _P, _P, _P]),
     "fq_minres": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
     "fq_cg": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
+    "fq_hx_cg": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _DP, _DP, ctypes.POINTER(SolveOpts),
+                                ctypes.POINTER(_Report)]),
+    "fq_hx_apply": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _DP, _DP]),
     "fq_mixed_create": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
     "fq_mixed_reassemble": (ctypes.c_int, [_P]),
     "fq_mixed_solve": (ctypes.c_int, [_P, _DP, _DP, _DP, _DP, ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
@@ -570,3 +575,24 @@ def minres(a: Matrix, b_ptr: int, x_ptr: int, inv_diag_ptr: int = 0, opts=None) 
 def cg(a: Matrix, b_ptr: int, x_ptr: int, inv_diag_ptr: int = 0, opts=None) -> Report:
     """krylov::cg on device pointers (FP64)."""
     return _krylov("fq_cg", a, b_ptr, x_ptr, inv_diag_ptr, opts)
+
+
+def hx_cg(mesh: Mesh, grade: int, bc: int, rhs: np.ndarray, opts: Optional[SolveOpts] = None):
+    """GradeKHodgeHx::with_multigrid(..).solve (formoniq/src/hx.rs): HX-preconditioned CG on hdif_gram(grade)."""
+    rhs = np.ascontiguousarray(rhs, np.float64)
+    x = np.zeros_like(rhs)
+    rep = _Report()
+    opts = opts or SolveOpts.default()
+    s = mesh.ctx.L.fq_hx_cg(mesh.ctx.h, mesh.h, int(grade), int(bc), _dp(rhs), _dp(x), ctypes.byref(opts),
+                            ctypes.byref(rep))
+    if s not in (0, 3):
+        mesh.ctx.check(s, "fq_hx_cg")
+    return x, Report.of(rep)
+
+
+def hx_apply(mesh: Mesh, grade: int, bc: int, r: np.ndarray) -> np.ndarray:
+    """One application y = B r of the grade-`grade` HX preconditioner (AuxiliarySpace::apply)."""
+    r = np.ascontiguousarray(r, np.float64)
+    y = np.zeros_like(r)
+    mesh.ctx.check(mesh.ctx.L.fq_hx_apply(mesh.ctx.h, mesh.h, int(grade), int(bc), _dp(r), _dp(y)), "fq_hx_apply")
+    return y

@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "fq_hx.h"
 #include "fq_internal.h"
 
 namespace fq {
@@ -22,11 +23,11 @@ double uniform_pm1(uint64_t seed, uint64_t counter);
 void compute_orientation(fq_mesh* m, const std::vector<int32_t>& facet_of_cell);
 
 template <typename VT>
-fq_status minres_run(fq_ctx*, const int32_t*, const int32_t*, const VT*, int64_t, int64_t, const VT*, const VT*, VT*,
-                     double, int64_t, fq_report*);
+fq_status minres_run(fq_ctx*, const int32_t*, const int32_t*, const VT*, int64_t, int64_t, const VT*,
+                     const HxPrecond*, const VT*, VT*, double, int64_t, fq_report*);
 template <typename VT>
-fq_status cg_run(fq_ctx*, const int32_t*, const int32_t*, const VT*, int64_t, int64_t, const VT*, const VT*, VT*,
-                 double, int64_t, fq_report*);
+fq_status cg_run(fq_ctx*, const int32_t*, const int32_t*, const VT*, int64_t, int64_t, const VT*, const HxPrecond*,
+                 const VT*, VT*, double, int64_t, fq_report*);
 fq_status residual64(fq_ctx*, const int32_t*, const int32_t*, const double*, int64_t, const double*, const double*,
                      double*, double*, double*);
 void launch_to_float(const double* a, float* o, int64_t n, cudaStream_t st);
@@ -172,6 +173,61 @@ static fq_status empty_matrix(fq_ctx* ctx, fq_mesh* mesh, int64_t rows, int64_t 
   return FQ_OK;
 }
 
+// Coboundary D_k (Complex::coboundary_operator, topology/complex.rs:215-217):
+// rows the (k+1)-simplices, entry (-1)^p at the face omitting vertex position p;
+// the relative complex keeps interior simplices on both sides.
+void coboundary_host(const fq_mesh* m, int k, int bc, HCsr& out) {
+  out = HCsr();
+  out.nrows = ndofs(m, k + 1, bc);
+  out.ncols = ndofs(m, k, bc);
+  if (k < 0 || k >= m->dim || out.nrows == 0 || out.ncols == 0) {
+    out.rp.assign(size_t(out.nrows) + 1, 0);
+    return;
+  }
+  const int w = k + 2;
+  const auto& sk = m->skel[k + 1];
+  const auto& low = m->skel[k];
+  const int fw = w - 1;
+  for (int64_t r = 0; r < m->nsimp[k + 1]; ++r) {
+    if (bc == FQ_RELATIVE && m->boundary[k + 1][r]) continue;
+    std::vector<std::pair<int32_t, double>> ent;
+    for (int p = 0; p < w; ++p) {
+      int32_t tup[5];
+      int q = 0;
+      for (int i = 0; i < w; ++i)
+        if (i != p) tup[q++] = sk[r * w + i];
+      int64_t lo = 0, hi = m->nsimp[k] - 1, found = -1;
+      while (lo <= hi) {
+        const int64_t mid = (lo + hi) / 2;
+        int cmp = 0;
+        for (int i = fw - 1; i >= 0; --i)
+          if (low[mid * fw + i] != tup[i]) {
+            cmp = low[mid * fw + i] < tup[i] ? -1 : 1;
+            break;
+          }
+        if (cmp == 0) {
+          found = mid;
+          break;
+        }
+        if (cmp < 0)
+          lo = mid + 1;
+        else
+          hi = mid - 1;
+      }
+      int64_t c = found;
+      if (bc == FQ_RELATIVE) c = m->interior_map[k][found];
+      if (c < 0) continue;
+      ent.emplace_back(int32_t(c), (p % 2) ? -1.0 : 1.0);
+    }
+    std::sort(ent.begin(), ent.end());
+    for (auto& e : ent) {
+      out.ci.push_back(e.first);
+      out.v.push_back(e.second);
+    }
+    out.rp.push_back(int32_t(out.ci.size()));
+  }
+}
+
 }  // namespace fq
 
 using namespace fq;
@@ -201,6 +257,10 @@ struct fq_mixed {
   const float* val32 = nullptr;
   int64_t nnz32 = 0;
   fq_matrix sysview;  // non-owning view handed out by fq_mixed_system
+  // HX-multigrid block preconditioner, built at the first solve that asks for it
+  // and rebuilt after a reassembly; hx_failed remembers an FQ_PC_AUTO fallback
+  std::unique_ptr<HxPrecond> hx;
+  bool hx_stale = true, hx_failed = false;
   ~fq_mixed() {
     delete kkt;
     delete kkt32;
@@ -255,7 +315,7 @@ static fq_status mixed_harmonic(fq_mixed* P) {
     vec_recip(d.as<double>(), dinv.as<double>(), nullptr, nu, 0, ctx->stream);
     fq_report rep{};
     FQ_TRY(cg_run<double>(ctx, mass->rp, mass->ci, mass->values.as<double>(), nu, mass->nnz, dinv.as<double>(),
-                          tmp.as<double>(), g.as<double>(), 1e-14, 10000, &rep));
+                          nullptr, tmp.as<double>(), g.as<double>(), 1e-14, 10000, &rep));
     std::vector<double> gh(nu);
     FQ_CUDA(ctx, cudaMemcpyAsync(gh.data(), g.p, nu * 8, cudaMemcpyDeviceToHost, ctx->stream));
     FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -272,6 +332,7 @@ static fq_status mixed_harmonic(fq_mixed* P) {
 static fq_status mixed_assemble(fq_mixed* P) {
   fq_ctx* ctx = P->ctx;
   fq_mesh* m = P->mesh;
+  P->hx_stale = true;
   if (P->kkt) {
     FQ_TRY(assemble_into(ctx, P->kkt));
   } else {
@@ -335,12 +396,48 @@ static fq_status mixed_assemble(fq_mixed* P) {
 }
 
 // Solve the assembled (bordered) system for rhs (device, size n) into x (device).
+// The block preconditioner the options ask for: HX-multigrid blocks for the
+// grades k-1 and k (the blocks hdif_gram(k-1), hdif_gram(k) of
+// mixed_block_preconditioner, problems/elliptic.rs:29-47), or null for the
+// Jacobi diagonal.
+static fq_status mixed_precond(fq_mixed* P, const fq_solve_opts* o, const HxPrecond** out) {
+  *out = nullptr;
+  const int want = o->preconditioner;
+  if (want == FQ_PC_JACOBI) return FQ_OK;
+  if (want != FQ_PC_AUTO && want != FQ_PC_HX) return set_error(P->ctx, FQ_INVALID_ARG, "unknown preconditioner");
+  if (P->hx && !P->hx_stale) {
+    *out = P->hx.get();
+    return FQ_OK;
+  }
+  if (want == FQ_PC_AUTO && P->hx_failed && P->hx_stale == false) return FQ_OK;
+  std::vector<int> grades;
+  if (P->grade >= 1) grades.push_back(P->grade - 1);
+  grades.push_back(P->grade);
+  auto hx = std::make_unique<HxPrecond>();
+  fq_status s = hx_supported(P->mesh) ? hx_build(P->ctx, P->mesh, P->bc, grades, P->nh, P->diag.as<double>(), *hx)
+                                      : set_error(P->ctx, FQ_UNSUPPORTED, "HX multigrid needs a Kuhn cube mesh");
+  if (s == FQ_OK && P->precision == FQ_FP32) s = hx->make_f32(P->ctx);
+  P->hx_stale = false;
+  if (s != FQ_OK) {
+    P->hx.reset();
+    P->hx_failed = true;
+    if (want == FQ_PC_HX) return s;
+    return FQ_OK;  // FQ_PC_AUTO: Jacobi
+  }
+  P->hx_failed = false;
+  P->hx = std::move(hx);
+  *out = P->hx.get();
+  return FQ_OK;
+}
+
 static fq_status mixed_krylov(fq_mixed* P, const double* rhs, double* x, const fq_solve_opts* o, fq_report* rep) {
   fq_ctx* ctx = P->ctx;
   const int64_t n = P->n;
   rep->refinements = 0;
+  const HxPrecond* pc = nullptr;
+  FQ_TRY(mixed_precond(P, o, &pc));
   if (P->precision != FQ_FP32 || !P->kkt32) {
-    FQ_TRY(minres_run<double>(ctx, P->rp, P->ci, P->val, n, P->nnz, P->dinv.as<double>(), rhs, x, o->rtol,
+    FQ_TRY(minres_run<double>(ctx, P->rp, P->ci, P->val, n, P->nnz, P->dinv.as<double>(), pc, rhs, x, o->rtol,
                               o->max_iters, rep));
   } else {
     // FP64 residual and update around an FP32 MINRES (iterative refinement).
@@ -356,7 +453,7 @@ static fq_status mixed_krylov(fq_mixed* P, const double* rhs, double* x, const f
       FQ_TRY(residual64(ctx, P->rp, P->ci, P->val, n, x, rhs, r.as<double>(), &rn, &bn));
       if (bn == 0.0 || rn <= o->refine_rtol * bn || ref == o->max_refinements) break;
       launch_to_float_scaled(r.as<double>(), r32.as<float>(), 1.0 / rn, n, ctx->stream);
-      FQ_TRY(minres_run<float>(ctx, P->rp32, P->ci32, P->val32, n, P->nnz32, P->dinv32.as<float>(),
+      FQ_TRY(minres_run<float>(ctx, P->rp32, P->ci32, P->val32, n, P->nnz32, P->dinv32.as<float>(), pc,
                                r32.as<float>(), d32.as<float>(), o->rtol, o->max_iters, &inner));
       launch_axpy_from_float(x, d32.as<float>(), rn, n, ctx->stream);
       total += inner.iters;
@@ -429,6 +526,7 @@ void fq_default_solve_opts(fq_solve_opts* o) {
   o->precision = FQ_FP64;
   o->refine_rtol = 1e-12;
   o->max_refinements = 6;
+  o->preconditioner = FQ_PC_AUTO;
 }
 
 fq_status fq_ctx_create(int device, void* stream, uint64_t budget, fq_ctx** out) {
@@ -754,69 +852,26 @@ fq_status fq_coboundary(fq_ctx* ctx, fq_mesh* m, int k, fq_bc bc, fq_matrix** ou
   FQ_GUARD_BEGIN
   const int64_t nr = ndofs(m, k + 1, bc), nc = ndofs(m, k, bc);
   if (k < 0 || k >= m->dim || nr == 0 || nc == 0) return empty_matrix(ctx, m, nr, nc, FQ_FP64, out);
-  // rows: (k+1)-simplices; entries (-1)^p at the face omitting position p.
-  const int w = k + 2;
-  std::vector<int32_t> rp(1, 0), ci;
-  std::vector<double> val;
-  const auto& sk = m->skel[k + 1];
-  const auto& low = m->skel[k];
-  const int fw = w - 1;
-  for (int64_t r = 0; r < m->nsimp[k + 1]; ++r) {
-    if (bc == FQ_RELATIVE && m->boundary[k + 1][r]) continue;
-    std::vector<std::pair<int32_t, double>> ent;
-    for (int p = 0; p < w; ++p) {
-      int32_t tup[5];
-      int q = 0;
-      for (int i = 0; i < w; ++i)
-        if (i != p) tup[q++] = sk[r * w + i];
-      int64_t lo = 0, hi = m->nsimp[k] - 1, found = -1;
-      while (lo <= hi) {
-        const int64_t mid = (lo + hi) / 2;
-        int cmp = 0;
-        for (int i = fw - 1; i >= 0; --i)
-          if (low[mid * fw + i] != tup[i]) {
-            cmp = low[mid * fw + i] < tup[i] ? -1 : 1;
-            break;
-          }
-        if (cmp == 0) {
-          found = mid;
-          break;
-        }
-        if (cmp < 0)
-          lo = mid + 1;
-        else
-          hi = mid - 1;
-      }
-      int64_t c = found;
-      if (bc == FQ_RELATIVE) c = m->interior_map[k][found];
-      if (c < 0) continue;
-      ent.emplace_back(int32_t(c), (p % 2) ? -1.0 : 1.0);
-    }
-    std::sort(ent.begin(), ent.end());
-    for (auto& e : ent) {
-      ci.push_back(e.first);
-      val.push_back(e.second);
-    }
-    rp.push_back(int32_t(ci.size()));
-  }
+  HCsr h;
+  coboundary_host(m, k, int(bc), h);
   auto* mat = new fq_matrix();
   mat->ctx = ctx;
   mat->mesh = m;
   mat->nrows = nr;
   mat->ncols = nc;
-  mat->nnz = int64_t(ci.size());
+  mat->nnz = int64_t(h.ci.size());
   mat->precision = FQ_FP64;
-  fq_status s = mat->row_ptr.alloc(ctx, rp.size() * 4);
-  if (s == FQ_OK) s = mat->col_idx.alloc(ctx, std::max<size_t>(ci.size(), 1) * 4);
-  if (s == FQ_OK) s = mat->values.alloc(ctx, std::max<size_t>(val.size(), 1) * 8);
+  fq_status s = mat->row_ptr.alloc(ctx, h.rp.size() * 4);
+  if (s == FQ_OK) s = mat->col_idx.alloc(ctx, std::max<size_t>(h.ci.size(), 1) * 4);
+  if (s == FQ_OK) s = mat->values.alloc(ctx, std::max<size_t>(h.v.size(), 1) * 8);
   if (s != FQ_OK) {
     delete mat;
     return s;
   }
-  cudaMemcpyAsync(mat->row_ptr.p, rp.data(), rp.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
-  if (!ci.empty()) {
-    cudaMemcpyAsync(mat->col_idx.p, ci.data(), ci.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(mat->values.p, val.data(), val.size() * 8, cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(mat->row_ptr.p, h.rp.data(), h.rp.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+  if (!h.ci.empty()) {
+    cudaMemcpyAsync(mat->col_idx.p, h.ci.data(), h.ci.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(mat->values.p, h.v.data(), h.v.size() * 8, cudaMemcpyHostToDevice, ctx->stream);
   }
   FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   mat->rp = mat->row_ptr.as<int32_t>();
@@ -898,7 +953,7 @@ fq_status fq_minres(fq_ctx* ctx, const fq_matrix* a, const double* dinv, const d
   fq_default_solve_opts(&d);
   if (!o) o = &d;
   fq_report r{};
-  FQ_TRY(minres_run<double>(ctx, a->rp, a->ci, a->values.as<double>(), a->nrows, a->nnz, dinv, b, x, o->rtol,
+  FQ_TRY(minres_run<double>(ctx, a->rp, a->ci, a->values.as<double>(), a->nrows, a->nnz, dinv, nullptr, b, x, o->rtol,
                             o->max_iters, &r));
   if (rep) *rep = r;
   return r.converged ? FQ_OK : FQ_NOT_CONVERGED;
@@ -914,10 +969,78 @@ fq_status fq_cg(fq_ctx* ctx, const fq_matrix* a, const double* dinv, const doubl
   fq_default_solve_opts(&d);
   if (!o) o = &d;
   fq_report r{};
-  FQ_TRY(cg_run<double>(ctx, a->rp, a->ci, a->values.as<double>(), a->nrows, a->nnz, dinv, b, x, o->rtol,
+  FQ_TRY(cg_run<double>(ctx, a->rp, a->ci, a->values.as<double>(), a->nrows, a->nnz, dinv, nullptr, b, x, o->rtol,
                         o->max_iters, &r));
   if (rep) *rep = r;
   return r.converged ? FQ_OK : FQ_NOT_CONVERGED;
+  FQ_GUARD_END(ctx)
+}
+
+// ---- HX multigrid on one grade ------------------------------------------------
+// A = hdif_gram(grade) and its grade-`grade` HX preconditioner.
+static fq_status hx_single(fq_ctx* ctx, fq_mesh* m, int grade, int bc, std::unique_ptr<fq_matrix>& A,
+                           HxPrecond& pc, DevBuf& diag) {
+  if (grade < 0 || grade > m->dim) return set_error(ctx, FQ_INVALID_ARG, "grade out of range");
+  if (!hx_supported(m)) return set_error(ctx, FQ_UNSUPPORTED, "HX multigrid needs a Kuhn cube mesh with lengths");
+  if (ndofs(m, grade, bc) == 0) return set_error(ctx, FQ_INVALID_ARG, "no degrees of freedom at this grade");
+  fq_matrix* a = nullptr;
+  FQ_TRY(make_matrix(ctx, m, EK_HDIF, grade, bc, FQ_FP64, 0.0, &a));
+  A.reset(a);
+  FQ_TRY(diag.alloc(ctx, std::max<int64_t>(a->nrows, 1) * 8));
+  vec_diag(a, diag.as<double>(), ctx->stream);
+  ctx->launches++;
+  return hx_build(ctx, m, bc, std::vector<int>{grade}, 0, diag.as<double>(), pc);
+}
+
+fq_status fq_hx_cg(fq_ctx* ctx, fq_mesh* m, int grade, fq_bc bc, const double* rhs_h, double* x_h,
+                   const fq_solve_opts* o, fq_report* rep) {
+  if (!ctx || !m || !rhs_h || !x_h) return FQ_INVALID_ARG;
+  FQ_GUARD_BEGIN
+  fq_solve_opts d;
+  fq_default_solve_opts(&d);
+  if (!o) o = &d;
+  std::unique_ptr<fq_matrix> A;
+  HxPrecond pc;
+  DevBuf diag, b, x;
+  FQ_TRY(hx_single(ctx, m, grade, int(bc), A, pc, diag));
+  const int64_t n = A->nrows;
+  FQ_TRY(b.alloc(ctx, n * 8));
+  FQ_TRY(x.alloc(ctx, n * 8));
+  FQ_CUDA(ctx, cudaMemcpyAsync(b.p, rhs_h, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+  fq_report r{};
+  FQ_TRY(cg_run<double>(ctx, A->rp, A->ci, A->values.as<double>(), n, A->nnz, nullptr, &pc, b.as<double>(),
+                        x.as<double>(), o->rtol, o->max_iters, &r));
+  {
+    DevBuf rr;
+    FQ_TRY(rr.alloc(ctx, n * 8));
+    double rn = 0, bn = 0;
+    FQ_TRY(residual64(ctx, A->rp, A->ci, A->values.as<double>(), n, x.as<double>(), b.as<double>(), rr.as<double>(),
+                      &rn, &bn));
+    r.true_residual = bn > 0 ? rn / bn : 0.0;
+  }
+  FQ_CUDA(ctx, cudaMemcpyAsync(x_h, x.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (rep) *rep = r;
+  return r.converged ? FQ_OK : FQ_NOT_CONVERGED;
+  FQ_GUARD_END(ctx)
+}
+
+fq_status fq_hx_apply(fq_ctx* ctx, fq_mesh* m, int grade, fq_bc bc, const double* r_h, double* y_h) {
+  if (!ctx || !m || !r_h || !y_h) return FQ_INVALID_ARG;
+  FQ_GUARD_BEGIN
+  std::unique_ptr<fq_matrix> A;
+  HxPrecond pc;
+  DevBuf diag, r, y;
+  FQ_TRY(hx_single(ctx, m, grade, int(bc), A, pc, diag));
+  const int64_t n = A->nrows;
+  FQ_TRY(r.alloc(ctx, n * 8));
+  FQ_TRY(y.alloc(ctx, n * 8));
+  FQ_CUDA(ctx, cudaMemcpyAsync(r.p, r_h, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+  hx_apply<double>(pc, r.as<double>(), y.as<double>(), nullptr, ctx->stream);
+  FQ_CUDA(ctx, cudaGetLastError());
+  FQ_CUDA(ctx, cudaMemcpyAsync(y_h, y.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return FQ_OK;
   FQ_GUARD_END(ctx)
 }
 
@@ -1132,7 +1255,7 @@ fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* m, double mass_term, const
   ctx->launches += 5;
   fq_report r{};
   FQ_TRY(minres_run<double>(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, sii->nnz, dinv.as<double>(),
-                            rhs.as<double>(), x.as<double>(), o->rtol, o->max_iters, &r));
+                            nullptr, rhs.as<double>(), x.as<double>(), o->rtol, o->max_iters, &r));
   {
     DevBuf rr;
     FQ_TRY(rr.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <vector>
 
+#include "fq_hx.h"
 #include "fq_internal.h"
 
 namespace fq {
@@ -148,6 +149,7 @@ template <typename VT>
 struct MinresVecs {
   VT *x, *r1, *r2, *y, *v, *z, *w, *w2;
   const VT* dinv;  // may be null: identity preconditioner
+  int external;    // 1: y = P r2 is applied by separate kernels (dinv unused)
   const VT* b;
   double *partA, *partB;
 };
@@ -242,14 +244,30 @@ __global__ void __launch_bounds__(KT) minres_b(MinresVecs<VT> m, SolverState* __
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
     const VT r2 = m.r2[i];
     const VT zi = m.z[i] + c2 * r2;
-    const VT yi = m.dinv ? zi * m.dinv[i] : zi;
     m.r1[i] = r2;
     m.r2[i] = zi;
-    m.y[i] = yi;
-    acc += double(zi) * double(yi);
+    if (!m.external) {
+      const VT yi = m.dinv ? zi * m.dinv[i] : zi;
+      m.y[i] = yi;
+      acc += double(zi) * double(yi);
+    }
   }
+  if (m.external) return;  // y = P r2 and its partials come from the preconditioner
   acc = block_sum(acc, sh);
   if (threadIdx.x == 0) m.partB[blockIdx.x] = acc;
+}
+
+// Partials of a.b (after an external preconditioner wrote b = P a).
+template <typename VT>
+__global__ void __launch_bounds__(KT) dot_partials(const VT* __restrict__ a, const VT* __restrict__ b,
+                                                   double* __restrict__ part, int64_t n, const int* __restrict__ done) {
+  __shared__ double sh[32];
+  if (done && *done) return;
+  double acc = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    acc += double(a[i]) * double(b[i]);
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
 // C: rotation (identical in every block), w/x update, state -> the other slot
@@ -319,6 +337,7 @@ template <typename VT>
 struct CgVecs {
   VT *x, *r, *z, *p, *ap;
   const VT* dinv;
+  int external;  // 1: z = P r is applied by separate kernels (dinv unused)
   const VT* b;
   double *partA, *partB, *partC;
 };
@@ -403,18 +422,34 @@ __global__ void __launch_bounds__(KT) cg_b(CgVecs<VT> c, const SolverState* __re
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
     c.x[i] = c.x[i] + at * c.p[i];
     const VT ri = c.r[i] + mat * c.ap[i];
-    const VT zi = c.dinv ? ri * c.dinv[i] : ri;
     c.r[i] = ri;
-    c.z[i] = zi;
-    rz += double(ri) * double(zi);
+    if (!c.external) {
+      const VT zi = c.dinv ? ri * c.dinv[i] : ri;
+      c.z[i] = zi;
+      rz += double(ri) * double(zi);
+    }
     rr += double(ri) * double(ri);
   }
   rz = block_sum(rz, sh);
   rr = block_sum(rr, sh);
   if (threadIdx.x == 0) {
-    c.partB[blockIdx.x] = rz;
+    if (!c.external) c.partB[blockIdx.x] = rz;
     c.partC[blockIdx.x] = rr;
   }
+}
+
+// External preconditioner, first step: p = z (= P b), partials of b.z.
+template <typename VT>
+__global__ void __launch_bounds__(KT) cg_init_p(CgVecs<VT> c, int64_t n) {
+  __shared__ double sh[32];
+  double rz = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const VT zi = c.z[i];
+    c.p[i] = zi;
+    rz += double(c.b[i]) * double(zi);
+  }
+  rz = block_sum(rz, sh);
+  if (threadIdx.x == 0) c.partB[blockIdx.x] = rz;
 }
 
 // C: beta = rz_next / rz; p = beta p + z; state
@@ -467,7 +502,7 @@ struct Workspace {
 // always has the next batch queued; iterations after convergence are no-ops.
 template <typename F>
 static fq_status run_graph_loop(fq_ctx* ctx, SolverState* S, int64_t max_iters, F&& one_iteration,
-                                SolverState* final_state) {
+                                SolverState* final_state, int64_t max_batch = 64) {
   cudaStream_t st = ctx->stream;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -525,7 +560,7 @@ static fq_status run_graph_loop(fq_ctx* ctx, SolverState* S, int64_t max_iters, 
       cudaEventSynchronize(ev[1 - slot]);
       break;
     }
-    batch = std::min<int64_t>(batch * 2, 64);
+    batch = std::min<int64_t>(batch * 2, max_batch);
   }
   FQ_CUDA(ctx, cudaStreamSynchronize(st));
   cudaError_t e = cudaMemcpy(final_state, S, sizeof(SolverState), cudaMemcpyDeviceToHost);
@@ -540,7 +575,8 @@ static fq_status run_graph_loop(fq_ctx* ctx, SolverState* S, int64_t max_iters, 
 
 template <typename VT>
 fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* val, int64_t n, int64_t nnz,
-                     const VT* dinv, const VT* b, VT* x, double rtol, int64_t max_iters, fq_report* rep) {
+                     const VT* dinv, const HxPrecond* pc, const VT* b, VT* x, double rtol, int64_t max_iters,
+                     fq_report* rep) {
   cudaStream_t st = ctx->stream;
   DevBuf vecs, parts, state;
   const size_t vb = size_t(std::max<int64_t>(n, 1)) * sizeof(VT);
@@ -557,7 +593,8 @@ fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT
   m.z = reinterpret_cast<VT*>(base + 4 * vb);
   m.w = reinterpret_cast<VT*>(base + 5 * vb);
   m.w2 = reinterpret_cast<VT*>(base + 6 * vb);
-  m.dinv = dinv;
+  m.dinv = pc ? nullptr : dinv;
+  m.external = pc ? 1 : 0;
   m.b = b;
   m.partA = parts.as<double>();
   m.partB = parts.as<double>() + KBLOCKS;
@@ -566,6 +603,10 @@ fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT
   const int ga = std::min(spmv_blocks(n, W), KBLOCKS);
   const int gv = int(std::max<int64_t>(1, std::min<int64_t>((n + KT - 1) / KT, KBLOCKS)));
   minres_init<VT><<<gv, KT, 0, st>>>(m, n);
+  if (pc) {
+    hx_apply<VT>(*pc, b, m.y, nullptr, st);
+    dot_partials<VT><<<gv, KT, 0, st>>>(b, m.y, m.partB, n, nullptr);
+  }
   minres_init_state<<<1, KT, 0, st>>>(S, S + 1, m.partB, gv, rtol, (long long)max_iters);
   ctx->launches += 2;
   SolverState hs{};
@@ -585,9 +626,16 @@ fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT
         break;
     }
     minres_b<VT><<<gv, KT, 0, st>>>(m, S + cur, ga, n);
+    if (pc) {
+      const int* done = &(S + cur)->done;
+      hx_apply<VT>(*pc, m.r2, m.y, done, st);
+      dot_partials<VT><<<gv, KT, 0, st>>>(m.r2, m.y, m.partB, n, done);
+    }
     minres_c<VT><<<gv, KT, 0, st>>>(m, S + cur, S + (1 - cur), ga, gv, rtol, (long long)max_iters, n);
   };
-  FQ_TRY(run_graph_loop(ctx, S, max_iters, iteration, &hs));
+  // a preconditioned iteration costs more: poll more often so fewer finished
+  // iterations are queued past convergence
+  FQ_TRY(run_graph_loop(ctx, S, max_iters, iteration, &hs, pc ? 4 : 64));
   rep->iters = hs.iters;
   rep->residual = hs.residual;
   rep->converged = hs.converged;
@@ -597,7 +645,8 @@ fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT
 
 template <typename VT>
 fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* val, int64_t n, int64_t nnz,
-                 const VT* dinv, const VT* b, VT* x, double rtol, int64_t max_iters, fq_report* rep) {
+                 const VT* dinv, const HxPrecond* pc, const VT* b, VT* x, double rtol, int64_t max_iters,
+                 fq_report* rep) {
   cudaStream_t st = ctx->stream;
   DevBuf vecs, parts, state;
   const size_t vb = size_t(std::max<int64_t>(n, 1)) * sizeof(VT);
@@ -611,7 +660,8 @@ fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* va
   c.z = reinterpret_cast<VT*>(base + 1 * vb);
   c.p = reinterpret_cast<VT*>(base + 2 * vb);
   c.ap = reinterpret_cast<VT*>(base + 3 * vb);
-  c.dinv = dinv;
+  c.dinv = pc ? nullptr : dinv;
+  c.external = pc ? 1 : 0;
   c.b = b;
   c.partA = parts.as<double>();
   c.partB = parts.as<double>() + KBLOCKS;
@@ -621,6 +671,10 @@ fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* va
   const int ga = std::min(spmv_blocks(n, W), KBLOCKS);
   const int gv = int(std::max<int64_t>(1, std::min<int64_t>((n + KT - 1) / KT, KBLOCKS)));
   cg_init<VT><<<gv, KT, 0, st>>>(c, n);
+  if (pc) {
+    hx_apply<VT>(*pc, b, c.z, nullptr, st);
+    cg_init_p<VT><<<gv, KT, 0, st>>>(c, n);
+  }
   cg_init_state<<<1, KT, 0, st>>>(S, S + 1, c.partB, c.partC, gv, rtol, (long long)max_iters);
   ctx->launches += 2;
   SolverState hs{};
@@ -640,9 +694,14 @@ fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* va
         break;
     }
     cg_b<VT><<<gv, KT, 0, st>>>(c, S + cur, ga, n);
+    if (pc) {
+      const int* done = &(S + cur)->done;
+      hx_apply<VT>(*pc, c.r, c.z, done, st);
+      dot_partials<VT><<<gv, KT, 0, st>>>(c.r, c.z, c.partB, n, done);
+    }
     cg_c<VT><<<gv, KT, 0, st>>>(c, S + cur, S + (1 - cur), gv, rtol, (long long)max_iters, n);
   };
-  FQ_TRY(run_graph_loop(ctx, S, max_iters, iteration, &hs));
+  FQ_TRY(run_graph_loop(ctx, S, max_iters, iteration, &hs, pc ? 4 : 64));
   rep->iters = hs.iters;
   rep->residual = hs.residual;
   rep->converged = hs.converged;
@@ -651,13 +710,16 @@ fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* va
 }
 
 template fq_status minres_run<double>(fq_ctx*, const int32_t*, const int32_t*, const double*, int64_t, int64_t,
-                                      const double*, const double*, double*, double, int64_t, fq_report*);
+                                      const double*, const HxPrecond*, const double*, double*, double, int64_t,
+                                      fq_report*);
 template fq_status minres_run<float>(fq_ctx*, const int32_t*, const int32_t*, const float*, int64_t, int64_t,
-                                     const float*, const float*, float*, double, int64_t, fq_report*);
+                                     const float*, const HxPrecond*, const float*, float*, double, int64_t,
+                                     fq_report*);
 template fq_status cg_run<double>(fq_ctx*, const int32_t*, const int32_t*, const double*, int64_t, int64_t,
-                                  const double*, const double*, double*, double, int64_t, fq_report*);
+                                  const double*, const HxPrecond*, const double*, double*, double, int64_t,
+                                  fq_report*);
 template fq_status cg_run<float>(fq_ctx*, const int32_t*, const int32_t*, const float*, int64_t, int64_t,
-                                 const float*, const float*, float*, double, int64_t, fq_report*);
+                                 const float*, const HxPrecond*, const float*, float*, double, int64_t, fq_report*);
 
 // ---------------------------------------------------------------------------
 // Small vector kernels used by the problem drivers

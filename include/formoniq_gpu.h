@@ -65,6 +65,17 @@ typedef enum fq_precision {
   FQ_FP64_IEEE = 2  /* FP64 values computed in IEEE double throughout */
 } fq_precision;
 
+/* Block preconditioner of the mixed Hodge-Laplace solve. The reference
+ * (problems/elliptic.rs:29-47) inverts each diagonal block hdif_gram(j) exactly
+ * by a sparse Cholesky factorization; here a block is approximated. */
+typedef enum fq_precond {
+  FQ_PC_AUTO = 0,   /* FQ_PC_HX where it applies, else FQ_PC_JACOBI */
+  FQ_PC_JACOBI = 1, /* diagonal of each block (Jacobi::new, iterative/src/precond.rs:62-64) */
+  FQ_PC_HX = 2      /* Hiptmair-Xu auxiliary-space blocks over a nodal multigrid V-cycle
+                       (formoniq/src/hx.rs, multigrid.rs): Kuhn cube meshes with positive
+                       squared lengths; FQ_UNSUPPORTED elsewhere */
+} fq_precond;
+
 typedef struct fq_ctx fq_ctx;
 typedef struct fq_mesh fq_mesh;
 typedef struct fq_matrix fq_matrix;
@@ -77,6 +88,7 @@ typedef struct fq_solve_opts {
   int precision;           /* fq_precision of the inner Krylov solve */
   double refine_rtol;      /* FQ_FP32: outer FP64 refinement target (relative residual) */
   int64_t max_refinements; /* FQ_FP32: cap on outer refinement steps */
+  int preconditioner;      /* fq_precond of the mixed solves; default FQ_PC_AUTO */
 } fq_solve_opts;
 
 /* Report (iterative/src/lib.rs:212-219) plus refinement telemetry. */
@@ -219,6 +231,17 @@ fq_status fq_minres(fq_ctx* ctx, const fq_matrix* a, const double* inv_diag, con
 /* krylov::cg (iterative/src/krylov.rs:48-95), same conventions. */
 fq_status fq_cg(fq_ctx* ctx, const fq_matrix* a, const double* inv_diag, const double* b, double* x,
                 const fq_solve_opts* opts, fq_report* report);
+/* GradeKHodgeHx::with_multigrid(..).solve (formoniq/src/hx.rs:140-240): CG on
+ * hdif_gram(grade) (M_k + D_k^T M_{k+1} D_k) preconditioned by the grade-`grade`
+ * Hiptmair-Xu auxiliary-space preconditioner whose auxiliary blocks are nodal
+ * multigrid V-cycles (2 Jacobi sweeps, weight 2/3). Kuhn cube meshes with
+ * positive squared lengths, else FQ_UNSUPPORTED. rhs_host and x_host hold the
+ * grade's degrees of freedom (interior ones for FQ_RELATIVE). */
+fq_status fq_hx_cg(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, const double* rhs_host, double* x_host,
+                   const fq_solve_opts* opts, fq_report* report);
+/* ApproxInverse::apply of that preconditioner (AuxiliarySpace::apply,
+ * iterative/src/aux_space.rs): y = B r once, host arrays. */
+fq_status fq_hx_apply(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, const double* r_host, double* y_host);
 
 /* ---- the mixed Hodge-Laplace source problem ------------------------------ */
 /* The resident form of elliptic::solve_source (problems/elliptic.rs:132-182):
