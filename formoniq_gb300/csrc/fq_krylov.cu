@@ -29,6 +29,7 @@ namespace fq {
 
 constexpr int KT = 256;          // threads per block of the vector kernels
 constexpr int KBLOCKS = 152 * 4; // grid of the vector kernels: 4 blocks per SM
+constexpr int PBLOCKS = 152 * 8; // grid cap of the fused SpMV kernels: 8 resident blocks per SM
 
 struct SolverState {
   double beta1, beta, oldb, dbar, epsln, phibar, cs, sn;  // MINRES
@@ -71,11 +72,20 @@ template <int W, typename VT>
 __device__ __forceinline__ VT row_dot(const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                                       const VT* __restrict__ val, const VT* __restrict__ x, int64_t row, bool valid,
                                       int lane) {
-  VT acc = VT(0);
+  // two independent accumulators keep two gathers in flight per lane
+  VT acc0 = VT(0), acc1 = VT(0);
   if (valid) {
     const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
-    for (int t = b + lane; t < e; t += W) acc += __ldg(val + t) * __ldg(x + __ldg(ci + t));
+    int t = b + lane;
+    for (; t + W < e; t += 2 * W) {
+      const int c0 = __ldg(ci + t), c1 = __ldg(ci + t + W);
+      const VT v0 = __ldg(val + t), v1 = __ldg(val + t + W);
+      acc0 += v0 * __ldg(x + c0);
+      acc1 += v1 * __ldg(x + c1);
+    }
+    if (t < e) acc0 += __ldg(val + t) * __ldg(x + __ldg(ci + t));
   }
+  VT acc = acc0 + acc1;
 #pragma unroll
   for (int o = W / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, W);
   return acc;
@@ -102,7 +112,7 @@ static int pick_w(int64_t nnz, int64_t nrows) {
   const double avg = nrows > 0 ? double(nnz) / double(nrows) : 0.0;
   if (avg <= 6) return 4;
   if (avg <= 14) return 8;
-  if (avg <= 40) return 16;
+  if (avg <= 80) return 16;
   return 32;
 }
 
@@ -581,7 +591,7 @@ fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT
   DevBuf vecs, parts, state;
   const size_t vb = size_t(std::max<int64_t>(n, 1)) * sizeof(VT);
   FQ_TRY(vecs.alloc(ctx, vb * 7));
-  FQ_TRY(parts.alloc(ctx, 2 * KBLOCKS * sizeof(double)));
+  FQ_TRY(parts.alloc(ctx, 2 * PBLOCKS * sizeof(double)));
   FQ_TRY(state.alloc(ctx, 2 * sizeof(SolverState)));
   MinresVecs<VT> m;
   char* base = vecs.as<char>();
@@ -597,10 +607,10 @@ fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT
   m.external = pc ? 1 : 0;
   m.b = b;
   m.partA = parts.as<double>();
-  m.partB = parts.as<double>() + KBLOCKS;
+  m.partB = parts.as<double>() + PBLOCKS;
   SolverState* S = state.as<SolverState>();
   const int W = pick_w<VT>(nnz, n);
-  const int ga = std::min(spmv_blocks(n, W), KBLOCKS);
+  const int ga = std::min(spmv_blocks(n, W), PBLOCKS);
   const int gv = int(std::max<int64_t>(1, std::min<int64_t>((n + KT - 1) / KT, KBLOCKS)));
   minres_init<VT><<<gv, KT, 0, st>>>(m, n);
   if (pc) {
@@ -651,7 +661,7 @@ fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* va
   DevBuf vecs, parts, state;
   const size_t vb = size_t(std::max<int64_t>(n, 1)) * sizeof(VT);
   FQ_TRY(vecs.alloc(ctx, vb * 4));
-  FQ_TRY(parts.alloc(ctx, 3 * KBLOCKS * sizeof(double)));
+  FQ_TRY(parts.alloc(ctx, 3 * PBLOCKS * sizeof(double)));
   FQ_TRY(state.alloc(ctx, 2 * sizeof(SolverState)));
   CgVecs<VT> c;
   char* base = vecs.as<char>();
@@ -664,11 +674,11 @@ fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* va
   c.external = pc ? 1 : 0;
   c.b = b;
   c.partA = parts.as<double>();
-  c.partB = parts.as<double>() + KBLOCKS;
-  c.partC = parts.as<double>() + 2 * KBLOCKS;
+  c.partB = parts.as<double>() + PBLOCKS;
+  c.partC = parts.as<double>() + 2 * PBLOCKS;
   SolverState* S = state.as<SolverState>();
   const int W = pick_w<VT>(nnz, n);
-  const int ga = std::min(spmv_blocks(n, W), KBLOCKS);
+  const int ga = std::min(spmv_blocks(n, W), PBLOCKS);
   const int gv = int(std::max<int64_t>(1, std::min<int64_t>((n + KT - 1) / KT, KBLOCKS)));
   cg_init<VT><<<gv, KT, 0, st>>>(c, n);
   if (pc) {

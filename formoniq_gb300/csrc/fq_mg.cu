@@ -45,6 +45,33 @@ __global__ void __launch_bounds__(MT) gen_spmv_kernel(const int32_t* __restrict_
   }
 }
 
+// The same with W lanes per row (rows with many entries).
+template <int W, typename VT>
+__global__ void __launch_bounds__(MT) gen_spmv_w_kernel(const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                                        const VT* __restrict__ val, const VT* __restrict__ x,
+                                                        VT* __restrict__ y, int64_t nrows, const VT* __restrict__ s,
+                                                        const VT* __restrict__ r, int acc, int nI, int m, int c0,
+                                                        const int* __restrict__ done) {
+  if (done && *done) return;
+  const int lane = threadIdx.x % W;
+  const int64_t rows_per_grid = int64_t(gridDim.x) * (blockDim.x / W);
+  for (int64_t base = int64_t(blockIdx.x) * (blockDim.x / W); base < nrows; base += rows_per_grid) {
+    const int64_t row = base + threadIdx.x / W;
+    VT a = VT(0);
+    if (row < nrows) {
+      const int b = rp[row], e = rp[row + 1];
+      for (int t = b + lane; t < e; t += W) a += val[t] * x[ci[t]];
+    }
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o, W);
+    if (row < nrows && lane == 0) {
+      if (s) a += s[row] * r[row];
+      const int64_t o = nI == 1 && m == 1 ? row : (row / nI) * m + c0 + row % nI;
+      y[o] = acc ? y[o] + a : a;
+    }
+  }
+}
+
 template <typename VT>
 __global__ void __launch_bounds__(MT) mg_jacobi_first(const VT* __restrict__ dinv, const VT* __restrict__ r,
                                                       VT* __restrict__ x, int64_t n, int m, const int* done) {
@@ -90,18 +117,22 @@ __global__ void __launch_bounds__(MT) mg_spmm(const int32_t* __restrict__ rp, co
   }
 }
 
-// x[a][c] = sum_b Ainv[a][b] r[b][c]  (coarsest level, dense inverse)
+// x[a][c] = sum_b Ainv[a][b] r[b][c]  (coarsest level, dense inverse): one block
+// per coarse row, one warp per slot, lanes over b (coalesced reads of the row).
 template <typename VT>
 __global__ void __launch_bounds__(MT) mg_dense(const VT* __restrict__ ainv, const VT* __restrict__ r,
                                                VT* __restrict__ x, int64_t nc, int m, const int* done) {
   if (done && *done) return;
-  const int64_t total = nc * m;
-  for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t a = t / m;
-    const int c = int(t - a * m);
-    VT acc = VT(0);
-    for (int64_t b = 0; b < nc; ++b) acc += ainv[a * nc + b] * r[b * m + c];
-    x[t] = acc;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int64_t a = blockIdx.x; a < nc; a += gridDim.x) {
+    const VT* row = ainv + a * nc;
+    for (int c = warp; c < m; c += nwarps) {
+      VT acc = VT(0);
+      for (int64_t b = lane; b < nc; b += 32) acc += row[b] * r[b * m + c];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) x[a * m + c] = acc;
+    }
   }
 }
 
@@ -193,8 +224,21 @@ template <typename VT>
 void gen_spmv(const DCsr& A, const VT* x, VT* y, const VT* s, const VT* r, int acc, int nI, int m, int c0,
               const int* done, cudaStream_t st) {
   if (A.nrows == 0) return;
-  gen_spmv_kernel<VT><<<grid_for_n(A.nrows), MT, 0, st>>>(A.rp, A.ci, A.val<VT>(), x, y, A.nrows, s, r, acc, nI, m, c0,
-                                                          done);
+  const double avg = double(A.nnz) / double(A.nrows);
+  auto blocks = [&](int W) { return grid_for_n(A.nrows * W); };
+  if (avg <= 8) {
+    gen_spmv_kernel<VT><<<grid_for_n(A.nrows), MT, 0, st>>>(A.rp, A.ci, A.val<VT>(), x, y, A.nrows, s, r, acc, nI, m,
+                                                            c0, done);
+  } else if (avg <= 24) {
+    gen_spmv_w_kernel<4, VT><<<blocks(4), MT, 0, st>>>(A.rp, A.ci, A.val<VT>(), x, y, A.nrows, s, r, acc, nI, m, c0,
+                                                       done);
+  } else if (avg <= 64) {
+    gen_spmv_w_kernel<8, VT><<<blocks(8), MT, 0, st>>>(A.rp, A.ci, A.val<VT>(), x, y, A.nrows, s, r, acc, nI, m, c0,
+                                                       done);
+  } else {
+    gen_spmv_w_kernel<16, VT><<<blocks(16), MT, 0, st>>>(A.rp, A.ci, A.val<VT>(), x, y, A.nrows, s, r, acc, nI, m,
+                                                         c0, done);
+  }
 }
 
 template <typename VT>
@@ -219,7 +263,8 @@ VT* vcycle(const NodalHierarchy& mg, size_t l, int m, const int* done, cudaStrea
   const int64_t tot = L.n * m;
   if (L.n == 0) return x0;
   if (l + 1 == mg.lv.size()) {
-    mg_dense<VT><<<grid_for_n(tot), MT, 0, st>>>(pick<VT>(mg.coarse_inv64, mg.coarse_inv32), r, x0, L.n, m, done);
+    mg_dense<VT><<<int(std::min<int64_t>(L.n, 152 * 8)), MT, 0, st>>>(pick<VT>(mg.coarse_inv64, mg.coarse_inv32), r,
+                                                                      x0, L.n, m, done);
     return x0;
   }
   const VT* dinv = pick<VT>(L.dinv64, L.dinv32);
