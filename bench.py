@@ -17,6 +17,7 @@ independent replicas, one per rank, with no collective on the data path.
 from __future__ import annotations
 
 import argparse
+import collections
 import json
 import math
 import os
@@ -453,6 +454,98 @@ def run_precision(args):
     print(json.dumps(out))
 
 
+# ---------------------------------------------------------------------------
+# serving workload: a Poisson stream of Hodge-Laplace and Minkowski Dirac solves
+# ---------------------------------------------------------------------------
+
+def serve_stream(fq, n, seed, rate_per_s, max_cells_hodge=5e5, max_cells_dirac=3e5):
+    """Seeded request stream: half (i) Riemannian Kuhn n in {2,3,4}, cells
+    log-uniform in [1e3, 5e5], k uniform in 0..n, bc uniform, jittered 0.1h,
+    Hodge-Laplace source problem; half (ii) Minkowski 1+2 Kuhn, cells in
+    [1e3, 3e5], squared lengths s(1 + U(-0.05, 0.05)), Dirac with m = 1.5."""
+    rng = np.random.default_rng(seed)
+    t, reqs = 0.0, []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate_per_s)
+        if rng.random() < 0.5:
+            dim = int(rng.integers(2, 5))
+            cells = math.exp(rng.uniform(math.log(1e3), math.log(max_cells_hodge)))
+            nb = max(1, round((cells / math.factorial(dim)) ** (1.0 / dim)))
+            reqs.append(dict(kind=fq.FQ_REQ_HODGE, dim=dim, nbox=nb, grade=int(rng.integers(0, dim + 1)),
+                             bc=int(rng.integers(0, 2)), jitter=0.1, seed=seed * 100003 + i, arrival_ms=t * 1e3))
+        else:
+            cells = math.exp(rng.uniform(math.log(1e3), math.log(max_cells_dirac)))
+            nb = max(1, round((cells / 6.0) ** (1.0 / 3.0)))
+            reqs.append(dict(kind=fq.FQ_REQ_DIRAC, dim=3, nbox=nb, minkowski=True, jitter=0.05, mass_term=1.5,
+                             seed=seed * 100003 + i, arrival_ms=t * 1e3))
+    return reqs
+
+
+def run_stream(fq, reqs, lanes, cache, mixed_precision, dirac_iters):
+    """Submit the whole stream (the server releases each request at its
+    arrival time); returns per-request results in stream order."""
+    fp64 = fq.SolveOpts.default(rtol=1e-10)
+    fp32 = fq.SolveOpts.default(rtol=1e-5, precision=fq.FQ_FP32, refine_rtol=1e-10, max_refinements=8)
+    dirac = fq.SolveOpts.default(rtol=1e-10, max_iters=dirac_iters)
+    with fq.Server(lanes=lanes, cache=cache) as srv:
+        t0 = time.perf_counter()
+        tickets = []
+        for r in reqs:
+            if r["kind"] == fq.FQ_REQ_DIRAC:
+                opts = dirac
+            else:
+                opts = fp32 if mixed_precision else fp64
+            tickets.append(srv.submit(**r, opts=opts))
+        res = [srv.wait(t) for t in tickets]
+        wall = time.perf_counter() - t0
+        stats = srv.stats()
+    return res, wall, stats
+
+
+def stream_summary(reqs, res, wall, kind=None):
+    pairs = [(q, r) for q, r in zip(reqs, res) if kind is None or q["kind"] == kind]
+    if not pairs:
+        return None
+    lat = sorted(r["latency_ms"] for _, r in pairs)
+    ok = [r for _, r in pairs if r["status"] == 0 and r["report"].converged]
+    first = min(q["arrival_ms"] for q in reqs)
+    span_ms = max(r["end_ms"] for r in res) - first
+
+    def pct(p):
+        return lat[min(len(lat) - 1, int(math.ceil(p / 100 * len(lat))) - 1)]
+
+    return {"solves_per_s": len(ok) / (span_ms * 1e-3), "p50_ms": pct(50), "p99_ms": pct(99),
+            "mean_run_ms": sum(r["run_ms"] for _, r in pairs) / len(pairs), "converged": len(ok), "n": len(pairs),
+            "wall_s": wall, "cache_hits": sum(r["cache_hit"] for _, r in pairs)}
+
+
+def run_serve(args):
+    import formoniq_gb300 as fq
+
+    reqs = serve_stream(fq, args.requests, SEED, args.rate)
+    served, wall_s, st = run_stream(fq, reqs, args.lanes, True, True, args.dirac_iters)
+    plain, wall_p, _ = run_stream(fq, reqs, 1, False, False, args.dirac_iters)
+    errs = []
+    for q, a, b in zip(reqs, served, plain):
+        if q["kind"] == fq.FQ_REQ_HODGE and a["status"] == 0 and b["status"] == 0 and b["checksum"] > 0:
+            # relative difference of the solution norms, served (FP32 inner) vs plain (FP64)
+            errs.append(abs(math.sqrt(a["checksum"]) - math.sqrt(b["checksum"])) / math.sqrt(b["checksum"]))
+    kinds = collections.Counter("hodge" if q["kind"] == fq.FQ_REQ_HODGE else "dirac" for q in reqs)
+
+    def side(res, wall, **kw):
+        return dict(all=stream_summary(reqs, res, wall), hodge=stream_summary(reqs, res, wall, fq.FQ_REQ_HODGE),
+                    dirac=stream_summary(reqs, res, wall, fq.FQ_REQ_DIRAC), **kw)
+
+    out = {"metric": "solves/s and p50/p99 latency, served vs plain", "requests": len(reqs), "rate_per_s": args.rate,
+           "mix": dict(kinds), "data": "synthetic (seeded stream)", "dirac_max_iters": args.dirac_iters,
+           "served": side(served, wall_s, lanes=args.lanes, cache=True,
+                          precision="FP32 inner MINRES + FP64 refinement (Hodge), FP64 (Dirac)",
+                          peak_committed_gb=st["peak_committed_bytes"] / 1e9),
+           "plain": side(plain, wall_p, lanes=1, cache=False, precision="FP64"),
+           "hodge_max_rel_norm_diff_served_vs_plain": max(errs) if errs else None}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -466,13 +559,21 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-solve", action="store_true", help="skip the solve phase (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer phase (profiling runs)")
-    ap.add_argument("--workload", default="assembly", choices=["assembly", "precision"],
-                    help="assembly: the headline line; precision: the 4D FP32-with-refinement study")
+    ap.add_argument("--workload", default="assembly", choices=["assembly", "precision", "serve"],
+                    help="assembly: the headline line; precision: the 4D FP32-with-refinement study; "
+                         "serve: the request stream, served vs plain")
+    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate (requests/s)")
+    ap.add_argument("--lanes", type=int, default=4)
+    ap.add_argument("--dirac-iters", type=int, default=2000,
+                    help="serve: MINRES cap of the Lorentzian Dirac requests")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "precision":
         run_precision(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_ours(args)
 

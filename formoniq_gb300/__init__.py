@@ -29,13 +29,14 @@ __all__ = [
     "FQ_MASS", "FQ_DIF_TRIAL", "FQ_DIF_TEST", "FQ_DIF_BOTH", "FQ_ABSOLUTE", "FQ_RELATIVE", "FQ_FP64", "FQ_FP32", "FQ_FP64_IEEE",
     "FqError", "FqUnavailable", "Context", "Mesh", "Matrix", "WhitneyComplex", "MixedProblem", "SolveOpts",
     "Report", "solve_source", "solve_dirac_source", "dirac_system", "minres", "cg", "hx_cg", "hx_apply", "lib_path",
-    "load", "exported_symbols", "FQ_PC_AUTO", "FQ_PC_JACOBI", "FQ_PC_HX",
+    "load", "exported_symbols", "FQ_PC_AUTO", "FQ_PC_JACOBI", "FQ_PC_HX", "Server", "FQ_REQ_HODGE", "FQ_REQ_DIRAC",
 ]
 
 FQ_MASS, FQ_DIF_TRIAL, FQ_DIF_TEST, FQ_DIF_BOTH = 0, 1, 2, 3
 FQ_ABSOLUTE, FQ_RELATIVE = 0, 1
 FQ_FP64, FQ_FP32, FQ_FP64_IEEE = 0, 1, 2
 FQ_PC_AUTO, FQ_PC_JACOBI, FQ_PC_HX = 0, 1, 2
+FQ_REQ_HODGE, FQ_REQ_DIRAC = 0, 1
 
 _STATUS = {
     0: "FQ_OK", 1: "FQ_INVALID_ARG", 2: "FQ_DEGENERATE_CELL", 3: "FQ_NOT_CONVERGED", 4: "FQ_BREAKDOWN",
@@ -78,6 +79,27 @@ class SolveOpts(ctypes.Structure):
 class _Report(ctypes.Structure):
     _fields_ = [("iters", ctypes.c_int64), ("residual", ctypes.c_double), ("converged", ctypes.c_int32),
                 ("refinements", ctypes.c_int32), ("true_residual", ctypes.c_double)]
+
+
+class _Request(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("dim", ctypes.c_int), ("nbox", ctypes.c_int), ("grade", ctypes.c_int),
+                ("bc", ctypes.c_int), ("minkowski", ctypes.c_int), ("jitter", ctypes.c_double),
+                ("seed", ctypes.c_uint64), ("mass_term", ctypes.c_double), ("arrival_ms", ctypes.c_double),
+                ("lengths", ctypes.c_void_p), ("source", ctypes.c_void_p), ("solution", ctypes.c_void_p),
+                ("opts", SolveOpts)]
+
+
+class _Result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("lane", ctypes.c_int32), ("report", _Report),
+                ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("start_ms", ctypes.c_double), ("end_ms", ctypes.c_double), ("checksum", ctypes.c_double),
+                ("ndofs", ctypes.c_uint64), ("cache_hit", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("cache_hits", ctypes.c_uint64),
+                ("evictions", ctypes.c_uint64), ("peak_committed_bytes", ctypes.c_uint64),
+                ("resident_bytes", ctypes.c_uint64), ("busy_ms", ctypes.c_double)]
 
 
 @dataclass
@@ -149,6 +171,11 @@ _SIGNATURES = {
     "fq_hx_cg": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _DP, _DP, ctypes.POINTER(SolveOpts),
                                 ctypes.POINTER(_Report)]),
     "fq_hx_apply": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _DP, _DP]),
+    "fq_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(_P)]),
+    "fq_server_submit": (ctypes.c_int, [_P, ctypes.POINTER(_Request), ctypes.POINTER(ctypes.c_uint64)]),
+    "fq_server_wait": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.POINTER(_Result)]),
+    "fq_server_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(_ServerStats)]),
+    "fq_server_destroy": (None, [_P]),
     "fq_mixed_create": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
     "fq_mixed_reassemble": (ctypes.c_int, [_P]),
     "fq_mixed_solve": (ctypes.c_int, [_P, _DP, _DP, _DP, _DP, ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
@@ -596,3 +623,67 @@ def hx_apply(mesh: Mesh, grade: int, bc: int, r: np.ndarray) -> np.ndarray:
     y = np.zeros_like(r)
     mesh.ctx.check(mesh.ctx.L.fq_hx_apply(mesh.ctx.h, mesh.h, int(grade), int(bc), _dp(r), _dp(y)), "fq_hx_apply")
     return y
+
+
+class Server:
+    """The serving loop (fq_server_*): lanes with their own streams, HBM-budget
+    admission, meshes and solver state resident between requests."""
+
+    def __init__(self, device: int = 0, lanes: int = 4, budget_bytes: int = 0, cache: bool = True):
+        self.L = load()
+        h = _P()
+        s = self.L.fq_server_create(int(device), int(lanes), int(budget_bytes), int(bool(cache)), ctypes.byref(h))
+        if s != 0:
+            raise FqError(s, f"fq_server_create: {_STATUS.get(s, s)}")
+        self.h = h
+        self._keep = {}
+
+    def submit(self, kind: int, dim: int, nbox: int, grade: int = 0, bc: int = FQ_ABSOLUTE, minkowski: bool = False,
+               jitter: float = 0.1, seed: int = 0, mass_term: float = 1.5, arrival_ms: float = -1.0,
+               lengths: Optional[np.ndarray] = None, source: Optional[np.ndarray] = None,
+               solution: Optional[np.ndarray] = None, opts: Optional[SolveOpts] = None) -> int:
+        keep = []
+        r = _Request()
+        r.kind, r.dim, r.nbox, r.grade, r.bc = int(kind), int(dim), int(nbox), int(grade), int(bc)
+        r.minkowski, r.jitter, r.seed, r.mass_term = int(bool(minkowski)), float(jitter), int(seed), float(mass_term)
+        r.arrival_ms = float(arrival_ms)
+        for name, arr in (("lengths", lengths), ("source", source), ("solution", solution)):
+            if arr is not None:
+                if arr.dtype != np.float64 or not arr.flags["C_CONTIGUOUS"]:
+                    raise ValueError(f"{name} must be a contiguous float64 array")
+                keep.append(arr)
+                setattr(r, name, arr.ctypes.data)
+        r.opts = opts or SolveOpts.default()
+        t = ctypes.c_uint64()
+        s = self.L.fq_server_submit(self.h, ctypes.byref(r), ctypes.byref(t))
+        if s != 0:
+            raise FqError(s, f"fq_server_submit: {_STATUS.get(s, s)}")
+        self._keep[t.value] = keep
+        return t.value
+
+    def wait(self, ticket: int) -> dict:
+        res = _Result()
+        s = self.L.fq_server_wait(self.h, ctypes.c_uint64(ticket), ctypes.byref(res))
+        if s != 0:
+            raise FqError(s, f"fq_server_wait: {_STATUS.get(s, s)}")
+        self._keep.pop(ticket, None)
+        return {"status": res.status, "lane": res.lane, "report": Report.of(res.report), "queue_ms": res.queue_ms,
+                "run_ms": res.run_ms, "latency_ms": res.latency_ms, "start_ms": res.start_ms, "end_ms": res.end_ms,
+                "checksum": res.checksum, "ndofs": res.ndofs, "cache_hit": bool(res.cache_hit)}
+
+    def stats(self) -> dict:
+        st = _ServerStats()
+        self.L.fq_server_get_stats(self.h, ctypes.byref(st))
+        return {f: getattr(st, f) for f, _ in _ServerStats._fields_}
+
+    def close(self):
+        if self.h:
+            self.L.fq_server_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -64,12 +64,15 @@ fq_status DevBuf::alloc(fq_ctx* c, size_t nbytes) {
   if (c->budget && c->in_use + nbytes > c->budget)
     return set_error(c, FQ_OOM_BUDGET, "HBM budget exceeded: " + std::to_string(c->in_use + nbytes) + " > " +
                                            std::to_string(c->budget) + " bytes");
+  // Stream-ordered allocation from the device's memory pool: neither this nor
+  // the matching free synchronizes the device, so contexts on other streams (the
+  // lanes of a server) keep running while one allocates.
   void* q = nullptr;
-  cudaError_t e = cudaMalloc(&q, nbytes);
+  cudaError_t e = cudaMallocAsync(&q, nbytes, c->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return set_error(c, e == cudaErrorMemoryAllocation ? FQ_OOM_BUDGET : FQ_CUDA_ERROR,
-                     std::string("cudaMalloc: ") + cudaGetErrorString(e));
+                     std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
   }
   ctx = c;
   p = q;
@@ -80,8 +83,12 @@ fq_status DevBuf::alloc(fq_ctx* c, size_t nbytes) {
 
 void DevBuf::release() {
   if (p) {
-    cudaFree(p);
-    if (ctx) ctx->in_use -= bytes;
+    if (ctx) {
+      cudaFreeAsync(p, ctx->stream);  // after the work already queued on the owner's stream
+      ctx->in_use -= bytes;
+    } else {
+      cudaFree(p);
+    }
   }
   p = nullptr;
   bytes = 0;
@@ -405,27 +412,31 @@ static fq_status mixed_precond(fq_mixed* P, const fq_solve_opts* o, const HxPrec
   const int want = o->preconditioner;
   if (want == FQ_PC_JACOBI) return FQ_OK;
   if (want != FQ_PC_AUTO && want != FQ_PC_HX) return set_error(P->ctx, FQ_INVALID_ARG, "unknown preconditioner");
-  if (P->hx && !P->hx_stale) {
-    *out = P->hx.get();
-    return FQ_OK;
+  if (!P->hx_stale) {
+    if (P->hx && !P->hx_failed) {
+      *out = P->hx.get();
+      return FQ_OK;
+    }
+    if (P->hx_failed && want == FQ_PC_AUTO) return FQ_OK;  // Jacobi, as decided for these lengths
   }
-  if (want == FQ_PC_AUTO && P->hx_failed && P->hx_stale == false) return FQ_OK;
   std::vector<int> grades;
   if (P->grade >= 1) grades.push_back(P->grade - 1);
   grades.push_back(P->grade);
-  auto hx = std::make_unique<HxPrecond>();
-  fq_status s = hx_supported(P->mesh) ? hx_build(P->ctx, P->mesh, P->bc, grades, P->nh, P->diag.as<double>(), *hx)
-                                      : set_error(P->ctx, FQ_UNSUPPORTED, "HX multigrid needs a Kuhn cube mesh");
-  if (s == FQ_OK && P->precision == FQ_FP32) s = hx->make_f32(P->ctx);
-  P->hx_stale = false;
-  if (s != FQ_OK) {
-    P->hx.reset();
-    P->hx_failed = true;
-    if (want == FQ_PC_HX) return s;
-    return FQ_OK;  // FQ_PC_AUTO: Jacobi
+  fq_status s = FQ_OK;
+  if (!hx_supported(P->mesh)) {
+    s = set_error(P->ctx, FQ_UNSUPPORTED, "HX multigrid needs a Kuhn cube mesh");
+  } else if (P->hx && hx_matches(*P->hx, P->mesh, P->bc, grades, P->nh)) {
+    // new lengths on the same mesh: keep the lattice structure, refresh the numbers
+    s = hx_refresh(P->ctx, P->mesh, P->diag.as<double>(), *P->hx);
+  } else {
+    auto hx = std::make_unique<HxPrecond>();
+    s = hx_build(P->ctx, P->mesh, P->bc, grades, P->nh, P->diag.as<double>(), *hx);
+    if (s == FQ_OK) P->hx = std::move(hx);
   }
-  P->hx_failed = false;
-  P->hx = std::move(hx);
+  if (s == FQ_OK && P->precision == FQ_FP32) s = P->hx->make_f32(P->ctx);
+  P->hx_stale = false;
+  P->hx_failed = s != FQ_OK;
+  if (s != FQ_OK) return want == FQ_PC_HX ? s : FQ_OK;  // FQ_PC_AUTO: Jacobi
   *out = P->hx.get();
   return FQ_OK;
 }
@@ -555,8 +566,18 @@ fq_status fq_ctx_create(int device, void* stream, uint64_t budget, fq_ctx** out)
     }
     ctx->owns_stream = true;
   }
+  {
+    // keep freed pool memory with the process instead of returning it at every
+    // synchronization, so steady-state solves do not go back to the driver
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
   if (ctx->status.alloc(ctx, 8 * sizeof(int)) != FQ_OK ||
-      cudaMallocHost(reinterpret_cast<void**>(&ctx->host_status), 8 * sizeof(int)) != cudaSuccess) {
+      cudaMallocHost(reinterpret_cast<void**>(&ctx->host_status), 8 * sizeof(int)) != cudaSuccess ||
+      cudaMallocHost(&ctx->host_solver, 1024) != cudaSuccess) {
     fq_ctx_destroy(ctx);
     return FQ_CUDA_ERROR;
   }
@@ -572,7 +593,9 @@ void fq_ctx_destroy(fq_ctx* ctx) {
     if (e) cudaEventDestroy(e);
   ctx->status.release();
   ctx->scratch.release();
+  cudaStreamSynchronize(ctx->stream);
   if (ctx->host_status) cudaFreeHost(ctx->host_status);
+  if (ctx->host_solver) cudaFreeHost(ctx->host_solver);
   if (ctx->owns_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

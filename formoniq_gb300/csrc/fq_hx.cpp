@@ -30,12 +30,14 @@ namespace fq {
 fq_status make_matrix(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int bc, int precision, double param,
                       fq_matrix** out);
 void coboundary_host(const fq_mesh* m, int k, int bc, HCsr& out);
+fq_status assemble_into(fq_ctx* ctx, fq_matrix* m);
 fq_status device_scaled_recip(fq_ctx* ctx, const double* d, int64_t n, double omega, DevBuf& out);
 
 namespace {
 
 constexpr double kOmega = 2.0 / 3.0;  // Jacobi::smoother (iterative/src/precond.rs:92-94)
 constexpr int64_t kCoarseMax = 256;
+const double kUnit[4] = {1.0, 1.0, 1.0, 1.0};  // lattice frame before scaling
 
 int64_t ipow(int64_t b, int e) {
   int64_t r = 1;
@@ -179,31 +181,6 @@ int64_t find_edge(const fq_mesh* m, int32_t u, int32_t v) {
   return -1;
 }
 
-// Root mean squared length of the lattice edges along each axis; false if some
-// squared length is not positive (no Riemannian frame).
-bool lattice_spacing(const fq_mesh* m, const std::vector<double>& len, double* h) {
-  const int n = m->dim, nb = m->kuhn_nbox;
-  const int64_t nv = ipow(nb + 1, n);
-  int c[4];
-  for (int a = 0; a < n; ++a) {
-    double s = 0.0;
-    int64_t cnt = 0;
-    const int64_t stride = ipow(nb + 1, a);
-    for (int64_t v = 0; v < nv; ++v) {
-      lattice_coords(v, n, nb, c);
-      if (c[a] >= nb) continue;
-      const int64_t e = find_edge(m, int32_t(v), int32_t(v + stride));
-      if (e < 0) return false;
-      if (!(len[e] > 0.0)) return false;
-      s += len[e];
-      ++cnt;
-    }
-    if (cnt == 0) return false;
-    h[a] = std::sqrt(s / double(cnt));
-  }
-  return true;
-}
-
 double small_det(double (*e)[4], int j) {
   if (j == 0) return 1.0;
   if (j == 1) return e[0][0];
@@ -228,6 +205,7 @@ double small_det(double (*e)[4], int j) {
 // Pi_j with columns as offsets into the interleaved nodal block (node * m +
 // slot + I), and its transpose with rows ordered (node, I).
 void vector_nodal(const fq_mesh* m, int j, int bc, const double* h, int mslots, int slot, HCsr& Pi, HCsr& Pit) {
+  // (h is the unit spacing at build time: the values are scaled per component on the device)
   const int n = m->dim, nb = m->kuhn_nbox;
   const int ncomp = j == 0 ? 1 : binom(n, j);
   const int64_t n0 = level_nodes(n, nb, bc);
@@ -254,7 +232,11 @@ void vector_nodal(const fq_mesh* m, int j, int bc, const double* h, int mslots, 
     int64_t trow;
     int32_t row;
     double v;
+    uint8_t mask;
   };
+  std::vector<uint8_t> masks(size_t(ncomp), 0);
+  for (int q = 0; q < ncomp && j > 0; ++q)
+    for (int a : subsets[q]) masks[q] |= uint8_t(1u << a);
   std::vector<Ent> tr;
   const int w = j + 1;
   int32_t row = 0;
@@ -276,7 +258,7 @@ void vector_nodal(const fq_mesh* m, int j, int bc, const double* h, int mslots, 
           for (int cc = 0; cc < j; ++cc) sub[r][cc] = E[subsets[q][r]][cc];
         comp[q] = small_det(sub, j);
       }
-    std::vector<std::pair<int64_t, double>> ent;
+    std::vector<std::pair<int64_t, double>> ent;  // (column, value); column - node*m - slot = component
     for (int i = 0; i < w; ++i) {
       int cv[4];
       lattice_coords(vs[i], n, nb, cv);
@@ -286,13 +268,14 @@ void vector_nodal(const fq_mesh* m, int j, int bc, const double* h, int mslots, 
         const double val = factor * comp[q];
         if (val == 0.0) continue;
         ent.emplace_back(node * mslots + slot + q, val);
-        tr.push_back({node * ncomp + q, row, val});
+        tr.push_back({node * ncomp + q, row, val, masks[q]});
       }
     }
     std::sort(ent.begin(), ent.end());
     for (auto& e : ent) {
       Pi.ci.push_back(int32_t(e.first));
       Pi.v.push_back(e.second);
+      Pi.mask.push_back(masks[int((e.first % mslots) - slot)]);
     }
     Pi.rp.push_back(int32_t(Pi.ci.size()));
     ++row;
@@ -308,11 +291,13 @@ void vector_nodal(const fq_mesh* m, int j, int bc, const double* h, int mslots, 
   Pit.rp = cnt;
   Pit.ci.resize(tr.size());
   Pit.v.resize(tr.size());
+  Pit.mask.resize(tr.size());
   std::vector<int32_t> pos(cnt.begin(), cnt.end() - 1);
   for (auto& e : tr) {
     const int32_t p = pos[e.trow]++;
     Pit.ci[p] = e.row;
     Pit.v[p] = e.v;
+    Pit.mask[p] = e.mask;
   }
 }
 
@@ -328,9 +313,11 @@ void slot_identity(int64_t n0, int mslots, int slot, HCsr& Pi, HCsr& Pit) {
   for (int64_t i = 0; i < n0; ++i) {
     Pi.ci.push_back(int32_t(i * mslots + slot));
     Pi.v.push_back(1.0);
+    Pi.mask.push_back(0);
     Pi.rp.push_back(int32_t(i + 1));
     Pit.ci.push_back(int32_t(i));
     Pit.v.push_back(1.0);
+    Pit.mask.push_back(0);
     Pit.rp.push_back(int32_t(i + 1));
   }
 }
@@ -360,19 +347,45 @@ HCsr transpose(const HCsr& a) {
 
 bool hx_supported(const fq_mesh* m) { return m && m->kuhn_nbox > 0 && m->dim >= 1 && m->dim <= 4 && m->has_lengths; }
 
+bool hx_matches(const HxPrecond& pc, const fq_mesh* m, int bc, const std::vector<int>& grades, int64_t ident) {
+  return pc.mesh == m && pc.bc == bc && pc.grades == grades && pc.ident_len == ident;
+}
+
 fq_status hx_build(fq_ctx* ctx, fq_mesh* m, int bc, const std::vector<int>& grades, int64_t ident,
                    const double* diag_blocks, HxPrecond& out) {
   if (!hx_supported(m)) return set_error(ctx, FQ_UNSUPPORTED, "HX multigrid needs a Kuhn cube mesh with lengths");
   const int n = m->dim, nb = m->kuhn_nbox;
   cudaStream_t st = ctx->stream;
-  std::vector<double> len(m->nsimp[1]);
-  FQ_CUDA(ctx, cudaMemcpyAsync(len.data(), m->lengths.p, len.size() * 8, cudaMemcpyDeviceToHost, st));
-  FQ_CUDA(ctx, cudaStreamSynchronize(st));
-  double h[4] = {1, 1, 1, 1};
-  if (!lattice_spacing(m, len, h))
-    return set_error(ctx, FQ_UNSUPPORTED, "HX multigrid needs positive squared lengths (a Riemannian metric)");
-
   out = HxPrecond();
+  out.mesh = m;
+  out.bc = bc;
+  out.grades = grades;
+
+  // lattice edges per axis, for the frame scaling
+  {
+    std::vector<int32_t> edges;
+    out.axis_off.assign(1, 0);
+    const int64_t nv = ipow(nb + 1, n);
+    int c[4];
+    for (int a = 0; a < n; ++a) {
+      const int64_t stride = ipow(nb + 1, a);
+      for (int64_t v = 0; v < nv; ++v) {
+        lattice_coords(v, n, nb, c);
+        if (c[a] >= nb) continue;
+        const int64_t e = find_edge(m, int32_t(v), int32_t(v + stride));
+        if (e < 0) return set_error(ctx, FQ_UNSUPPORTED, "mesh is not a Kuhn lattice");
+        edges.push_back(int32_t(e));
+      }
+      out.axis_off.push_back(int64_t(edges.size()));
+    }
+    FQ_TRY(out.axis_edges.alloc(ctx, std::max<size_t>(edges.size(), 1) * 4));
+    if (!edges.empty())
+      FQ_CUDA(ctx, cudaMemcpyAsync(out.axis_edges.p, edges.data(), edges.size() * 4, cudaMemcpyHostToDevice, st));
+    FQ_TRY(out.hprod.alloc(ctx, 16 * 8));
+    FQ_TRY(out.flag.alloc(ctx, 8));
+    FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  }
+
   // slot layout
   int mslots = 0;
   out.blocks.resize(grades.size());
@@ -397,7 +410,7 @@ fq_status hx_build(fq_ctx* ctx, fq_mesh* m, int bc, const std::vector<int>& grad
   out.n = off + ident;
   out.m = mslots;
 
-  // nodal hierarchy
+  // nodal hierarchy: lattices, prolongations, work blocks
   NodalHierarchy& mg = out.mg;
   mg.dim = n;
   mg.bc = bc;
@@ -405,23 +418,10 @@ fq_status hx_build(fq_ctx* ctx, fq_mesh* m, int bc, const std::vector<int>& grad
   std::vector<int> boxes{nb};
   while (level_nodes(n, boxes.back(), bc) > kCoarseMax && boxes.back() > 2) boxes.push_back((boxes.back() + 1) / 2);
   mg.lv.resize(boxes.size());
-  {
-    fq_matrix* a0 = nullptr;
-    FQ_TRY(make_matrix(ctx, m, EK_HDIF, 0, bc, FQ_FP64, 0.0, &a0));
-    std::unique_ptr<fq_matrix> guard(a0);
-    // own a copy: the matrix object is freed below
-    HCsr ha;
-    DCsr view;
-    view.view(a0);
-    FQ_TRY(device_to_host(ctx, view, ha));
-    FQ_TRY(upload(ctx, ha, mg.lv[0].A));
-  }
   for (size_t l = 0; l < boxes.size(); ++l) {
     NodalLevel& L = mg.lv[l];
     L.nbox = boxes[l];
     L.n = level_nodes(n, boxes[l], bc);
-    if (L.A.nrows != L.n) return set_error(ctx, FQ_UNSUPPORTED, "nodal operator size does not match the lattice");
-    FQ_TRY(device_diag_recip(ctx, L.A, kOmega, L.dinv64));
     const size_t wb = size_t(std::max<int64_t>(L.n * mslots, 1)) * 8;
     FQ_TRY(L.x[0].alloc(ctx, wb));
     FQ_TRY(L.x[1].alloc(ctx, wb));
@@ -429,38 +429,27 @@ fq_status hx_build(fq_ctx* ctx, fq_mesh* m, int bc, const std::vector<int>& grad
     FQ_TRY(L.t.alloc(ctx, wb));
     if (l + 1 < boxes.size()) {
       HCsr P = lattice_prolongation(n, boxes[l], boxes[l + 1], bc);
-      HCsr R = transpose(P);
       FQ_TRY(upload(ctx, P, L.P));
-      FQ_TRY(upload(ctx, R, L.R));
-      FQ_TRY(galerkin_product(ctx, L.A, L.P, mg.lv[l + 1].A));
+      FQ_TRY(upload(ctx, transpose(P), L.R));
     }
   }
   {
-    NodalLevel& C = mg.lv.back();
-    mg.nc = C.n;
-    HCsr hc;
-    FQ_TRY(device_to_host(ctx, C.A, hc));
-    std::vector<double> dense(size_t(std::max<int64_t>(C.n * C.n, 1)), 0.0);
-    for (int64_t r = 0; r < C.n; ++r)
-      for (int32_t q = hc.rp[r]; q < hc.rp[r + 1]; ++q) dense[r * C.n + hc.ci[q]] += hc.v[q];
-    if (C.n > 0 && !spd_inverse(dense, C.n))
-      return set_error(ctx, FQ_UNSUPPORTED, "coarsest nodal operator is not positive definite");
-    FQ_TRY(mg.coarse_inv64.alloc(ctx, dense.size() * 8));
-    FQ_CUDA(ctx, cudaMemcpyAsync(mg.coarse_inv64.p, dense.data(), dense.size() * 8, cudaMemcpyHostToDevice, st));
-    FQ_CUDA(ctx, cudaStreamSynchronize(st));
+    fq_matrix* a0 = nullptr;
+    FQ_TRY(make_matrix(ctx, m, EK_HDIF, 0, bc, FQ_FP64, 0.0, &a0));
+    out.a0.reset(a0);
+    if (a0->nrows != mg.lv[0].n) return set_error(ctx, FQ_UNSUPPORTED, "nodal operator size does not match the lattice");
   }
 
-  // blocks
+  // blocks: transfer maps (lattice values; scaled by the spacing in hx_refresh)
   const int64_t n0 = mg.lv[0].n;
   for (HxBlock& B : out.blocks) {
-    FQ_TRY(device_scaled_recip(ctx, diag_blocks + B.off, B.size, kOmega, B.s64));
     HCsr Pi, Pit;
     if (B.grade == 0)
       slot_identity(n0, mslots, B.vec_slot, Pi, Pit);
     else
-      vector_nodal(m, B.grade, bc, h, mslots, B.vec_slot, Pi, Pit);
-    FQ_TRY(upload(ctx, Pi, B.Pi));
-    FQ_TRY(upload(ctx, Pit, B.Pit));
+      vector_nodal(m, B.grade, bc, kUnit, mslots, B.vec_slot, Pi, Pit);
+    FQ_TRY(upload_scalable(ctx, Pi, B.Pi));
+    FQ_TRY(upload_scalable(ctx, Pit, B.Pit));
     if (B.grade >= 1) {
       const int g = B.grade - 1;
       HCsr D;
@@ -474,30 +463,96 @@ fq_status hx_build(fq_ctx* ctx, fq_mesh* m, int bc, const std::vector<int>& grad
       if (g == 0)
         slot_identity(n0, mslots, B.grad_slot, PiL, PiLt);
       else
-        vector_nodal(m, g, bc, h, mslots, B.grad_slot, PiL, PiLt);
-      FQ_TRY(upload(ctx, PiL, B.PiL));
-      FQ_TRY(upload(ctx, PiLt, B.PiLt));
-      // S_{g}: the smoother of hdif_gram(g): a block's own diagonal when the
-      // operator has a block of that grade, else assembled here.
-      const HxBlock* same = nullptr;
-      for (const HxBlock& o : out.blocks)
-        if (o.grade == g) same = &o;
-      if (same) {
-        FQ_TRY(device_scaled_recip(ctx, diag_blocks + same->off, same->size, kOmega, B.sl64));
-      } else if (g == 0) {
-        FQ_TRY(device_diag_recip(ctx, mg.lv[0].A, kOmega, B.sl64));
-      } else {
+        vector_nodal(m, g, bc, kUnit, mslots, B.grad_slot, PiL, PiLt);
+      FQ_TRY(upload_scalable(ctx, PiL, B.PiL));
+      FQ_TRY(upload_scalable(ctx, PiLt, B.PiLt));
+      // a gradient smoother of a grade that is neither a block nor the nodal one
+      bool have = g == 0;
+      for (int o : grades) have = have || o == g;
+      for (int o : out.aux_grade) have = have || o == g;
+      if (!have) {
         fq_matrix* ag = nullptr;
         FQ_TRY(make_matrix(ctx, m, EK_HDIF, g, bc, FQ_FP64, 0.0, &ag));
-        std::unique_ptr<fq_matrix> guard(ag);
-        DCsr view;
-        view.view(ag);
-        FQ_TRY(device_diag_recip(ctx, view, kOmega, B.sl64));
-        FQ_CUDA(ctx, cudaStreamSynchronize(st));
+        out.aux.emplace_back(ag);
+        out.aux_grade.push_back(g);
       }
     }
   }
+  return hx_refresh(ctx, m, diag_blocks, out);
+}
+
+fq_status hx_refresh(fq_ctx* ctx, fq_mesh* m, const double* diag_blocks, HxPrecond& pc) {
+  cudaStream_t st = ctx->stream;
+  const int n = m->dim;
+  NodalHierarchy& mg = pc.mg;
+  // frame spacing from the current lengths
+  launch_lattice_spacing(m->lengths.as<double>(), pc.axis_edges.as<int32_t>(), pc.axis_off.data(), n,
+                         pc.hprod.as<double>(), pc.flag.as<int>(), st);
+  int bad = 0;
+  FQ_CUDA(ctx, cudaMemcpyAsync(&bad, pc.flag.p, 4, cudaMemcpyDeviceToHost, st));
   FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  if (bad) return set_error(ctx, FQ_UNSUPPORTED, "HX multigrid needs positive squared lengths (a Riemannian metric)");
+  auto scale = [&](DCsr& d) {
+    if (d.scalable)
+      launch_scale_by_mask(d.own_base.as<double>(), d.own_mask.as<uint8_t>(), pc.hprod.as<double>(),
+                           d.own_v64.as<double>(), d.nnz, st);
+  };
+  for (HxBlock& B : pc.blocks) {
+    scale(B.Pi);
+    scale(B.Pit);
+    if (B.grade >= 1) {
+      scale(B.PiL);
+      scale(B.PiLt);
+    }
+  }
+  // operators: the nodal operator and the Galerkin products
+  FQ_TRY(assemble_into(ctx, pc.a0.get()));
+  for (auto& a : pc.aux) FQ_TRY(assemble_into(ctx, a.get()));
+  mg.lv[0].A.view(pc.a0.get());
+  for (size_t l = 0; l < mg.lv.size(); ++l) {
+    NodalLevel& L = mg.lv[l];
+    FQ_TRY(device_diag_recip(ctx, L.A, kOmega, L.dinv64));
+    if (l + 1 < mg.lv.size()) FQ_TRY(galerkin_product(ctx, L.A, L.P, mg.lv[l + 1].A));
+  }
+  {
+    NodalLevel& C = mg.lv.back();
+    mg.nc = C.n;
+    HCsr hc;
+    FQ_TRY(device_to_host(ctx, C.A, hc));
+    std::vector<double> dense(size_t(std::max<int64_t>(C.n * C.n, 1)), 0.0);
+    for (int64_t r = 0; r < C.n; ++r)
+      for (int32_t q = hc.rp[r]; q < hc.rp[r + 1]; ++q) dense[r * C.n + hc.ci[q]] += hc.v[q];
+    if (C.n > 0 && !spd_inverse(dense, C.n))
+      return set_error(ctx, FQ_UNSUPPORTED, "coarsest nodal operator is not positive definite");
+    FQ_TRY(mg.coarse_inv64.alloc(ctx, dense.size() * 8));
+    FQ_CUDA(ctx, cudaMemcpyAsync(mg.coarse_inv64.p, dense.data(), dense.size() * 8, cudaMemcpyHostToDevice, st));
+  }
+  // smoothers
+  for (HxBlock& B : pc.blocks) {
+    FQ_TRY(device_scaled_recip(ctx, diag_blocks + B.off, B.size, kOmega, B.s64));
+    if (B.grade < 1) continue;
+    const int g = B.grade - 1;
+    const HxBlock* same = nullptr;
+    for (const HxBlock& o : pc.blocks)
+      if (o.grade == g) same = &o;
+    if (same) {
+      FQ_TRY(device_scaled_recip(ctx, diag_blocks + same->off, same->size, kOmega, B.sl64));
+    } else if (g == 0) {
+      FQ_TRY(device_diag_recip(ctx, mg.lv[0].A, kOmega, B.sl64));
+    } else {
+      for (size_t i = 0; i < pc.aux.size(); ++i)
+        if (pc.aux_grade[i] == g) {
+          DCsr view;
+          view.view(pc.aux[i].get());
+          FQ_TRY(device_diag_recip(ctx, view, kOmega, B.sl64));
+        }
+    }
+  }
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  if (pc.has_f32) {
+    pc.has_f32 = false;
+    FQ_TRY(pc.make_f32(ctx));
+  }
   return FQ_OK;
 }
 

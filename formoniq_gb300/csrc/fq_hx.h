@@ -21,6 +21,7 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 #include "fq_internal.h"
@@ -36,6 +37,10 @@ struct DCsr {
   const double* v64 = nullptr;
   const float* v32 = nullptr;
   DevBuf own_rp, own_ci, own_v64, own_v32;
+  // Vector-nodal maps keep their lattice values (unit spacing) and, per entry,
+  // the axis set I of its component: value = base * prod_{a in I} h_a.
+  DevBuf own_base, own_mask;
+  bool scalable = false;
 
   fq_status upload(fq_ctx* ctx, int64_t nr, int64_t nc, const std::vector<int32_t>& hrp,
                    const std::vector<int32_t>& hci, const std::vector<double>& hv);
@@ -50,6 +55,7 @@ struct HCsr {
   int64_t nrows = 0, ncols = 0;
   std::vector<int32_t> rp{0}, ci;
   std::vector<double> v;
+  std::vector<uint8_t> mask;  // optional: axis set of each entry's component
 };
 HCsr transpose(const HCsr& a);
 
@@ -96,6 +102,17 @@ struct HxPrecond {
   int64_t ident_off = 0, ident_len = 0;  // identity tail (harmonic border)
   int m = 0;                 // nodal slots
   bool has_f32 = false;
+  // structure key: what the lattice-only parts were built for
+  const fq_mesh* mesh = nullptr;
+  int bc = 0;
+  std::vector<int> grades;
+  // length-dependent inputs, reassembled by hx_refresh
+  std::unique_ptr<fq_matrix> a0;                 // hdif_gram(0)
+  std::vector<std::unique_ptr<fq_matrix>> aux;   // hdif_gram(g) of gradient smoothers
+  std::vector<int> aux_grade;
+  DevBuf axis_edges;                             // lattice edge kidx per axis, concatenated
+  std::vector<int64_t> axis_off;                 // [n+1]
+  DevBuf hprod, flag;                            // [16] products of spacings; [1] non-positive length seen
   fq_status make_f32(fq_ctx* ctx);
 };
 
@@ -109,12 +126,24 @@ bool hx_supported(const fq_mesh* m);
 // block vector layout). Recomputes everything that depends on the lengths.
 fq_status hx_build(fq_ctx* ctx, fq_mesh* m, int bc, const std::vector<int>& grades, int64_t ident,
                    const double* diag_blocks, HxPrecond& out);
+// Whether `pc` was built for this mesh, boundary condition and block grades.
+bool hx_matches(const HxPrecond& pc, const fq_mesh* m, int bc, const std::vector<int>& grades, int64_t ident);
+// Recompute everything that depends on the lengths (operators, Galerkin
+// products, coarse inverse, smoothers, frame scaling), keeping the structure.
+fq_status hx_refresh(fq_ctx* ctx, fq_mesh* m, const double* diag_blocks, HxPrecond& pc);
 
 // ---- device parts (fq_mg.cu) ----
 fq_status galerkin_product(fq_ctx* ctx, const DCsr& A, const DCsr& P, DCsr& out);
 fq_status device_diag_recip(fq_ctx* ctx, const DCsr& A, double omega, DevBuf& out);
 fq_status device_to_host(fq_ctx* ctx, const DCsr& A, HCsr& out);
 void launch_f64_to_f32(const double* a, float* o, int64_t n, cudaStream_t st);
+// h_a = sqrt(mean of the axis-a lattice edge lengths), hprod[I] = prod_{a in I} h_a;
+// flag = 1 when a length is not positive.
+void launch_lattice_spacing(const double* lengths, const int32_t* axis_edges, const int64_t* off_host, int n,
+                            double* hprod, int* flag, cudaStream_t st);
+fq_status upload_scalable(fq_ctx* ctx, const HCsr& h, DCsr& d);
+void launch_scale_by_mask(const double* base, const uint8_t* mask, const double* hprod, double* out, int64_t nnz,
+                          cudaStream_t st);
 
 // y = B r on `st`; every kernel returns at once when *done != 0 (a Krylov loop
 // that has converged), so the preconditioner can sit inside a captured graph.

@@ -123,6 +123,7 @@ struct fq_ctx {
   std::string last_error;
   fq::DevBuf status;       // int [8] device status words
   int* host_status = nullptr;  // pinned mirror
+  void* host_solver = nullptr; // pinned slots for polling Krylov state (1 KiB)
   fq::DevBuf scratch;      // reusable temporary storage
   // instrumentation: CUDA events on `stream` around element passes (slot 0) and
   // scatters (slot 1) of every assembly while `profiling` is set

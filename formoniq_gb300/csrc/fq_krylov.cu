@@ -522,16 +522,19 @@ static fq_status run_graph_loop(fq_ctx* ctx, SolverState* S, int64_t max_iters, 
     one_iteration(0);
     one_iteration(1);
     cudaError_t ce = cudaStreamEndCapture(st, &graph);
-    if (ce != cudaSuccess) return cuda_check(ctx, ce, "cudaStreamEndCapture");
-    ce = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ce != cudaSuccess) return cuda_check(ctx, ce, "cudaGraphInstantiate");
+    if (ce == cudaSuccess) {
+      ce = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) exec = nullptr;
+    }
+    // a capture that failed leaves the iteration to direct launches
+    if (ce != cudaSuccess) cudaGetLastError();
   } else {
     cudaGetLastError();
   }
-  SolverState* pinned = nullptr;
+  static_assert(2 * sizeof(SolverState) <= 1024, "pinned polling slots");
+  SolverState* pinned = static_cast<SolverState*>(ctx->host_solver);
   cudaEvent_t ev[2];
-  FQ_CUDA(ctx, cudaMallocHost(reinterpret_cast<void**>(&pinned), 2 * sizeof(SolverState)));
   cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
   cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
   fq_status status = FQ_OK;
@@ -572,11 +575,11 @@ static fq_status run_graph_loop(fq_ctx* ctx, SolverState* S, int64_t max_iters, 
     }
     batch = std::min<int64_t>(batch * 2, max_batch);
   }
-  FQ_CUDA(ctx, cudaStreamSynchronize(st));
-  cudaError_t e = cudaMemcpy(final_state, S, sizeof(SolverState), cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaMemcpyAsync(pinned, S, sizeof(SolverState), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) *final_state = pinned[0];
   cudaEventDestroy(ev[0]);
   cudaEventDestroy(ev[1]);
-  cudaFreeHost(pinned);
   if (exec) cudaGraphExecDestroy(exec);
   if (status != FQ_OK) return status;
   if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMemcpy state");

@@ -354,6 +354,77 @@ __global__ void scaled_recip_kernel(const double* __restrict__ d, int64_t n, dou
     out[i] = d[i] != 0.0 ? omega / d[i] : 0.0;
 }
 
+struct AxisOffsets {
+  int64_t o[5];
+};
+
+// One block: deterministic per-axis means, then the 2^n products.
+__global__ void lattice_spacing_kernel(const double* __restrict__ len, const int32_t* __restrict__ edges, AxisOffsets off,
+                                       int n, double* __restrict__ hprod, int* __restrict__ flag) {
+  __shared__ double sh[32];
+  __shared__ double h[4];
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int a = 0; a < n; ++a) {
+    double acc = 0.0;
+    for (int64_t i = off.o[a] + threadIdx.x; i < off.o[a + 1]; i += blockDim.x) {
+      const double v = len[edges[i]];
+      if (!(v > 0.0)) bad = 1;
+      acc += v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < int(blockDim.x >> 5); ++w) t += sh[w];
+      const int64_t cnt = off.o[a + 1] - off.o[a];
+      h[a] = cnt > 0 ? sqrt(fmax(t / double(cnt), 0.0)) : 1.0;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 16) {
+    double p = 1.0;
+    for (int a = 0; a < n; ++a)
+      if (threadIdx.x & (1u << a)) p *= h[a];
+    hprod[threadIdx.x] = p;
+  }
+  if (threadIdx.x == 0) *flag = bad;
+}
+
+__global__ void scale_by_mask_kernel(const double* __restrict__ base, const uint8_t* __restrict__ mask,
+                                     const double* __restrict__ hprod, double* __restrict__ out, int64_t nnz) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nnz; i += int64_t(gridDim.x) * blockDim.x)
+    out[i] = base[i] * hprod[mask[i]];
+}
+
+void launch_lattice_spacing(const double* lengths, const int32_t* axis_edges, const int64_t* off_host, int n,
+                            double* hprod, int* flag, cudaStream_t st) {
+  AxisOffsets o{};
+  for (int a = 0; a <= n; ++a) o.o[a] = off_host[a];
+  lattice_spacing_kernel<<<1, 1024, 0, st>>>(lengths, axis_edges, o, n, hprod, flag);
+}
+
+void launch_scale_by_mask(const double* base, const uint8_t* mask, const double* hprod, double* out, int64_t nnz,
+                          cudaStream_t st) {
+  if (nnz > 0) scale_by_mask_kernel<<<grid_for_n(nnz), MT, 0, st>>>(base, mask, hprod, out, nnz);
+}
+
+fq_status upload_scalable(fq_ctx* ctx, const HCsr& h, DCsr& d) {
+  FQ_TRY(d.upload(ctx, h.nrows, h.ncols, h.rp, h.ci, h.v));
+  FQ_TRY(d.own_base.alloc(ctx, std::max<int64_t>(d.nnz, 1) * 8));
+  FQ_TRY(d.own_mask.alloc(ctx, std::max<int64_t>(d.nnz, 1)));
+  if (d.nnz) {
+    FQ_CUDA(ctx, cudaMemcpyAsync(d.own_base.p, d.own_v64.p, d.nnz * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    FQ_CUDA(ctx, cudaMemcpyAsync(d.own_mask.p, h.mask.data(), d.nnz, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  d.scalable = true;
+  return FQ_OK;
+}
+
 fq_status device_scaled_recip(fq_ctx* ctx, const double* d, int64_t n, double omega, DevBuf& out) {
   FQ_TRY(out.alloc(ctx, std::max<int64_t>(n, 1) * 8));
   if (n > 0) scaled_recip_kernel<<<grid_for_n(n), MT, 0, ctx->stream>>>(d, n, omega, out.as<double>());

@@ -281,6 +281,71 @@ fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* mesh, double mass_term, co
 /* The assembled relative Dirac system S (for parity tests); caller destroys. */
 fq_status fq_dirac_system(fq_ctx* ctx, fq_mesh* mesh, double mass_term, fq_matrix** out);
 
+/* ---- serving: continuously batched solve requests ----------------------- */
+/* No counterpart in the reference (one problem per call there). A server runs
+ * `lanes` lanes, each a host thread with its own context and CUDA stream, so the
+ * device work of concurrent requests overlaps. Requests are taken in arrival
+ * order; the next one starts as soon as a lane is free and its estimated HBM
+ * footprint fits the budget beside the running requests and the resident
+ * meshes (it always starts when nothing runs). With cache != 0, meshes, scatter
+ * plans, operators and preconditioner hierarchies stay resident per lane and a
+ * request goes to a free lane that holds its mesh; lanes drop resident meshes
+ * when the budget needs the room. Results do not depend on the lane or on the
+ * other requests in flight (deterministic kernels). */
+typedef struct fq_server fq_server;
+
+typedef enum fq_request_kind {
+  FQ_REQ_HODGE = 0, /* elliptic::solve_source on a Kuhn cube (problems/elliptic.rs:132-182) */
+  FQ_REQ_DIRAC = 1  /* dirac::solve_dirac_source, lift 0 (problems/dirac.rs:473-531) */
+} fq_request_kind;
+
+typedef struct fq_request {
+  int kind;               /* fq_request_kind */
+  int dim;                /* Kuhn cube dimension 1..4 */
+  int nbox;               /* boxes per axis */
+  int grade;              /* FQ_REQ_HODGE: form degree k */
+  int bc;                 /* FQ_REQ_HODGE: fq_bc */
+  int minkowski;          /* 1: Minkowski lengths (axis 0 timelike, time scale 0.7) */
+  double jitter;          /* Riemannian: vertex jitter in units of h; Minkowski: relative length jitter */
+  uint64_t seed;          /* lengths and source when not given */
+  double mass_term;       /* FQ_REQ_DIRAC: m (nonzero) */
+  double arrival_ms;      /* >= 0: arrival time after server creation (latency counts from it); < 0: now */
+  const double* lengths;  /* optional host lengths (NULL: generated from seed); read while the request runs */
+  const double* source;   /* optional host source / load (NULL: seeded N(0,1)); read while it runs */
+  double* solution;       /* optional host output: (sigma, u) for HODGE, x for DIRAC */
+  fq_solve_opts opts;
+} fq_request;
+
+typedef struct fq_result {
+  int32_t status;       /* fq_status of the request */
+  int32_t lane;         /* lane that ran it */
+  fq_report report;
+  double queue_ms;      /* arrival -> start */
+  double run_ms;        /* start -> done */
+  double latency_ms;    /* arrival -> done */
+  double start_ms;      /* start, ms after server creation */
+  double end_ms;        /* done, ms after server creation */
+  double checksum;      /* sum of squares of the solution */
+  uint64_t ndofs;       /* length of the solution */
+  int32_t cache_hit;    /* 1 when the mesh was resident on the lane */
+  int32_t pad;
+} fq_result;
+
+typedef struct fq_server_stats {
+  uint64_t submitted, completed, cache_hits, evictions;
+  uint64_t peak_committed_bytes; /* running estimates + resident bytes, at most */
+  uint64_t resident_bytes;       /* bytes the idle lanes hold now */
+  double busy_ms;                /* summed run time of completed requests */
+} fq_server_stats;
+
+fq_status fq_server_create(int device, int lanes, uint64_t hbm_budget_bytes, int cache, fq_server** out);
+fq_status fq_server_submit(fq_server* server, const fq_request* request, uint64_t* ticket);
+/* Blocks until the request is done; each ticket is waited on once. */
+fq_status fq_server_wait(fq_server* server, uint64_t ticket, fq_result* result);
+fq_status fq_server_get_stats(fq_server* server, fq_server_stats* stats);
+/* Finishes the submitted requests, then stops the lanes. */
+void fq_server_destroy(fq_server* server);
+
 #ifdef __cplusplus
 }
 #endif

@@ -128,3 +128,32 @@ def test_hx_refuses_non_kuhn_and_lorentzian_meshes(oracle, ctx):
     with pytest.raises(fq.FqError):
         fq.hx_apply(mesh, 1, fq.FQ_ABSOLUTE, np.ones(mesh.nsimplices(1)))
     mesh.close()
+
+
+def test_refresh_after_new_lengths_equals_a_fresh_build(oracle, ctx):
+    """Reassembly with new lengths refreshes the preconditioner's numbers on the
+    kept lattice structure; the solve is then the one a fresh problem gives."""
+    dim, nb, grade = 3, 6, 1
+    cx, coords = oracle.cartesian_unit(dim, nb)
+    l1 = cx.edge_lengths_sq(oracle.jitter_coords(coords, nb, 1, 0.1))
+    l2 = cx.edge_lengths_sq(oracle.jitter_coords(coords, nb, 2, 0.15))
+    src = np.random.default_rng(5).standard_normal(cx.nsimplices(grade))
+    opts = fq.SolveOpts.default(rtol=1e-12, preconditioner=fq.FQ_PC_HX)
+    mesh = fq.Mesh.kuhn_cube(ctx, dim, nb)
+    mesh.set_lengths_sq(l1)
+    prob = fq.MixedProblem(mesh, grade, fq.FQ_ABSOLUTE, fq.FQ_FP64)
+    prob.solve(src, opts)
+    mesh.set_lengths_sq(l2)
+    prob.reassemble()
+    s1, u1, _, r1 = prob.solve(src, opts)
+    prob.close()
+    mesh.close()
+    fresh = fq.Mesh.kuhn_cube(ctx, dim, nb)
+    fresh.set_lengths_sq(l2)
+    prob2 = fq.MixedProblem(fresh, grade, fq.FQ_ABSOLUTE, fq.FQ_FP64)
+    s2, u2, _, r2 = prob2.solve(src, opts)
+    prob2.close()
+    fresh.close()
+    assert r1.iters == r2.iters, (r1, r2)
+    np.testing.assert_array_equal(u1, u2)
+    np.testing.assert_array_equal(s1, s2)
