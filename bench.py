@@ -546,6 +546,101 @@ def run_serve(args):
     print(json.dumps(out))
 
 
+# ---------------------------------------------------------------------------
+# batching workload: 512 Kuhn meshes of uneven dimension, size and degree
+# ---------------------------------------------------------------------------
+
+def batch_specs(n, seed):
+    """n in U{2,3,4}, cells log-uniform in [1e3, 2e5], N = max(1, round((cells/n!)^(1/n))),
+    k in U{0..n}."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(n):
+        dim = int(rng.integers(2, 5))
+        cells = math.exp(rng.uniform(math.log(1e3), math.log(2e5)))
+        nb = max(1, round((cells / math.factorial(dim)) ** (1.0 / dim)))
+        specs.append((dim, nb, int(rng.integers(0, dim + 1))))
+    return specs
+
+
+def run_batch(args):
+    import torch
+
+    import formoniq_gb300 as fq
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = fq.Context(0, stream=stream.cuda_stream)
+    specs = batch_specs(args.meshes, SEED + 3)
+    t0 = time.perf_counter()
+    meshes = []
+    for i, (dim, nb, _) in enumerate(specs):
+        m = fq.Mesh.kuhn_cube(ctx, dim, nb)
+        m.kuhn_lengths(jitter=JITTER, seed=SEED + 1000 + i)
+        meshes.append(m)
+    grades = [k for _, _, k in specs]
+    mesh_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    batch = fq.Batch(ctx, meshes, grades, fq.FQ_BATCH_HDIF)
+    plan_s = time.perf_counter() - t0
+    batch.assemble()
+    t0 = time.perf_counter()
+    batch.tune(reps=2)
+    tune_s = time.perf_counter() - t0
+    info = batch.info()
+    batch.assemble()  # validates (status words) once with the tuned shape
+    # the drop-in path: one fq_reassemble per mesh (element + scatter + status read per mesh)
+    mats = [fq.WhitneyComplex(m).hdif_gram(k) for m, k in zip(meshes, grades)]
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def timed(fn, steps):
+        ts = []
+        for _ in range(steps):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.median(ts)
+
+    for _ in range(args.warmup):
+        batch.assemble(check=False)
+        batch.assemble_per_mesh(check=False)
+    torch.cuda.synchronize()
+    ms_batched = timed(lambda: batch.assemble(check=False), args.steps)
+    ms_launches = timed(lambda: batch.assemble_per_mesh(check=False), args.steps)
+
+    def dropin():
+        for m, mat in zip(meshes, mats):
+            mat.reassemble(m)
+
+    ms_dropin = timed(dropin, max(1, args.steps // 2))
+    cells = info["cells"]
+    out = {"metric": "assembled cells/s (batched vs per-mesh launches)", "meshes": len(meshes),
+           "form": "hdif_gram(k) = M_k + dif_both(k+1), FP64 values (float-float compute)",
+           "workload": f"{len(meshes)} Kuhn cubes, n in {{2,3,4}}, cells log-uniform [1e3, 2e5], k in 0..n, "
+                       f"seed {SEED + 3}", "data": "synthetic",
+           "cells": cells, "slots": info["slots"], "classes": info["classes"],
+           "launches_batched": info["launches_per_assembly"], "launches_per_mesh": 2 * len(meshes),
+           "tuned": {"scatter_threads_per_slot": info["scatter_threads_per_slot"],
+                     "scatter_grid": info["scatter_grid"], "element_grids": info["element_grids"]},
+           "batched": {"ms": ms_batched, "cells_per_s": cells / (ms_batched * 1e-3)},
+           "per_mesh_launches": {"ms": ms_launches, "cells_per_s": cells / (ms_launches * 1e-3)},
+           "per_mesh_dropin_reassemble": {"ms": ms_dropin, "cells_per_s": cells / (ms_dropin * 1e-3)},
+           "setup_s": {"meshes": mesh_s, "plans": plan_s, "tune": tune_s},
+           "l2": "flushed before every timed assembly (256 MiB write)"}
+    for m in mats:
+        m.close()
+    batch.close()
+    for m in meshes:
+        m.close()
+    ctx.close()
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -559,10 +654,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-solve", action="store_true", help="skip the solve phase (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer phase (profiling runs)")
-    ap.add_argument("--workload", default="assembly", choices=["assembly", "precision", "serve"],
+    ap.add_argument("--workload", default="assembly", choices=["assembly", "precision", "serve", "batch"],
                     help="assembly: the headline line; precision: the 4D FP32-with-refinement study; "
                          "serve: the request stream, served vs plain")
     ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--meshes", type=int, default=512, help="batch: number of meshes")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--lanes", type=int, default=4)
     ap.add_argument("--dirac-iters", type=int, default=2000,
@@ -574,6 +670,8 @@ def main():
         run_precision(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 

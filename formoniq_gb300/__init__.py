@@ -30,6 +30,7 @@ __all__ = [
     "FqError", "FqUnavailable", "Context", "Mesh", "Matrix", "WhitneyComplex", "MixedProblem", "SolveOpts",
     "Report", "solve_source", "solve_dirac_source", "dirac_system", "minres", "cg", "hx_cg", "hx_apply", "lib_path",
     "load", "exported_symbols", "FQ_PC_AUTO", "FQ_PC_JACOBI", "FQ_PC_HX", "Server", "FQ_REQ_HODGE", "FQ_REQ_DIRAC",
+    "Batch", "FQ_BATCH_MASS", "FQ_BATCH_HDIF",
 ]
 
 FQ_MASS, FQ_DIF_TRIAL, FQ_DIF_TEST, FQ_DIF_BOTH = 0, 1, 2, 3
@@ -37,6 +38,7 @@ FQ_ABSOLUTE, FQ_RELATIVE = 0, 1
 FQ_FP64, FQ_FP32, FQ_FP64_IEEE = 0, 1, 2
 FQ_PC_AUTO, FQ_PC_JACOBI, FQ_PC_HX = 0, 1, 2
 FQ_REQ_HODGE, FQ_REQ_DIRAC = 0, 1
+FQ_BATCH_MASS, FQ_BATCH_HDIF = 0, 1
 
 _STATUS = {
     0: "FQ_OK", 1: "FQ_INVALID_ARG", 2: "FQ_DEGENERATE_CELL", 3: "FQ_NOT_CONVERGED", 4: "FQ_BREAKDOWN",
@@ -171,6 +173,18 @@ _SIGNATURES = {
     "fq_hx_cg": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _DP, _DP, ctypes.POINTER(SolveOpts),
                                 ctypes.POINTER(_Report)]),
     "fq_hx_apply": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _DP, _DP]),
+    "fq_batch_create": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_P), _I32P, ctypes.c_int, ctypes.POINTER(_P)]),
+    "fq_batch_tune": (ctypes.c_int, [_P, ctypes.c_int]),
+    "fq_batch_set_launch": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "fq_batch_assemble": (ctypes.c_int, [_P, ctypes.c_int]),
+    "fq_batch_assemble_per_mesh": (ctypes.c_int, [_P, ctypes.c_int]),
+    "fq_batch_info": (ctypes.c_int, [_P, _I64P, _I64P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "fq_batch_launch_config": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                              ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
+    "fq_batch_matrix": (ctypes.c_int, [_P, ctypes.c_int, _I64P, _I64P, ctypes.POINTER(_P), ctypes.POINTER(_P),
+                                       ctypes.POINTER(_P)]),
+    "fq_batch_copy_to_host": (ctypes.c_int, [_P, ctypes.c_int, _I32P, _I32P, _DP]),
+    "fq_batch_destroy": (None, [_P]),
     "fq_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(_P)]),
     "fq_server_submit": (ctypes.c_int, [_P, ctypes.POINTER(_Request), ctypes.POINTER(ctypes.c_uint64)]),
     "fq_server_wait": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.POINTER(_Result)]),
@@ -687,3 +701,60 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class Batch:
+    """Batched assembly of one form per mesh (fq_batch_*)."""
+
+    def __init__(self, ctx: Context, meshes, grades, form: int = FQ_BATCH_HDIF):
+        self.ctx, self.meshes, self.grades = ctx, list(meshes), [int(g) for g in grades]
+        arr = (_P * len(self.meshes))(*[m.h for m in self.meshes])
+        g = np.ascontiguousarray(self.grades, np.int32)
+        h = _P()
+        ctx.check(ctx.L.fq_batch_create(ctx.h, len(self.meshes), arr, g.ctypes.data_as(_I32P), int(form),
+                                        ctypes.byref(h)), "fq_batch_create")
+        self.h = h
+        ctx._adopt(self)
+
+    def tune(self, reps: int = 3):
+        self.ctx.check(self.ctx.L.fq_batch_tune(self.h, int(reps)), "fq_batch_tune")
+
+    def set_launch(self, element_grid: int = 0, scatter_tps: int = 1, scatter_grid: int = 0):
+        self.ctx.check(self.ctx.L.fq_batch_set_launch(self.h, element_grid, scatter_tps, scatter_grid),
+                       "fq_batch_set_launch")
+
+    def assemble(self, check: bool = True):
+        self.ctx.check(self.ctx.L.fq_batch_assemble(self.h, int(check)), "fq_batch_assemble")
+
+    def assemble_per_mesh(self, check: bool = True):
+        self.ctx.check(self.ctx.L.fq_batch_assemble_per_mesh(self.h, int(check)), "fq_batch_assemble_per_mesh")
+
+    def info(self) -> dict:
+        c, s = ctypes.c_int64(), ctypes.c_int64()
+        k, n = ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(self.ctx.L.fq_batch_info(self.h, ctypes.byref(c), ctypes.byref(s), ctypes.byref(k),
+                                                ctypes.byref(n)))
+        tps, sg = ctypes.c_int(), ctypes.c_int()
+        grids = (ctypes.c_int * 64)()
+        self.ctx.L.fq_batch_launch_config(self.h, ctypes.byref(tps), ctypes.byref(sg), grids, 64)
+        return {"cells": c.value, "slots": s.value, "classes": k.value, "launches_per_assembly": n.value,
+                "scatter_threads_per_slot": tps.value, "scatter_grid": sg.value,
+                "element_grids": list(grids)[:k.value]}
+
+    def to_scipy(self, i: int):
+        import scipy.sparse as sp
+
+        nr, nnz = ctypes.c_int64(), ctypes.c_int64()
+        self.ctx.check(self.ctx.L.fq_batch_matrix(self.h, int(i), ctypes.byref(nr), ctypes.byref(nnz), None, None,
+                                                  None))
+        rp = np.zeros(nr.value + 1, np.int32)
+        ci = np.zeros(max(nnz.value, 1), np.int32)
+        v = np.zeros(max(nnz.value, 1))
+        self.ctx.check(self.ctx.L.fq_batch_copy_to_host(self.h, int(i), rp.ctypes.data_as(_I32P),
+                                                        ci.ctypes.data_as(_I32P), _dp(v)))
+        return sp.csr_matrix((v[:nnz.value], ci[:nnz.value], rp), shape=(nr.value, nr.value))
+
+    def close(self):
+        if self.h:
+            self.ctx.L.fq_batch_destroy(self.h)
+            self.h = None

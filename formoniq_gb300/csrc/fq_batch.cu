@@ -1,0 +1,458 @@
+// Batched assembly: many meshes of uneven size, dimension and degree assembled
+// together.
+//
+// No counterpart in the reference (one mesh per assemble_matrix call,
+// galerkin.rs:138-188). The batch keeps, per mesh, the scatter plan of its
+// element program (built by the same plan builder as a single assembly) and
+// slices of two batch-wide buffers: element values and CSR values. One
+// assembly of the batch is a CUDA graph of
+//   - one element launch per (dimension, degree) class present: a grid-stride
+//     kernel over the concatenated cells of the class, each thread finding its
+//     mesh by binary search over the class's cell offsets (a class shares one
+//     kernel instance: register allocation is per kernel, so one launch over
+//     all classes would run every program at the heaviest program's occupancy);
+//   - one scatter launch over the concatenated CSR slots of all meshes,
+//     `tps` threads per slot.
+// The grid sizes and `tps` come from a tuner that times the candidates on the
+// batch itself. Per mesh, the element values and the summation order of every
+// slot are those of a single assembly (with tps = 1 bit for bit).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "fq_df64.cuh"
+#include "fq_internal.h"
+
+namespace fq {
+
+fq_status get_plan(fq_ctx* ctx, fq_mesh* m, int kind, int grade, int row_bc, int col_bc, Plan** out);
+
+struct ScatterBatchEntry {
+  int64_t begin, nslots;
+  const int32_t* slot_ptr;
+  const int32_t* perm;
+  const df64* elem;
+  double* values;
+};
+
+namespace {
+
+__device__ __forceinline__ bool nz_bits(float v) { return (__float_as_int(v) << 1) != 0; }
+
+// tps lanes per slot (tps divides 32), contributions strided over the lanes and
+// combined in a fixed shuffle order.
+template <int TPS>
+__global__ void __launch_bounds__(256) scatter_batch_kernel(const ScatterBatchEntry* __restrict__ tab, int ntab,
+                                                            int64_t total, int* zero_count) {
+  const int lane = threadIdx.x % TPS;
+  const int64_t groups_per_grid = int64_t(gridDim.x) * (blockDim.x / TPS);
+  for (int64_t base = int64_t(blockIdx.x) * (blockDim.x / TPS); base < total; base += groups_per_grid) {
+    const int64_t g = base + threadIdx.x / TPS;
+    const bool valid = g < total;
+    df64 acc(0.f, 0.f);
+    bool nz = false;
+    int lo = 0;
+    if (valid) {
+      int hi = ntab - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tab[mid].begin <= g)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      const ScatterBatchEntry& e = tab[lo];
+      const int64_t s = g - e.begin;
+      const int b = __ldg(e.slot_ptr + s), en = __ldg(e.slot_ptr + s + 1);
+      for (int t = b + lane; t < en; t += TPS) {
+        const df64 v = e.elem[__ldg(e.perm + t)];
+        acc += v;
+        nz |= nz_bits(v.hi) || nz_bits(v.lo);
+      }
+    }
+    if constexpr (TPS > 1) {
+#pragma unroll
+      for (int o = TPS / 2; o > 0; o >>= 1) {
+        const df64 other(__shfl_down_sync(0xffffffffu, acc.hi, o, TPS), __shfl_down_sync(0xffffffffu, acc.lo, o, TPS));
+        const int onz = __shfl_down_sync(0xffffffffu, int(nz), o, TPS);
+        acc += other;
+        nz = nz || onz;
+      }
+    }
+    if (valid && lane == 0) {
+      const ScatterBatchEntry& e = tab[lo];
+      e.values[g - e.begin] = acc.to_double();
+      if (!nz) atomicAdd(zero_count, 1);
+    }
+  }
+}
+
+void launch_scatter_batch(const ScatterBatchEntry* tab, int ntab, int64_t total, int tps, int grid, int* zc,
+                          cudaStream_t st) {
+  if (total <= 0) return;
+  const int threads = 256;
+  const int64_t need = (total * tps + threads - 1) / threads;
+  const unsigned blocks = unsigned(grid > 0 ? std::min<int64_t>(grid, need) : need);
+  switch (tps) {
+    case 2:
+      scatter_batch_kernel<2><<<blocks, threads, 0, st>>>(tab, ntab, total, zc);
+      break;
+    case 4:
+      scatter_batch_kernel<4><<<blocks, threads, 0, st>>>(tab, ntab, total, zc);
+      break;
+    default:
+      scatter_batch_kernel<1><<<blocks, threads, 0, st>>>(tab, ntab, total, zc);
+      break;
+  }
+}
+
+}  // namespace
+}  // namespace fq
+
+using namespace fq;
+
+struct fq_batch {
+  fq_ctx* ctx = nullptr;
+  int kind = 0;
+  struct Member {
+    fq_mesh* mesh = nullptr;
+    int grade = 0;
+    Plan* plan = nullptr;
+    int64_t elem_off = 0, val_off = 0;  // element offset in df64 units, value offset in doubles
+  };
+  std::vector<Member> members;
+  struct Class {
+    int dim = 0, grade = 0;
+    int64_t total = 0;
+    DevBuf table;  // ElemBatchEntry[]
+    int n = 0;
+    int nent = 0;  // element entries per cell of the class's program
+    int grid = 0;  // tuned CTAs (0 = one thread per cell)
+  };
+  std::vector<Class> classes;
+  DevBuf elem, values, stable, flags;
+  int64_t total_cells = 0, total_slots = 0, max_slots = 0;
+  int tps = 1, sgrid = 0;
+  cudaGraphExec_t graph = nullptr;
+  ~fq_batch() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
+};
+
+namespace {
+
+fq_status enqueue_batch(fq_batch* B) {
+  fq_ctx* ctx = B->ctx;
+  cudaStream_t st = ctx->stream;
+  for (auto& c : B->classes) {
+    ElemArgs a;
+    a.ncells = 0;
+    a.lengths = nullptr;
+    a.cell_edges = nullptr;
+    a.out = nullptr;
+    a.ginv_out = a.det_out = a.vol_out = nullptr;
+    a.param = 0.0;
+    a.status = ctx->status.as<int>();
+    a.nent = c.nent;
+    a.batch = c.table.as<ElemBatchEntry>();
+    a.nbatch = c.n;
+    a.total = c.total;
+    a.grid = c.grid;
+    if (launch_element(c.dim, c.grade, B->kind, FQ_FP64, a, st) != 0)
+      return set_error(ctx, FQ_UNSUPPORTED, "no element program for this dimension/grade");
+  }
+  launch_scatter_batch(B->stable.as<ScatterBatchEntry>(), int(B->members.size()), B->total_slots, B->tps, B->sgrid,
+                       ctx->status.as<int>() + 1, st);
+  return FQ_OK;
+}
+
+fq_status capture(fq_batch* B) {
+  fq_ctx* ctx = B->ctx;
+  if (B->graph) {
+    cudaGraphExecDestroy(B->graph);
+    B->graph = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return FQ_OK;  // uncapturable stream: direct launches
+  }
+  fq_status s = enqueue_batch(B);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (s != FQ_OK) {
+    if (g) cudaGraphDestroy(g);
+    return s;
+  }
+  if (e == cudaSuccess) {
+    e = cudaGraphInstantiate(&B->graph, g, 0);
+    cudaGraphDestroy(g);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    B->graph = nullptr;
+  }
+  return FQ_OK;
+}
+
+fq_status check_status(fq_ctx* ctx) {
+  FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->host_status[0] & 2) return set_error(ctx, FQ_INVALID_ARG, "element program wrote outside its layout");
+  if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
+  if (ctx->host_status[1] > 0)
+    return set_error(ctx, FQ_UNSUPPORTED,
+                     "some slots summed exact zeros only (the reference drops them): assemble those meshes alone");
+  return FQ_OK;
+}
+
+float time_once(fq_batch* B, int reps) {
+  fq_ctx* ctx = B->ctx;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  enqueue_batch(B);  // warm-up
+  cudaEventRecord(a, ctx->stream);
+  for (int r = 0; r < reps; ++r) enqueue_batch(B);
+  cudaEventRecord(b, ctx->stream);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / float(std::max(reps, 1));
+}
+
+}  // namespace
+
+extern "C" {
+
+fq_status fq_batch_create(fq_ctx* ctx, int nmeshes, fq_mesh* const* meshes, const int* grades, int form,
+                          fq_batch** out) {
+  if (!ctx || !out || nmeshes < 1 || !meshes || !grades) return FQ_INVALID_ARG;
+  int kind = 0;
+  if (form == FQ_BATCH_MASS)
+    kind = EK_MASS;
+  else if (form == FQ_BATCH_HDIF)
+    kind = EK_HDIF;
+  else
+    return set_error(ctx, FQ_INVALID_ARG, "unknown batch form");
+  auto B = std::make_unique<fq_batch>();
+  B->ctx = ctx;
+  B->kind = kind;
+  std::map<std::pair<int, int>, std::vector<int>> byclass;
+  int64_t eoff = 0, voff = 0;
+  for (int i = 0; i < nmeshes; ++i) {
+    fq_mesh* m = meshes[i];
+    if (!m || m->ctx != ctx) return set_error(ctx, FQ_INVALID_ARG, "batch meshes must belong to the context");
+    if (!m->has_lengths) return set_error(ctx, FQ_INVALID_ARG, "mesh has no edge lengths");
+    if (grades[i] < 0 || grades[i] > m->dim) return set_error(ctx, FQ_INVALID_ARG, "grade out of range");
+    fq_batch::Member mb;
+    mb.mesh = m;
+    mb.grade = grades[i];
+    FQ_TRY(get_plan(ctx, m, kind, grades[i], FQ_ABSOLUTE, FQ_ABSOLUTE, &mb.plan));
+    mb.elem_off = eoff;
+    mb.val_off = voff;
+    eoff += (int64_t(mb.plan->nent) * m->ncells + 31) & ~int64_t(31);
+    voff += (mb.plan->nslots + 31) & ~int64_t(31);
+    B->total_cells += m->ncells;
+    B->max_slots = std::max(B->max_slots, mb.plan->nslots);
+    byclass[{m->dim, grades[i]}].push_back(i);
+    B->members.push_back(mb);
+  }
+  FQ_TRY(B->elem.alloc(ctx, std::max<int64_t>(eoff, 1) * 8));
+  FQ_TRY(B->values.alloc(ctx, std::max<int64_t>(voff, 1) * 8));
+  FQ_TRY(B->flags.alloc(ctx, std::max<int64_t>(B->max_slots, 1)));
+  // element tables per class
+  for (auto& kv : byclass) {
+    fq_batch::Class c;
+    c.dim = kv.first.first;
+    c.grade = kv.first.second;
+    std::vector<ElemBatchEntry> tab;
+    for (int i : kv.second) {
+      const auto& mb = B->members[i];
+      ElemBatchEntry e;
+      e.begin = c.total;
+      e.ncells = mb.mesh->ncells;
+      e.lengths = mb.mesh->lengths.as<double>();
+      e.cell_edges = mb.mesh->dim >= 1 ? mb.mesh->cell_faces[1].as<int32_t>() : nullptr;
+      e.out = B->elem.as<df64>() + mb.elem_off;
+      tab.push_back(e);
+      c.total += e.ncells;
+    }
+    c.n = int(tab.size());
+    c.nent = B->members[kv.second.front()].plan->nent;
+    FQ_TRY(c.table.alloc(ctx, tab.size() * sizeof(ElemBatchEntry)));
+    FQ_CUDA(ctx, cudaMemcpyAsync(c.table.p, tab.data(), tab.size() * sizeof(ElemBatchEntry), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    B->classes.push_back(std::move(c));
+  }
+  // scatter table over all meshes
+  std::vector<ScatterBatchEntry> st;
+  for (auto& mb : B->members) {
+    ScatterBatchEntry e;
+    e.begin = B->total_slots;
+    e.nslots = mb.plan->nslots;
+    e.slot_ptr = mb.plan->slot_ptr.as<int32_t>();
+    e.perm = mb.plan->perm.as<int32_t>();
+    e.elem = B->elem.as<df64>() + mb.elem_off;
+    e.values = B->values.as<double>() + mb.val_off;
+    st.push_back(e);
+    B->total_slots += e.nslots;
+  }
+  FQ_TRY(B->stable.alloc(ctx, st.size() * sizeof(ScatterBatchEntry)));
+  FQ_CUDA(ctx, cudaMemcpyAsync(B->stable.p, st.data(), st.size() * sizeof(ScatterBatchEntry), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  FQ_TRY(capture(B.get()));
+  *out = B.release();
+  return FQ_OK;
+}
+
+fq_status fq_batch_tune(fq_batch* B, int reps) {
+  if (!B) return FQ_INVALID_ARG;
+  fq_ctx* ctx = B->ctx;
+  reps = std::max(reps, 1);
+  int dev_sms = 152;
+  cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  // element stage: CTAs per SM of each class's grid-stride launch (0 = one thread per cell)
+  const int per_sm[] = {0, 2, 4, 8, 16};
+  for (auto& c : B->classes) {
+    float best = 1e30f;
+    int pick = 0;
+    for (int ps : per_sm) {
+      c.grid = ps * dev_sms;
+      const float t = time_once(B, reps);
+      if (t < best) {
+        best = t;
+        pick = c.grid;
+      }
+    }
+    c.grid = pick;
+  }
+  // scatter stage: threads per slot and CTAs per SM
+  float best = 1e30f;
+  int btps = 1, bgrid = 0;
+  for (int tps : {1, 2, 4})
+    for (int ps : per_sm) {
+      B->tps = tps;
+      B->sgrid = ps * dev_sms;
+      const float t = time_once(B, reps);
+      if (t < best) {
+        best = t;
+        btps = tps;
+        bgrid = B->sgrid;
+      }
+    }
+  B->tps = btps;
+  B->sgrid = bgrid;
+  FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
+  FQ_TRY(capture(B));
+  return FQ_OK;
+}
+
+fq_status fq_batch_set_launch(fq_batch* B, int element_grid, int scatter_tps, int scatter_grid) {
+  if (!B || (scatter_tps != 1 && scatter_tps != 2 && scatter_tps != 4)) return FQ_INVALID_ARG;
+  for (auto& c : B->classes) c.grid = element_grid;
+  B->tps = scatter_tps;
+  B->sgrid = scatter_grid;
+  return capture(B);
+}
+
+fq_status fq_batch_assemble(fq_batch* B, int check) {
+  if (!B) return FQ_INVALID_ARG;
+  fq_ctx* ctx = B->ctx;
+  FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
+  if (B->graph) {
+    FQ_CUDA(ctx, cudaGraphLaunch(B->graph, ctx->stream));
+  } else {
+    FQ_TRY(enqueue_batch(B));
+  }
+  ctx->launches += B->classes.size() + 1;
+  return check ? check_status(ctx) : FQ_OK;
+}
+
+fq_status fq_batch_assemble_per_mesh(fq_batch* B, int check) {
+  if (!B) return FQ_INVALID_ARG;
+  fq_ctx* ctx = B->ctx;
+  cudaStream_t st = ctx->stream;
+  FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), st));
+  for (auto& mb : B->members) {
+    ElemArgs a;
+    a.ncells = mb.mesh->ncells;
+    a.lengths = mb.mesh->lengths.as<double>();
+    a.cell_edges = mb.mesh->dim >= 1 ? mb.mesh->cell_faces[1].as<int32_t>() : nullptr;
+    a.out = B->elem.as<df64>() + mb.elem_off;
+    a.ginv_out = a.det_out = a.vol_out = nullptr;
+    a.param = 0.0;
+    a.status = ctx->status.as<int>();
+    a.nent = mb.plan->nent;
+    if (launch_element(mb.mesh->dim, mb.grade, B->kind, FQ_FP64, a, st) != 0)
+      return set_error(ctx, FQ_UNSUPPORTED, "no element program for this dimension/grade");
+    launch_scatter(*mb.plan, a.out, B->values.as<double>() + mb.val_off, B->flags.as<uint8_t>(),
+                   ctx->status.as<int>() + 1, FQ_FP64, st);
+    ctx->launches += 2;
+  }
+  return check ? check_status(ctx) : FQ_OK;
+}
+
+fq_status fq_batch_info(const fq_batch* B, int64_t* total_cells, int64_t* total_slots, int* nclasses,
+                        int* launches) {
+  if (!B) return FQ_INVALID_ARG;
+  if (total_cells) *total_cells = B->total_cells;
+  if (total_slots) *total_slots = B->total_slots;
+  if (nclasses) *nclasses = int(B->classes.size());
+  if (launches) *launches = int(B->classes.size()) + 1;
+  return FQ_OK;
+}
+
+fq_status fq_batch_launch_config(const fq_batch* B, int* scatter_tps, int* scatter_grid, int* element_grids,
+                                 int max_classes) {
+  if (!B) return FQ_INVALID_ARG;
+  if (scatter_tps) *scatter_tps = B->tps;
+  if (scatter_grid) *scatter_grid = B->sgrid;
+  if (element_grids)
+    for (int i = 0; i < max_classes && i < int(B->classes.size()); ++i) element_grids[i] = B->classes[i].grid;
+  return FQ_OK;
+}
+
+fq_status fq_batch_matrix(const fq_batch* B, int i, int64_t* nrows, int64_t* nnz, const int32_t** row_ptr,
+                          const int32_t** col_idx, const double** values) {
+  if (!B || i < 0 || i >= int(B->members.size())) return FQ_INVALID_ARG;
+  const auto& mb = B->members[i];
+  if (nrows) *nrows = mb.plan->nrows;
+  if (nnz) *nnz = mb.plan->nslots;
+  if (row_ptr) *row_ptr = mb.plan->row_ptr.as<int32_t>();
+  if (col_idx) *col_idx = mb.plan->col_idx.as<int32_t>();
+  if (values) *values = B->values.as<double>() + mb.val_off;
+  return FQ_OK;
+}
+
+fq_status fq_batch_copy_to_host(const fq_batch* B, int i, int32_t* row_ptr, int32_t* col_idx, double* values) {
+  if (!B || i < 0 || i >= int(B->members.size())) return FQ_INVALID_ARG;
+  fq_ctx* ctx = B->ctx;
+  const auto& mb = B->members[i];
+  cudaStream_t st = ctx->stream;
+  if (row_ptr)
+    FQ_CUDA(ctx, cudaMemcpyAsync(row_ptr, mb.plan->row_ptr.p, (mb.plan->nrows + 1) * 4, cudaMemcpyDeviceToHost, st));
+  if (mb.plan->nslots > 0) {
+    if (col_idx)
+      FQ_CUDA(ctx, cudaMemcpyAsync(col_idx, mb.plan->col_idx.p, mb.plan->nslots * 4, cudaMemcpyDeviceToHost, st));
+    if (values)
+      FQ_CUDA(ctx, cudaMemcpyAsync(values, B->values.as<double>() + mb.val_off, mb.plan->nslots * 8,
+                                   cudaMemcpyDeviceToHost, st));
+  }
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  return FQ_OK;
+}
+
+void fq_batch_destroy(fq_batch* B) {
+  if (!B) return;
+  cudaStreamSynchronize(B->ctx->stream);
+  delete B;
+}
+
+}  // extern "C"

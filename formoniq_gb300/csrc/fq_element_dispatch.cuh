@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "fq_element_kernel.cuh"
@@ -14,8 +15,10 @@ namespace fq {
 template <int N, int K, int KIND, typename T>
 int launch_one_t(const ElemArgs& a, cudaStream_t st) {
   constexpr int threads = 128;
-  const unsigned blocks = unsigned((a.ncells + threads - 1) / threads);
-  if (blocks == 0) return 0;
+  const int64_t total = a.batch ? a.total : a.ncells;
+  if (total <= 0) return 0;
+  const int64_t need = (total + threads - 1) / threads;
+  const unsigned blocks = unsigned(a.grid > 0 ? std::min<int64_t>(a.grid, need) : need);
   element_kernel<N, K, KIND, T><<<blocks, threads, 0, st>>>(a);
   return 0;
 }

@@ -166,37 +166,58 @@ FQ_HD void element_entries(const double (&ginv)[N > 0 ? N : 1][N > 0 ? N : 1], d
 
 template <int N, int K, int KIND, typename T>
 __global__ void __launch_bounds__(128) element_kernel(ElemArgs a) {
-  const int64_t cell = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (cell >= a.ncells) return;
-  const int64_t nc = a.ncells;
-  constexpr int NE = cbinom(N + 1, 2);
-  double s[NE > 0 ? NE : 1];
-#pragma unroll
-  for (int e = 0; e < NE; ++e) s[e] = __ldg(a.lengths + __ldg(a.cell_edges + int64_t(e) * nc + cell));
-  double g[N > 0 ? N : 1][N > 0 ? N : 1];
-  double ginv[N > 0 ? N : 1][N > 0 ? N : 1];
-  regge_metric<N>(s, g);
-  const double det = sym_inverse<N>(g, ginv);
-  const double vol = sqrt(fabs(det)) * (1.0 / double(cfact(N)));
-  if (!(det != 0.0) || !isfinite(det)) atomicOr(a.status, 1);
-  if constexpr (KIND == EK_METRIC) {
-    if (a.ginv_out) {
-#pragma unroll
-      for (int i = 0; i < N; ++i)
-#pragma unroll
-        for (int j = 0; j < N; ++j) a.ginv_out[int64_t(i * N + j) * nc + cell] = ginv[i][j];
+  const int64_t total = a.batch ? a.total : a.ncells;
+  for (int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < total; g += int64_t(gridDim.x) * blockDim.x) {
+    // the cell's mesh: the launch's own, or the batch entry holding index g
+    int64_t cell = g, nc = a.ncells;
+    const double* lengths = a.lengths;
+    const int32_t* cell_edges = a.cell_edges;
+    void* outp = a.out;
+    if (a.batch) {
+      int lo = 0, hi = a.nbatch - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.batch[mid].begin <= g)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      const ElemBatchEntry& b = a.batch[lo];
+      cell = g - b.begin;
+      nc = b.ncells;
+      lengths = b.lengths;
+      cell_edges = b.cell_edges;
+      outp = b.out;
     }
-    if (a.det_out) a.det_out[cell] = det;
-    if (a.vol_out) a.vol_out[cell] = vol;
-  } else {
-    T* out = static_cast<T*>(a.out);
-    const int nent = a.nent;
-    element_entries<N, K, KIND, T>(ginv, vol, a.param, [&](int e, T v) {
-      if (e < nent)
-        out[int64_t(e) * nc + cell] = v;
-      else
-        atomicOr(a.status, 2);
-    });
+    constexpr int NE = cbinom(N + 1, 2);
+    double s[NE > 0 ? NE : 1];
+#pragma unroll
+    for (int e = 0; e < NE; ++e) s[e] = __ldg(lengths + __ldg(cell_edges + int64_t(e) * nc + cell));
+    double gm[N > 0 ? N : 1][N > 0 ? N : 1];
+    double ginv[N > 0 ? N : 1][N > 0 ? N : 1];
+    regge_metric<N>(s, gm);
+    const double det = sym_inverse<N>(gm, ginv);
+    const double vol = sqrt(fabs(det)) * (1.0 / double(cfact(N)));
+    if (!(det != 0.0) || !isfinite(det)) atomicOr(a.status, 1);
+    if constexpr (KIND == EK_METRIC) {
+      if (a.ginv_out) {
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+#pragma unroll
+          for (int j = 0; j < N; ++j) a.ginv_out[int64_t(i * N + j) * nc + cell] = ginv[i][j];
+      }
+      if (a.det_out) a.det_out[cell] = det;
+      if (a.vol_out) a.vol_out[cell] = vol;
+    } else {
+      T* out = static_cast<T*>(outp);
+      const int nent = a.nent;
+      element_entries<N, K, KIND, T>(ginv, vol, a.param, [&](int e, T v) {
+        if (e < nent)
+          out[int64_t(e) * nc + cell] = v;
+        else
+          atomicOr(a.status, 2);
+      });
+    }
   }
 }
 

@@ -30,6 +30,15 @@ FQ_HD constexpr int grade_offset(int n, int j) {
 // cell, none at grade 0 (Lambda^{-1} = 0).
 FQ_HD constexpr int kkt_sigma_local(int n, int k) { return k > 0 ? cbinom(n + 1, k) : 0; }
 
+// One mesh of a batched element launch: its cells are the global cell indices
+// [begin, begin + ncells) of the launch.
+struct ElemBatchEntry {
+  int64_t begin, ncells;
+  const double* lengths;
+  const int32_t* cell_edges;
+  void* out;
+};
+
 // Arguments of the per-cell kernel (device pointers).
 struct ElemArgs {
   int64_t ncells;
@@ -43,6 +52,12 @@ struct ElemArgs {
   int* status;               // bit 0: a singular or non-finite cell metric;
                              // bit 1: an element entry index outside [0, nent)
   int nent;                  // entries per cell the output buffer holds
+  // Batched launch (null for one mesh): `nbatch` meshes sorted by begin,
+  // `total` cells in all; the single-mesh fields above are then unused.
+  const ElemBatchEntry* batch = nullptr;
+  int nbatch = 0;
+  int64_t total = 0;
+  int grid = 0;              // CTAs of the launch (0: one thread per cell)
 };
 
 }  // namespace fq

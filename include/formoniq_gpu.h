@@ -281,6 +281,46 @@ fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* mesh, double mass_term, co
 /* The assembled relative Dirac system S (for parity tests); caller destroys. */
 fq_status fq_dirac_system(fq_ctx* ctx, fq_mesh* mesh, double mass_term, fq_matrix** out);
 
+/* ---- batched assembly --------------------------------------------------- */
+/* No counterpart in the reference (one mesh per assemble_matrix call,
+ * galerkin.rs:138-188). A batch assembles one form per mesh on many meshes of
+ * the context at once: per mesh the same element program, scatter plan and
+ * summation order as fq_assemble (FP64 values, float-float compute, absolute
+ * complex, topological pattern), the whole batch as one CUDA graph with one
+ * grid-stride element launch per (dimension, degree) class present and one
+ * scatter launch over all meshes' CSR slots. */
+typedef struct fq_batch fq_batch;
+typedef enum fq_batch_form {
+  FQ_BATCH_MASS = 0, /* WhitneyPairing::mass(k)                    operators.rs:169-171 */
+  FQ_BATCH_HDIF = 1  /* HilbertComplex::hdif_gram(k) = M_k + dif_both(k+1), whitney_complex.rs:180-183 */
+} fq_batch_form;
+/* meshes[i] (with lengths) and grades[i]: the form at grade k on mesh i. */
+fq_status fq_batch_create(fq_ctx* ctx, int nmeshes, fq_mesh* const* meshes, const int* grades, int form,
+                          fq_batch** out);
+/* Tuner: times each candidate launch shape `reps` times on this batch (element
+ * CTAs per SM per class; scatter threads per slot 1/2/4 and CTAs per SM) and
+ * keeps the fastest. */
+fq_status fq_batch_tune(fq_batch* batch, int reps);
+/* Fixed launch shape: element grid (CTAs, 0 = one thread per cell), scatter
+ * threads per slot (1, 2 or 4) and grid. */
+fq_status fq_batch_set_launch(fq_batch* batch, int element_grid, int scatter_tps, int scatter_grid);
+/* One assembly of the whole batch (one graph launch). check != 0 waits and
+ * checks the status words (degenerate cells; a slot that summed exact zeros
+ * only, which the reference would drop: FQ_UNSUPPORTED). */
+fq_status fq_batch_assemble(fq_batch* batch, int check);
+/* The same assembly as two launches per mesh (the per-mesh baseline). */
+fq_status fq_batch_assemble_per_mesh(fq_batch* batch, int check);
+fq_status fq_batch_info(const fq_batch* batch, int64_t* total_cells, int64_t* total_slots, int* nclasses,
+                        int* launches_per_assembly);
+fq_status fq_batch_launch_config(const fq_batch* batch, int* scatter_tps, int* scatter_grid, int* element_grids,
+                                 int max_classes);
+/* Device CSR of mesh i (row_ptr/col_idx of its plan, values in the batch). */
+fq_status fq_batch_matrix(const fq_batch* batch, int i, int64_t* nrows, int64_t* nnz, const int32_t** row_ptr,
+                          const int32_t** col_idx, const double** values);
+/* Host copy of mesh i's CSR (row_ptr nrows+1, col_idx and values nnz). */
+fq_status fq_batch_copy_to_host(const fq_batch* batch, int i, int32_t* row_ptr, int32_t* col_idx, double* values);
+void fq_batch_destroy(fq_batch* batch);
+
 /* ---- serving: continuously batched solve requests ----------------------- */
 /* No counterpart in the reference (one problem per call there). A server runs
  * `lanes` lanes, each a host thread with its own context and CUDA stream, so the
