@@ -11,11 +11,13 @@
 //     mesh by binary search over the class's cell offsets (a class shares one
 //     kernel instance: register allocation is per kernel, so one launch over
 //     all classes would run every program at the heaviest program's occupancy);
-//   - one scatter launch over the concatenated CSR slots of all meshes,
-//     `tps` threads per slot.
+//   - one scatter launch over the concatenated CSR slots of all meshes:
+//     `tps` threads per slot, or warp-staged (tps = 0: a warp gathers the
+//     contributions of its 32 slots into shared memory, then each lane sums
+//     its slot in order).
 // The grid sizes and `tps` come from a tuner that times the candidates on the
 // batch itself. Per mesh, the element values and the summation order of every
-// slot are those of a single assembly (with tps = 1 bit for bit).
+// slot are those of a single assembly (with tps = 0 or 1 bit for bit).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -55,6 +57,7 @@ __global__ void __launch_bounds__(256) scatter_batch_kernel(const ScatterBatchEn
     df64 acc(0.f, 0.f);
     bool nz = false;
     int lo = 0;
+    bool live = valid;
     if (valid) {
       int hi = ntab - 1;
       while (lo < hi) {
@@ -64,6 +67,10 @@ __global__ void __launch_bounds__(256) scatter_batch_kernel(const ScatterBatchEn
         else
           hi = mid - 1;
       }
+      // each mesh's range is padded to a multiple of 32: a padding index has no slot
+      live = g - tab[lo].begin < tab[lo].nslots;
+    }
+    if (live) {
       const ScatterBatchEntry& e = tab[lo];
       const int64_t s = g - e.begin;
       const int b = __ldg(e.slot_ptr + s), en = __ldg(e.slot_ptr + s + 1);
@@ -82,9 +89,77 @@ __global__ void __launch_bounds__(256) scatter_batch_kernel(const ScatterBatchEn
         nz = nz || onz;
       }
     }
-    if (valid && lane == 0) {
+    if (live && lane == 0) {
       const ScatterBatchEntry& e = tab[lo];
       e.values[g - e.begin] = acc.to_double();
+      if (!nz) atomicAdd(zero_count, 1);
+    }
+  }
+}
+
+// Warp-staged form (tps = 0): each mesh's slot range starts at a multiple of 32
+// in the batch index space, so a warp's 32 slots belong to one mesh; staging and
+// summation order are those of the single-mesh scatter.
+constexpr int kBatchStage = 256;
+
+__global__ void __launch_bounds__(256) scatter_batch_warp_kernel(const ScatterBatchEntry* __restrict__ tab, int ntab,
+                                                                 int64_t total, int* zero_count) {
+  __shared__ df64 stage[8][kBatchStage];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t warps_per_grid = int64_t(gridDim.x) * 8;
+  for (int64_t w = int64_t(blockIdx.x) * 8 + warp; w * 32 < total; w += warps_per_grid) {
+    const int64_t g0 = w * 32;
+    int lo = 0, hi = ntab - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tab[mid].begin <= g0)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const ScatterBatchEntry& en = tab[lo];
+    const int64_t s0 = g0 - en.begin;
+    if (s0 >= en.nslots) continue;  // padding between meshes (uniform over the warp)
+    const int64_t s = s0 + lane;
+    const int64_t slast = min(s0 + 32, en.nslots);
+    const int tb = __ldg(en.slot_ptr + s0), te = __ldg(en.slot_ptr + slast);
+    const int count = te - tb;
+    int b = 0, e = 0;
+    if (s < en.nslots) {
+      b = __ldg(en.slot_ptr + s) - tb;
+      e = __ldg(en.slot_ptr + s + 1) - tb;
+    }
+    df64 acc(0.f, 0.f);
+    bool nz = false;
+    if (count <= kBatchStage) {
+      df64* st = stage[warp];
+      int t = lane;
+      for (; t + 96 < count; t += 128) {
+        const int p0 = __ldg(en.perm + tb + t), p1 = __ldg(en.perm + tb + t + 32);
+        const int p2 = __ldg(en.perm + tb + t + 64), p3 = __ldg(en.perm + tb + t + 96);
+        const df64 v0 = en.elem[p0], v1 = en.elem[p1], v2 = en.elem[p2], v3 = en.elem[p3];
+        st[t] = v0;
+        st[t + 32] = v1;
+        st[t + 64] = v2;
+        st[t + 96] = v3;
+      }
+      for (; t < count; t += 32) st[t] = en.elem[__ldg(en.perm + tb + t)];
+      __syncwarp();
+      for (int q = b; q < e; ++q) {
+        const df64 v = st[q];
+        acc += v;
+        nz |= nz_bits(v.hi) || nz_bits(v.lo);
+      }
+      __syncwarp();
+    } else {
+      for (int q = b; q < e; ++q) {
+        const df64 v = en.elem[__ldg(en.perm + tb + q)];
+        acc += v;
+        nz |= nz_bits(v.hi) || nz_bits(v.lo);
+      }
+    }
+    if (s < en.nslots) {
+      en.values[s] = acc.to_double();
       if (!nz) atomicAdd(zero_count, 1);
     }
   }
@@ -94,6 +169,12 @@ void launch_scatter_batch(const ScatterBatchEntry* tab, int ntab, int64_t total,
                           cudaStream_t st) {
   if (total <= 0) return;
   const int threads = 256;
+  if (tps == 0) {
+    const int64_t need = (total + threads - 1) / threads;
+    const unsigned blocks = unsigned(grid > 0 ? std::min<int64_t>(grid, need) : need);
+    scatter_batch_warp_kernel<<<blocks, threads, 0, st>>>(tab, ntab, total, zc);
+    return;
+  }
   const int64_t need = (total * tps + threads - 1) / threads;
   const unsigned blocks = unsigned(grid > 0 ? std::min<int64_t>(grid, need) : need);
   switch (tps) {
@@ -134,8 +215,9 @@ struct fq_batch {
   };
   std::vector<Class> classes;
   DevBuf elem, values, stable, flags;
-  int64_t total_cells = 0, total_slots = 0, max_slots = 0;
-  int tps = 1, sgrid = 0;
+  int64_t total_cells = 0, total_slots = 0, max_slots = 0;  // total_slots: padded batch index space
+  int64_t real_slots = 0;
+  int tps = 1, sgrid = 0;  // tps 0: warp-staged scatter
   cudaGraphExec_t graph = nullptr;
   ~fq_batch() {
     if (graph) cudaGraphExecDestroy(graph);
@@ -294,14 +376,15 @@ fq_status fq_batch_create(fq_ctx* ctx, int nmeshes, fq_mesh* const* meshes, cons
   std::vector<ScatterBatchEntry> st;
   for (auto& mb : B->members) {
     ScatterBatchEntry e;
-    e.begin = B->total_slots;
+    e.begin = B->total_slots;  // a multiple of 32: warps never straddle meshes
     e.nslots = mb.plan->nslots;
     e.slot_ptr = mb.plan->slot_ptr.as<int32_t>();
     e.perm = mb.plan->perm.as<int32_t>();
     e.elem = B->elem.as<df64>() + mb.elem_off;
     e.values = B->values.as<double>() + mb.val_off;
     st.push_back(e);
-    B->total_slots += e.nslots;
+    B->total_slots += (e.nslots + 31) & ~int64_t(31);
+    B->real_slots += e.nslots;
   }
   FQ_TRY(B->stable.alloc(ctx, st.size() * sizeof(ScatterBatchEntry)));
   FQ_CUDA(ctx, cudaMemcpyAsync(B->stable.p, st.data(), st.size() * sizeof(ScatterBatchEntry), cudaMemcpyHostToDevice,
@@ -336,7 +419,7 @@ fq_status fq_batch_tune(fq_batch* B, int reps) {
   // scatter stage: threads per slot and CTAs per SM
   float best = 1e30f;
   int btps = 1, bgrid = 0;
-  for (int tps : {1, 2, 4})
+  for (int tps : {0, 1, 2, 4})
     for (int ps : per_sm) {
       B->tps = tps;
       B->sgrid = ps * dev_sms;
@@ -355,7 +438,7 @@ fq_status fq_batch_tune(fq_batch* B, int reps) {
 }
 
 fq_status fq_batch_set_launch(fq_batch* B, int element_grid, int scatter_tps, int scatter_grid) {
-  if (!B || (scatter_tps != 1 && scatter_tps != 2 && scatter_tps != 4)) return FQ_INVALID_ARG;
+  if (!B || (scatter_tps != 0 && scatter_tps != 1 && scatter_tps != 2 && scatter_tps != 4)) return FQ_INVALID_ARG;
   for (auto& c : B->classes) c.grid = element_grid;
   B->tps = scatter_tps;
   B->sgrid = scatter_grid;
@@ -403,7 +486,7 @@ fq_status fq_batch_info(const fq_batch* B, int64_t* total_cells, int64_t* total_
                         int* launches) {
   if (!B) return FQ_INVALID_ARG;
   if (total_cells) *total_cells = B->total_cells;
-  if (total_slots) *total_slots = B->total_slots;
+  if (total_slots) *total_slots = B->real_slots;
   if (nclasses) *nclasses = int(B->classes.size());
   if (launches) *launches = int(B->classes.size()) + 1;
   return FQ_OK;

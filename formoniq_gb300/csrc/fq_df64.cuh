@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdint>
+#include <cstring>
 
 #include "fq_combinatorics.cuh"
 
@@ -60,19 +62,97 @@ FQ_HDI float f_from_double(double d) {
 #endif
 }
 
+// ---------------------------------------------------------------------------
+// Conversions between double and float pairs by integer operations on the IEEE
+// bit layouts (binary64: 1/11/52, binary32: 1/8/23). GB300 issues two FP64
+// instructions per SM and clock, and the double<->float conversions run on that
+// pipe; these run on the integer and FP32 pipes. Values outside the range where
+// both float parts are normal take the conversion instructions instead.
+// ---------------------------------------------------------------------------
+FQ_HDI uint64_t bits_of(double d) {
+#if defined(__CUDA_ARCH__)
+  return uint64_t(__double_as_longlong(d));
+#else
+  uint64_t u;
+  std::memcpy(&u, &d, 8);
+  return u;
+#endif
+}
+FQ_HDI double double_of(uint64_t u) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)u);
+#else
+  double d;
+  std::memcpy(&d, &u, 8);
+  return d;
+#endif
+}
+FQ_HDI uint32_t bits_of(float f) {
+#if defined(__CUDA_ARCH__)
+  return uint32_t(__float_as_uint(f));
+#else
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return u;
+#endif
+}
+FQ_HDI float float_of(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+// 2^k for -126 <= k <= 127
+FQ_HDI float pow2f(int k) { return float_of(uint32_t(k + 127) << 23); }
+
+// float -> double, exact.
+FQ_HDI double widen(float f) {
+  const uint32_t u = bits_of(f);
+  const uint32_t ex = (u >> 23) & 0xffu;
+  if (ex == 0u || ex == 0xffu) {
+    if ((u & 0x7fffffffu) == 0u) return double_of(uint64_t(u) << 32);  // signed zero
+    return double(f);                                                 // subnormal, inf, nan
+  }
+  return double_of((uint64_t(u & 0x80000000u) << 32) | (uint64_t(ex + 896u) << 52) |
+                   (uint64_t(u & 0x7fffffu) << 29));
+}
+
 struct df64 {
   float hi, lo;
 
   FQ_HDI df64() : hi(0.f), lo(0.f) {}
   FQ_HDI df64(float h, float l) : hi(h), lo(l) {}
-  // Split a double into the nearest float and the float nearest the remainder
-  // (d - hi is exact in double: hi carries d's leading 24 bits).
+  // Split a double into the nearest float (ties to even) and the float nearest
+  // the remainder d - hi, which is exact: the 53-bit significand m is divided
+  // into its leading 24 bits (rounded) and a signed remainder of at most 29 bits.
   FQ_HDI explicit df64(double d) {
-    hi = f_from_double(d);
-    lo = f_from_double(d - double(hi));
+    const uint64_t u = bits_of(d);
+    const int e = int((u >> 52) & 0x7ffu) - 1023;  // unbiased exponent
+    if (e < -60 || e > 60) {
+      hi = f_from_double(d);
+      lo = f_from_double(d - double(hi));
+      return;
+    }
+    const uint64_t m = (u & 0xfffffffffffffull) | (1ull << 52);  // d = +-m 2^(e-52)
+    uint32_t h = uint32_t(m >> 29);                             // 24 bits
+    const uint32_t r = uint32_t(m & 0x1fffffffu);
+    if (r > 0x10000000u || (r == 0x10000000u && (h & 1u))) ++h;
+    const int32_t rem = int32_t(int64_t(m) - (int64_t(h) << 29));  // |rem| <= 2^28
+    const uint32_t sign = uint32_t(u >> 63) << 31;
+    // hi = h 2^(e-23): h is 2^23..2^24 (2^24 after a carry: one binade up)
+    hi = h == (1u << 24) ? float_of(sign | (uint32_t(e + 1 + 127) << 23))
+                         : float_of(sign | (uint32_t(e + 127) << 23) | (h & 0x7fffffu));
+    // lo = rem 2^(e-52), rounded once by the int -> float conversion, scaled
+    // exactly (|e| <= 60 keeps both factors and the product normal)
+    const float lr = float(rem) * pow2f(-60) * pow2f(e + 8);
+    lo = sign ? -lr : lr;
   }
   FQ_HDI explicit df64(int i) : hi(float(i)), lo(0.f) {}
-  FQ_HDI double to_double() const { return double(hi) + double(lo); }
+  // hi + lo rounded to double: both parts widened exactly, one FP64 add.
+  FQ_HDI double to_double() const { return widen(hi) + widen(lo); }
 };
 
 FQ_HDI df64 two_sum(float a, float b) {
@@ -118,6 +198,19 @@ FQ_HDI df64& operator-=(df64& a, df64 b) {
 }
 
 FQ_HDI bool is_zero(df64 a) { return a.hi == 0.f && a.lo == 0.f; }
+
+FQ_HDI df64 dd_abs(df64 a) { return a.hi < 0.f ? -a : a; }
+
+// Square root: the FP32 root of the leading part, corrected once by the Newton
+// step of Karp and Markstein, s = q + (a - q^2) / (2 q) with the residual in
+// float-float and the division in FP32 (the correction only needs 24 bits).
+FQ_HDI df64 dd_sqrt(df64 a) {
+  if (!(a.hi > 0.f)) return df64(0.f, 0.f);
+  const float q = sqrtf(a.hi);
+  const df64 qq(q, 0.f);
+  const df64 res = a - qq * qq;
+  return fast_two_sum(q, res.hi / (q + q));
+}
 
 // Storage: a df64 occupies the same 8 bytes as a double.
 static_assert(sizeof(df64) == 8, "df64 must pack into 8 bytes");

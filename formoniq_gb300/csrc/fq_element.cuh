@@ -27,6 +27,7 @@
 #include <utility>
 
 #include "fq_combinatorics.cuh"
+#include "fq_df64.cuh"
 
 namespace fq {
 
@@ -47,6 +48,33 @@ struct Tab {
 // Local edge index of vertices (a, b), a < b: colex rank C(b,2) + a
 // (simplicial/src/topology/simplex.rs:209-211).
 FQ_HD constexpr int edge_index(int a, int b) { return (b * (b - 1)) / 2 + a; }
+
+// ---------------------------------------------------------------------------
+// Arithmetic that differs per type: exact doubling, reciprocal
+// ---------------------------------------------------------------------------
+template <typename T>
+FQ_HDI T twice(T x) {
+  return x + x;
+}
+FQ_HDI df64 twice(df64 x) { return df64(f_mul(x.hi, 2.f), f_mul(x.lo, 2.f)); }  // exact
+template <typename T>
+FQ_HDI T halve(T x) {
+  return x * T(0.5);
+}
+FQ_HDI df64 halve(df64 x) { return df64(f_mul(x.hi, 0.5f), f_mul(x.lo, 0.5f)); }  // exact (no underflow here)
+template <typename T>
+FQ_HDI T recip(T x) {
+  return T(1) / x;
+}
+// Float-float reciprocal: the FP32 reciprocal of the leading part refined by one
+// Newton-Raphson step r = q + q (1 - a q) carried out in float-float (the
+// division of Bailey's double-double arithmetic); the step squares the 2^-24
+// error of q to about 2^-48.
+FQ_HDI df64 recip(df64 a) {
+  const df64 q(1.0f / a.hi, 0.f);
+  const df64 e = df64(1.f, 0.f) - a * q;
+  return q + q * e;
+}
 
 // ---------------------------------------------------------------------------
 // kernel (a): Gram matrix, determinant, inverse (FP64)
@@ -140,6 +168,89 @@ FQ_HDI double sym_inverse(const double (&a)[N > 0 ? N : 1][N > 0 ? N : 1],
   }
 }
 
+// The same three steps in an arithmetic type T (float-float in FQ_FP64, where
+// the FP64 pipe would otherwise bound the kernel): metric from lengths, inverse
+// by cofactors with det, and below the barycentric Gramian.
+template <int N, typename T>
+FQ_HDI void regge_metric_t(const T* s, T (&g)[N > 0 ? N : 1][N > 0 ? N : 1]) {
+#pragma unroll
+  for (int i = 0; i < N; ++i) g[i][i] = s[edge_index(0, i + 1)];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = i + 1; j < N; ++j) {
+      const T v = halve(s[edge_index(0, i + 1)] + s[edge_index(0, j + 1)] - s[edge_index(i + 1, j + 1)]);
+      g[i][j] = v;
+      g[j][i] = v;
+    }
+}
+
+template <int N, typename T>
+FQ_HDI T sym_inverse_t(const T (&a)[N > 0 ? N : 1][N > 0 ? N : 1], T (&inv)[N > 0 ? N : 1][N > 0 ? N : 1]) {
+  if constexpr (N == 0) {
+    return T(1);
+  } else if constexpr (N == 1) {
+    inv[0][0] = recip(a[0][0]);
+    return a[0][0];
+  } else if constexpr (N == 2) {
+    const T det = a[0][0] * a[1][1] - a[0][1] * a[0][1];
+    const T r = recip(det);
+    inv[0][0] = a[1][1] * r;
+    inv[1][1] = a[0][0] * r;
+    inv[0][1] = inv[1][0] = -(a[0][1] * r);
+    return det;
+  } else if constexpr (N == 3) {
+    const T c00 = a[1][1] * a[2][2] - a[1][2] * a[1][2];
+    const T c01 = a[0][2] * a[1][2] - a[0][1] * a[2][2];
+    const T c02 = a[0][1] * a[1][2] - a[0][2] * a[1][1];
+    const T c11 = a[0][0] * a[2][2] - a[0][2] * a[0][2];
+    const T c12 = a[0][1] * a[0][2] - a[0][0] * a[1][2];
+    const T c22 = a[0][0] * a[1][1] - a[0][1] * a[0][1];
+    const T det = a[0][0] * c00 + a[0][1] * c01 + a[0][2] * c02;
+    const T r = recip(det);
+    inv[0][0] = c00 * r;
+    inv[1][1] = c11 * r;
+    inv[2][2] = c22 * r;
+    inv[0][1] = inv[1][0] = c01 * r;
+    inv[0][2] = inv[2][0] = c02 * r;
+    inv[1][2] = inv[2][1] = c12 * r;
+    return det;
+  } else {
+    static_assert(N == 4, "dimension above 4");
+    const T s0 = a[0][0] * a[1][1] - a[1][0] * a[0][1];
+    const T s1 = a[0][0] * a[1][2] - a[1][0] * a[0][2];
+    const T s2 = a[0][0] * a[1][3] - a[1][0] * a[0][3];
+    const T s3 = a[0][1] * a[1][2] - a[1][1] * a[0][2];
+    const T s4 = a[0][1] * a[1][3] - a[1][1] * a[0][3];
+    const T s5 = a[0][2] * a[1][3] - a[1][2] * a[0][3];
+    const T c5 = a[2][2] * a[3][3] - a[3][2] * a[2][3];
+    const T c4 = a[2][1] * a[3][3] - a[3][1] * a[2][3];
+    const T c3 = a[2][1] * a[3][2] - a[3][1] * a[2][2];
+    const T c2 = a[2][0] * a[3][3] - a[3][0] * a[2][3];
+    const T c1 = a[2][0] * a[3][2] - a[3][0] * a[2][2];
+    const T c0 = a[2][0] * a[3][1] - a[3][0] * a[2][1];
+    const T det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+    const T r = recip(det);
+    inv[0][0] = (a[1][1] * c5 - a[1][2] * c4 + a[1][3] * c3) * r;
+    inv[0][1] = (a[0][2] * c4 - a[0][1] * c5 - a[0][3] * c3) * r;
+    inv[0][2] = (a[3][1] * s5 - a[3][2] * s4 + a[3][3] * s3) * r;
+    inv[0][3] = (a[2][2] * s4 - a[2][1] * s5 - a[2][3] * s3) * r;
+    inv[1][1] = (a[0][0] * c5 - a[0][2] * c2 + a[0][3] * c1) * r;
+    inv[1][2] = (a[3][2] * s2 - a[3][0] * s5 - a[3][3] * s1) * r;
+    inv[1][3] = (a[2][0] * s5 - a[2][2] * s2 + a[2][3] * s1) * r;
+    inv[2][2] = (a[3][0] * s4 - a[3][1] * s2 + a[3][3] * s0) * r;
+    inv[2][3] = (a[2][1] * s2 - a[2][0] * s4 - a[2][3] * s0) * r;
+    inv[3][3] = (a[2][0] * s3 - a[2][1] * s1 + a[2][2] * s0) * r;
+    inv[1][0] = inv[0][1];
+    inv[2][0] = inv[0][2];
+    inv[3][0] = inv[0][3];
+    inv[2][1] = inv[1][2];
+    inv[3][1] = inv[1][3];
+    inv[3][2] = inv[2][3];
+    return det;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Barycentric Gramian B and its compounds H_j = Lambda^j B
 // ---------------------------------------------------------------------------
@@ -148,30 +259,44 @@ struct Bary {
   T b[N + 1][N + 1];
 };
 
+// B from an inverse metric already in T (the float-float path).
 template <int N, typename T>
-FQ_HDI void bary_gramian(const double (&ginv)[N > 0 ? N : 1][N > 0 ? N : 1],
-                                             Bary<N, T>& B) {
-  // B[i+1][j+1] = ginv[i][j]; row/col 0 is minus the column sums (sum of dlambda = 0).
-  double col[N > 0 ? N : 1];
-  double tot = 0.0;
+FQ_HDI void bary_gramian_t(const T (&ginv)[N > 0 ? N : 1][N > 0 ? N : 1], Bary<N, T>& B) {
+  T col[N > 0 ? N : 1];
+  T tot = T(0);
 #pragma unroll
   for (int j = 0; j < N; ++j) {
-    double c = 0.0;
+    T c = T(0);
 #pragma unroll
-    for (int i = 0; i < N; ++i) c += ginv[i][j];
+    for (int i = 0; i < N; ++i) c = c + ginv[i][j];
     col[j] = c;
-    tot += c;
+    tot = tot + c;
   }
-  B.b[0][0] = T(tot);
+  B.b[0][0] = tot;
 #pragma unroll
   for (int j = 0; j < N; ++j) {
-    B.b[0][j + 1] = T(-col[j]);
-    B.b[j + 1][0] = T(-col[j]);
+    B.b[0][j + 1] = -col[j];
+    B.b[j + 1][0] = -col[j];
   }
 #pragma unroll
   for (int i = 0; i < N; ++i)
 #pragma unroll
-    for (int j = 0; j < N; ++j) B.b[i + 1][j + 1] = T(ginv[i][j]);
+    for (int j = 0; j < N; ++j) B.b[i + 1][j + 1] = ginv[i][j];
+}
+
+// B from an IEEE-double inverse metric: the unique entries are converted to T
+// once and the rest is built in T.
+template <int N, typename T>
+FQ_HDI void bary_gramian(const double (&ginv)[N > 0 ? N : 1][N > 0 ? N : 1], Bary<N, T>& B) {
+  T gt[N > 0 ? N : 1][N > 0 ? N : 1];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = i; j < N; ++j) {
+      gt[i][j] = T(ginv[i][j]);
+      gt[j][i] = gt[i][j];
+    }
+  bary_gramian_t<N, T>(gt, B);
 }
 
 // The members of a compile-time vertex mask, increasing.
@@ -299,9 +424,9 @@ FQ_HDI T mass_sum(const Blades<N, KG, T>& H) {
       else if constexpr (coef == -1)
         acc -= h;
       else if constexpr (coef == 2)
-        acc += T(2) * h;
+        acc += twice(h);
       else
-        acc -= T(2) * h;
+        acc -= twice(h);
     });
   });
   return acc;

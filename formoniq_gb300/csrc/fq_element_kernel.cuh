@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cmath>
+#include <type_traits>
 
 #include "fq_df64.cuh"
 #include "fq_element.cuh"
@@ -16,16 +17,55 @@ namespace fq {
 // cell's inverse metric and volume, handed to put(entry, value) in the entry
 // numbering of the program (packed upper triangle, or row-major for the
 // rectangular dif_test/dif_trial). Shared by the device kernel and host checks.
+// Kernel (a) for the element programs: from a cell's squared lengths to the
+// barycentric Gramian B in T, with the metric determinant (as a double). In
+// float-float for n <= 3 the metric, its inverse and determinant of a
+// Riemannian cell (every squared length positive) are float-float too (the
+// FP64 pipe runs at 1/62 of the FP32 rate on GB300 and would bound the
+// kernel); the cofactor cancellation then costs about 20x the IEEE-double
+// rounding, 2e-13 relative at 3D on 0.15h-jittered cells, which leaves the
+// 1e-12 element tolerance a margin. At 4D the same loss reaches 9e-13, and a
+// Lorentzian cell may be near null, so for those, as in the other modes, they
+// stay IEEE double.
+template <int N, typename T>
+FQ_HD T cell_bary(const double* s, Bary<N, T>& B, bool& bad) {
+  constexpr int NE = cbinom(N + 1, 2);
+  bool riemannian = true;
+#pragma unroll
+  for (int e = 0; e < NE; ++e) riemannian = riemannian && s[e] > 0.0;
+  if (std::is_same<T, df64>::value && N <= 3 && riemannian) {
+    if constexpr (std::is_same<T, df64>::value && N <= 3) {
+      df64 sd[NE > 0 ? NE : 1];
+#pragma unroll
+      for (int e = 0; e < NE; ++e) sd[e] = df64(s[e]);
+      df64 g[N > 0 ? N : 1][N > 0 ? N : 1];
+      df64 gi[N > 0 ? N : 1][N > 0 ? N : 1];
+      regge_metric_t<N, df64>(sd, g);
+      const df64 det = sym_inverse_t<N, df64>(g, gi);
+      bary_gramian_t<N, df64>(gi, B);
+      bad = !(det.hi != 0.f) || !isfinite(det.hi);
+      // vol = sqrt|det| / n!  (regge/src/lib.rs:26-28)
+      return dd_sqrt(dd_abs(det)) * df64(1.0 / double(cfact(N)));
+    }
+  }
+  double g[N > 0 ? N : 1][N > 0 ? N : 1];
+  double gi[N > 0 ? N : 1][N > 0 ? N : 1];
+  regge_metric<N>(s, g);
+  const double det = sym_inverse<N>(g, gi);
+  bary_gramian<N, T>(gi, B);
+  bad = !(det != 0.0) || !isfinite(det);
+  return T(sqrt(fabs(det)) * (1.0 / double(cfact(N))));
+}
+
 template <int N, int K, int KIND, typename T, typename Put>
-FQ_HD void element_entries(const double (&ginv)[N > 0 ? N : 1][N > 0 ? N : 1], double vol, double param, Put&& put) {
+FQ_HD void element_entries(const Bary<N, T>& B, T vol, double param, Put&& put) {
   static_assert(KIND != EK_METRIC, "the metric program has no element entries");
-  Bary<N, T> B;
-  bary_gramian<N, T>(ginv, B);
   // mass scale vol (k!)^2 / ((n+1)(n+2)); dif_test scale vol (k!)^2 / (n+1);
   // stiffness scale vol (k!)^2.
-  auto mscale = [&](int k) { return T(vol * double(cfact(k)) * double(cfact(k)) / double((N + 1) * (N + 2))); };
-  auto tscale = [&](int k) { return T(vol * double(cfact(k)) * double(cfact(k)) / double(N + 1)); };
-  auto bscale = [&](int k) { return T(vol * double(cfact(k)) * double(cfact(k))); };
+  // (the constant factors are compile-time constants converted to T)
+  auto mscale = [&](int k) { return vol * T(double(cfact(k)) * double(cfact(k)) / double((N + 1) * (N + 2))); };
+  auto tscale = [&](int k) { return vol * T(double(cfact(k)) * double(cfact(k)) / double(N + 1)); };
+  auto bscale = [&](int k) { return vol * T(double(cfact(k)) * double(cfact(k))); };
 
   if constexpr (KIND == EK_MASS) {
     constexpr int L = cbinom(N + 1, K + 1);
@@ -193,13 +233,13 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs a) {
     double s[NE > 0 ? NE : 1];
 #pragma unroll
     for (int e = 0; e < NE; ++e) s[e] = __ldg(lengths + __ldg(cell_edges + int64_t(e) * nc + cell));
-    double gm[N > 0 ? N : 1][N > 0 ? N : 1];
-    double ginv[N > 0 ? N : 1][N > 0 ? N : 1];
-    regge_metric<N>(s, gm);
-    const double det = sym_inverse<N>(gm, ginv);
-    const double vol = sqrt(fabs(det)) * (1.0 / double(cfact(N)));
-    if (!(det != 0.0) || !isfinite(det)) atomicOr(a.status, 1);
     if constexpr (KIND == EK_METRIC) {
+      double gm[N > 0 ? N : 1][N > 0 ? N : 1];
+      double ginv[N > 0 ? N : 1][N > 0 ? N : 1];
+      regge_metric<N>(s, gm);
+      const double det = sym_inverse<N>(gm, ginv);
+      const double vol = sqrt(fabs(det)) * (1.0 / double(cfact(N)));
+      if (!(det != 0.0) || !isfinite(det)) atomicOr(a.status, 1);
       if (a.ginv_out) {
 #pragma unroll
         for (int i = 0; i < N; ++i)
@@ -209,9 +249,13 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs a) {
       if (a.det_out) a.det_out[cell] = det;
       if (a.vol_out) a.vol_out[cell] = vol;
     } else {
+      Bary<N, T> B;
+      bool bad = false;
+      const T vol = cell_bary<N, T>(s, B, bad);
+      if (bad) atomicOr(a.status, 1);
       T* out = static_cast<T*>(outp);
       const int nent = a.nent;
-      element_entries<N, K, KIND, T>(ginv, vol, a.param, [&](int e, T v) {
+      element_entries<N, K, KIND, T>(B, vol, a.param, [&](int e, T v) {
         if (e < nent)
           out[int64_t(e) * nc + cell] = v;
         else

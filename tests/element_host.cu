@@ -44,14 +44,12 @@ struct HostSink {
 
 template <int N, int K, int KIND, typename T>
 int run_program(const double* s, double param, double* out, int cap, double* det_out) {
-  double g[N > 0 ? N : 1][N > 0 ? N : 1];
-  double ginv[N > 0 ? N : 1][N > 0 ? N : 1];
-  regge_metric<N>(s, g);
-  const double det = sym_inverse<N>(g, ginv);
-  if (det_out) *det_out = det;
-  const double vol = std::sqrt(std::fabs(det)) / double(cfact(N));
+  Bary<N, T> B;
+  bool bad = false;
+  const T vol = cell_bary<N, T>(s, B, bad);
+  if (det_out) *det_out = bad ? 0.0 : 1.0;
   HostSink<T> sink{out, cap, 0, false};
-  element_entries<N, K, KIND, T>(ginv, vol, param, sink);
+  element_entries<N, K, KIND, T>(B, vol, param, sink);
   return sink.overflow ? -2 : sink.nent;
 }
 
@@ -117,3 +115,24 @@ using EhT = double;
 extern "C" int EH_NAME(int k, int kind, const double* lengths_sq, double param, double* out, int cap, double* det) {
   return run_n<EH_DIM, EhT>(k, kind, lengths_sq, param, out, cap, det);
 }
+
+#if EH_DIM == 1 && EH_TYPE == 0
+// The float-float conversions and square root, for the CPU tests.
+extern "C" void eh_df64_split(const double* d, float* hi, float* lo, int n) {
+  for (int i = 0; i < n; ++i) {
+    const df64 v(d[i]);
+    hi[i] = v.hi;
+    lo[i] = v.lo;
+  }
+}
+extern "C" void eh_df64_to_double(const float* hi, const float* lo, double* out, int n) {
+  for (int i = 0; i < n; ++i) out[i] = df64(hi[i], lo[i]).to_double();
+}
+extern "C" void eh_df64_sqrt(const float* hi, const float* lo, float* ohi, float* olo, int n) {
+  for (int i = 0; i < n; ++i) {
+    const df64 r = dd_sqrt(df64(hi[i], lo[i]));
+    ohi[i] = r.hi;
+    olo[i] = r.lo;
+  }
+}
+#endif

@@ -154,3 +154,44 @@ def test_float_float_beats_float(oracle, host_lib, dim):
             e_df = rel_frob(unpack_sym(run(host_lib, DF64, dim, grade, DIF_BOTH, ll)[0], L), expect)
             e_f = rel_frob(unpack_sym(run(host_lib, F32, dim, grade, DIF_BOTH, ll)[0], L), expect)
             assert e_df < TOL[DF64] and e_df < 1e-4 * e_f, (grade, e_df, e_f)
+
+
+def test_float_float_conversions_match_rounded_conversions(host_lib):
+    """df64(double): the nearest float and the float nearest the exact
+    remainder (the conversion instructions' results); to_double: the double
+    nearest hi + lo; dd_sqrt: 48-bit square root."""
+    lib = ctypes.CDLL(LIB)
+    rng = np.random.default_rng(11)
+    mant = rng.uniform(1.0, 2.0, 4000)
+    expo = rng.integers(-70, 70, 4000).astype(np.float64)
+    d = np.concatenate([mant * 2.0 ** expo * rng.choice([-1.0, 1.0], 4000),
+                        [0.0, -0.0, 1.0, 3.0, 1e-300, 1e300, 2.0 ** -60, 2.0 ** 60],
+                        # ties at the 24-bit boundary: 1 + 2^-24 (round to even) and 1 + 3 2^-24
+                        [1.0 + 2.0 ** -24, 1.0 + 3 * 2.0 ** -24, -(1.0 + 2.0 ** -24), 2.0 - 2.0 ** -53]])
+    d = np.ascontiguousarray(d)
+    n = len(d)
+    hi = np.zeros(n, np.float32)
+    lo = np.zeros(n, np.float32)
+    f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    lib.eh_df64_split.argtypes = [f64p, f32p, f32p, ctypes.c_int]
+    lib.eh_df64_split(d, hi, lo, n)
+    want_hi = d.astype(np.float32)
+    with np.errstate(over="ignore", invalid="ignore"):
+        want_lo = (d - want_hi.astype(np.float64)).astype(np.float32)
+    np.testing.assert_array_equal(hi, want_hi)
+    finite = np.isfinite(want_hi)
+    np.testing.assert_array_equal(lo[finite], want_lo[finite])
+    back = np.zeros(n)
+    lib.eh_df64_to_double.argtypes = [f32p, f32p, f64p, ctypes.c_int]
+    lib.eh_df64_to_double(hi, lo, back, n)
+    np.testing.assert_array_equal(back[finite], (hi.astype(np.float64) + lo.astype(np.float64))[finite])
+    pos = np.ascontiguousarray(np.abs(d[:4000]))
+    ph = pos.astype(np.float32)
+    pl = (pos - ph.astype(np.float64)).astype(np.float32)
+    sh, sl = np.zeros(4000, np.float32), np.zeros(4000, np.float32)
+    lib.eh_df64_sqrt.argtypes = [f32p, f32p, f32p, f32p, ctypes.c_int]
+    lib.eh_df64_sqrt(ph, pl, sh, sl, 4000)
+    got = sh.astype(np.float64) + sl.astype(np.float64)
+    want = np.sqrt(ph.astype(np.float64) + pl.astype(np.float64))
+    assert np.max(np.abs(got - want) / want) < 2e-14
