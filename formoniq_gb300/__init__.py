@@ -159,9 +159,11 @@ _SIGNATURES = {
     "fq_assemble": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                    ctypes.POINTER(_P)]),
     "fq_reassemble": (ctypes.c_int, [_P, _P, _P]),
+    "fq_reassemble_many": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.c_int]),
     "fq_hdif_gram": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
     "fq_coboundary": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
     "fq_assemble_host": (ctypes.c_int, [_P, _P, _P, _DP, _P]),
+    "fq_assemble_host_many": (ctypes.c_int, [_P, _P, _DP, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.c_int]),
     "fq_reassemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P]),
     "fq_matrix_info": (ctypes.c_int, [_P, _I64P, _I64P, _I64P, ctypes.POINTER(ctypes.c_int)]),
     "fq_matrix_device_arrays": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
@@ -348,6 +350,17 @@ class Matrix:
 
     def reassemble(self, mesh: "Mesh"):
         self.ctx.check(self.ctx.L.fq_reassemble(self.ctx.h, mesh.h, self.h), "fq_reassemble")
+
+    @staticmethod
+    def reassemble_many(mats):
+        """fq_reassemble_many: re-assemble every matrix (of one context) with one
+        status read at the end."""
+        mats = list(mats)
+        if not mats:
+            return
+        ctx = mats[0].ctx
+        arr = (_P * len(mats))(*[m.h for m in mats])
+        ctx.check(ctx.L.fq_reassemble_many(ctx.h, arr, len(mats)), "fq_reassemble_many")
 
     def reassemble_noalloc(self, mesh: "Mesh", values_ptr: int):
         """Values of this matrix's pattern into a caller-owned device buffer,

@@ -591,6 +591,12 @@ void fq_ctx_destroy(fq_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
+  for (auto e : ctx->prof_events) cudaEventDestroy(e);
+  for (auto e : ctx->copy_events) cudaEventDestroy(e);
+  if (ctx->copy_stream) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
+  }
   ctx->status.release();
   ctx->scratch.release();
   cudaStreamSynchronize(ctx->stream);
@@ -861,6 +867,15 @@ fq_status fq_reassemble(fq_ctx* ctx, fq_mesh* m, fq_matrix* mat) {
   FQ_GUARD_END(ctx)
 }
 
+fq_status fq_reassemble_many(fq_ctx* ctx, fq_matrix* const* mats, int count) {
+  if (!ctx || (count > 0 && !mats) || count < 0) return FQ_INVALID_ARG;
+  for (int i = 0; i < count; ++i)
+    if (!mats[i] || mats[i]->ctx != ctx) return set_error(ctx, FQ_INVALID_ARG, "matrix of another context");
+  FQ_GUARD_BEGIN
+  return assemble_many(ctx, mats, count);
+  FQ_GUARD_END(ctx)
+}
+
 fq_status fq_hdif_gram(fq_ctx* ctx, fq_mesh* m, int grade, fq_bc bc, fq_matrix** out) {
   if (!ctx || !m || !out) return FQ_INVALID_ARG;
   FQ_GUARD_BEGIN
@@ -914,6 +929,18 @@ fq_status fq_assemble_host(fq_ctx* ctx, fq_mesh* m, fq_matrix* mat, const double
     FQ_CUDA(ctx, cudaMemcpyAsync(values_out, mat->values.p, mat->nnz * w, cudaMemcpyDeviceToHost, ctx->stream));
   FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return FQ_OK;
+  FQ_GUARD_END(ctx)
+}
+
+fq_status fq_assemble_host_many(fq_ctx* ctx, fq_mesh* m, const double* lengths, fq_matrix* const* mats,
+                                void* const* values_out, int count) {
+  if (!ctx || !m || !lengths || count < 0 || (count > 0 && (!mats || !values_out))) return FQ_INVALID_ARG;
+  for (int i = 0; i < count; ++i) {
+    if (!mats[i] || mats[i]->mesh != m) return set_error(ctx, FQ_INVALID_ARG, "every matrix must be of this mesh");
+    if (!values_out[i] && mats[i]->nnz > 0) return FQ_INVALID_ARG;
+  }
+  FQ_GUARD_BEGIN
+  return assemble_host_many(ctx, m, lengths, mats, values_out, count);
   FQ_GUARD_END(ctx)
 }
 
@@ -1211,6 +1238,125 @@ fq_status fq_dirac_system(fq_ctx* ctx, fq_mesh* m, double mass_term, fq_matrix**
   FQ_GUARD_END(ctx)
 }
 
+// A mesh with m's topology (host tables and device face tables copied) and no
+// lengths, plans or element buffer.
+static fq_status clone_topology(fq_ctx* ctx, const fq_mesh* m, std::unique_ptr<fq_mesh>& out) {
+  auto c = std::make_unique<fq_mesh>();
+  c->ctx = ctx;
+  c->dim = m->dim;
+  c->ncells = m->ncells;
+  c->kuhn_nbox = m->kuhn_nbox;
+  for (int k = 0; k < 6; ++k) c->nsimp[k] = m->nsimp[k];
+  for (int k = 0; k < 5; ++k) {
+    c->skel[k] = m->skel[k];
+    c->boundary[k] = m->boundary[k];
+    c->interior_map[k] = m->interior_map[k];
+    c->ninterior[k] = m->ninterior[k];
+    c->cell_faces_host[k] = m->cell_faces_host[k];
+    if (m->cell_faces[k].p) {
+      FQ_TRY(c->cell_faces[k].alloc(ctx, m->cell_faces[k].bytes));
+      FQ_CUDA(ctx, cudaMemcpyAsync(c->cell_faces[k].p, m->cell_faces[k].p, m->cell_faces[k].bytes,
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    if (m->interior_dev[k].p) {
+      FQ_TRY(c->interior_dev[k].alloc(ctx, m->interior_dev[k].bytes));
+      FQ_CUDA(ctx, cudaMemcpyAsync(c->interior_dev[k].p, m->interior_dev[k].p, m->interior_dev[k].bytes,
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+  }
+  c->orientation = m->orientation;
+  out = std::move(c);
+  return FQ_OK;
+}
+
+// Euclidean comparison lengths of a Kuhn lattice mesh with signed squared
+// lengths: every lattice axis gets the mean |s| of its single-axis edges, h_a^2,
+// and an edge spanning the axis set I gets sum_{a in I} h_a^2 -- the lattice
+// with the metric's signs made positive (time and space scales kept), the
+// Riemannian geometry the reference measures Lorentzian fields against
+// (examples/minkowski_dirac.rs). Kuhn edges join lattice points whose
+// coordinates differ by 0 or 1 on each axis.
+static fq_status comparison_lengths(fq_ctx* ctx, const fq_mesh* m, std::vector<double>& out) {
+  const int n = m->dim, nb = m->kuhn_nbox;
+  const int64_t ne = m->nsimp[1];
+  std::vector<double> l(size_t(std::max<int64_t>(ne, 1)));
+  if (ne > 0) FQ_CUDA(ctx, cudaMemcpyAsync(l.data(), m->lengths.p, ne * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  std::vector<int> axes(size_t(std::max<int64_t>(ne, 1)), 0);
+  double sum[4] = {0, 0, 0, 0}, cnt[4] = {0, 0, 0, 0};
+  for (int64_t e = 0; e < ne; ++e) {
+    int64_t a = m->skel[1][2 * e], b = m->skel[1][2 * e + 1];
+    int mask = 0;
+    for (int ax = 0; ax < n; ++ax) {
+      if (a % (nb + 1) != b % (nb + 1)) mask |= 1 << ax;
+      a /= nb + 1;
+      b /= nb + 1;
+    }
+    axes[e] = mask;
+    if (mask && !(mask & (mask - 1))) {
+      const int ax = __builtin_ctz(unsigned(mask));
+      sum[ax] += std::fabs(l[e]);
+      cnt[ax] += 1;
+    }
+  }
+  double h2[4];
+  for (int ax = 0; ax < n; ++ax) {
+    if (cnt[ax] == 0 || !(sum[ax] > 0)) return set_error(ctx, FQ_UNSUPPORTED, "lattice axis without lengths");
+    h2[ax] = sum[ax] / cnt[ax];
+  }
+  out.assign(size_t(ne), 0.0);
+  for (int64_t e = 0; e < ne; ++e)
+    for (int ax = 0; ax < n; ++ax)
+      if (axes[e] & (1 << ax)) out[e] += h2[ax];
+  return FQ_OK;
+}
+
+// SPD preconditioners of the relative Dirac system on a Kuhn mesh, both from
+// the Euclidean comparison geometry (the operator's Lorentzian mass is
+// indefinite, so |diag(S)| = m |diag(M)| weighs time-like faces badly):
+//   FQ_PC_AUTO: the inverse diagonal of the comparison masses M_j, j = 0..n
+//     (the L^2 Riesz map's diagonal; as cheap per iteration as Jacobi);
+//   FQ_PC_HX:   diag(hdif_gram(j)) of the comparison geometry, each block an HX
+//     multigrid (the H Lambda Riesz map; fewer iterations on small meshes, a
+//     V-cycle per iteration).
+// MINRES needs no more than a fixed SPD operator.
+struct DiracPrecond {
+  std::unique_ptr<fq_mesh> cmp;
+  std::vector<std::unique_ptr<fq_matrix>> mats;
+  DevBuf diag, dinv;
+  HxPrecond hx;
+  bool use_hx = false;
+};
+
+static fq_status dirac_comparison(fq_ctx* ctx, fq_mesh* m, bool hx, DiracPrecond& dp) {
+  std::vector<double> le;
+  FQ_TRY(comparison_lengths(ctx, m, le));
+  FQ_TRY(clone_topology(ctx, m, dp.cmp));
+  FQ_TRY(fq_mesh_set_lengths_sq(dp.cmp.get(), le.data(), 0));
+  const int n = m->dim;
+  int64_t nrel = 0;
+  for (int k = 0; k <= n; ++k) nrel += m->ninterior[k];
+  FQ_TRY(dp.diag.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));
+  std::vector<int> grades;
+  int64_t off = 0;
+  for (int j = 0; j <= n; ++j) {
+    grades.push_back(j);
+    if (m->ninterior[j] == 0) continue;
+    fq_matrix* a = nullptr;
+    FQ_TRY(make_matrix(ctx, dp.cmp.get(), hx ? EK_HDIF : EK_MASS, j, FQ_RELATIVE, FQ_FP64, 0.0, &a));
+    dp.mats.emplace_back(a);
+    vec_diag(a, dp.diag.as<double>() + off, ctx->stream);
+    ctx->launches++;
+    off += m->ninterior[j];
+  }
+  dp.use_hx = hx;
+  if (hx) return hx_build(ctx, dp.cmp.get(), FQ_RELATIVE, grades, 0, dp.diag.as<double>(), dp.hx);
+  FQ_TRY(dp.dinv.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));
+  vec_recip(dp.diag.as<double>(), dp.dinv.as<double>(), nullptr, nrel, 1, ctx->stream);
+  ctx->launches++;
+  return FQ_OK;
+}
+
 fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* m, double mass_term, const double* load_h,
                                 const double* lift_h, double* x_h, const fq_solve_opts* o, fq_report* rep) {
   if (!ctx || !m || !load_h || !x_h) return FQ_INVALID_ARG;
@@ -1276,9 +1422,20 @@ fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* m, double mass_term, const
   vec_diag(sii, diag.as<double>(), st);
   vec_recip(diag.as<double>(), dinv.as<double>(), nullptr, nrel, 1, st);
   ctx->launches += 5;
+  // preconditioner: HX blocks of the comparison geometry on Kuhn meshes, else |diag(S)|
+  const int pcsel = o->preconditioner;
+  if (pcsel == FQ_PC_HX && m->kuhn_nbox <= 0)
+    return set_error(ctx, FQ_UNSUPPORTED, "the HX Dirac preconditioner needs a Kuhn cube mesh");
+  std::unique_ptr<DiracPrecond> dp;
+  if (pcsel != FQ_PC_JACOBI && m->kuhn_nbox > 0 && nrel > 0) {
+    dp = std::make_unique<DiracPrecond>();
+    FQ_TRY(dirac_comparison(ctx, m, pcsel == FQ_PC_HX, *dp));
+  }
+  const double* pc_diag = !dp ? dinv.as<double>() : (dp->use_hx ? nullptr : dp->dinv.as<double>());
   fq_report r{};
-  FQ_TRY(minres_run<double>(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, sii->nnz, dinv.as<double>(),
-                            nullptr, rhs.as<double>(), x.as<double>(), o->rtol, o->max_iters, &r));
+  FQ_TRY(minres_run<double>(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, sii->nnz, pc_diag,
+                            dp && dp->use_hx ? &dp->hx : nullptr, rhs.as<double>(), x.as<double>(), o->rtol,
+                            o->max_iters, &r));
   {
     DevBuf rr;
     FQ_TRY(rr.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));

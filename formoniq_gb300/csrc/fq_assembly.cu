@@ -433,8 +433,15 @@ __device__ __forceinline__ double store_value(double v) { return v; }
 __device__ __forceinline__ float store_value(float v) { return v; }
 __device__ __forceinline__ double store_value(df64 v) { return v.to_double(); }
 
-// One thread per CSR slot; contributions summed in cell order. E is the element
-// type (df64, float or double), V the stored value type.
+// Contributions of a slot whose loads a thread issues together.
+constexpr int kScatterUnroll = 4;
+
+// One thread per CSR slot; contributions summed in cell order. The plan
+// indices of up to kScatterUnroll contributions are loaded together, then their
+// element values, so a slot of up to four contributions (all of them on the 3D
+// and 4D forms but the vertex masses) costs three dependent loads: slot_ptr,
+// plan index, element value. E is the element type (df64, float or double), V
+// the stored value type.
 template <typename E, typename V>
 __global__ void __launch_bounds__(256) scatter_kernel(const int32_t* __restrict__ slot_ptr,
                                                       const int32_t* __restrict__ perm, const E* __restrict__ elem,
@@ -445,10 +452,19 @@ __global__ void __launch_bounds__(256) scatter_kernel(const int32_t* __restrict_
   const int b = __ldg(slot_ptr + s), e = __ldg(slot_ptr + s + 1);
   E acc = E(0);
   bool nz = false;
-  for (int t = b; t < e; ++t) {
-    const E v = elem[__ldg(perm + t)];
-    acc += v;
-    nz |= nonzero_bits(v);
+  for (int t = b; t < e; t += kScatterUnroll) {
+    int p[kScatterUnroll];
+#pragma unroll
+    for (int u = 0; u < kScatterUnroll; ++u) p[u] = t + u < e ? __ldg(perm + t + u) : 0;
+    E v[kScatterUnroll];
+#pragma unroll
+    for (int u = 0; u < kScatterUnroll; ++u) v[u] = t + u < e ? elem[p[u]] : E(0);
+#pragma unroll
+    for (int u = 0; u < kScatterUnroll; ++u)
+      if (t + u < e) {
+        acc += v[u];
+        nz |= nonzero_bits(v[u]);
+      }
   }
   values[s] = store_value(acc);
   zflag[s] = nz ? 0 : 1;
@@ -644,8 +660,10 @@ fq_status get_plan(fq_ctx* ctx, fq_mesh* m, int kind, int grade, int row_bc, int
   return FQ_OK;
 }
 
-// Element pass + scatter (+ compaction when needed) into m.
-fq_status assemble_into(fq_ctx* ctx, fq_matrix* m) {
+// Queues the element pass and the scatter of m on the context's stream: status
+// bits go to ctx->status[0], the count of all-zero slots to ctx->status[1]. With
+// `ev` (four events) the two kernels are bracketed for profiling.
+static fq_status assemble_launch(fq_ctx* ctx, fq_matrix* m, cudaEvent_t* ev) {
   fq_mesh* mesh = m->mesh;
   Plan& p = *m->plan;
   const int mode = m->precision;
@@ -655,39 +673,171 @@ fq_status assemble_into(fq_ctx* ctx, fq_matrix* m) {
   if (m->zero_flags.bytes < size_t(std::max<int64_t>(p.nslots, 1)))
     FQ_TRY(m->zero_flags.alloc(ctx, std::max<int64_t>(p.nslots, 1)));
   int* zc = ctx->status.as<int>() + 1;
-  FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
-  const bool prof = ctx->profiling && ctx->ev[0];
-  if (prof) FQ_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+  if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[0], ctx->stream));
   if (p.nslots > 0 || p.ndiag_trip > 0) FQ_TRY(element_pass(ctx, mesh, m->kind, m->grade, mode, m->param, mesh->elem, p.nent));
-  if (prof) FQ_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
-  if (prof) FQ_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+  if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[1], ctx->stream));
+  if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[2], ctx->stream));
   launch_scatter(p, mesh->elem.p, m->full_values.p, m->zero_flags.as<uint8_t>(), zc, mode, ctx->stream);
-  if (prof) FQ_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+  if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[3], ctx->stream));
   if (p.nslots > 0) ctx->launches++;
+  return FQ_OK;
+}
+
+static fq_status accumulate_profile(fq_ctx* ctx, cudaEvent_t* ev) {
+  float a = 0.f, b = 0.f;
+  FQ_CUDA(ctx, cudaEventElapsedTime(&a, ev[0], ev[1]));
+  FQ_CUDA(ctx, cudaEventElapsedTime(&b, ev[2], ev[3]));
+  ctx->prof_ms[0] += a;
+  ctx->prof_ms[1] += b;
+  ctx->prof_n[0] += 1;
+  ctx->prof_n[1] += 1;
+  return FQ_OK;
+}
+
+// After the stream has drained: the scatter output becomes the matrix values,
+// or, when `nzero` slots summed exact zeros only, the compacted CSR.
+static fq_status assemble_adopt(fq_ctx* ctx, fq_matrix* m, int64_t nzero) {
+  Plan& p = *m->plan;
+  if (nzero > 0) return compact_csr(ctx, m, nzero);
+  m->nnz = p.nslots;
+  m->rp = p.row_ptr.as<int32_t>();
+  m->ci = p.col_idx.as<int32_t>();
+  m->compacted = false;
+  // values live in full_values: swap roles to avoid a copy
+  std::swap(m->values, m->full_values);
+  return FQ_OK;
+}
+
+static fq_status check_status_words(fq_ctx* ctx) {
+  if (ctx->host_status[0] & 2) return set_error(ctx, FQ_INVALID_ARG, "element program wrote outside its layout");
+  if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
+  return FQ_OK;
+}
+
+// Element pass + scatter (+ compaction when needed) into m.
+fq_status assemble_into(fq_ctx* ctx, fq_matrix* m) {
+  FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
+  cudaEvent_t* ev = ctx->profiling && ctx->ev[0] ? ctx->ev : nullptr;
+  FQ_TRY(assemble_launch(ctx, m, ev));
   FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost,
                                ctx->stream));
   FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ev) FQ_TRY(accumulate_profile(ctx, ev));
+  FQ_TRY(check_status_words(ctx));
+  return assemble_adopt(ctx, m, ctx->host_status[1]);
+}
+
+__global__ void count_flags_kernel(const uint8_t* __restrict__ f, int64_t n, int* count) {
+  int c = 0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    c += f[i];
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+// Several matrices queued back to back with one read of the status words. The
+// element buffer of a mesh is reused in stream order; the rare matrices with
+// all-zero slots are found by counting their flags afterwards.
+fq_status assemble_many(fq_ctx* ctx, fq_matrix* const* mats, int count) {
+  const bool prof = ctx->profiling && ctx->ev[0];
   if (prof) {
-    float a = 0.f, b = 0.f;
-    FQ_CUDA(ctx, cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]));
-    FQ_CUDA(ctx, cudaEventElapsedTime(&b, ctx->ev[2], ctx->ev[3]));
-    ctx->prof_ms[0] += a;
-    ctx->prof_ms[1] += b;
-    ctx->prof_n[0] += 1;
-    ctx->prof_n[1] += 1;
+    while (ctx->prof_events.size() < size_t(count) * 4) {
+      cudaEvent_t e;
+      FQ_CUDA(ctx, cudaEventCreate(&e));
+      ctx->prof_events.push_back(e);
+    }
   }
-  if (ctx->host_status[0] & 2) return set_error(ctx, FQ_INVALID_ARG, "element program wrote outside its layout");
-  if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
-  const int nzero = ctx->host_status[1];
-  if (nzero > 0) {
-    FQ_TRY(compact_csr(ctx, m, nzero));
-  } else {
-    m->nnz = p.nslots;
-    m->rp = p.row_ptr.as<int32_t>();
-    m->ci = p.col_idx.as<int32_t>();
-    m->compacted = false;
-    // values live in full_values: swap roles to avoid a copy
-    std::swap(m->values, m->full_values);
+  FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
+  for (int i = 0; i < count; ++i)
+    if (mats[i]->plan) FQ_TRY(assemble_launch(ctx, mats[i], prof ? ctx->prof_events.data() + 4 * i : nullptr));
+  FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (prof)
+    for (int i = 0; i < count; ++i)
+      if (mats[i]->plan) FQ_TRY(accumulate_profile(ctx, ctx->prof_events.data() + 4 * i));
+  FQ_TRY(check_status_words(ctx));
+  const bool any_zero = ctx->host_status[1] > 0;
+  for (int i = 0; i < count; ++i) {
+    fq_matrix* m = mats[i];
+    if (!m->plan) continue;
+    int64_t nzero = 0;
+    if (any_zero && m->plan->nslots > 0) {
+      int* cnt = ctx->status.as<int>() + 2;
+      FQ_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int), ctx->stream));
+      count_flags_kernel<<<grid_for(m->plan->nslots, 256), 256, 0, ctx->stream>>>(m->zero_flags.as<uint8_t>(),
+                                                                               m->plan->nslots, cnt);
+      ctx->launches++;
+      FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status + 2, cnt, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      nzero = ctx->host_status[2];
+    }
+    FQ_TRY(assemble_adopt(ctx, m, nzero));
+  }
+  return FQ_OK;
+}
+
+// The host-buffer form of assemble_many for one mesh: the lengths go up once,
+// and the values of every matrix come down on a second stream while the next
+// matrix's kernels run (the copy of matrix i waits on an event after its
+// scatter). A matrix that was compacted before, or that compacts now, is
+// downloaded after the status read instead (its value count is known only then).
+fq_status assemble_host_many(fq_ctx* ctx, fq_mesh* mesh, const double* lengths, fq_matrix* const* mats,
+                             void* const* out, int count) {
+  cudaStream_t st = ctx->stream;
+  if (!ctx->copy_stream) FQ_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+  while (ctx->copy_events.size() < size_t(count) + 1) {
+    cudaEvent_t e;
+    FQ_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ctx->copy_events.push_back(e);
+  }
+  const int64_t ne = mesh->dim >= 1 ? mesh->nsimp[1] : 0;
+  if (mesh->lengths.bytes < size_t(std::max<int64_t>(ne, 1)) * 8)
+    FQ_TRY(mesh->lengths.alloc(ctx, std::max<int64_t>(ne, 1) * 8));
+  if (ne > 0) FQ_CUDA(ctx, cudaMemcpyAsync(mesh->lengths.p, lengths, ne * 8, cudaMemcpyHostToDevice, st));
+  mesh->has_lengths = true;
+  FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), st));
+  std::vector<char> streamed(size_t(count), 0);
+  for (int i = 0; i < count; ++i) {
+    fq_matrix* m = mats[i];
+    if (!m->plan) continue;
+    FQ_TRY(assemble_launch(ctx, m, nullptr));
+    if (!m->compacted && m->plan->nslots > 0) {
+      const size_t w = m->precision == FQ_FP32 ? 4 : 8;
+      FQ_CUDA(ctx, cudaEventRecord(ctx->copy_events[i], st));
+      FQ_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_events[i], 0));
+      FQ_CUDA(ctx, cudaMemcpyAsync(out[i], m->full_values.p, size_t(m->plan->nslots) * w, cudaMemcpyDeviceToHost,
+                                   ctx->copy_stream));
+      streamed[i] = 1;
+    }
+  }
+  // the caller's stream resumes after the downloads
+  FQ_CUDA(ctx, cudaEventRecord(ctx->copy_events[count], ctx->copy_stream));
+  FQ_CUDA(ctx, cudaStreamWaitEvent(st, ctx->copy_events[count], 0));
+  FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  FQ_TRY(check_status_words(ctx));
+  const bool any_zero = ctx->host_status[1] > 0;
+  for (int i = 0; i < count; ++i) {
+    fq_matrix* m = mats[i];
+    if (!m->plan) continue;
+    int64_t nzero = 0;
+    if (any_zero && m->plan->nslots > 0) {
+      int* cnt = ctx->status.as<int>() + 2;
+      FQ_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int), st));
+      count_flags_kernel<<<grid_for(m->plan->nslots, 256), 256, 0, st>>>(m->zero_flags.as<uint8_t>(),
+                                                                       m->plan->nslots, cnt);
+      ctx->launches++;
+      FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status + 2, cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
+      FQ_CUDA(ctx, cudaStreamSynchronize(st));
+      nzero = ctx->host_status[2];
+    }
+    FQ_TRY(assemble_adopt(ctx, m, nzero));
+    if ((!streamed[i] || nzero > 0) && m->nnz > 0) {
+      const size_t w = m->precision == FQ_FP32 ? 4 : 8;
+      FQ_CUDA(ctx, cudaMemcpyAsync(out[i], m->values.p, size_t(m->nnz) * w, cudaMemcpyDeviceToHost, st));
+      FQ_CUDA(ctx, cudaStreamSynchronize(st));
+    }
   }
   return FQ_OK;
 }

@@ -129,6 +129,9 @@ struct fq_ctx {
   // scatters (slot 1) of every assembly while `profiling` is set
   bool profiling = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::vector<cudaEvent_t> prof_events;  // four per matrix of a multi-matrix assembly
+  cudaStream_t copy_stream = nullptr;     // downloads overlapped with kernels (host-buffer assembly)
+  std::vector<cudaEvent_t> copy_events;
   double prof_ms[4] = {0, 0, 0, 0};
   int64_t prof_n[4] = {0, 0, 0, 0};
 };
@@ -170,6 +173,9 @@ fq_status element_pass(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int mode
                        int nent);
 fq_status get_plan(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int row_bc, int col_bc, Plan** out);
 fq_status assemble_into(fq_ctx* ctx, fq_matrix* m);
+fq_status assemble_many(fq_ctx* ctx, fq_matrix* const* mats, int count);
+fq_status assemble_host_many(fq_ctx* ctx, fq_mesh* mesh, const double* lengths, fq_matrix* const* mats,
+                             void* const* out, int count);
 fq_status make_matrix(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int bc, int precision, double param,
                       fq_matrix** out);
 

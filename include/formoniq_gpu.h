@@ -185,6 +185,13 @@ fq_status fq_assemble(fq_ctx* ctx, fq_mesh* mesh, fq_form form, int grade, fq_bc
 /* Re-assemble into an existing matrix (same mesh, form, grade, bc, precision)
  * after new lengths: the hot loop of a geometry sweep. */
 fq_status fq_reassemble(fq_ctx* ctx, fq_mesh* mesh, fq_matrix* mat);
+/* Several fq_reassemble calls in one (a geometry sweep that refreshes a set of
+ * operators, e.g. the HilbertComplex masses and stiffnesses, whitney_complex.rs:
+ * 130-183, each a BilinearForm::assemble, galerkin.rs:52-57): the element passes
+ * and scatters of all matrices (any meshes of this context) are queued back to
+ * back on the context's stream and the status is read once at the end. Same
+ * results and errors as calling fq_reassemble on each in order. */
+fq_status fq_reassemble_many(fq_ctx* ctx, fq_matrix* const* mats, int count);
 /* HilbertComplex::hdif_gram (whitney_complex.rs:180-183): M_k + dif_both(k+1). */
 fq_status fq_hdif_gram(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, fq_matrix** out);
 /* HilbertComplex::dif (whitney_complex.rs:417-423, relative :640-643): the
@@ -195,6 +202,13 @@ fq_status fq_coboundary(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, fq_matr
  * values_out. The pattern comes from fq_matrix_copy_to_host of a prior fq_assemble. */
 fq_status fq_assemble_host(fq_ctx* ctx, fq_mesh* mesh, fq_matrix* mat, const double* lengths_sq_host,
                            void* values_out_host);
+/* fq_assemble_host for several matrices of one mesh (the operators a geometry
+ * sweep refreshes, each a BilinearForm::assemble, galerkin.rs:52-57): the
+ * lengths are uploaded once and each matrix's values are downloaded into
+ * values_out_host[i] (its current nnz entries) while the next matrix's kernels
+ * run. Pinned host buffers let the copies overlap. */
+fq_status fq_assemble_host_many(fq_ctx* ctx, fq_mesh* mesh, const double* lengths_sq_host, fq_matrix* const* mats,
+                                void* const* values_out_host, int count);
 
 /* Re-assembly that allocates no device memory. It has no counterpart in the
  * reference. For callers that cannot let this library call cudaMalloc (a host
@@ -272,9 +286,14 @@ fq_status fq_solve_source(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, const
 /* ---- the covariant Hodge-Dirac source problem ---------------------------- */
 /* dirac::solve_dirac_source (problems/dirac.rs:473-531) with MINRES in place of
  * the reference's sparse LU: S = A + m M of HodgeDirac::assemble_selfadjoint
- * (:205-260) on the relative complex, rhs = E^T (load - S lift), |diag(S)|
- * Jacobi preconditioner. load/lift/x are host, flattened by grade (ambient
- * offsets of HodgeDirac, :181-200). mass_term must be nonzero. */
+ * (:205-260) on the relative complex, rhs = E^T (load - S lift). Preconditioner
+ * (opts->preconditioner), on Kuhn cube meshes from the Euclidean comparison
+ * lattice (the signed lengths' axis scales made positive): FQ_PC_AUTO the
+ * inverse diagonal of its relative masses M_j, j = 0..n; FQ_PC_HX its relative
+ * hdif_gram(j) blocks, each an HX multigrid. FQ_PC_JACOBI and other meshes:
+ * |diag(S)|. load/lift/x are host,
+ * flattened by grade (ambient offsets of HodgeDirac, :181-200). mass_term must
+ * be nonzero. */
 fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* mesh, double mass_term, const double* load_host,
                                 const double* lift_host, double* x_host, const fq_solve_opts* opts,
                                 fq_report* report);

@@ -229,6 +229,30 @@ def test_reassembly_is_deterministic(oracle, ctx):
     assert rel_frob(m.to_scipy(), oracle.WhitneyComplex(cx, lengths2).mass(1)) < FP64_TOL
 
 
+def test_reassemble_many_equals_one_by_one(oracle, ctx):
+    """fq_reassemble_many over forms of two meshes, one of them unjittered (its
+    exact-zero slots are compacted away): the same patterns and values, bit for
+    bit, as fq_reassemble on each matrix."""
+    _, mesh_a, _, _ = make_pair(oracle, ctx, 3, 3)
+    cx_b, mesh_b, lengths_b, _ = make_pair(oracle, ctx, 2, 2, jitter=0.0)
+    forms = [(mesh_a, "mass", 1), (mesh_a, "mass", 2), (mesh_a, "dif_both", 2), (mesh_a, "dif_both", 3),
+             (mesh_b, "mass", 1), (mesh_b, "dif_test", 1), (mesh_b, "dif_both", 2)]
+    wcs = {id(mesh_a): fq.WhitneyComplex(mesh_a), id(mesh_b): fq.WhitneyComplex(mesh_b)}
+    many = [getattr(wcs[id(m)], name)(k) for m, name, k in forms]
+    single = [getattr(wcs[id(m)], name)(k) for m, name, k in forms]
+    for (m, _, _), mat in zip(forms, single):
+        mat.reassemble(m)
+    fq.Matrix.reassemble_many(many)
+    for a, b in zip(many, single):
+        sa, sb = a.to_scipy(), b.to_scipy()
+        np.testing.assert_array_equal(sa.indptr, sb.indptr)
+        np.testing.assert_array_equal(sa.indices, sb.indices)
+        np.testing.assert_array_equal(sa.data, sb.data)
+    # the unjittered mesh's pattern is the oracle's (exact zeros dropped)
+    ref = oracle.WhitneyComplex(cx_b, lengths_b).dif_both(2)
+    pattern_difference_is_roundoff(many[-1].to_scipy(), ref)
+
+
 def test_fq_assemble_host_e2e(oracle, ctx):
     import ctypes
 
@@ -241,6 +265,39 @@ def test_fq_assemble_host_e2e(oracle, ctx):
                                      out.ctypes.data_as(ctypes.c_void_p)))
     ref = oracle.WhitneyComplex(cx, l2).dif_both(2)
     assert rel_frob(out, ref.data) < FP64_TOL
+
+
+def test_fq_assemble_host_many_e2e(oracle, ctx):
+    """Host lengths in, every matrix's host values out, downloads overlapped with
+    the next matrix's kernels; an unjittered mesh's exact-zero slots still come
+    out compacted."""
+    import ctypes
+
+    import torch
+
+    for dim, nb, jit in ((3, 3, 0.1), (2, 2, 0.0)):
+        cx, mesh, lengths, _ = make_pair(oracle, ctx, dim, nb, jitter=jit)
+        gwc = fq.WhitneyComplex(mesh)
+        forms = [("mass", 1), ("dif_both", 2), ("dif_test", 1), ("mass", 0)]
+        mats = [getattr(gwc, n)(k) for n, k in forms]
+        l2 = np.ascontiguousarray(lengths * 0.75)
+        owc = oracle.WhitneyComplex(cx, l2)
+        for pinned in (True, False):
+            outs = [torch.zeros(m.nnz, dtype=torch.float64) for m in mats]
+            if pinned:
+                outs = [o.pin_memory() for o in outs]
+            arr = (ctypes.c_void_p * len(mats))(*[m.h for m in mats])
+            oarr = (ctypes.c_void_p * len(mats))(*[o.data_ptr() for o in outs])
+            ctx.check(ctx.L.fq_assemble_host_many(ctx.h, mesh.h, l2.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                  arr, oarr, len(mats)))
+            for (n, k), m, o in zip(forms, mats, outs):
+                ref = getattr(owc, n)(k)
+                got = m.to_scipy()
+                np.testing.assert_array_equal(o.numpy()[:m.nnz], got.data)
+                pattern_difference_is_roundoff(got, ref)
+                if jit > 0:
+                    np.testing.assert_array_equal(got.indptr, ref.indptr)
+                    assert rel_frob(got, ref) < FP64_TOL
 
 
 # ---------------------------------------------------------------------------
@@ -393,6 +450,37 @@ def test_dirac_minkowski_matches_direct(oracle, ctx):
     x, rep = fq.solve_dirac_source(mesh, 1.5, load, lift, fq.SolveOpts.default(rtol=1e-13, max_iters=50000))
     assert rep.converged, rep
     assert np.linalg.norm(x - x_o) / np.linalg.norm(x_o) < SOLVE_TOL
+
+
+@pytest.mark.parametrize("nb,mink,pc", [(4, True, fq.FQ_PC_AUTO), (5, True, fq.FQ_PC_AUTO), (4, False, fq.FQ_PC_AUTO),
+                                        (4, True, fq.FQ_PC_HX), (4, False, fq.FQ_PC_HX)])
+def test_dirac_comparison_preconditioners(oracle, ctx, nb, mink, pc):
+    """Kuhn cube meshes: MINRES preconditioned from the Euclidean comparison
+    lattice (its mass diagonal, or HX blocks of its hdif_gram) converges where
+    |diag(S)| Jacobi does not (Minkowski N = 5: not converged after 20,000
+    iterations in the oracle's MINRES) and matches the direct solve."""
+    dim = 3
+    if mink:
+        cx, coords, signs = oracle.minkowski(dim, nb)
+        lengths = cx.edge_lengths_sq(coords, signs)
+    else:
+        cx, coords = oracle.cartesian_unit(dim, nb)
+        lengths = cx.edge_lengths_sq(coords)
+    lengths = lengths * (1.0 + 0.05 * oracle.uniform_pm1(8, np.arange(len(lengths), dtype=np.uint64)))
+    mesh = fq.Mesh.kuhn_cube(ctx, dim, nb)
+    mesh.set_lengths_sq(lengths)
+    ntot = sum(cx.nsimplices(k) for k in range(dim + 1))
+    load = np.random.default_rng(6).standard_normal(ntot)
+    x_o = oracle.dirac_solve_source(cx, lengths, 1.5, load, np.zeros(ntot))
+    x, rep = fq.solve_dirac_source(mesh, 1.5, load, None,
+                                   fq.SolveOpts.default(rtol=1e-12, max_iters=20000, preconditioner=pc))
+    assert rep.converged, rep
+    assert np.linalg.norm(x - x_o) / np.linalg.norm(x_o) < SOLVE_TOL
+    if mink:
+        _, jrep = fq.solve_dirac_source(mesh, 1.5, load, None,
+                                        fq.SolveOpts.default(rtol=1e-12, max_iters=20000,
+                                                             preconditioner=fq.FQ_PC_JACOBI))
+        assert not jrep.converged or jrep.iters > 2 * rep.iters, (rep, jrep)
 
 
 # ---------------------------------------------------------------------------
