@@ -30,7 +30,7 @@ __all__ = [
     "FqError", "FqUnavailable", "Context", "Mesh", "Matrix", "WhitneyComplex", "MixedProblem", "SolveOpts",
     "Report", "solve_source", "solve_dirac_source", "dirac_system", "minres", "cg", "hx_cg", "hx_apply", "lib_path",
     "load", "exported_symbols", "FQ_PC_AUTO", "FQ_PC_JACOBI", "FQ_PC_HX", "Server", "FQ_REQ_HODGE", "FQ_REQ_DIRAC",
-    "Batch", "FQ_BATCH_MASS", "FQ_BATCH_HDIF",
+    "Batch", "FQ_BATCH_MASS", "FQ_BATCH_HDIF", "ElementOperator", "derham_map",
 ]
 
 FQ_MASS, FQ_DIF_TRIAL, FQ_DIF_TEST, FQ_DIF_BOTH = 0, 1, 2, 3
@@ -160,6 +160,15 @@ _SIGNATURES = {
                                    ctypes.POINTER(_P)]),
     "fq_reassemble": (ctypes.c_int, [_P, _P, _P]),
     "fq_reassemble_many": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.c_int]),
+    "fq_elemop_create": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
+    "fq_elemop_info": (ctypes.c_int, [_P, _I64P, _I64P]),
+    "fq_elemop_apply": (ctypes.c_int, [_P, _P, _P]),
+    "fq_elemop_diagonal": (ctypes.c_int, [_P, _P]),
+    "fq_elemop_cg": (ctypes.c_int, [_P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
+    "fq_elemop_destroy": (None, [_P]),
+    "fq_derham_npoints": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "fq_derham_nodes": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
+    "fq_derham_reduce": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P]),
     "fq_hdif_gram": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
     "fq_coboundary": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
     "fq_assemble_host": (ctypes.c_int, [_P, _P, _P, _DP, _P]),
@@ -601,6 +610,80 @@ def solve_dirac_source(mesh: Mesh, mass_term: float, load_: np.ndarray, lift: Op
     if s not in (0, 3):
         ctx.check(s, "fq_solve_dirac_source")
     return x, Report.of(rep)
+
+
+class ElementOperator:
+    """matfree::ElementOperator: a Whitney pairing applied without assembly.
+    Vectors are device pointers (apply, diagonal, cg) or numpy arrays
+    (apply_host)."""
+
+    def __init__(self, mesh: Mesh, form: int, grade: int, bc: int = FQ_ABSOLUTE):
+        self.ctx, self.mesh = mesh.ctx, mesh
+        h = _P()
+        self.ctx.check(self.ctx.L.fq_elemop_create(self.ctx.h, mesh.h, form, grade, bc, ctypes.byref(h)),
+                       "fq_elemop_create")
+        self.h = h
+        self.ctx._adopt(self)
+
+    @property
+    def shape(self):
+        nr, nc = ctypes.c_int64(), ctypes.c_int64()
+        self.ctx.check(self.ctx.L.fq_elemop_info(self.h, ctypes.byref(nr), ctypes.byref(nc)))
+        return nr.value, nc.value
+
+    def apply(self, x_ptr: int, y_ptr: int):
+        self.ctx.check(self.ctx.L.fq_elemop_apply(self.h, _P(x_ptr), _P(y_ptr)), "fq_elemop_apply")
+
+    def diagonal(self, d_ptr: int):
+        self.ctx.check(self.ctx.L.fq_elemop_diagonal(self.h, _P(d_ptr)), "fq_elemop_diagonal")
+
+    def cg(self, b_ptr: int, x_ptr: int, inv_diag_ptr: int = 0, opts: Optional[SolveOpts] = None) -> "Report":
+        rep = _Report()
+        opts = opts or SolveOpts.default()
+        s = self.ctx.L.fq_elemop_cg(self.h, _P(b_ptr), _P(x_ptr), _P(inv_diag_ptr) if inv_diag_ptr else None,
+                                    ctypes.byref(opts), ctypes.byref(rep))
+        if s not in (0, 3):
+            self.ctx.check(s, "fq_elemop_cg")
+        return Report.of(rep)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.fq_elemop_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def derham_map(mesh: Mesh, coords, grade: int, field, degree: int = 3):
+    """derham::derham_map (derham/src/project.rs:53-96) on the device.
+
+    coords: torch CUDA tensor [N_0, adim] (float64). field: a callable taking
+    the quadrature nodes as a torch CUDA tensor [m, adim] and returning the form's
+    components [m, C(adim, grade)] on dx^I (I colex). Returns the cochain as a
+    torch CUDA tensor [N_grade]."""
+    import math
+
+    import torch
+
+    ctx = mesh.ctx
+    coords = coords.to(torch.float64).contiguous()
+    adim = coords.shape[1]
+    nq = ctx.L.fq_derham_npoints(grade, degree)
+    ns = mesh.nsimplices(grade)
+    nodes = torch.empty((ns * nq, adim), dtype=torch.float64, device=coords.device)
+    torch.cuda.synchronize()
+    ctx.check(ctx.L.fq_derham_nodes(ctx.h, mesh.h, _P(coords.data_ptr()), adim, grade, degree,
+                                    _P(nodes.data_ptr())), "fq_derham_nodes")
+    vals = field(nodes).to(torch.float64).reshape(ns * nq, math.comb(adim, grade)).contiguous()
+    out = torch.empty(ns, dtype=torch.float64, device=coords.device)
+    torch.cuda.synchronize()
+    ctx.check(ctx.L.fq_derham_reduce(ctx.h, mesh.h, _P(coords.data_ptr()), adim, grade, degree,
+                                     _P(vals.data_ptr()), _P(out.data_ptr())), "fq_derham_reduce")
+    return out
 
 
 def dirac_system(mesh: Mesh, mass_term: float) -> Matrix:

@@ -489,18 +489,6 @@ static fq_status mixed_krylov(fq_mixed* P, const double* rhs, double* x, const f
 // ============================================================================
 // extern "C"
 // ============================================================================
-#define FQ_GUARD_BEGIN try {
-#define FQ_GUARD_END(ctx)                                                  \
-  }                                                                        \
-  catch (const std::bad_alloc&) {                                          \
-    return fq::set_error(ctx, FQ_OOM_BUDGET, "host allocation failed");    \
-  }                                                                        \
-  catch (const std::exception& e) {                                        \
-    return fq::set_error(ctx, FQ_INVALID_ARG, e.what());                   \
-  }                                                                        \
-  catch (...) {                                                            \
-    return fq::set_error(ctx, FQ_INVALID_ARG, "unknown error");            \
-  }
 
 extern "C" {
 

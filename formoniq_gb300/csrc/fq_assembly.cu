@@ -187,6 +187,12 @@ __global__ void lower_bound_rows_kernel(const uint64_t* keys, int64_t nkeys, int
   }
 }
 
+void launch_lower_bound_rows(const uint64_t* keys, int64_t nkeys, int64_t nrows, uint64_t stride, int32_t* out,
+                             cudaStream_t st) {
+  const int64_t b = std::max<int64_t>(1, std::min<int64_t>((nrows + 256) / 256, 152 * 32));
+  lower_bound_rows_kernel<<<unsigned(b), 256, 0, st>>>(keys, nkeys, nrows, stride, out);
+}
+
 __global__ void col_from_key_kernel(const uint64_t* ukeys, int64_t n, uint64_t ncols, int32_t* col) {
   for (int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; s < n; s += int64_t(gridDim.x) * blockDim.x)
     col[s] = int32_t(ukeys[s] % ncols);

@@ -5,7 +5,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <exception>
 #include <map>
+#include <new>
 #include <memory>
 #include <string>
 #include <tuple>
@@ -89,6 +91,7 @@ struct fq_mesh {
   // device topology: cell -> face kidx, entry-major [C(n+1,k+1)][ncells]
   fq::DevBuf cell_faces[5];
   fq::DevBuf interior_dev[5];  // int32 relative map
+  fq::DevBuf skel_dev[5];      // int32 [N_k][k+1], uploaded on first use
   // geometry
   fq::DevBuf lengths;  // double [N_1]
   bool has_lengths = false;
@@ -151,6 +154,20 @@ fq_status cuda_check(fq_ctx* ctx, cudaError_t e, const char* what);
     if (_s != FQ_OK) return _s;       \
   } while (0)
 
+// Exceptions never cross the C ABI: every extern "C" body sits in a guard.
+#define FQ_GUARD_BEGIN try {
+#define FQ_GUARD_END(ctx)                                                  \
+  }                                                                        \
+  catch (const std::bad_alloc&) {                                          \
+    return fq::set_error(ctx, FQ_OOM_BUDGET, "host allocation failed");    \
+  }                                                                        \
+  catch (const std::exception& e) {                                        \
+    return fq::set_error(ctx, FQ_INVALID_ARG, e.what());                   \
+  }                                                                        \
+  catch (...) {                                                            \
+    return fq::set_error(ctx, FQ_INVALID_ARG, "unknown error");            \
+  }
+
 // ---- device entry points (implemented in .cu files) ----
 struct ElemArgs;
 // mode = fq_precision: 0 float-float compute with FP64 values, 1 FP32, 2 IEEE FP64.
@@ -178,6 +195,19 @@ fq_status assemble_host_many(fq_ctx* ctx, fq_mesh* mesh, const double* lengths, 
                              void* const* out, int count);
 fq_status make_matrix(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int bc, int precision, double param,
                       fq_matrix** out);
+
+// An operator applied by its own kernels (matrix-free): y = A x on `st`, every
+// kernel returning at once when *done != 0 (a converged Krylov loop).
+struct OpHook {
+  void (*apply)(const void* self, const double* x, double* y, const int* done, cudaStream_t st) = nullptr;
+  const void* self = nullptr;
+};
+// CG (iterative/src/krylov.rs:48-95) on an operator hook, diagonal
+// preconditioner dinv (null = identity).
+fq_status cg_run_op(fq_ctx* ctx, const OpHook& hook, int64_t n, const double* dinv, const double* b, double* x,
+                    double rtol, int64_t max_iters, fq_report* rep);
+void launch_lower_bound_rows(const uint64_t* keys, int64_t nkeys, int64_t nrows, uint64_t stride, int32_t* out,
+                             cudaStream_t st);
 
 // SpMV and vector kernels
 void launch_spmv(const fq_matrix* a, const void* x, void* y, cudaStream_t st);

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "fq_hx.h"
@@ -656,10 +657,12 @@ fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT
   return FQ_OK;
 }
 
+// CG on A given either as CSR (rp, ci, val) or, with `hook`, as an operator
+// applied by its own kernels (matrix-free); the recurrences are the same.
 template <typename VT>
-fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* val, int64_t n, int64_t nnz,
-                 const VT* dinv, const HxPrecond* pc, const VT* b, VT* x, double rtol, int64_t max_iters,
-                 fq_report* rep) {
+static fq_status cg_impl(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* val, const OpHook* hook,
+                         int64_t n, int64_t nnz, const VT* dinv, const HxPrecond* pc, const VT* b, VT* x, double rtol,
+                         int64_t max_iters, fq_report* rep) {
   cudaStream_t st = ctx->stream;
   DevBuf vecs, parts, state;
   const size_t vb = size_t(std::max<int64_t>(n, 1)) * sizeof(VT);
@@ -692,7 +695,13 @@ fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* va
   ctx->launches += 2;
   SolverState hs{};
   auto iteration = [&](int cur) {
-    switch (W) {
+    if (hook) {
+      if constexpr (std::is_same<VT, double>::value) {
+        const int* done = &(S + cur)->done;
+        hook->apply(hook->self, c.p, c.ap, done, st);
+        dot_partials<VT><<<ga, KT, 0, st>>>(c.p, c.ap, c.partA, n, done);
+      }
+    } else switch (W) {
       case 4:
         cg_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
         break;
@@ -720,6 +729,18 @@ fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* va
   rep->converged = hs.converged;
   if (hs.breakdown) return set_error(ctx, FQ_BREAKDOWN, "CG breakdown (NaN)");
   return FQ_OK;
+}
+
+template <typename VT>
+fq_status cg_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT* val, int64_t n, int64_t nnz,
+                 const VT* dinv, const HxPrecond* pc, const VT* b, VT* x, double rtol, int64_t max_iters,
+                 fq_report* rep) {
+  return cg_impl<VT>(ctx, rp, ci, val, nullptr, n, nnz, dinv, pc, b, x, rtol, max_iters, rep);
+}
+
+fq_status cg_run_op(fq_ctx* ctx, const OpHook& hook, int64_t n, const double* dinv, const double* b, double* x,
+                    double rtol, int64_t max_iters, fq_report* rep) {
+  return cg_impl<double>(ctx, nullptr, nullptr, nullptr, &hook, n, n, dinv, nullptr, b, x, rtol, max_iters, rep);
 }
 
 template fq_status minres_run<double>(fq_ctx*, const int32_t*, const int32_t*, const double*, int64_t, int64_t,

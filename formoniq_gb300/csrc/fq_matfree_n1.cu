@@ -1,0 +1,6 @@
+// Matrix-free cell kernels for cell dimension 1.
+#include "fq_matfree.cuh"
+
+namespace fq {
+template int launch_elemop_cells<1>(int K, int kind, const ElemopArgs& a, cudaStream_t st);
+}  // namespace fq

@@ -283,6 +283,43 @@ fq_status fq_solve_source(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, const
                           double* sigma_host, double* u_host, double* p_host, const fq_solve_opts* opts,
                           fq_report* report);
 
+/* ---- matrix-free operators --------------------------------------------- */
+/* ElementOperator (formoniq/src/matfree.rs:54-141): a Whitney pairing applied
+ * without assembling it, y = sum_K P_K^T A_K P_K x. Nothing is stored per
+ * nonzero: every apply rebuilds each cell's element matrix from the mesh's
+ * current squared lengths (float-float, as FQ_FP64 assembly) and gathers the
+ * per-cell products at each degree of freedom in cell order, race-free. The
+ * operator reads the mesh's lengths at every apply (fq_mesh_set_lengths_sq
+ * takes effect at once). Rectangular for dif_test / dif_trial. */
+typedef struct fq_elemop fq_elemop;
+/* ElementOperator::new (matfree.rs:68-84): the test-face incidence, once. */
+fq_status fq_elemop_create(fq_ctx* ctx, fq_mesh* mesh, fq_form form, int grade, fq_bc bc, fq_elemop** out);
+fq_status fq_elemop_info(const fq_elemop* op, int64_t* nrows, int64_t* ncols);
+/* ElementOperator::apply (matfree.rs:98-131): device x [ncols] -> y [nrows], FP64. */
+fq_status fq_elemop_apply(fq_elemop* op, const double* x, double* y);
+/* matfree::diagonal (:148-172): the assembled diagonal, gathered (square forms). */
+fq_status fq_elemop_diagonal(fq_elemop* op, double* diag);
+/* krylov::cg (iterative/src/krylov.rs:48-95) driven by the apply; inv_diag (device,
+ * may be NULL) is the Jacobi preconditioner (matfree::jacobi, :174-180). */
+fq_status fq_elemop_cg(fq_elemop* op, const double* b, double* x, const double* inv_diag, const fq_solve_opts* opts,
+                       fq_report* report);
+void fq_elemop_destroy(fq_elemop* op);
+
+/* ---- the de Rham map (the right-hand-side side of a solve) --------------- */
+/* derham_map (derham/src/project.rs:53-96): (R w)_s = integral of the k-form w
+ * over each k-simplex s, by the Grundmann-Moeller rule exact to `degree`
+ * (simplicial/src/atlas/quadrature.rs:38-82), paired with the simplex's tangent
+ * blade (metric-free). A field is caller code, so it is evaluated by the caller
+ * between two calls: fq_derham_nodes writes the nodes x[s][q][adim] of every
+ * k-simplex (device coords [N_0][adim], adim <= 4), the caller writes
+ * w(x)[s][q][C(adim,k)] (components on dx^I, I the k-subsets of the axes in
+ * colex order), fq_derham_reduce writes the cochain [N_k]. All device arrays. */
+int fq_derham_npoints(int grade, int degree);
+fq_status fq_derham_nodes(fq_ctx* ctx, fq_mesh* mesh, const double* coords, int adim, int grade, int degree,
+                          double* nodes);
+fq_status fq_derham_reduce(fq_ctx* ctx, fq_mesh* mesh, const double* coords, int adim, int grade, int degree,
+                           const double* values, double* cochain);
+
 /* ---- the covariant Hodge-Dirac source problem ---------------------------- */
 /* dirac::solve_dirac_source (problems/dirac.rs:473-531) with MINRES in place of
  * the reference's sparse LU: S = A + m M of HodgeDirac::assemble_selfadjoint

@@ -18,6 +18,7 @@ rounding is unpinned beyond the tolerances those tests assert.
 from __future__ import annotations
 
 import ctypes
+import itertools
 import math
 import os
 from dataclasses import dataclass
@@ -704,3 +705,58 @@ def dirac_solve_source(cx, lengths, mass_term, load, lift):
     out = lift.copy()
     out[keep] += interior
     return out
+
+
+# ---------------------------------------------------------------------------
+# The de Rham map (derham/src/project.rs:53-96) with the Grundmann-Moeller rule
+# (simplicial/src/atlas/quadrature.rs:38-82)
+# ---------------------------------------------------------------------------
+
+def gm_rule(k: int, degree: int):
+    """SimplexQuadRule::degree(k, degree): the Grundmann-Moeller rule of index
+    s = degree // 2 on the k-simplex, barycentric points [nq, k+1] and weights
+    normalised to sum 1."""
+    s = degree // 2
+    d = 2 * s + 1
+    pts, w = [], []
+
+    def compositions(parts, total):
+        if parts == 1:
+            yield (total,)
+            return
+        for b in range(total, -1, -1):
+            for rest in compositions(parts - 1, total - b):
+                yield (b,) + rest
+
+    for i in range(s + 1):
+        den = d + k - 2 * i
+        wi = (-1) ** i * 2.0 ** (-2 * s) * float(den) ** d / (math.factorial(i) * math.factorial(d + k - i))
+        for beta in compositions(k + 1, s - i):
+            pts.append([(2 * b + 1) / den for b in beta])
+            w.append(wi)
+    w = np.array(w)
+    return np.array(pts, np.float64).reshape(len(w), k + 1), w / w.sum()
+
+
+def colex_subsets(n: int, k: int):
+    """k-subsets of range(n) in colex order (compare from the largest element)."""
+    return sorted(itertools.combinations(range(n), k), key=lambda c: c[::-1])
+
+
+def derham_map(cx: Complex, coords: np.ndarray, k: int, field, degree: int = 3) -> np.ndarray:
+    """derham_map (project.rs:53-69) + integrate_face (:77-96) for an ambient
+    form: (R w)_s = (1/k!) sum_q w_q <w(x_q), v_1 ^ ... ^ v_k>, v_i = x_{s_i} - x_{s_0}.
+    `field` maps nodes [m, adim] to components [m, C(adim, k)] on dx^I, I colex."""
+    simp = cx.simplices(k)
+    adim = coords.shape[1]
+    bary, w = gm_rule(k, degree)
+    x = coords[simp]  # [ns, k+1, adim]
+    nodes = np.einsum("qi,sia->sqa", bary, x)
+    vals = np.asarray(field(nodes.reshape(-1, adim)), np.float64).reshape(len(simp), len(w), -1)
+    subs = colex_subsets(adim, k)
+    if k == 0:
+        blade = np.ones((len(simp), 1))
+    else:
+        v = x[:, 1:, :] - x[:, :1, :]  # [ns, k, adim]
+        blade = np.stack([np.linalg.det(v[:, :, list(I)]) for I in subs], axis=1)
+    return np.einsum("q,sqc,sc->s", w, vals, blade) / math.factorial(k)
