@@ -30,7 +30,7 @@ __all__ = [
     "FqError", "FqUnavailable", "Context", "Mesh", "Matrix", "WhitneyComplex", "MixedProblem", "SolveOpts",
     "Report", "solve_source", "solve_dirac_source", "dirac_system", "minres", "cg", "hx_cg", "hx_apply", "lib_path",
     "load", "exported_symbols", "FQ_PC_AUTO", "FQ_PC_JACOBI", "FQ_PC_HX", "Server", "FQ_REQ_HODGE", "FQ_REQ_DIRAC",
-    "Batch", "FQ_BATCH_MASS", "FQ_BATCH_HDIF", "ElementOperator", "derham_map",
+    "Batch", "FQ_BATCH_MASS", "FQ_BATCH_HDIF", "ElementOperator", "derham_map", "Leapfrog",
 ]
 
 FQ_MASS, FQ_DIF_TRIAL, FQ_DIF_TEST, FQ_DIF_BOTH = 0, 1, 2, 3
@@ -167,6 +167,11 @@ _SIGNATURES = {
     "fq_elemop_cg": (ctypes.c_int, [_P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
     "fq_elemop_destroy": (None, [_P]),
     "fq_derham_npoints": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "fq_leapfrog_create": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.POINTER(_P)]),
+    "fq_leapfrog_info": (ctypes.c_int, [_P, _I64P, _I64P, _I64P]),
+    "fq_leapfrog_step": (ctypes.c_int, [_P, _P, ctypes.c_int64]),
+    "fq_leapfrog_energy": (ctypes.c_int, [_P, _P, _DP, _DP]),
+    "fq_leapfrog_destroy": (None, [_P]),
     "fq_derham_nodes": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
     "fq_derham_reduce": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P]),
     "fq_hdif_gram": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
@@ -649,6 +654,58 @@ class ElementOperator:
     def close(self):
         if getattr(self, "h", None):
             self.ctx.L.fq_elemop_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Leapfrog:
+    """solve_dirac_leapfrog / time::Leapfrog on the device: y is a torch CUDA
+    float64 tensor in the complex's DOFs, flat by grade (offsets())."""
+
+    def __init__(self, mesh: Mesh, bc: int, dt: float, mass_rtol: float = 0.0):
+        self.ctx, self.mesh = mesh.ctx, mesh
+        h = _P()
+        self.ctx.check(self.ctx.L.fq_leapfrog_create(self.ctx.h, mesh.h, bc, float(dt), float(mass_rtol),
+                                                     ctypes.byref(h)), "fq_leapfrog_create")
+        self.h = h
+        self.ctx._adopt(self)
+
+    def offsets(self):
+        n = self.mesh.dim
+        off = np.zeros(n + 2, np.int64)
+        self.ctx.check(self.ctx.L.fq_leapfrog_info(self.h, None, off.ctypes.data_as(_I64P), None))
+        return off
+
+    @property
+    def inner_iters(self) -> int:
+        it = ctypes.c_int64()
+        self.ctx.check(self.ctx.L.fq_leapfrog_info(self.h, None, None, ctypes.byref(it)))
+        return it.value
+
+    def step(self, y, nsteps: int = 1):
+        import torch
+
+        torch.cuda.synchronize()
+        self.ctx.check(self.ctx.L.fq_leapfrog_step(self.h, _P(y.data_ptr()), int(nsteps)), "fq_leapfrog_step")
+
+    def energy(self, y):
+        """(1/2 u^T M u, the leapfrog's conserved staggered energy)."""
+        import torch
+
+        torch.cuda.synchronize()
+        e, c = ctypes.c_double(), ctypes.c_double()
+        self.ctx.check(self.ctx.L.fq_leapfrog_energy(self.h, _P(y.data_ptr()), ctypes.byref(e), ctypes.byref(c)),
+                       "fq_leapfrog_energy")
+        return e.value, c.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.fq_leapfrog_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -305,6 +305,25 @@ fq_status fq_elemop_cg(fq_elemop* op, const double* b, double* x, const double* 
                        fq_report* report);
 void fq_elemop_destroy(fq_elemop* op);
 
+/* ---- Maxwell evolution: explicit leapfrog ---------------------------------- */
+/* solve_dirac_leapfrog (problems/dirac.rs:404-434) with time::Leapfrog
+ * (time.rs:271-420): M du/dt = A u, A = dif - delta (HodgeDirac::assemble,
+ * dirac.rs:196-198), grades 2-coloured by parity, one step = half-kick of the odd
+ * grades, drift of the even ones, half-kick. The coupling blocks are the
+ * assembled dif_trial(k) / dif_test(k); each mass block is inverted by
+ * Jacobi-preconditioned CG to mass_rtol (<= 0: 1e-13) where the reference
+ * Cholesky-factors it. y is a device vector in the complex's DOFs (bc), flat by
+ * grade at the offsets fq_leapfrog_info returns (n+2 entries); stable under
+ * the CFL condition dt <= h_min / c, as the reference. */
+typedef struct fq_leapfrog fq_leapfrog;
+fq_status fq_leapfrog_create(fq_ctx* ctx, fq_mesh* mesh, fq_bc bc, double dt, double mass_rtol, fq_leapfrog** out);
+fq_status fq_leapfrog_info(const fq_leapfrog* lf, int64_t* ndofs, int64_t* offsets, int64_t* inner_iters);
+/* Leapfrog::step, nsteps times, in place. */
+fq_status fq_leapfrog_step(fq_leapfrog* lf, double* y, int64_t nsteps);
+/* HodgeDirac::energy (1/2 u^T M u) and Leapfrog::conserved_energy (time.rs:401-420). */
+fq_status fq_leapfrog_energy(fq_leapfrog* lf, const double* y, double* energy, double* conserved);
+void fq_leapfrog_destroy(fq_leapfrog* lf);
+
 /* ---- the de Rham map (the right-hand-side side of a solve) --------------- */
 /* derham_map (derham/src/project.rs:53-96): (R w)_s = integral of the k-form w
  * over each k-simplex s, by the Grundmann-Moeller rule exact to `degree`

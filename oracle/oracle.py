@@ -636,6 +636,12 @@ def dirac_selfadjoint(full: WhitneyComplex):
     """HodgeDirac::assemble_signed(+1): block-diagonal mass M and the
     block-tridiagonal A with U_k = M_k D_{k-1} (global product) below and U_k^T
     above. Returns (offsets, M, A)."""
+    return dirac_signed(full, 1.0)
+
+
+def dirac_signed(full: WhitneyComplex, delta_sign: float):
+    """HodgeDirac::assemble_signed (dirac.rs:213-260): the super-diagonal block is
+    delta_sign U_k^T (-1: the skew evolution generator dif - delta)."""
     n = full.dim
     masses = [full.mass(k) for k in range(n + 1)]
     difs = [full.dif(k) for k in range(n)]
@@ -655,7 +661,7 @@ def dirac_selfadjoint(full: WhitneyComplex):
         # interleave (r,c) and (c,r) pushes as the reference does
         ar.append(np.stack([row + u.row, col + u.col], 1).ravel())
         ac.append(np.stack([col + u.col, row + u.row], 1).ravel())
-        av.append(np.stack([u.data, u.data], 1).ravel())
+        av.append(np.stack([u.data, delta_sign * u.data], 1).ravel())
     a = coo_to_csr(np.concatenate(ar) if ar else [], np.concatenate(ac) if ac else [],
                    np.concatenate(av) if av else [], (tot, tot))
     return offsets, mb, a
@@ -760,3 +766,61 @@ def derham_map(cx: Complex, coords: np.ndarray, k: int, field, degree: int = 3) 
         v = x[:, 1:, :] - x[:, :1, :]  # [ns, k, adim]
         blade = np.stack([np.linalg.det(v[:, :, list(I)]) for I in subs], axis=1)
     return np.einsum("q,sqc,sc->s", w, vals, blade) / math.factorial(k)
+
+
+# ---------------------------------------------------------------------------
+# Maxwell evolution: time::Leapfrog (formoniq/src/time.rs:292-420) as used by
+# solve_dirac_leapfrog (problems/dirac.rs:404-434)
+# ---------------------------------------------------------------------------
+
+def grade_parity_coloring(offsets: np.ndarray) -> np.ndarray:
+    """HodgeDirac::grade_parity_coloring (dirac.rs:337-349): True on odd grades."""
+    color = np.zeros(int(offsets[-1]), bool)
+    for k in range(1, len(offsets) - 1, 2):
+        color[offsets[k]:offsets[k + 1]] = True
+    return color
+
+
+class Leapfrog:
+    """Leapfrog::new / step / conserved_energy with exact block solves."""
+
+    def __init__(self, mass: sp.csr_matrix, op: sp.csr_matrix, color: np.ndarray, dt: float):
+        self.idx0 = np.flatnonzero(~color)
+        self.idx1 = np.flatnonzero(color)
+        m = sp.csr_matrix(mass)
+        a = sp.csr_matrix(op)
+        self.mass0 = m[self.idx0][:, self.idx0].tocsc()
+        self.mass1 = m[self.idx1][:, self.idx1].tocsc()
+        self.a01 = a[self.idx0][:, self.idx1].tocsr()
+        self.a10 = a[self.idx1][:, self.idx0].tocsr()
+        self.lu0 = spla.splu(self.mass0) if self.mass0.shape[0] else None
+        self.lu1 = spla.splu(self.mass1) if self.mass1.shape[0] else None
+        self.dt = dt
+        self.n = m.shape[0]
+
+    def _solve(self, lu, r):
+        return lu.solve(r) if lu is not None else r
+
+    def step(self, y0: np.ndarray) -> np.ndarray:
+        q = y0[self.idx0].copy()
+        p = y0[self.idx1].copy()
+        p += 0.5 * self.dt * self._solve(self.lu1, self.a10 @ q)
+        q += self.dt * self._solve(self.lu0, self.a01 @ p)
+        p += 0.5 * self.dt * self._solve(self.lu1, self.a10 @ q)
+        y1 = np.zeros(self.n)
+        y1[self.idx0] = q
+        y1[self.idx1] = p
+        return y1
+
+    def conserved_energy(self, y: np.ndarray) -> float:
+        q, p = y[self.idx0], y[self.idx1]
+        a10q = self.a10 @ q
+        defect = a10q @ self._solve(self.lu1, a10q)
+        return 0.5 * q @ (self.mass0 @ q) + 0.5 * p @ (self.mass1 @ p) - self.dt ** 2 / 8.0 * defect
+
+
+def leapfrog_for(wc: WhitneyComplex, dt: float):
+    """solve_dirac_leapfrog's set-up on a (full or relative) complex: returns
+    (offsets, mass block, Leapfrog)."""
+    offsets, mb, a = dirac_signed(wc, -1.0)
+    return offsets, mb, Leapfrog(mb, a, grade_parity_coloring(offsets), dt)
