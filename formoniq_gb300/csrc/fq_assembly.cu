@@ -198,6 +198,45 @@ __global__ void col_from_key_kernel(const uint64_t* ukeys, int64_t n, uint64_t n
     col[s] = int32_t(ukeys[s] % ncols);
 }
 
+// ---- symmetric plans: the upper slots and their mirrors ----
+__global__ void upper_flags_kernel(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                                   int64_t nrows, int32_t* flag) {
+  for (int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; r < nrows; r += int64_t(gridDim.x) * blockDim.x)
+    for (int32_t s = row_ptr[r]; s < row_ptr[r + 1]; ++s) flag[s] = col[s] >= r ? 1 : 0;
+}
+
+// For every upper slot: its index, its mirror (binary search of the row in the
+// mirror row's sorted columns; -1 if absent) and its contribution count.
+__global__ void upper_list_kernel(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                                  const int32_t* __restrict__ slot_ptr, const int32_t* __restrict__ flag,
+                                  const int32_t* __restrict__ pos, int64_t nrows, int2* pair, int32_t* len) {
+  for (int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; r < nrows; r += int64_t(gridDim.x) * blockDim.x)
+    for (int32_t s = row_ptr[r]; s < row_ptr[r + 1]; ++s) {
+      if (!flag[s]) continue;
+      const int32_t c = col[s];
+      int32_t lo = row_ptr[c], hi = row_ptr[c + 1];
+      while (lo < hi) {
+        const int32_t mid = (lo + hi) >> 1;
+        if (col[mid] < int32_t(r))
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      const int32_t mirror = (lo < row_ptr[c + 1] && col[lo] == int32_t(r)) ? lo : -1;
+      pair[pos[s]] = make_int2(s, mirror);
+      len[pos[s]] = slot_ptr[s + 1] - slot_ptr[s];
+    }
+}
+
+__global__ void upper_perm_kernel(const int2* __restrict__ pair, const int32_t* __restrict__ up_ptr,
+                                  const int32_t* __restrict__ slot_ptr, const int32_t* __restrict__ perm, int64_t nup,
+                                  int32_t* up_perm) {
+  for (int64_t u = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; u < nup; u += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t s = pair[u].x, b = slot_ptr[s], e = slot_ptr[s + 1], o = up_ptr[u];
+    for (int32_t t = b; t < e; ++t) up_perm[o + (t - b)] = perm[t];
+  }
+}
+
 static int grid_for(int64_t n, int threads) {
   int64_t b = (n + threads - 1) / threads;
   return int(std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32)));
@@ -393,6 +432,50 @@ fq_status build_plan(fq_ctx* ctx, fq_mesh* m, Plan& plan, const Layout& lay) {
   if (ntrip > 0)
     FQ_CUDA(ctx, cudaMemcpyAsync(plan.perm.p, vals2.p, size_t(ntrip) * 4, cudaMemcpyDeviceToDevice, st));
 
+  // symmetric programs on one space: the upper half of the slots with mirrors
+  const bool sym = plan.kind != EK_DIF_TEST && plan.kind != EK_DIF_TRIAL && plan.kind != EK_METRIC &&
+                   plan.row_bc == plan.col_bc && nrows == ncols;
+  if (sym && nruns_h > 0) {
+    DevBuf flag, pos, len;
+    FQ_TRY(flag.alloc(ctx, (nruns_h + 1) * 4));
+    FQ_TRY(pos.alloc(ctx, (nruns_h + 1) * 4));
+    FQ_CUDA(ctx, cudaMemsetAsync(flag.p, 0, (nruns_h + 1) * 4, st));
+    upper_flags_kernel<<<grid_for(nrows, 256), 256, 0, st>>>(plan.row_ptr.as<int32_t>(), plan.col_idx.as<int32_t>(),
+                                                             nrows, flag.as<int32_t>());
+    size_t tmp_bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, flag.as<int32_t>(), pos.as<int32_t>(), int(nruns_h + 1), st);
+    DevBuf tmp;
+    FQ_TRY(tmp.alloc(ctx, std::max<size_t>(tmp_bytes, 16)));
+    FQ_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp.p, tmp_bytes, flag.as<int32_t>(), pos.as<int32_t>(),
+                                               int(nruns_h + 1), st));
+    int32_t nup = 0;
+    FQ_CUDA(ctx, cudaMemcpyAsync(&nup, pos.as<int32_t>() + nruns_h, 4, cudaMemcpyDeviceToHost, st));
+    FQ_CUDA(ctx, cudaStreamSynchronize(st));
+    plan.nup = nup;
+    FQ_TRY(plan.up_pair.alloc(ctx, std::max<int64_t>(nup, 1) * 8));
+    FQ_TRY(len.alloc(ctx, (int64_t(nup) + 1) * 4));
+    FQ_TRY(plan.up_ptr.alloc(ctx, (int64_t(nup) + 1) * 4));
+    FQ_CUDA(ctx, cudaMemsetAsync(len.p, 0, (int64_t(nup) + 1) * 4, st));
+    upper_list_kernel<<<grid_for(nrows, 256), 256, 0, st>>>(
+        plan.row_ptr.as<int32_t>(), plan.col_idx.as<int32_t>(), plan.slot_ptr.as<int32_t>(), flag.as<int32_t>(),
+        pos.as<int32_t>(), nrows, plan.up_pair.as<int2>(), len.as<int32_t>());
+    tmp_bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, len.as<int32_t>(), plan.up_ptr.as<int32_t>(), int(nup + 1), st);
+    DevBuf tmp2;
+    FQ_TRY(tmp2.alloc(ctx, std::max<size_t>(tmp_bytes, 16)));
+    FQ_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp2.p, tmp_bytes, len.as<int32_t>(), plan.up_ptr.as<int32_t>(),
+                                               int(nup + 1), st));
+    int32_t ntu = 0;
+    FQ_CUDA(ctx, cudaMemcpyAsync(&ntu, plan.up_ptr.as<int32_t>() + nup, 4, cudaMemcpyDeviceToHost, st));
+    FQ_CUDA(ctx, cudaStreamSynchronize(st));
+    plan.ntrip_up = ntu;
+    FQ_TRY(plan.up_perm.alloc(ctx, std::max<int64_t>(ntu, 1) * 4));
+    upper_perm_kernel<<<grid_for(nup, 256), 256, 0, st>>>(plan.up_pair.as<int2>(), plan.up_ptr.as<int32_t>(),
+                                                         plan.slot_ptr.as<int32_t>(), plan.perm.as<int32_t>(), nup,
+                                                         plan.up_perm.as<int32_t>());
+    ctx->launches += 3;
+  }
+
   // diagonal plan (preconditioner of the mixed system)
   if (!lay.diag_entry.empty()) {
     const int64_t dtotal = nc * lr;
@@ -477,6 +560,53 @@ __global__ void __launch_bounds__(256) scatter_kernel(const int32_t* __restrict_
   if (!nz) atomicAdd(zero_count, 1);
 }
 
+// Symmetric plans: one thread per upper slot sums its contributions (in cell
+// order, as scatter_kernel) and writes the value to the slot and its mirror.
+// A mirror the pattern lacks (never, for a structurally symmetric program) sets
+// status bit 2.
+template <typename E, typename V>
+__global__ void __launch_bounds__(256) scatter_sym_kernel(const int2* __restrict__ pair,
+                                                          const int32_t* __restrict__ up_ptr,
+                                                          const int32_t* __restrict__ perm,
+                                                          const E* __restrict__ elem, V* __restrict__ values,
+                                                          uint8_t* __restrict__ zflag, int* status, int64_t nup) {
+  const int64_t u = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (u >= nup) return;
+  const int2 sm = __ldg(pair + u);
+  const int b = __ldg(up_ptr + u), e = __ldg(up_ptr + u + 1);
+  E acc = E(0);
+  bool nz = false;
+  for (int t = b; t < e; t += kScatterUnroll) {
+    int p[kScatterUnroll];
+#pragma unroll
+    for (int k = 0; k < kScatterUnroll; ++k) p[k] = t + k < e ? __ldg(perm + t + k) : 0;
+    E v[kScatterUnroll];
+#pragma unroll
+    for (int k = 0; k < kScatterUnroll; ++k) v[k] = t + k < e ? elem[p[k]] : E(0);
+#pragma unroll
+    for (int k = 0; k < kScatterUnroll; ++k)
+      if (t + k < e) {
+        acc += v[k];
+        nz |= nonzero_bits(v[k]);
+      }
+  }
+  const V out = store_value(acc);
+  const uint8_t z = nz ? 0 : 1;
+  values[sm.x] = out;
+  zflag[sm.x] = z;
+  int nzero = nz ? 0 : 1;
+  if (sm.y != sm.x) {
+    if (sm.y >= 0) {
+      values[sm.y] = out;
+      zflag[sm.y] = z;
+      nzero += nz ? 0 : 1;
+    } else {
+      atomicOr(status, 4);
+    }
+  }
+  if (nzero) atomicAdd(status + 1, nzero);
+}
+
 template <typename E>
 __global__ void __launch_bounds__(256) scatter_diag_kernel(const int32_t* __restrict__ ptr,
                                                            const int32_t* __restrict__ perm,
@@ -501,9 +631,29 @@ void launch_df64_to_double(const void* in, double* out, int64_t n, cudaStream_t 
   df64_to_double_kernel<<<g, 256, 0, st>>>(static_cast<const df64*>(in), out, n);
 }
 
-void launch_scatter(const Plan& plan, const void* elem, void* values, uint8_t* zero_flags, int* zero_count,
-                    int mode, cudaStream_t st) {
+void launch_scatter(const Plan& plan, const void* elem, void* values, uint8_t* zero_flags, int* status, int mode,
+                    cudaStream_t st) {
   if (plan.nslots == 0) return;
+  int* zero_count = status + 1;
+  if (plan.nup > 0) {
+    const unsigned blocks = unsigned((plan.nup + 255) / 256);
+    const int2* pr = plan.up_pair.as<int2>();
+    const int32_t* up = plan.up_ptr.as<int32_t>();
+    const int32_t* pm = plan.up_perm.as<int32_t>();
+    if (mode == 1)
+      scatter_sym_kernel<float, float><<<blocks, 256, 0, st>>>(pr, up, pm, static_cast<const float*>(elem),
+                                                               static_cast<float*>(values), zero_flags, status,
+                                                               plan.nup);
+    else if (mode == 2)
+      scatter_sym_kernel<double, double><<<blocks, 256, 0, st>>>(pr, up, pm, static_cast<const double*>(elem),
+                                                                 static_cast<double*>(values), zero_flags, status,
+                                                                 plan.nup);
+    else
+      scatter_sym_kernel<df64, double><<<blocks, 256, 0, st>>>(pr, up, pm, static_cast<const df64*>(elem),
+                                                               static_cast<double*>(values), zero_flags, status,
+                                                               plan.nup);
+    return;
+  }
   const int threads = 256;
   const unsigned blocks = unsigned((plan.nslots + threads - 1) / threads);
   const int32_t* sp = plan.slot_ptr.as<int32_t>();
@@ -678,7 +828,7 @@ static fq_status assemble_launch(fq_ctx* ctx, fq_matrix* m, cudaEvent_t* ev) {
     FQ_TRY(m->full_values.alloc(ctx, std::max<int64_t>(p.nslots, 1) * w));
   if (m->zero_flags.bytes < size_t(std::max<int64_t>(p.nslots, 1)))
     FQ_TRY(m->zero_flags.alloc(ctx, std::max<int64_t>(p.nslots, 1)));
-  int* zc = ctx->status.as<int>() + 1;
+  int* zc = ctx->status.as<int>();
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[0], ctx->stream));
   if (p.nslots > 0 || p.ndiag_trip > 0) FQ_TRY(element_pass(ctx, mesh, m->kind, m->grade, mode, m->param, mesh->elem, p.nent));
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[1], ctx->stream));
@@ -715,6 +865,7 @@ static fq_status assemble_adopt(fq_ctx* ctx, fq_matrix* m, int64_t nzero) {
 }
 
 static fq_status check_status_words(fq_ctx* ctx) {
+  if (ctx->host_status[0] & 4) return set_error(ctx, FQ_CUDA_ERROR, "symmetric plan without a mirror slot");
   if (ctx->host_status[0] & 2) return set_error(ctx, FQ_INVALID_ARG, "element program wrote outside its layout");
   if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
   return FQ_OK;

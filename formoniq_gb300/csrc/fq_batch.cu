@@ -283,6 +283,7 @@ fq_status check_status(fq_ctx* ctx) {
   FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost,
                                ctx->stream));
   FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->host_status[0] & 4) return set_error(ctx, FQ_CUDA_ERROR, "symmetric plan without a mirror slot");
   if (ctx->host_status[0] & 2) return set_error(ctx, FQ_INVALID_ARG, "element program wrote outside its layout");
   if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
   if (ctx->host_status[1] > 0)
@@ -476,7 +477,7 @@ fq_status fq_batch_assemble_per_mesh(fq_batch* B, int check) {
     if (launch_element(mb.mesh->dim, mb.grade, B->kind, FQ_FP64, a, st) != 0)
       return set_error(ctx, FQ_UNSUPPORTED, "no element program for this dimension/grade");
     launch_scatter(*mb.plan, a.out, B->values.as<double>() + mb.val_off, B->flags.as<uint8_t>(),
-                   ctx->status.as<int>() + 1, FQ_FP64, st);
+                   ctx->status.as<int>(), FQ_FP64, st);
     ctx->launches += 2;
   }
   return check ? check_status(ctx) : FQ_OK;

@@ -53,6 +53,14 @@ struct Plan {
   DevBuf col_idx;       // int32 [nslots]
   DevBuf slot_ptr;      // int32 [nslots+1]
   DevBuf perm;          // int32 [ntrip]: element buffer index entry*ncells + cell
+  // Symmetric programs on one space (row space = column space): the slots with
+  // row <= col, each with its own index and its mirror's ((col,row); itself on
+  // the diagonal), and their contributions. Slot (i,j) and (j,i) sum the same
+  // packed element entries in the same cell order, so one sum serves both.
+  int64_t nup = 0, ntrip_up = 0;
+  DevBuf up_pair;       // int2 [nup]: (slot, mirror slot)
+  DevBuf up_ptr;        // int32 [nup+1]
+  DevBuf up_perm;       // int32 [ntrip_up]
   // Diagonal plan (EK_KKT preconditioner): slots = rows.
   int64_t ndiag_trip = 0;
   DevBuf diag_ptr;      // int32 [nrows+1]
@@ -177,9 +185,10 @@ int launch_element(int n, int grade, int kind, int mode, const ElemArgs& a, cuda
 fq_status build_plan(fq_ctx* ctx, fq_mesh* mesh, Plan& plan, const Layout& lay);
 
 // values[s] = sum of elem[perm[t]] over the slot's contributions; zero_flags[s]
-// = 1 when every contribution was exactly 0.0; *zero_count += count.
-void launch_scatter(const Plan& plan, const void* elem, void* values, uint8_t* zero_flags, int* zero_count,
-                    int mode, cudaStream_t st);
+// = 1 when every contribution was exactly 0.0; status[1] += count of such
+// slots; status[0] |= 4 if a symmetric plan misses a mirror slot.
+void launch_scatter(const Plan& plan, const void* elem, void* values, uint8_t* zero_flags, int* status, int mode,
+                    cudaStream_t st);
 void launch_scatter_diag(const Plan& plan, const void* elem, double* out, int mode, cudaStream_t st);
 void launch_df64_to_double(const void* in, double* out, int64_t n, cudaStream_t st);
 

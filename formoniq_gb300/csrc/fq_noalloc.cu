@@ -94,12 +94,13 @@ extern "C" fq_status fq_reassemble_noalloc(fq_ctx* ctx, fq_mesh* mesh, const fq_
       return set_error(ctx, FQ_UNSUPPORTED, "no element program for this dimension/grade");
     ctx->launches++;
     FQ_CUDA(ctx, cudaGetLastError());
-    launch_scatter(p, base, values_out, base + elem_bytes, ctx->status.as<int>() + 1, mode, st);
+    launch_scatter(p, base, values_out, base + elem_bytes, ctx->status.as<int>(), mode, st);
     ctx->launches++;
     FQ_CUDA(ctx, cudaGetLastError());
   }
   FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
   FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  if (ctx->host_status[0] & 4) return set_error(ctx, FQ_CUDA_ERROR, "symmetric plan without a mirror slot");
   if (ctx->host_status[0] & 2) return set_error(ctx, FQ_INVALID_ARG, "element program wrote outside its layout");
   if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
   if (ctx->host_status[1] > 0)
