@@ -183,57 +183,6 @@ static fq_status empty_matrix(fq_ctx* ctx, fq_mesh* mesh, int64_t rows, int64_t 
 // Coboundary D_k (Complex::coboundary_operator, topology/complex.rs:215-217):
 // rows the (k+1)-simplices, entry (-1)^p at the face omitting vertex position p;
 // the relative complex keeps interior simplices on both sides.
-void coboundary_host(const fq_mesh* m, int k, int bc, HCsr& out) {
-  out = HCsr();
-  out.nrows = ndofs(m, k + 1, bc);
-  out.ncols = ndofs(m, k, bc);
-  if (k < 0 || k >= m->dim || out.nrows == 0 || out.ncols == 0) {
-    out.rp.assign(size_t(out.nrows) + 1, 0);
-    return;
-  }
-  const int w = k + 2;
-  const auto& sk = m->skel[k + 1];
-  const auto& low = m->skel[k];
-  const int fw = w - 1;
-  for (int64_t r = 0; r < m->nsimp[k + 1]; ++r) {
-    if (bc == FQ_RELATIVE && m->boundary[k + 1][r]) continue;
-    std::vector<std::pair<int32_t, double>> ent;
-    for (int p = 0; p < w; ++p) {
-      int32_t tup[5];
-      int q = 0;
-      for (int i = 0; i < w; ++i)
-        if (i != p) tup[q++] = sk[r * w + i];
-      int64_t lo = 0, hi = m->nsimp[k] - 1, found = -1;
-      while (lo <= hi) {
-        const int64_t mid = (lo + hi) / 2;
-        int cmp = 0;
-        for (int i = fw - 1; i >= 0; --i)
-          if (low[mid * fw + i] != tup[i]) {
-            cmp = low[mid * fw + i] < tup[i] ? -1 : 1;
-            break;
-          }
-        if (cmp == 0) {
-          found = mid;
-          break;
-        }
-        if (cmp < 0)
-          lo = mid + 1;
-        else
-          hi = mid - 1;
-      }
-      int64_t c = found;
-      if (bc == FQ_RELATIVE) c = m->interior_map[k][found];
-      if (c < 0) continue;
-      ent.emplace_back(int32_t(c), (p % 2) ? -1.0 : 1.0);
-    }
-    std::sort(ent.begin(), ent.end());
-    for (auto& e : ent) {
-      out.ci.push_back(e.first);
-      out.v.push_back(e.second);
-    }
-    out.rp.push_back(int32_t(out.ci.size()));
-  }
-}
 
 }  // namespace fq
 
@@ -878,28 +827,18 @@ fq_status fq_coboundary(fq_ctx* ctx, fq_mesh* m, int k, fq_bc bc, fq_matrix** ou
   FQ_GUARD_BEGIN
   const int64_t nr = ndofs(m, k + 1, bc), nc = ndofs(m, k, bc);
   if (k < 0 || k >= m->dim || nr == 0 || nc == 0) return empty_matrix(ctx, m, nr, nc, FQ_FP64, out);
-  HCsr h;
-  coboundary_host(m, k, int(bc), h);
+  DCsr d;
+  FQ_TRY(coboundary_device(ctx, m, k, int(bc), d));
   auto* mat = new fq_matrix();
   mat->ctx = ctx;
   mat->mesh = m;
   mat->nrows = nr;
   mat->ncols = nc;
-  mat->nnz = int64_t(h.ci.size());
+  mat->nnz = d.nnz;
   mat->precision = FQ_FP64;
-  fq_status s = mat->row_ptr.alloc(ctx, h.rp.size() * 4);
-  if (s == FQ_OK) s = mat->col_idx.alloc(ctx, std::max<size_t>(h.ci.size(), 1) * 4);
-  if (s == FQ_OK) s = mat->values.alloc(ctx, std::max<size_t>(h.v.size(), 1) * 8);
-  if (s != FQ_OK) {
-    delete mat;
-    return s;
-  }
-  cudaMemcpyAsync(mat->row_ptr.p, h.rp.data(), h.rp.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
-  if (!h.ci.empty()) {
-    cudaMemcpyAsync(mat->col_idx.p, h.ci.data(), h.ci.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(mat->values.p, h.v.data(), h.v.size() * 8, cudaMemcpyHostToDevice, ctx->stream);
-  }
-  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  mat->row_ptr = std::move(d.own_rp);
+  mat->col_idx = std::move(d.own_ci);
+  mat->values = std::move(d.own_v64);
   mat->rp = mat->row_ptr.as<int32_t>();
   mat->ci = mat->col_idx.as<int32_t>();
   *out = mat;

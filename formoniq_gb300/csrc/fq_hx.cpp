@@ -29,7 +29,6 @@ namespace fq {
 
 fq_status make_matrix(fq_ctx* ctx, fq_mesh* mesh, int kind, int grade, int bc, int precision, double param,
                       fq_matrix** out);
-void coboundary_host(const fq_mesh* m, int k, int bc, HCsr& out);
 fq_status assemble_into(fq_ctx* ctx, fq_matrix* m);
 fq_status device_scaled_recip(fq_ctx* ctx, const double* d, int64_t n, double omega, DevBuf& out);
 
@@ -37,7 +36,6 @@ namespace {
 
 constexpr double kOmega = 2.0 / 3.0;  // Jacobi::smoother (iterative/src/precond.rs:92-94)
 constexpr int64_t kCoarseMax = 256;
-const double kUnit[4] = {1.0, 1.0, 1.0, 1.0};  // lattice frame before scaling
 
 int64_t ipow(int64_t b, int e) {
   int64_t r = 1;
@@ -179,126 +177,6 @@ int64_t find_edge(const fq_mesh* m, int32_t u, int32_t v) {
       hi = mid - 1;
   }
   return -1;
-}
-
-double small_det(double (*e)[4], int j) {
-  if (j == 0) return 1.0;
-  if (j == 1) return e[0][0];
-  if (j == 2) return e[0][0] * e[1][1] - e[0][1] * e[1][0];
-  if (j == 3)
-    return e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) - e[0][1] * (e[1][0] * e[2][2] - e[1][2] * e[2][0]) +
-           e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0]);
-  // j == 4: expansion along the first row
-  double d = 0.0;
-  for (int col = 0; col < 4; ++col) {
-    double sub[4][4];
-    for (int r = 1; r < 4; ++r) {
-      int q = 0;
-      for (int cc = 0; cc < 4; ++cc)
-        if (cc != col) sub[r - 1][q++] = e[r][cc];
-    }
-    d += ((col % 2) ? -1.0 : 1.0) * e[0][col] * small_det(sub, 3);
-  }
-  return d;
-}
-
-// Pi_j with columns as offsets into the interleaved nodal block (node * m +
-// slot + I), and its transpose with rows ordered (node, I).
-void vector_nodal(const fq_mesh* m, int j, int bc, const double* h, int mslots, int slot, HCsr& Pi, HCsr& Pit) {
-  // (h is the unit spacing at build time: the values are scaled per component on the device)
-  const int n = m->dim, nb = m->kuhn_nbox;
-  const int ncomp = j == 0 ? 1 : binom(n, j);
-  const int64_t n0 = level_nodes(n, nb, bc);
-  // colex j-subsets of the axes
-  std::vector<std::vector<int>> subsets;
-  for (unsigned mask = 0; mask < (1u << n); ++mask)
-    if (__builtin_popcount(mask) == j) {
-      std::vector<int> s;
-      for (int a = 0; a < n; ++a)
-        if (mask & (1u << a)) s.push_back(a);
-      subsets.push_back(s);
-    }
-  std::sort(subsets.begin(), subsets.end(), [](const std::vector<int>& x, const std::vector<int>& y) {
-    for (int i = int(x.size()) - 1; i >= 0; --i)
-      if (x[i] != y[i]) return x[i] < y[i];
-    return false;
-  });
-  double fact = 1.0;
-  for (int i = 2; i <= j + 1; ++i) fact *= i;
-  const double factor = 1.0 / fact;
-  Pi = HCsr();
-  Pi.ncols = n0 * mslots;
-  struct Ent {
-    int64_t trow;
-    int32_t row;
-    double v;
-    uint8_t mask;
-  };
-  std::vector<uint8_t> masks(size_t(ncomp), 0);
-  for (int q = 0; q < ncomp && j > 0; ++q)
-    for (int a : subsets[q]) masks[q] |= uint8_t(1u << a);
-  std::vector<Ent> tr;
-  const int w = j + 1;
-  int32_t row = 0;
-  for (int64_t s = 0; s < m->nsimp[j]; ++s) {
-    if (bc == FQ_RELATIVE && m->boundary[j][s]) continue;
-    const int32_t* vs = &m->skel[j][s * w];
-    int c0[4], ci[4];
-    lattice_coords(vs[0], n, nb, c0);
-    double E[4][4] = {};  // E[axis][edge]
-    for (int i = 1; i <= j; ++i) {
-      lattice_coords(vs[i], n, nb, ci);
-      for (int a = 0; a < n; ++a) E[a][i - 1] = double(ci[a] - c0[a]) * h[a];
-    }
-    std::vector<double> comp(ncomp, 1.0);
-    if (j > 0)
-      for (int q = 0; q < ncomp; ++q) {
-        double sub[4][4] = {};
-        for (int r = 0; r < j; ++r)
-          for (int cc = 0; cc < j; ++cc) sub[r][cc] = E[subsets[q][r]][cc];
-        comp[q] = small_det(sub, j);
-      }
-    std::vector<std::pair<int64_t, double>> ent;  // (column, value); column - node*m - slot = component
-    for (int i = 0; i < w; ++i) {
-      int cv[4];
-      lattice_coords(vs[i], n, nb, cv);
-      const int64_t node = node_index(cv, n, nb, bc);
-      if (node < 0) continue;
-      for (int q = 0; q < ncomp; ++q) {
-        const double val = factor * comp[q];
-        if (val == 0.0) continue;
-        ent.emplace_back(node * mslots + slot + q, val);
-        tr.push_back({node * ncomp + q, row, val, masks[q]});
-      }
-    }
-    std::sort(ent.begin(), ent.end());
-    for (auto& e : ent) {
-      Pi.ci.push_back(int32_t(e.first));
-      Pi.v.push_back(e.second);
-      Pi.mask.push_back(masks[int((e.first % mslots) - slot)]);
-    }
-    Pi.rp.push_back(int32_t(Pi.ci.size()));
-    ++row;
-  }
-  Pi.nrows = row;
-  // transpose (stable by source row within each target row)
-  Pit = HCsr();
-  Pit.nrows = n0 * ncomp;
-  Pit.ncols = row;
-  std::vector<int32_t> cnt(size_t(Pit.nrows) + 1, 0);
-  for (auto& e : tr) cnt[e.trow + 1]++;
-  for (int64_t i = 0; i < Pit.nrows; ++i) cnt[i + 1] += cnt[i];
-  Pit.rp = cnt;
-  Pit.ci.resize(tr.size());
-  Pit.v.resize(tr.size());
-  Pit.mask.resize(tr.size());
-  std::vector<int32_t> pos(cnt.begin(), cnt.end() - 1);
-  for (auto& e : tr) {
-    const int32_t p = pos[e.trow]++;
-    Pit.ci[p] = e.row;
-    Pit.v[p] = e.v;
-    Pit.mask[p] = e.mask;
-  }
 }
 
 // Identity from unknown i to slot `slot` of node i (and its transpose, the
@@ -443,29 +321,29 @@ fq_status hx_build(fq_ctx* ctx, fq_mesh* m, int bc, const std::vector<int>& grad
   // blocks: transfer maps (lattice values; scaled by the spacing in hx_refresh)
   const int64_t n0 = mg.lv[0].n;
   for (HxBlock& B : out.blocks) {
-    HCsr Pi, Pit;
-    if (B.grade == 0)
+    if (B.grade == 0) {
+      HCsr Pi, Pit;
       slot_identity(n0, mslots, B.vec_slot, Pi, Pit);
-    else
-      vector_nodal(m, B.grade, bc, kUnit, mslots, B.vec_slot, Pi, Pit);
-    FQ_TRY(upload_scalable(ctx, Pi, B.Pi));
-    FQ_TRY(upload_scalable(ctx, Pit, B.Pit));
+      FQ_TRY(upload_scalable(ctx, Pi, B.Pi));
+      FQ_TRY(upload_scalable(ctx, Pit, B.Pit));
+    } else {
+      FQ_TRY(vector_nodal_device(ctx, m, B.grade, bc, mslots, B.vec_slot, B.Pi, B.Pit));
+    }
     if (B.grade >= 1) {
       const int g = B.grade - 1;
-      HCsr D;
-      coboundary_host(m, g, bc, D);
-      FQ_TRY(upload(ctx, D, B.D));
-      FQ_TRY(upload(ctx, transpose(D), B.Dt));
-      const int64_t nl = D.ncols;
+      FQ_TRY(coboundary_device(ctx, m, g, bc, B.D));
+      FQ_TRY(device_transpose(ctx, B.D, nullptr, B.D.ncols, 0, 0, 1, B.Dt, nullptr));
+      const int64_t nl = B.D.ncols;
       FQ_TRY(B.t.alloc(ctx, std::max<int64_t>(nl, 1) * 8));
       FQ_TRY(B.t2.alloc(ctx, std::max<int64_t>(nl, 1) * 8));
-      HCsr PiL, PiLt;
-      if (g == 0)
+      if (g == 0) {
+        HCsr PiL, PiLt;
         slot_identity(n0, mslots, B.grad_slot, PiL, PiLt);
-      else
-        vector_nodal(m, g, bc, kUnit, mslots, B.grad_slot, PiL, PiLt);
-      FQ_TRY(upload_scalable(ctx, PiL, B.PiL));
-      FQ_TRY(upload_scalable(ctx, PiLt, B.PiLt));
+        FQ_TRY(upload_scalable(ctx, PiL, B.PiL));
+        FQ_TRY(upload_scalable(ctx, PiLt, B.PiLt));
+      } else {
+        FQ_TRY(vector_nodal_device(ctx, m, g, bc, mslots, B.grad_slot, B.PiL, B.PiLt));
+      }
       // a gradient smoother of a grade that is neither a block nor the nodal one
       bool have = g == 0;
       for (int o : grades) have = have || o == g;

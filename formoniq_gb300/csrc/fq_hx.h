@@ -132,6 +132,18 @@ bool hx_matches(const HxPrecond& pc, const fq_mesh* m, int bc, const std::vector
 // products, coarse inverse, smoothers, frame scaling), keeping the structure.
 fq_status hx_refresh(fq_ctx* ctx, fq_mesh* m, const double* diag_blocks, HxPrecond& pc);
 
+// ---- device builders of the set-up maps (fq_hx_setup.cu) ----
+// The device skeleton of grade k ([N_k][k+1]), uploaded on first use.
+fq_status device_skeleton(fq_ctx* ctx, fq_mesh* m, int k, const int32_t** out);
+// The coboundary D_k (rows (k+1)-simplices, columns k-simplices; relative: interior ones).
+fq_status coboundary_device(fq_ctx* ctx, fq_mesh* m, int k, int bc, DCsr& D);
+// The vector-nodal map Pi_j (columns node * mslots + slot + I) and its transpose
+// with rows (node, I), both scalable (lattice values in own_base, axis sets in own_mask).
+fq_status vector_nodal_device(fq_ctx* ctx, fq_mesh* m, int j, int bc, int mslots, int slot, DCsr& Pi, DCsr& Pit);
+// A^T (mslots == 0), stable; with mask, the per-entry masks follow the entries.
+fq_status device_transpose(fq_ctx* ctx, const DCsr& a, const uint8_t* mask, int64_t nt_rows, int mslots, int slot,
+                           int ncomp, DCsr& out, DevBuf* out_mask);
+
 // ---- device parts (fq_mg.cu) ----
 fq_status galerkin_product(fq_ctx* ctx, const DCsr& A, const DCsr& P, DCsr& out);
 fq_status device_diag_recip(fq_ctx* ctx, const DCsr& A, double omega, DevBuf& out);
