@@ -40,9 +40,61 @@ struct ScatterBatchEntry {
   double* values;
 };
 
+// Symmetric plans: the upper slots of each mesh (index, mirror) and their
+// contributions, in a batch index space padded per mesh to a multiple of 32.
+struct ScatterSymEntry {
+  int64_t begin, nup;
+  const int2* pair;
+  const int32_t* up_ptr;
+  const int32_t* perm;
+  const df64* elem;
+  double* values;
+};
+
 namespace {
 
 __device__ __forceinline__ bool nz_bits(float v) { return (__float_as_int(v) << 1) != 0; }
+
+// tps = -1: one thread per upper slot of every mesh, the value written to the
+// slot and its mirror; per slot the summation of the single-mesh scatter.
+__global__ void __launch_bounds__(256) scatter_batch_sym_kernel(const ScatterSymEntry* __restrict__ tab, int ntab,
+                                                                int64_t total, int* status) {
+  for (int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < total;
+       g += int64_t(gridDim.x) * blockDim.x) {
+    int lo = 0, hi = ntab - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tab[mid].begin <= g)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const ScatterSymEntry& e = tab[lo];
+    const int64_t u = g - e.begin;
+    if (u >= e.nup) continue;  // padding between meshes
+    const int2 sm = __ldg(e.pair + u);
+    const int b = __ldg(e.up_ptr + u), en = __ldg(e.up_ptr + u + 1);
+    df64 acc(0.f, 0.f);
+    bool nz = false;
+    for (int t = b; t < en; ++t) {
+      const df64 v = e.elem[__ldg(e.perm + t)];
+      acc += v;
+      nz |= nz_bits(v.hi) || nz_bits(v.lo);
+    }
+    const double out = acc.to_double();
+    e.values[sm.x] = out;
+    int nzero = nz ? 0 : 1;
+    if (sm.y != sm.x) {
+      if (sm.y >= 0) {
+        e.values[sm.y] = out;
+        nzero += nz ? 0 : 1;
+      } else {
+        atomicOr(status, 4);
+      }
+    }
+    if (nzero) atomicAdd(status + 1, nzero);
+  }
+}
 
 // tps lanes per slot (tps divides 32), contributions strided over the lanes and
 // combined in a fixed shuffle order.
@@ -165,6 +217,14 @@ __global__ void __launch_bounds__(256) scatter_batch_warp_kernel(const ScatterBa
   }
 }
 
+void launch_scatter_batch_sym(const ScatterSymEntry* tab, int ntab, int64_t total, int grid, int* status,
+                              cudaStream_t st) {
+  if (total <= 0) return;
+  const int64_t need = (total + 255) / 256;
+  const unsigned blocks = unsigned(grid > 0 ? std::min<int64_t>(grid, need) : need);
+  scatter_batch_sym_kernel<<<blocks, 256, 0, st>>>(tab, ntab, total, status);
+}
+
 void launch_scatter_batch(const ScatterBatchEntry* tab, int ntab, int64_t total, int tps, int grid, int* zc,
                           cudaStream_t st) {
   if (total <= 0) return;
@@ -214,10 +274,11 @@ struct fq_batch {
     int grid = 0;  // tuned CTAs (0 = one thread per cell)
   };
   std::vector<Class> classes;
-  DevBuf elem, values, stable, flags;
+  DevBuf elem, values, stable, flags, symtable;
   int64_t total_cells = 0, total_slots = 0, max_slots = 0;  // total_slots: padded batch index space
   int64_t real_slots = 0;
-  int tps = 1, sgrid = 0;  // tps 0: warp-staged scatter
+  int64_t total_up = 0;  // padded upper-slot index space (0: some plan is not symmetric)
+  int tps = 1, sgrid = 0;  // tps 0: warp-staged scatter, -1: symmetric
   cudaGraphExec_t graph = nullptr;
   ~fq_batch() {
     if (graph) cudaGraphExecDestroy(graph);
@@ -246,8 +307,12 @@ fq_status enqueue_batch(fq_batch* B) {
     if (launch_element(c.dim, c.grade, B->kind, FQ_FP64, a, st) != 0)
       return set_error(ctx, FQ_UNSUPPORTED, "no element program for this dimension/grade");
   }
-  launch_scatter_batch(B->stable.as<ScatterBatchEntry>(), int(B->members.size()), B->total_slots, B->tps, B->sgrid,
-                       ctx->status.as<int>() + 1, st);
+  if (B->tps == -1)
+    launch_scatter_batch_sym(B->symtable.as<ScatterSymEntry>(), int(B->members.size()), B->total_up, B->sgrid,
+                             ctx->status.as<int>(), st);
+  else
+    launch_scatter_batch(B->stable.as<ScatterBatchEntry>(), int(B->members.size()), B->total_slots, B->tps,
+                         B->sgrid, ctx->status.as<int>() + 1, st);
   return FQ_OK;
 }
 
@@ -390,6 +455,27 @@ fq_status fq_batch_create(fq_ctx* ctx, int nmeshes, fq_mesh* const* meshes, cons
   FQ_TRY(B->stable.alloc(ctx, st.size() * sizeof(ScatterBatchEntry)));
   FQ_CUDA(ctx, cudaMemcpyAsync(B->stable.p, st.data(), st.size() * sizeof(ScatterBatchEntry), cudaMemcpyHostToDevice,
                                ctx->stream));
+  // the symmetric table, when every member's plan has one
+  bool all_sym = true;
+  for (auto& mb : B->members) all_sym = all_sym && mb.plan->nup > 0;
+  if (all_sym && !B->members.empty()) {
+    std::vector<ScatterSymEntry> sy;
+    for (auto& mb : B->members) {
+      ScatterSymEntry e;
+      e.begin = B->total_up;
+      e.nup = mb.plan->nup;
+      e.pair = mb.plan->up_pair.as<int2>();
+      e.up_ptr = mb.plan->up_ptr.as<int32_t>();
+      e.perm = mb.plan->up_perm.as<int32_t>();
+      e.elem = B->elem.as<df64>() + mb.elem_off;
+      e.values = B->values.as<double>() + mb.val_off;
+      sy.push_back(e);
+      B->total_up += (e.nup + 31) & ~int64_t(31);
+    }
+    FQ_TRY(B->symtable.alloc(ctx, sy.size() * sizeof(ScatterSymEntry)));
+    FQ_CUDA(ctx, cudaMemcpyAsync(B->symtable.p, sy.data(), sy.size() * sizeof(ScatterSymEntry),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+  }
   FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   FQ_TRY(capture(B.get()));
   *out = B.release();
@@ -420,8 +506,9 @@ fq_status fq_batch_tune(fq_batch* B, int reps) {
   // scatter stage: threads per slot and CTAs per SM
   float best = 1e30f;
   int btps = 1, bgrid = 0;
-  for (int tps : {0, 1, 2, 4})
+  for (int tps : {-1, 0, 1, 2, 4})
     for (int ps : per_sm) {
+      if (tps == -1 && B->total_up == 0) continue;
       B->tps = tps;
       B->sgrid = ps * dev_sms;
       const float t = time_once(B, reps);
@@ -439,7 +526,9 @@ fq_status fq_batch_tune(fq_batch* B, int reps) {
 }
 
 fq_status fq_batch_set_launch(fq_batch* B, int element_grid, int scatter_tps, int scatter_grid) {
-  if (!B || (scatter_tps != 0 && scatter_tps != 1 && scatter_tps != 2 && scatter_tps != 4)) return FQ_INVALID_ARG;
+  if (!B || (scatter_tps != -1 && scatter_tps != 0 && scatter_tps != 1 && scatter_tps != 2 && scatter_tps != 4))
+    return FQ_INVALID_ARG;
+  if (scatter_tps == -1 && B->total_up == 0) return set_error(B->ctx, FQ_UNSUPPORTED, "no symmetric plans in batch");
   for (auto& c : B->classes) c.grid = element_grid;
   B->tps = scatter_tps;
   B->sgrid = scatter_grid;

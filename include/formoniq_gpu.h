@@ -373,11 +373,12 @@ typedef enum fq_batch_form {
 fq_status fq_batch_create(fq_ctx* ctx, int nmeshes, fq_mesh* const* meshes, const int* grades, int form,
                           fq_batch** out);
 /* Tuner: times each candidate launch shape `reps` times on this batch (element
- * CTAs per SM per class; scatter warp-staged or 1/2/4 threads per slot, and
- * CTAs per SM) and keeps the fastest. */
+ * CTAs per SM per class; scatter symmetric, warp-staged or 1/2/4 threads per
+ * slot, and CTAs per SM) and keeps the fastest. */
 fq_status fq_batch_tune(fq_batch* batch, int reps);
 /* Fixed launch shape: element grid (CTAs, 0 = one thread per cell), scatter
- * threads per slot (0 = warp-staged, 1, 2 or 4) and grid. */
+ * threads per slot (-1 = one per upper slot of the symmetric plans, 0 =
+ * warp-staged, 1, 2 or 4) and grid. */
 fq_status fq_batch_set_launch(fq_batch* batch, int element_grid, int scatter_tps, int scatter_grid);
 /* One assembly of the whole batch (one graph launch). check != 0 waits and
  * checks the status words (degenerate cells; a slot that summed exact zeros
