@@ -177,6 +177,18 @@ FQ_HDI df64 operator+(df64 a, df64 b) {
   return fast_two_sum(s.hi, s.lo);
 }
 
+// Dekker's float-float add (T. J. Dekker, "A floating-point technique for
+// extending the available precision", 1971; the "sloppy" add of the QD
+// library): one TwoSum of the leading parts, the trailing parts added in FP32,
+// one renormalisation. 11 FP32 operations against the accurate add's 20; its
+// error is bounded by about 2^-44 (|a| + |b|), relative to the operands rather
+// than to the sum.
+FQ_HDI df64 dd_add_dekker(df64 a, df64 b) {
+  const df64 s = two_sum(a.hi, b.hi);
+  const float e = f_add(s.lo, f_add(a.lo, b.lo));
+  return fast_two_sum(s.hi, e);
+}
+
 FQ_HDI df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
 FQ_HDI df64 operator-(df64 a, df64 b) { return a + (-b); }
 

@@ -257,6 +257,7 @@ FQ_HDI T sym_inverse_t(const T (&a)[N > 0 ? N : 1][N > 0 ? N : 1], T (&inv)[N > 
 template <int N, typename T>
 struct Bary {
   T b[N + 1][N + 1];
+  T rdet;  // 1 / det G
 };
 
 // B from an inverse metric already in T (the float-float path).
@@ -299,6 +300,25 @@ FQ_HDI void bary_gramian(const double (&ginv)[N > 0 ? N : 1][N > 0 ? N : 1], Bar
   bary_gramian_t<N, T>(gt, B);
 }
 
+// Sums and differences inside the element programs (2 x 2 minors of B, the
+// pullback and sandwich sums). In float-float they use Dekker's add: its error
+// is bounded by the magnitudes that formed each entry, and the element
+// tolerance is relative to the element matrix, so the accurate add's second
+// TwoSum buys nothing here. The metric, its inverse and determinant
+// (cell_bary) and the 3 x 3 and 4 x 4 minors of B, where cancellation is the
+// rule, keep the accurate add. In FP32 and IEEE FP64 these are the plain
+// operations.
+template <typename T>
+FQ_HDI T eadd(T a, T b) {
+  return a + b;
+}
+template <typename T>
+FQ_HDI T esub(T a, T b) {
+  return a - b;
+}
+FQ_HDI df64 eadd(df64 a, df64 b) { return dd_add_dekker(a, b); }
+FQ_HDI df64 esub(df64 a, df64 b) { return dd_add_dekker(a, -b); }
+
 // The members of a compile-time vertex mask, increasing.
 template <unsigned M, int J>
 struct MaskList {
@@ -321,10 +341,11 @@ FQ_HDI T minor_det(const Bary<N, T>& B) {
     if constexpr (J == 1) {
       return B.b[rl.v[0]][cl.v[0]];
     } else if constexpr (J == 2) {
-      return B.b[rl.v[0]][cl.v[0]] * B.b[rl.v[1]][cl.v[1]] - B.b[rl.v[0]][cl.v[1]] * B.b[rl.v[1]][cl.v[0]];
+      return esub(B.b[rl.v[0]][cl.v[0]] * B.b[rl.v[1]][cl.v[1]], B.b[rl.v[0]][cl.v[1]] * B.b[rl.v[1]][cl.v[0]]);
     } else if constexpr (J == 3) {
       constexpr int r0 = rl.v[0], r1 = rl.v[1], r2 = rl.v[2];
       constexpr int c0 = cl.v[0], c1 = cl.v[1], c2 = cl.v[2];
+      // 3 x 3 minors of the rank-n B cancel strongly on distorted cells: accurate adds
       const T m0 = B.b[r1][c1] * B.b[r2][c2] - B.b[r1][c2] * B.b[r2][c1];
       const T m1 = B.b[r1][c0] * B.b[r2][c2] - B.b[r1][c2] * B.b[r2][c0];
       const T m2 = B.b[r1][c0] * B.b[r2][c1] - B.b[r1][c1] * B.b[r2][c0];
@@ -365,10 +386,35 @@ struct Blades {
   }
 };
 
+// Top compound in closed form: with L the (n+1) x n matrix of the barycentric
+// differentials, Cauchy-Binet gives Lambda^n B = (Lambda^n L)(Lambda^n G^{-1})
+// (Lambda^n L)^T, where Lambda^n G^{-1} = 1 / det G and the n x n minor of L
+// without row v is (-1)^v. So H_n[I][K] = (-1)^(o_I + o_K) / det G, o_I the
+// vertex the n-subset I omits -- exact where the n x n minors of the rank-n B
+// cancel to roundoff.
+template <int N, int I, int K, typename T>
+FQ_HDI T top_blade(const Bary<N, T>& B) {
+  constexpr unsigned full = (1u << (N + 1)) - 1u;
+  constexpr unsigned oi = full & ~Tab<N + 1, N>::v.mask[I];
+  constexpr unsigned ok = full & ~Tab<N + 1, N>::v.mask[K];
+  constexpr int parity = (cpopcount(oi - 1u) + cpopcount(ok - 1u)) % 2;  // o_I + o_K, from the omitted bits
+  if constexpr (parity)
+    return -B.rdet;
+  else
+    return B.rdet;
+}
+
 template <int N, int J, typename T>
 FQ_HDI void compute_blades(const Bary<N, T>& B, Blades<N, J, T>& H) {
   constexpr int L = Blades<N, J, T>::L;
-  if constexpr (J > N) {
+  if constexpr (J == N && N >= 1) {
+    static_for<L>([&](auto I) {
+      static_for<L>([&](auto K) {
+        constexpr int i = decltype(I)::value, k = decltype(K)::value;
+        if constexpr (i <= k) H.h[packed_index(i, k, L)] = top_blade<N, i, k, T>(B);
+      });
+    });
+  } else if constexpr (J > N) {
     // Lambda^{n+1} B = det B = 0: the barycentric differentials sum to zero.
 #pragma unroll
     for (int i = 0; i < Blades<N, J, T>::P; ++i) H.h[i] = T(0);
@@ -390,6 +436,8 @@ template <int N, int J, int I, int K, typename T>
 FQ_HDI T blade_entry(const Bary<N, T>& B) {
   if constexpr (J > N) {
     return T(0);
+  } else if constexpr (J == N && N >= 1) {
+    return top_blade<N, I, K, T>(B);
   } else {
     constexpr unsigned rm = Tab<N + 1, J>::v.mask[I];
     constexpr unsigned cm = Tab<N + 1, J>::v.mask[K];
@@ -420,13 +468,13 @@ FQ_HDI T mass_sum(const Blades<N, KG, T>& H) {
       constexpr int coef = sgn * w;
       const T h = H.template at<ra, rb>();
       if constexpr (coef == 1)
-        acc += h;
+        acc = eadd(acc, h);
       else if constexpr (coef == -1)
-        acc -= h;
+        acc = esub(acc, h);
       else if constexpr (coef == 2)
-        acc += twice(h);
+        acc = eadd(acc, twice(h));
       else
-        acc -= twice(h);
+        acc = esub(acc, twice(h));
     });
   });
   return acc;
@@ -444,9 +492,9 @@ FQ_HDI T dif_test_sum(const Blades<N, KG, T>& H) {
     constexpr int rb = mask_rank(mt & ~(1u << vt));
     const T h = H.template at<rb, R>();
     if constexpr (q % 2)
-      acc -= h;
+      acc = esub(acc, h);
     else
-      acc += h;
+      acc = eadd(acc, h);
   });
   return acc;
 }

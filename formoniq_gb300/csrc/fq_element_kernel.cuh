@@ -43,6 +43,7 @@ FQ_HD T cell_bary(const double* s, Bary<N, T>& B, bool& bad) {
       regge_metric_t<N, df64>(sd, g);
       const df64 det = sym_inverse_t<N, df64>(g, gi);
       bary_gramian_t<N, df64>(gi, B);
+      B.rdet = recip(det);
       bad = !(det.hi != 0.f) || !isfinite(det.hi);
       // vol = sqrt|det| / n!  (regge/src/lib.rs:26-28)
       return dd_sqrt(dd_abs(det)) * df64(1.0 / double(cfact(N)));
@@ -53,6 +54,7 @@ FQ_HD T cell_bary(const double* s, Bary<N, T>& B, bool& bad) {
   regge_metric<N>(s, g);
   const double det = sym_inverse<N>(g, gi);
   bary_gramian<N, T>(gi, B);
+  B.rdet = T(1.0 / det);
   bad = !(det != 0.0) || !isfinite(det);
   return T(sqrt(fabs(det)) * (1.0 / double(cfact(N))));
 }

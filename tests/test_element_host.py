@@ -195,3 +195,23 @@ def test_float_float_conversions_match_rounded_conversions(host_lib):
     got = sh.astype(np.float64) + sl.astype(np.float64)
     want = np.sqrt(ph.astype(np.float64) + pl.astype(np.float64))
     assert np.max(np.abs(got - want) / want) < 2e-14
+
+
+@pytest.mark.parametrize("dim", [2, 3, 4])
+def test_top_grade_mass_is_the_inverse_volume(oracle, host_lib, dim):
+    """The Whitney n-form of an n-cell is 1/vol times its volume form, so its
+    mass is exactly 1/vol. The top compound Lambda^n B is formed in closed form
+    (+-1/det G), so the float-float program meets this to 1e-13 even on
+    strongly distorted cells (0.2h jitter), where the n x n minors of the rank-n
+    B -- and the reference's determinant of G^{-1} -- cancel to about 1e-11."""
+    cx, coords = oracle.cartesian_unit(dim, 2)
+    worst = 0.0
+    for seed in range(3):
+        c2 = oracle.jitter_coords(coords, 2, seed, 0.2, side=np.ones(dim))
+        lengths = cx.edge_lengths_sq(c2)
+        edges = cx.cell_faces(1)
+        _, _, _, vol, _ = cx.cell_metrics(lengths)
+        for c in range(cx.ncells()):
+            v, _ = run(host_lib, DF64, dim, dim, 0, lengths[edges[c]])
+            worst = max(worst, abs(v[0] * vol[c] - 1.0))
+    assert worst < 1e-13, worst
