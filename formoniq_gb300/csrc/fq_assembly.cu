@@ -556,7 +556,7 @@ __global__ void __launch_bounds__(256) scatter_kernel(const int32_t* __restrict_
       }
   }
   values[s] = store_value(acc);
-  zflag[s] = nz ? 0 : 1;
+  if (zflag) zflag[s] = nz ? 0 : 1;
   if (!nz) atomicAdd(zero_count, 1);
 }
 
@@ -593,12 +593,12 @@ __global__ void __launch_bounds__(256) scatter_sym_kernel(const int2* __restrict
   const V out = store_value(acc);
   const uint8_t z = nz ? 0 : 1;
   values[sm.x] = out;
-  zflag[sm.x] = z;
+  if (zflag) zflag[sm.x] = z;
   int nzero = nz ? 0 : 1;
   if (sm.y != sm.x) {
     if (sm.y >= 0) {
       values[sm.y] = out;
-      zflag[sm.y] = z;
+      if (zflag) zflag[sm.y] = z;
       nzero += nz ? 0 : 1;
     } else {
       atomicOr(status, 4);
@@ -818,8 +818,10 @@ fq_status get_plan(fq_ctx* ctx, fq_mesh* m, int kind, int grade, int row_bc, int
 
 // Queues the element pass and the scatter of m on the context's stream: status
 // bits go to ctx->status[0], the count of all-zero slots to ctx->status[1]. With
-// `ev` (four events) the two kernels are bracketed for profiling.
-static fq_status assemble_launch(fq_ctx* ctx, fq_matrix* m, cudaEvent_t* ev) {
+// `ev` (four events) the two kernels are bracketed for profiling. Per-slot
+// zero flags are written only `with_flags` (the rare re-assembly that a
+// nonzero count triggers, assemble_flagged).
+static fq_status assemble_launch(fq_ctx* ctx, fq_matrix* m, cudaEvent_t* ev, bool with_flags = false) {
   fq_mesh* mesh = m->mesh;
   Plan& p = *m->plan;
   const int mode = m->precision;
@@ -833,7 +835,8 @@ static fq_status assemble_launch(fq_ctx* ctx, fq_matrix* m, cudaEvent_t* ev) {
   if (p.nslots > 0 || p.ndiag_trip > 0) FQ_TRY(element_pass(ctx, mesh, m->kind, m->grade, mode, m->param, mesh->elem, p.nent));
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[1], ctx->stream));
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[2], ctx->stream));
-  launch_scatter(p, mesh->elem.p, m->full_values.p, m->zero_flags.as<uint8_t>(), zc, mode, ctx->stream);
+  launch_scatter(p, mesh->elem.p, m->full_values.p, with_flags ? m->zero_flags.as<uint8_t>() : nullptr, zc, mode,
+                 ctx->stream);
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[3], ctx->stream));
   if (p.nslots > 0) ctx->launches++;
   return FQ_OK;
@@ -871,6 +874,19 @@ static fq_status check_status_words(fq_ctx* ctx) {
   return FQ_OK;
 }
 
+// The rare path: some slot summed exact zeros only. m is assembled again with
+// per-slot flags and the count of its all-zero slots is returned.
+static fq_status assemble_flagged(fq_ctx* ctx, fq_matrix* m, int64_t* nzero) {
+  FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
+  FQ_TRY(assemble_launch(ctx, m, nullptr, true));
+  FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  FQ_TRY(check_status_words(ctx));
+  *nzero = ctx->host_status[1];
+  return FQ_OK;
+}
+
 // Element pass + scatter (+ compaction when needed) into m.
 fq_status assemble_into(fq_ctx* ctx, fq_matrix* m) {
   FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
@@ -881,20 +897,15 @@ fq_status assemble_into(fq_ctx* ctx, fq_matrix* m) {
   FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (ev) FQ_TRY(accumulate_profile(ctx, ev));
   FQ_TRY(check_status_words(ctx));
-  return assemble_adopt(ctx, m, ctx->host_status[1]);
+  int64_t nzero = 0;
+  if (ctx->host_status[1] > 0) FQ_TRY(assemble_flagged(ctx, m, &nzero));
+  return assemble_adopt(ctx, m, nzero);
 }
 
-__global__ void count_flags_kernel(const uint8_t* __restrict__ f, int64_t n, int* count) {
-  int c = 0;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
-    c += f[i];
-  c = __reduce_add_sync(0xffffffffu, c);
-  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
-}
 
 // Several matrices queued back to back with one read of the status words. The
-// element buffer of a mesh is reused in stream order; the rare matrices with
-// all-zero slots are found by counting their flags afterwards.
+// element buffer of a mesh is reused in stream order; when some slot summed
+// exact zeros only (rare), every matrix is assembled again with flags.
 fq_status assemble_many(fq_ctx* ctx, fq_matrix* const* mats, int count) {
   const bool prof = ctx->profiling && ctx->ev[0];
   if (prof) {
@@ -919,16 +930,7 @@ fq_status assemble_many(fq_ctx* ctx, fq_matrix* const* mats, int count) {
     fq_matrix* m = mats[i];
     if (!m->plan) continue;
     int64_t nzero = 0;
-    if (any_zero && m->plan->nslots > 0) {
-      int* cnt = ctx->status.as<int>() + 2;
-      FQ_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int), ctx->stream));
-      count_flags_kernel<<<grid_for(m->plan->nslots, 256), 256, 0, ctx->stream>>>(m->zero_flags.as<uint8_t>(),
-                                                                               m->plan->nslots, cnt);
-      ctx->launches++;
-      FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status + 2, cnt, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-      FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-      nzero = ctx->host_status[2];
-    }
+    if (any_zero && m->plan->nslots > 0) FQ_TRY(assemble_flagged(ctx, m, &nzero));
     FQ_TRY(assemble_adopt(ctx, m, nzero));
   }
   return FQ_OK;
@@ -979,16 +981,7 @@ fq_status assemble_host_many(fq_ctx* ctx, fq_mesh* mesh, const double* lengths, 
     fq_matrix* m = mats[i];
     if (!m->plan) continue;
     int64_t nzero = 0;
-    if (any_zero && m->plan->nslots > 0) {
-      int* cnt = ctx->status.as<int>() + 2;
-      FQ_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int), st));
-      count_flags_kernel<<<grid_for(m->plan->nslots, 256), 256, 0, st>>>(m->zero_flags.as<uint8_t>(),
-                                                                       m->plan->nslots, cnt);
-      ctx->launches++;
-      FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status + 2, cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
-      FQ_CUDA(ctx, cudaStreamSynchronize(st));
-      nzero = ctx->host_status[2];
-    }
+    if (any_zero && m->plan->nslots > 0) FQ_TRY(assemble_flagged(ctx, m, &nzero));
     FQ_TRY(assemble_adopt(ctx, m, nzero));
     if ((!streamed[i] || nzero > 0) && m->nnz > 0) {
       const size_t w = m->precision == FQ_FP32 ? 4 : 8;

@@ -24,7 +24,8 @@
 namespace fq {
 
 // 32 MiB: the element buffer of up to 4 Mi FP64 entries (e.g. M_1 of a
-// 199,728-cell 3D mesh, 21 entries per cell) plus one flag byte per CSR slot.
+// 199,728-cell 3D mesh, 21 entries per cell); the size rule also keeps one
+// byte per CSR slot of headroom.
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -94,7 +95,7 @@ extern "C" fq_status fq_reassemble_noalloc(fq_ctx* ctx, fq_mesh* mesh, const fq_
       return set_error(ctx, FQ_UNSUPPORTED, "no element program for this dimension/grade");
     ctx->launches++;
     FQ_CUDA(ctx, cudaGetLastError());
-    launch_scatter(p, base, values_out, base + elem_bytes, ctx->status.as<int>(), mode, st);
+    launch_scatter(p, base, values_out, nullptr, ctx->status.as<int>(), mode, st);
     ctx->launches++;
     FQ_CUDA(ctx, cudaGetLastError());
   }
