@@ -18,6 +18,7 @@ needs a CUDA device.
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import weakref
 from dataclasses import dataclass
@@ -31,6 +32,7 @@ __all__ = [
     "Report", "solve_source", "solve_dirac_source", "dirac_system", "minres", "cg", "hx_cg", "hx_apply", "lib_path",
     "load", "exported_symbols", "FQ_PC_AUTO", "FQ_PC_JACOBI", "FQ_PC_HX", "Server", "FQ_REQ_HODGE", "FQ_REQ_DIRAC",
     "Batch", "FQ_BATCH_MASS", "FQ_BATCH_HDIF", "ElementOperator", "derham_map", "Leapfrog",
+    "source_nodes", "source_form",
 ]
 
 FQ_MASS, FQ_DIF_TRIAL, FQ_DIF_TEST, FQ_DIF_BOTH = 0, 1, 2, 3
@@ -167,6 +169,10 @@ _SIGNATURES = {
     "fq_elemop_cg": (ctypes.c_int, [_P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
     "fq_elemop_destroy": (None, [_P]),
     "fq_derham_npoints": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "fq_source_npoints": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "fq_source_nodes": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, _P]),
+    "fq_source_assemble": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int, _P,
+                                          _P]),
     "fq_leapfrog_create": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.POINTER(_P)]),
     "fq_leapfrog_info": (ctypes.c_int, [_P, _I64P, _I64P, _I64P]),
     "fq_leapfrog_step": (ctypes.c_int, [_P, _P, ctypes.c_int64]),
@@ -257,6 +263,7 @@ class Context:
             raise FqError(s, "fq_ctx_create")
         self.h = h
         self.L = L
+        self.device = device
         # native objects made on this context, closed before it (the C ABI needs
         # meshes, matrices and problems destroyed before their context)
         self._children = weakref.WeakSet()
@@ -740,6 +747,64 @@ def derham_map(mesh: Mesh, coords, grade: int, field, degree: int = 3):
     torch.cuda.synchronize()
     ctx.check(ctx.L.fq_derham_reduce(ctx.h, mesh.h, _P(coords.data_ptr()), adim, grade, degree,
                                      _P(vals.data_ptr()), _P(out.data_ptr())), "fq_derham_reduce")
+    return out
+
+
+def source_nodes(mesh: Mesh, degree: int = 1, coords=None):
+    """The quadrature nodes of the source load (CellQuadrature, formoniq/src/operators.rs:222-261).
+
+    coords None: the barycentric nodes [nq, n+1] shared by every cell; coords a
+    torch CUDA tensor [N_0, adim]: the ambient nodes [ncells, nq, adim]."""
+    import torch
+
+    ctx = mesh.ctx
+    n = mesh.dim
+    nq = ctx.L.fq_source_npoints(n, degree)
+    if nq <= 0:
+        raise FqError(1, f"no quadrature rule of degree {degree} on the {n}-simplex")
+    dev = torch.device("cuda", ctx.device)
+    if coords is None:
+        out = torch.empty((nq, n + 1), dtype=torch.float64, device=dev)
+        cptr, adim = None, 0
+    else:
+        coords = coords.to(torch.float64).contiguous()
+        adim = coords.shape[1]
+        out = torch.empty((mesh.ncells(), nq, adim), dtype=torch.float64, device=coords.device)
+        cptr = _P(coords.data_ptr())
+    torch.cuda.synchronize()
+    ctx.check(ctx.L.fq_source_nodes(ctx.h, mesh.h, cptr, adim, degree, _P(out.data_ptr())), "fq_source_nodes")
+    return out
+
+
+def source_form(mesh: Mesh, grade: int, values, degree: int = 1, coords=None, bc: int = FQ_ABSOLUTE):
+    """SourceForm::new(source, qr).assemble(topology, lengths) on the device
+    (formoniq/src/operators.rs:598-635, galerkin.rs:279-312).
+
+    values: a torch CUDA tensor [ncells, nq, ncomp], or a callable taking
+    ``source_nodes(mesh, degree, coords)`` and returning it. With coords None
+    the components are the section's in each cell's reference frame (ncomp =
+    C(n, grade), on dxi^J with xi_j = lambda_{j+1}); with coords [N_0, adim]
+    they are a flat ambient form's on dx^A (ncomp = C(adim, grade)), pulled back
+    cell by cell. Returns the Galerkin vector [ndofs(grade, bc)] as a torch CUDA
+    tensor (FQ_RELATIVE: the interior entries)."""
+    import torch
+
+    ctx = mesh.ctx
+    if coords is not None:
+        coords = coords.to(torch.float64).contiguous()
+    adim = 0 if coords is None else coords.shape[1]
+    if callable(values):
+        values = values(source_nodes(mesh, degree, coords))
+    values = values.to(torch.float64).contiguous()
+    nq = ctx.L.fq_source_npoints(mesh.dim, degree)
+    ncomp = math.comb(adim if coords is not None else mesh.dim, grade)
+    if values.numel() != mesh.ncells() * nq * ncomp:
+        raise FqError(1, f"values must hold [ncells={mesh.ncells()}, nq={nq}, ncomp={ncomp}] entries")
+    out = torch.empty(mesh.ndofs(grade, bc), dtype=torch.float64, device=values.device)
+    torch.cuda.synchronize()
+    ctx.check(ctx.L.fq_source_assemble(ctx.h, mesh.h, grade, bc, degree,
+                                       None if coords is None else _P(coords.data_ptr()), adim,
+                                       _P(values.data_ptr()), _P(out.data_ptr())), "fq_source_assemble")
     return out
 
 

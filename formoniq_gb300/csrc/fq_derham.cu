@@ -159,19 +159,6 @@ int grid_for_n(int64_t n) { return int(std::max<int64_t>(1, std::min<int64_t>((n
 
 }  // namespace
 
-// The simplices of grade k on the device, [N_k][k+1] (uploaded once per mesh).
-static fq_status device_skeleton(fq_ctx* ctx, fq_mesh* m, int k, const int32_t** out) {
-  if (!m->skel_dev[k].p) {
-    const size_t bytes = std::max<size_t>(m->skel[k].size(), 1) * 4;
-    FQ_TRY(m->skel_dev[k].alloc(ctx, bytes));
-    if (!m->skel[k].empty())
-      FQ_CUDA(ctx, cudaMemcpyAsync(m->skel_dev[k].p, m->skel[k].data(), m->skel[k].size() * 4,
-                                   cudaMemcpyHostToDevice, ctx->stream));
-  }
-  *out = m->skel_dev[k].as<int32_t>();
-  return FQ_OK;
-}
-
 static fq_status derham_setup(fq_ctx* ctx, fq_mesh* m, int adim, int grade, int degree, DerhamArgs& a,
                               DevBuf& rule) {
   if (grade < 0 || grade > m->dim) return set_error(ctx, FQ_INVALID_ARG, "grade out of range");

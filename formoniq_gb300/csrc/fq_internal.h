@@ -107,6 +107,8 @@ struct fq_mesh {
   std::map<std::tuple<int, int, int, int>, std::unique_ptr<fq::Plan>> plans;
   // element buffer reused across assemblies
   fq::DevBuf elem;
+  // face incidences [bc][grade] of the vector assemblies, built on first use
+  fq::DevBuf inc_ptr[2][5], inc_src[2][5];
 };
 
 struct fq_matrix {
@@ -150,6 +152,10 @@ struct fq_ctx {
 namespace fq {
 
 fq_status set_error(fq_ctx* ctx, fq_status s, const std::string& msg);
+
+// The simplices of grade k on the device, [N_k][k+1] vertex ids (uploaded once
+// per mesh, kept by the mesh).
+fq_status device_skeleton(fq_ctx* ctx, fq_mesh* m, int k, const int32_t** out);
 fq_status cuda_check(fq_ctx* ctx, cudaError_t e, const char* what);
 #define FQ_CUDA(ctx, call)                                        \
   do {                                                            \

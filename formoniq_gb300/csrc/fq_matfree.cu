@@ -28,6 +28,11 @@ namespace fq {
 
 int launch_elemop_cells_dim(int n, int K, int kind, const ElemopArgs& a, cudaStream_t st);
 
+int64_t ndofs_of(const fq_mesh* m, int grade, int bc) {
+  if (grade < 0 || grade > m->dim) return 0;
+  return bc == FQ_RELATIVE ? m->ninterior[grade] : m->nsimp[grade];
+}
+
 namespace {
 
 __global__ void elemop_keys_kernel(const int32_t* __restrict__ row_faces, const int32_t* __restrict__ row_map,
@@ -65,6 +70,46 @@ int grid_of(int64_t n, int threads) {
 
 }  // namespace
 
+void launch_gather_rows(const int32_t* rp, const int32_t* src, const df64* contrib, double* y, int64_t nrows,
+                        const int* done, cudaStream_t st) {
+  if (nrows <= 0) return;
+  elemop_rows_kernel<<<grid_of(nrows, 256), 256, 0, st>>>(rp, src, contrib, y, nrows, done);
+}
+
+fq_status build_face_incidence(fq_ctx* ctx, fq_mesh* m, int grade, int bc, DevBuf& row_ptr, DevBuf& row_src) {
+  cudaStream_t st = ctx->stream;
+  const int64_t nc = m->ncells;
+  const int lr = cbinom(m->dim + 1, grade + 1);
+  const int64_t total = nc * lr;
+  const int64_t nrows = ndofs_of(m, grade, bc);
+  if (total >= (int64_t(1) << 31)) return set_error(ctx, FQ_UNSUPPORTED, "mesh too large for 32-bit slot indices");
+  DevBuf keys, keys2, vals;
+  FQ_TRY(keys.alloc(ctx, std::max<int64_t>(total, 1) * 8));
+  FQ_TRY(keys2.alloc(ctx, std::max<int64_t>(total, 1) * 8));
+  FQ_TRY(vals.alloc(ctx, std::max<int64_t>(total, 1) * 4));
+  FQ_TRY(row_src.alloc(ctx, std::max<int64_t>(total, 1) * 4));
+  FQ_TRY(row_ptr.alloc(ctx, (nrows + 1) * 4));
+  const uint64_t sentinel = uint64_t(std::max<int64_t>(nrows, 1));
+  int end_bit = 1;
+  while (end_bit < 64 && (sentinel >> end_bit)) ++end_bit;
+  elemop_keys_kernel<<<grid_of(total, 256), 256, 0, st>>>(
+      m->cell_faces[grade].as<int32_t>(), bc == FQ_RELATIVE ? m->interior_dev[grade].as<int32_t>() : nullptr, nc, lr,
+      sentinel, keys.as<uint64_t>(), vals.as<int32_t>());
+  ctx->launches++;
+  size_t tmp_bytes = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.as<uint64_t>(), keys2.as<uint64_t>(), vals.as<int32_t>(),
+                                  row_src.as<int32_t>(), int(total), 0, end_bit, st);
+  DevBuf tmp;
+  FQ_TRY(tmp.alloc(ctx, std::max<size_t>(tmp_bytes, 16)));
+  FQ_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.as<uint64_t>(), keys2.as<uint64_t>(),
+                                               vals.as<int32_t>(), row_src.as<int32_t>(), int(total), 0, end_bit, st));
+  launch_lower_bound_rows(keys2.as<uint64_t>(), total, nrows, 1, row_ptr.as<int32_t>(), st);
+  ctx->launches++;
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  FQ_CUDA(ctx, cudaGetLastError());
+  return FQ_OK;
+}
+
 // Both stages on the context's stream; x null = the diagonal.
 static void elemop_launch(const fq_elemop* op, const double* x, double* y, const int* done, cudaStream_t st) {
   fq_mesh* m = op->mesh;
@@ -80,8 +125,8 @@ static void elemop_launch(const fq_elemop* op, const double* x, double* y, const
   a.status = op->ctx->status.as<int>();
   a.grid = 152 * 12;
   launch_elemop_cells_dim(m->dim, op->grade, op->kind, a, st);
-  elemop_rows_kernel<<<grid_of(op->nrows, 256), 256, 0, st>>>(op->row_ptr.as<int32_t>(), op->row_src.as<int32_t>(),
-                                                               op->contrib.as<df64>(), y, op->nrows, done);
+  launch_gather_rows(op->row_ptr.as<int32_t>(), op->row_src.as<int32_t>(), op->contrib.as<df64>(), y, op->nrows,
+                     done, st);
   op->ctx->launches += 2;
 }
 
@@ -95,11 +140,6 @@ static fq_status elemop_status(fq_ctx* ctx) {
   FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (ctx->host_status[0] & 1) return set_error(ctx, FQ_DEGENERATE_CELL, "a cell metric is singular or not finite");
   return FQ_OK;
-}
-
-int64_t ndofs_of(const fq_mesh* m, int grade, int bc) {
-  if (grade < 0 || grade > m->dim) return 0;
-  return bc == FQ_RELATIVE ? m->ninterior[grade] : m->nsimp[grade];
 }
 
 }  // namespace fq
@@ -132,35 +172,8 @@ fq_status fq_elemop_create(fq_ctx* ctx, fq_mesh* m, fq_form form, int grade, fq_
     op->lc = cbinom(n + 1, cg + 1);
     op->nrows = ndofs_of(m, rg, int(bc));
     op->ncols = ndofs_of(m, cg, int(bc));
-    cudaStream_t st = ctx->stream;
-    const int64_t nc = m->ncells, total = nc * op->lr;
-    if (total >= (int64_t(1) << 31)) return set_error(ctx, FQ_UNSUPPORTED, "mesh too large for 32-bit slot indices");
-    DevBuf keys, keys2, vals;
-    FQ_TRY(keys.alloc(ctx, std::max<int64_t>(total, 1) * 8));
-    FQ_TRY(keys2.alloc(ctx, std::max<int64_t>(total, 1) * 8));
-    FQ_TRY(vals.alloc(ctx, std::max<int64_t>(total, 1) * 4));
-    FQ_TRY(op->row_src.alloc(ctx, std::max<int64_t>(total, 1) * 4));
-    FQ_TRY(op->row_ptr.alloc(ctx, (op->nrows + 1) * 4));
-    FQ_TRY(op->contrib.alloc(ctx, std::max<int64_t>(total, 1) * 8));
-    const uint64_t sentinel = uint64_t(std::max<int64_t>(op->nrows, 1));
-    int end_bit = 1;
-    while (end_bit < 64 && (sentinel >> end_bit)) ++end_bit;
-    elemop_keys_kernel<<<grid_of(total, 256), 256, 0, st>>>(
-        m->cell_faces[rg].as<int32_t>(), op->bc == FQ_RELATIVE ? m->interior_dev[rg].as<int32_t>() : nullptr, nc,
-        op->lr, sentinel, keys.as<uint64_t>(), vals.as<int32_t>());
-    ctx->launches++;
-    size_t tmp_bytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.as<uint64_t>(), keys2.as<uint64_t>(),
-                                    vals.as<int32_t>(), op->row_src.as<int32_t>(), int(total), 0, end_bit, st);
-    DevBuf tmp;
-    FQ_TRY(tmp.alloc(ctx, std::max<size_t>(tmp_bytes, 16)));
-    FQ_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.as<uint64_t>(), keys2.as<uint64_t>(),
-                                                 vals.as<int32_t>(), op->row_src.as<int32_t>(), int(total), 0,
-                                                 end_bit, st));
-    launch_lower_bound_rows(keys2.as<uint64_t>(), total, op->nrows, 1, op->row_ptr.as<int32_t>(), st);
-    ctx->launches++;
-    FQ_CUDA(ctx, cudaStreamSynchronize(st));
-    FQ_CUDA(ctx, cudaGetLastError());
+    FQ_TRY(op->contrib.alloc(ctx, std::max<int64_t>(m->ncells * op->lr, 1) * 8));
+    FQ_TRY(build_face_incidence(ctx, m, rg, int(bc), op->row_ptr, op->row_src));
     *out = op.release();
     return FQ_OK;
   } catch (const std::exception& e) {
@@ -227,7 +240,10 @@ namespace fq {
 extern template int launch_elemop_cells<1>(int, int, const ElemopArgs&, cudaStream_t);
 extern template int launch_elemop_cells<2>(int, int, const ElemopArgs&, cudaStream_t);
 extern template int launch_elemop_cells<3>(int, int, const ElemopArgs&, cudaStream_t);
-extern template int launch_elemop_cells<4>(int, int, const ElemopArgs&, cudaStream_t);
+extern template int launch_elemop_cells_sel<4, 1u << EK_MASS>(int, int, const ElemopArgs&, cudaStream_t);
+extern template int launch_elemop_cells_sel<4, 1u << EK_DIF_TRIAL>(int, int, const ElemopArgs&, cudaStream_t);
+extern template int launch_elemop_cells_sel<4, 1u << EK_DIF_TEST>(int, int, const ElemopArgs&, cudaStream_t);
+extern template int launch_elemop_cells_sel<4, 1u << EK_DIF_BOTH>(int, int, const ElemopArgs&, cudaStream_t);
 
 int launch_elemop_cells_dim(int n, int K, int kind, const ElemopArgs& a, cudaStream_t st) {
   switch (n) {
@@ -238,7 +254,18 @@ int launch_elemop_cells_dim(int n, int K, int kind, const ElemopArgs& a, cudaStr
     case 3:
       return launch_elemop_cells<3>(K, kind, a, st);
     case 4:
-      return launch_elemop_cells<4>(K, kind, a, st);
+      switch (kind) {
+        case EK_MASS:
+          return launch_elemop_cells_sel<4, 1u << EK_MASS>(K, kind, a, st);
+        case EK_DIF_TRIAL:
+          return launch_elemop_cells_sel<4, 1u << EK_DIF_TRIAL>(K, kind, a, st);
+        case EK_DIF_TEST:
+          return launch_elemop_cells_sel<4, 1u << EK_DIF_TEST>(K, kind, a, st);
+        case EK_DIF_BOTH:
+          return launch_elemop_cells_sel<4, 1u << EK_DIF_BOTH>(K, kind, a, st);
+        default:
+          return -1;
+      }
     default:
       return -1;
   }

@@ -12,8 +12,23 @@
 #pragma once
 
 #include "fq_element_kernel.cuh"
+#include "fq_internal.h"
 
 namespace fq {
+
+// The incidence of the grade-`grade` faces: for every degree of freedom (the
+// relative numbering under FQ_RELATIVE; boundary faces dropped), the slots
+// local face * ncells + cell of the cells containing it, in cell order. Built
+// by one stable radix sort of the cell -> face table; row_ptr has ndofs + 1
+// entries.
+fq_status build_face_incidence(fq_ctx* ctx, fq_mesh* m, int grade, int bc, DevBuf& row_ptr, DevBuf& row_src);
+
+// y[r] = sum over the incidence row r of contrib[slot], in cell order, summed in
+// float-float and rounded once (the second stage of the two-stage gather).
+void launch_gather_rows(const int32_t* rp, const int32_t* src, const df64* contrib, double* y, int64_t nrows,
+                        const int* done, cudaStream_t st);
+
+int64_t ndofs_of(const fq_mesh* m, int grade, int bc);
 
 struct ElemopArgs {
   int64_t ncells = 0;
@@ -94,22 +109,34 @@ int launch_elemop_one(const ElemopArgs& a, cudaStream_t st) {
   return 0;
 }
 
-// The four pairings at every grade of dimension N (one translation unit per N).
-template <int N>
-int launch_elemop_cells(int K, int kind, const ElemopArgs& a, cudaStream_t st) {
+// The pairings whose kinds are in KINDS (bit EK_x), at every grade of
+// dimension N; -1 when (K, kind) is not among them. The kinds of one dimension
+// may be split over several translation units to keep each compile short.
+template <int N, unsigned KINDS>
+int launch_elemop_cells_sel(int K, int kind, const ElemopArgs& a, cudaStream_t st) {
   int r = -1;
   static_for<N + 1>([&](auto KC) {
     constexpr int k = decltype(KC)::value;
     if (k != K) return;
-    if (kind == EK_MASS) r = launch_elemop_one<N, k, EK_MASS>(a, st);
+    if constexpr (bool(KINDS & (1u << EK_MASS)))
+      if (kind == EK_MASS) r = launch_elemop_one<N, k, EK_MASS>(a, st);
     if constexpr (k >= 1) {
-      if (kind == EK_DIF_TRIAL) r = launch_elemop_one<N, k, EK_DIF_TRIAL>(a, st);
-      if (kind == EK_DIF_TEST) r = launch_elemop_one<N, k, EK_DIF_TEST>(a, st);
-      if (kind == EK_DIF_BOTH) r = launch_elemop_one<N, k, EK_DIF_BOTH>(a, st);
+      if constexpr (bool(KINDS & (1u << EK_DIF_TRIAL)))
+        if (kind == EK_DIF_TRIAL) r = launch_elemop_one<N, k, EK_DIF_TRIAL>(a, st);
+      if constexpr (bool(KINDS & (1u << EK_DIF_TEST)))
+        if (kind == EK_DIF_TEST) r = launch_elemop_one<N, k, EK_DIF_TEST>(a, st);
+      if constexpr (bool(KINDS & (1u << EK_DIF_BOTH)))
+        if (kind == EK_DIF_BOTH) r = launch_elemop_one<N, k, EK_DIF_BOTH>(a, st);
     }
   });
   // dif_both(N+1) has no entries; callers never launch it
   return r;
+}
+
+// The four pairings at every grade of dimension N (one translation unit per N).
+template <int N>
+int launch_elemop_cells(int K, int kind, const ElemopArgs& a, cudaStream_t st) {
+  return launch_elemop_cells_sel<N, 0xFu>(K, kind, a, st);
 }
 
 }  // namespace fq

@@ -1,0 +1,6 @@
+// Source-load cell kernels for cell dimension 2.
+#include "fq_source.cuh"
+
+namespace fq {
+template int launch_source_cells<2>(int K, int adim, const SourceArgs& a, cudaStream_t st);
+}  // namespace fq

@@ -339,6 +339,28 @@ fq_status fq_derham_nodes(fq_ctx* ctx, fq_mesh* mesh, const double* coords, int 
 fq_status fq_derham_reduce(fq_ctx* ctx, fq_mesh* mesh, const double* coords, int adim, int grade, int degree,
                            const double* values, double* cochain);
 
+/* ---- the source load (the Galerkin vector of a source form) --------------- */
+/* SourceForm::element (formoniq/src/operators.rs:598-635) summed by
+ * assemble_vector (formoniq/src/galerkin.rs:279-312):
+ *   l_s = sum_K vol_K sum_q w_q <f(x_q), W_s(x_q)>_{Lambda^k g_K^{-1}}
+ * over the cells K containing the k-simplex s, in cell order, with the
+ * Grundmann-Moeller rule of `degree` on the cell (the reference's default
+ * CellQuadrature is degree 1). Like the de Rham map, the field is evaluated by
+ * the caller between two calls. fq_source_nodes writes, with coords null, the
+ * barycentric nodes [nq][n+1] shared by every cell; with device coords
+ * [N_0][adim] (n <= adim <= 4), the ambient nodes [ncells][nq][adim]. The caller
+ * writes values [ncells][nq][ncomp]: with coords null, the section's components
+ * in each cell's reference frame (ncomp = C(n,k), on dxi^J with xi_j =
+ * lambda_{j+1}, J colex; derham/src/section.rs:50-66); with coords, a flat
+ * ambient form's components on dx^A (ncomp = C(adim,k)), pulled back through
+ * each cell's affine map (Pullback::identity, section.rs:95-140).
+ * fq_source_assemble writes out [ndofs(k, bc)] (FQ_RELATIVE: the interior
+ * entries, RelativeWhitneyComplex::restrict). All arrays are device memory. */
+int fq_source_npoints(int dim, int degree);
+fq_status fq_source_nodes(fq_ctx* ctx, fq_mesh* mesh, const double* coords, int adim, int degree, double* nodes);
+fq_status fq_source_assemble(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, int degree, const double* coords,
+                             int adim, const double* values, double* out);
+
 /* ---- the covariant Hodge-Dirac source problem ---------------------------- */
 /* dirac::solve_dirac_source (problems/dirac.rs:473-531) with MINRES in place of
  * the reference's sparse LU: S = A + m M of HodgeDirac::assemble_selfadjoint

@@ -769,6 +769,83 @@ def derham_map(cx: Complex, coords: np.ndarray, k: int, field, degree: int = 3) 
 
 
 # ---------------------------------------------------------------------------
+# The source load: SourceForm::element (formoniq/src/operators.rs:598-635)
+# summed by assemble_vector (formoniq/src/galerkin.rs:279-312)
+# ---------------------------------------------------------------------------
+
+def _subset_dets(mats: np.ndarray, rows, cols) -> np.ndarray:
+    """det of mats[..., R, C] for every R in rows, C in cols: [..., len(rows), len(cols)]."""
+    out = np.empty(mats.shape[:-2] + (len(rows), len(cols)))
+    for i, r in enumerate(rows):
+        for j, c in enumerate(cols):
+            out[..., i, j] = np.linalg.det(mats[..., list(r), :][..., :, list(c)]) if len(r) else 1.0
+    return out
+
+
+def whitney_at(n: int, k: int, bary: np.ndarray) -> np.ndarray:
+    """WhitneyLsf::at_bary (derham/src/interpolate/form.rs:108-112) for every
+    local k-face s (colex (k+1)-subsets of {0..n}) at barycentric nodes [nq, n+1]:
+    W_s = k! sum_p (-1)^p lambda_{s_p} dlambda_{s without s_p}, with dlambda from
+    unit_difbarys (simplicial/src/atlas.rs:174-182), as components on dxi^J
+    (J colex k-subsets of {0..n-1}): [nq, C(n+1,k+1), C(n,k)]."""
+    L = np.zeros((n + 1, n))
+    L[0, :] = -1.0
+    L[1:, :] = np.eye(n)
+    taus = colex_subsets(n + 1, k)
+    D = _subset_dets(L, taus, colex_subsets(n, k))  # Lambda^k L
+    rank = {t: i for i, t in enumerate(taus)}
+    faces = colex_subsets(n + 1, k + 1)
+    W = np.zeros((len(bary), len(faces), D.shape[1]))
+    for si, s in enumerate(faces):
+        for p, v in enumerate(s):
+            W[:, si, :] += (-1) ** p * np.outer(bary[:, v], D[rank[s[:p] + s[p + 1:]]])
+    return math.factorial(k) * W
+
+
+def pullback_values(cx: Complex, coords: np.ndarray, k: int, values: np.ndarray) -> np.ndarray:
+    """Pullback::identity (derham/src/section.rs:95-140) of a flat ambient form:
+    components on dx^A [ncells, nq, C(adim,k)] -> the cells' reference frames
+    [ncells, nq, C(n,k)], f_J = sum_A w_A det(E[A, J]), E = [x_{v_j} - x_{v_0}]."""
+    n = cx.dim
+    cells = cx.simplices(n)
+    adim = coords.shape[1]
+    E = np.transpose(coords[cells[:, 1:]] - coords[cells[:, :1]], (0, 2, 1))  # [nc, adim, n]
+    P = _subset_dets(E, colex_subsets(adim, k), colex_subsets(n, k))  # [nc, C(adim,k), C(n,k)]
+    return np.einsum("cqa,caj->cqj", values, P)
+
+
+def whitney_interpolant_values(cx: Complex, k: int, cochain: np.ndarray, bary: np.ndarray) -> np.ndarray:
+    """WhitneyInterpolant of a cochain (derham/src/interpolate/interpolant.rs) at
+    the barycentric nodes of every cell, in the cells' reference frames:
+    [ncells, nq, C(n,k)]."""
+    W = whitney_at(cx.dim, k, bary)
+    return np.einsum("cs,qsj->cqj", cochain[cx.cell_faces(k)], W)
+
+
+def source_form(cx: Complex, lengths: np.ndarray, k: int, values: np.ndarray, degree: int = 1,
+                coords: np.ndarray | None = None, relative: bool = False) -> np.ndarray:
+    """SourceForm::new(source, qr).assemble(topology, lengths): per cell
+    vol sum_q w_q <f_q, W_s(x_q)>_{Lambda^k G^{-1}} (CellQuadrature::integrate,
+    operators.rs:246-261; inner, metric/src/tensor.rs:140-155, with the induced
+    form multiform_metric, :127-131), summed per face in cell order
+    (galerkin.rs:292-311). values: [ncells, nq, C(n,k)] in the cells' reference
+    frames, or a flat ambient form's [ncells, nq, C(adim,k)] when coords is given."""
+    n = cx.dim
+    bary, w = gm_rule(n, degree)
+    values = np.asarray(values, np.float64).reshape(cx.ncells(), len(w), -1)
+    if coords is not None:
+        values = pullback_values(cx, coords, k, values)
+    W = whitney_at(n, k, bary)
+    _, gi, _, vol, _ = cx.cell_metrics(lengths)
+    Js = colex_subsets(n, k)
+    lg = _subset_dets(gi, Js, Js)  # Lambda^k G^{-1} per cell
+    elvec = vol[:, None] * np.einsum("q,cqi,cij,qsj->cs", w, values, lg, W)
+    out = np.zeros(cx.nsimplices(k))
+    np.add.at(out, cx.cell_faces(k).ravel(), elvec.ravel())
+    return out[cx.interior(k)] if relative else out
+
+
+# ---------------------------------------------------------------------------
 # Maxwell evolution: time::Leapfrog (formoniq/src/time.rs:292-420) as used by
 # solve_dirac_leapfrog (problems/dirac.rs:404-434)
 # ---------------------------------------------------------------------------
