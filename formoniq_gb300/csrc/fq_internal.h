@@ -109,6 +109,10 @@ struct fq_mesh {
   fq::DevBuf elem;
   // face incidences [bc][grade] of the vector assemblies, built on first use
   fq::DevBuf inc_ptr[2][5], inc_src[2][5];
+  // source loads: the last quadrature table (degree, w_q lambda_q) and the
+  // per-cell slot buffer, kept across calls
+  int source_degree = -1;
+  fq::DevBuf source_rule, source_slots;
 };
 
 struct fq_matrix {

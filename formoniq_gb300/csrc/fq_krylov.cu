@@ -23,6 +23,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "fq_df64.cuh"
 #include "fq_hx.h"
 #include "fq_internal.h"
 
@@ -35,6 +36,7 @@ constexpr int PBLOCKS = 152 * 8; // grid cap of the fused SpMV kernels: 8 reside
 struct SolverState {
   double beta1, beta, oldb, dbar, epsln, phibar, cs, sn;  // MINRES
   double alfa;
+  double rbeta, c1;  // MINRES: 1 / beta and -beta / oldb for the next A kernel
   double rz, bnorm;                                       // CG
   double residual;
   long long iters;
@@ -68,6 +70,11 @@ __device__ __forceinline__ double reduce_partials(const double* part, int np, do
   return block_sum(v, sh);
 }
 
+// The scalar recurrences (FP64 divisions and square roots, each a sequence of
+// FP64 instructions) run on one thread per block and reach the others through
+// shared memory: repeated by every thread of a full grid they cost more on
+// GB300's narrow FP64 pipe than the vector work of the kernel.
+
 // Sub-warp CSR row product: W lanes per row, fixed lane order.
 template <int W, typename VT>
 __device__ __forceinline__ VT row_dot(const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
@@ -92,6 +99,47 @@ __device__ __forceinline__ VT row_dot(const int32_t* __restrict__ rp, const int3
   return acc;
 }
 
+// The same product for an FP64 operator evaluated on the FP32 pipe: values and
+// the gathered vector as float-float pairs (each split once from its double,
+// exactly to 48 bits), products and sums in float-float, one FP64 add per row
+// to round the result. GB300's FP64 pipe issues a small fraction of the FP32
+// rate, and an FP64 CSR product with ~30 entries per row is bound by it, not by
+// memory; the pairs occupy the same 8 bytes as the doubles.
+__device__ __forceinline__ df64 ldg_df(const df64* p) {
+  const float2 f = __ldg(reinterpret_cast<const float2*>(p));
+  return df64(f.x, f.y);
+}
+
+template <int W>
+__device__ __forceinline__ df64 row_dot_split(const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                              const df64* __restrict__ val, const df64* __restrict__ x, int64_t row,
+                                              bool valid, int lane) {
+  df64 acc0, acc1;
+  if (valid) {
+    const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
+    int t = b + lane;
+    for (; t + W < e; t += 2 * W) {
+      const int c0 = __ldg(ci + t), c1 = __ldg(ci + t + W);
+      const df64 v0 = ldg_df(val + t), v1 = ldg_df(val + t + W);
+      acc0 += v0 * ldg_df(x + c0);
+      acc1 += v1 * ldg_df(x + c1);
+    }
+    if (t < e) acc0 += ldg_df(val + t) * ldg_df(x + __ldg(ci + t));
+  }
+  df64 acc = acc0 + acc1;
+#pragma unroll
+  for (int o = W / 2; o > 0; o >>= 1) {
+    const df64 other(__shfl_xor_sync(0xffffffffu, acc.hi, o, W), __shfl_xor_sync(0xffffffffu, acc.lo, o, W));
+    acc = acc + other;
+  }
+  return acc;
+}
+
+__global__ void split_kernel(const double* __restrict__ a, df64* __restrict__ out, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    out[i] = df64(a[i]);
+}
+
 // ---------------------------------------------------------------------------
 // plain SpMV (LinearOperator::apply)
 // ---------------------------------------------------------------------------
@@ -108,13 +156,35 @@ __global__ void __launch_bounds__(KT) spmv_kernel(const int32_t* rp, const int32
   }
 }
 
+// Lanes per row of the sub-warp CSR kernels. In FP64 each lane's products, the
+// join of its two accumulators and every shuffle level are FP64 instructions,
+// and GB300 issues FP64 at a small fraction of the FP32 rate (the fused MINRES
+// SpMV measured FP64-pipe bound at W = 16), so FP64 rows get fewer lanes: more
+// rows per warp and fewer reduction adds per row. FP32 keeps the memory-tuned
+// choice.
 template <typename VT>
 static int pick_w(int64_t nnz, int64_t nrows) {
   const double avg = nrows > 0 ? double(nnz) / double(nrows) : 0.0;
+  if (std::is_same<VT, double>::value) {
+    if (avg <= 48) return 4;
+    if (avg <= 160) return 8;
+    return 16;
+  }
   if (avg <= 6) return 4;
   if (avg <= 14) return 8;
   if (avg <= 80) return 16;
   return 32;
+}
+
+// Lanes per row of the split (float-float) FP64 product. Its sums run on the
+// FP32 pipe, but the per-row epilogue (scaling, the dot partial) stays FP64 and
+// costs a warp instruction per row group, so rows keep few lanes: W = 4 puts 8
+// rows in each of those instructions.
+static int pick_w_split(int64_t nnz, int64_t nrows) {
+  const double avg = nrows > 0 ? double(nnz) / double(nrows) : 0.0;
+  if (avg <= 48) return 4;
+  if (avg <= 160) return 8;
+  return 16;
 }
 
 static int spmv_blocks(int64_t nrows, int W) {
@@ -163,6 +233,7 @@ struct MinresVecs {
   int external;    // 1: y = P r2 is applied by separate kernels (dinv unused)
   const VT* b;
   double *partA, *partB;
+  df64* y2;  // FP64: y as float-float pairs for the split product (null otherwise)
 };
 
 template <typename VT>
@@ -175,6 +246,8 @@ __global__ void __launch_bounds__(KT) minres_init(MinresVecs<VT> m, int64_t n) {
     m.r1[i] = bi;
     m.r2[i] = bi;
     m.y[i] = yi;
+    if constexpr (std::is_same<VT, double>::value)
+      if (m.y2) m.y2[i] = df64(yi);
     m.x[i] = VT(0);
     m.w[i] = VT(0);
     m.w2[i] = VT(0);
@@ -207,6 +280,8 @@ __global__ void minres_init_state(SolverState* s0, SolverState* s1, const double
       s.phibar = beta1;
       s.cs = -1.0;
       s.sn = 0.0;
+      s.rbeta = 1.0 / beta1;
+      s.c1 = 0.0;
       s.residual = 1.0;
       s.done = max_iters <= 0 ? 1 : 0;
     }
@@ -222,9 +297,7 @@ __global__ void __launch_bounds__(KT) minres_a(const int32_t* rp, const int32_t*
                                                const SolverState* __restrict__ S, int64_t n) {
   __shared__ double sh[32];
   if (S->done) return;
-  const double rb = 1.0 / S->beta;
-  const double c1 = S->iters >= 1 ? (-S->beta / S->oldb) : 0.0;
-  const VT rbt = VT(rb), c1t = VT(c1);
+  const VT rbt = VT(S->rbeta), c1t = VT(S->c1);
   const int lane = threadIdx.x % W;
   double acc = 0.0;
   const int64_t rows_per_grid = int64_t(gridDim.x) * (blockDim.x / W);
@@ -244,13 +317,43 @@ __global__ void __launch_bounds__(KT) minres_a(const int32_t* rp, const int32_t*
   if (threadIdx.x == 0) m.partA[blockIdx.x] = acc;
 }
 
+// A for an FP64 operator on the FP32 pipe (values and y as float-float pairs).
+template <int W>
+__global__ void __launch_bounds__(KT) minres_a_split(const int32_t* rp, const int32_t* ci, const df64* val,
+                                                     MinresVecs<double> m, const SolverState* __restrict__ S,
+                                                     int64_t n) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  const double rbt = S->rbeta, c1t = S->c1;
+  const int lane = threadIdx.x % W;
+  double acc = 0.0;
+  const int64_t rows_per_grid = int64_t(gridDim.x) * (blockDim.x / W);
+  for (int64_t base = int64_t(blockIdx.x) * (blockDim.x / W); base < n; base += rows_per_grid) {
+    const int64_t row = base + threadIdx.x / W;
+    const bool valid = row < n;
+    const df64 av = row_dot_split<W>(rp, ci, val, m.y2, row, valid, lane);
+    if (valid && lane == 0) {
+      const double vi = m.y[row] * rbt;
+      const double zi = av.to_double() * rbt + c1t * m.r1[row];
+      m.v[row] = vi;
+      m.z[row] = zi;
+      acc += vi * zi;
+    }
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) m.partA[blockIdx.x] = acc;
+}
+
 // B: alfa; z -= (alfa/beta) r2; r1 = r2; r2 = z; y = P r2; partial r2.y
 template <typename VT>
 __global__ void __launch_bounds__(KT) minres_b(MinresVecs<VT> m, SolverState* __restrict__ S, int npa, int64_t n) {
   __shared__ double sh[32];
+  __shared__ double coef;
   if (S->done) return;
   const double alfa = reduce_partials(m.partA, npa, sh);
-  const VT c2 = VT(-alfa / S->beta);
+  if (threadIdx.x == 0) coef = -alfa / S->beta;
+  __syncthreads();
+  const VT c2 = VT(coef);
   double acc = 0.0;
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
     const VT r2 = m.r2[i];
@@ -260,6 +363,8 @@ __global__ void __launch_bounds__(KT) minres_b(MinresVecs<VT> m, SolverState* __
     if (!m.external) {
       const VT yi = m.dinv ? zi * m.dinv[i] : zi;
       m.y[i] = yi;
+      if constexpr (std::is_same<VT, double>::value)
+        if (m.y2) m.y2[i] = df64(yi);
       acc += double(zi) * double(yi);
     }
   }
@@ -271,12 +376,16 @@ __global__ void __launch_bounds__(KT) minres_b(MinresVecs<VT> m, SolverState* __
 // Partials of a.b (after an external preconditioner wrote b = P a).
 template <typename VT>
 __global__ void __launch_bounds__(KT) dot_partials(const VT* __restrict__ a, const VT* __restrict__ b,
-                                                   double* __restrict__ part, int64_t n, const int* __restrict__ done) {
+                                                   double* __restrict__ part, int64_t n, const int* __restrict__ done,
+                                                   df64* __restrict__ b2 = nullptr) {
   __shared__ double sh[32];
   if (done && *done) return;
   double acc = 0.0;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
     acc += double(a[i]) * double(b[i]);
+    if constexpr (std::is_same<VT, double>::value)
+      if (b2) b2[i] = df64(b[i]);  // the split copy of b the next product gathers
+  }
   acc = block_sum(acc, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
@@ -291,23 +400,55 @@ __global__ void __launch_bounds__(KT) minres_c(MinresVecs<VT> m, const SolverSta
     if (blockIdx.x == 0 && threadIdx.x == 0) *Sout = *Sin;
     return;
   }
+  __shared__ double coef[4];
   const double alfa = reduce_partials(m.partA, npa, sh);
   const double beta_sq = reduce_partials(m.partB, npb, sh);
-  SolverState s = *Sin;
-  const double eps = DBL_EPSILON;
-  const double oldb = s.beta;
-  const double beta = sqrt(fmax(beta_sq, 0.0));
-  const double oldeps = s.epsln;
-  const double delta = s.cs * s.dbar + s.sn * alfa;
-  const double gbar = s.sn * s.dbar - s.cs * alfa;
-  const double epsln = s.sn * beta;
-  const double dbar = -s.cs * beta;
-  const double gamma = fmax(sqrt(gbar * gbar + beta * beta), eps);
-  const double cs = gbar / gamma;
-  const double sn = beta / gamma;
-  const double phi = cs * s.phibar;
-  const double phibar = s.phibar * sn;
-  const VT ce = VT(-oldeps), cd = VT(-delta), cg = VT(1.0 / gamma), cp = VT(phi);
+  if (threadIdx.x == 0) {
+    SolverState s = *Sin;
+    const double eps = DBL_EPSILON;
+    const double oldb = s.beta;
+    const double beta = sqrt(fmax(beta_sq, 0.0));
+    const double oldeps = s.epsln;
+    const double delta = s.cs * s.dbar + s.sn * alfa;
+    const double gbar = s.sn * s.dbar - s.cs * alfa;
+    const double epsln = s.sn * beta;
+    const double dbar = -s.cs * beta;
+    const double gamma = fmax(sqrt(gbar * gbar + beta * beta), eps);
+    const double cs = gbar / gamma;
+    const double sn = beta / gamma;
+    const double phi = cs * s.phibar;
+    const double phibar = s.phibar * sn;
+    coef[0] = -oldeps;
+    coef[1] = -delta;
+    coef[2] = 1.0 / gamma;
+    coef[3] = phi;
+    if (blockIdx.x == 0) {
+      s.oldb = oldb;
+      s.beta = beta;
+      s.epsln = epsln;
+      s.dbar = dbar;
+      s.cs = cs;
+      s.sn = sn;
+      s.phibar = phibar;
+      s.alfa = alfa;
+      s.rbeta = 1.0 / beta;
+      s.c1 = -beta / oldb;
+      s.iters += 1;
+      s.residual = phibar / s.beta1;
+      if (!isfinite(s.residual)) {
+        s.breakdown = 1;
+        s.done = 1;
+      }
+      if (s.residual <= rtol) {
+        s.converged = 1;
+        s.done = 1;
+      }
+      if (s.iters >= max_iters) s.done = 1;
+      *Sout = s;
+    }
+  }
+  __syncthreads();
+  const VT ce = VT(coef[0]), cd = VT(coef[1]), cg = VT(coef[2]), cp = VT(coef[3]);
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
     const VT w = m.w[i];
     VT wn = m.v[i] + ce * m.w2[i];
@@ -316,28 +457,6 @@ __global__ void __launch_bounds__(KT) minres_c(MinresVecs<VT> m, const SolverSta
     m.w2[i] = w;
     m.w[i] = wn;
     m.x[i] = m.x[i] + cp * wn;
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    s.oldb = oldb;
-    s.beta = beta;
-    s.epsln = epsln;
-    s.dbar = dbar;
-    s.cs = cs;
-    s.sn = sn;
-    s.phibar = phibar;
-    s.alfa = alfa;
-    s.iters += 1;
-    s.residual = phibar / s.beta1;
-    if (!isfinite(s.residual)) {
-      s.breakdown = 1;
-      s.done = 1;
-    }
-    if (s.residual <= rtol) {
-      s.converged = 1;
-      s.done = 1;
-    }
-    if (s.iters >= max_iters) s.done = 1;
-    *Sout = s;
   }
 }
 
@@ -351,6 +470,7 @@ struct CgVecs {
   int external;  // 1: z = P r is applied by separate kernels (dinv unused)
   const VT* b;
   double *partA, *partB, *partC;
+  df64* p2;  // FP64: p as float-float pairs for the split product (null otherwise)
 };
 
 template <typename VT>
@@ -364,6 +484,8 @@ __global__ void __launch_bounds__(KT) cg_init(CgVecs<VT> c, int64_t n) {
     c.r[i] = bi;
     c.z[i] = zi;
     c.p[i] = zi;
+    if constexpr (std::is_same<VT, double>::value)
+      if (c.p2) c.p2[i] = df64(zi);
     rz += double(bi) * double(zi);
     bb += double(bi) * double(bi);
   }
@@ -421,13 +543,39 @@ __global__ void __launch_bounds__(KT) cg_a(const int32_t* rp, const int32_t* ci,
   if (threadIdx.x == 0) c.partA[blockIdx.x] = acc;
 }
 
+// A for an FP64 operator on the FP32 pipe (values and p as float-float pairs).
+template <int W>
+__global__ void __launch_bounds__(KT) cg_a_split(const int32_t* rp, const int32_t* ci, const df64* val,
+                                                 CgVecs<double> c, const SolverState* __restrict__ S, int64_t n) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  const int lane = threadIdx.x % W;
+  double acc = 0.0;
+  const int64_t rows_per_grid = int64_t(gridDim.x) * (blockDim.x / W);
+  for (int64_t base = int64_t(blockIdx.x) * (blockDim.x / W); base < n; base += rows_per_grid) {
+    const int64_t row = base + threadIdx.x / W;
+    const bool valid = row < n;
+    const df64 av = row_dot_split<W>(rp, ci, val, c.p2, row, valid, lane);
+    if (valid && lane == 0) {
+      const double a = av.to_double();
+      c.ap[row] = a;
+      acc += c.p[row] * a;
+    }
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) c.partA[blockIdx.x] = acc;
+}
+
 // B: alpha = rz / p.ap; x += alpha p; r -= alpha ap; z = P r; partials r.z, r.r
 template <typename VT>
 __global__ void __launch_bounds__(KT) cg_b(CgVecs<VT> c, const SolverState* __restrict__ S, int npa, int64_t n) {
   __shared__ double sh[32];
+  __shared__ double coef;
   if (S->done) return;
   const double pap = reduce_partials(c.partA, npa, sh);
-  const double alpha = S->rz / pap;
+  if (threadIdx.x == 0) coef = S->rz / pap;
+  __syncthreads();
+  const double alpha = coef;
   const VT at = VT(alpha), mat = VT(-alpha);
   double rz = 0.0, rr = 0.0;
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
@@ -457,6 +605,8 @@ __global__ void __launch_bounds__(KT) cg_init_p(CgVecs<VT> c, int64_t n) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
     const VT zi = c.z[i];
     c.p[i] = zi;
+    if constexpr (std::is_same<VT, double>::value)
+      if (c.p2) c.p2[i] = df64(zi);
     rz += double(c.b[i]) * double(zi);
   }
   rz = block_sum(rz, sh);
@@ -473,12 +623,18 @@ __global__ void __launch_bounds__(KT) cg_c(CgVecs<VT> c, const SolverState* __re
     if (blockIdx.x == 0 && threadIdx.x == 0) *Sout = *Sin;
     return;
   }
+  __shared__ double coef;
   const double rz_next = reduce_partials(c.partB, npb, sh);
   const double rr = reduce_partials(c.partC, npb, sh);
-  const double beta = rz_next / Sin->rz;
-  const VT bt = VT(beta);
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
-    c.p[i] = c.p[i] * bt + c.z[i];
+  if (threadIdx.x == 0) coef = rz_next / Sin->rz;
+  __syncthreads();
+  const VT bt = VT(coef);
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const VT pi = c.p[i] * bt + c.z[i];
+    c.p[i] = pi;
+    if constexpr (std::is_same<VT, double>::value)
+      if (c.p2) c.p2[i] = df64(pi);
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     SolverState s = *Sin;
     s.rz = rz_next;
@@ -522,7 +678,14 @@ static fq_status run_graph_loop(fq_ctx* ctx, SolverState* S, int64_t max_iters, 
   if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
     one_iteration(0);
     one_iteration(1);
+    // a launch refused during capture leaves its kernel out of the graph: an
+    // error, not an iteration to run without it
+    const cudaError_t le = cudaGetLastError();
     cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    if (le != cudaSuccess) {
+      if (ce == cudaSuccess) cudaGraphDestroy(graph);
+      return cuda_check(ctx, le, "iteration launch (capture)");
+    }
     if (ce == cudaSuccess) {
       ce = cudaGraphInstantiate(&exec, graph, 0);
       cudaGraphDestroy(graph);
@@ -612,38 +775,74 @@ fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT
   m.b = b;
   m.partA = parts.as<double>();
   m.partB = parts.as<double>() + PBLOCKS;
+  m.y2 = nullptr;
   SolverState* S = state.as<SolverState>();
-  const int W = pick_w<VT>(nnz, n);
+  // FP64: the product runs on float-float pairs of the values and of y
+  constexpr bool split = std::is_same<VT, double>::value;
+  DevBuf val2, y2;
+  if constexpr (split) {
+    FQ_TRY(val2.alloc(ctx, size_t(std::max<int64_t>(nnz, 1)) * sizeof(df64)));
+    FQ_TRY(y2.alloc(ctx, size_t(std::max<int64_t>(n, 1)) * sizeof(df64)));
+    m.y2 = y2.as<df64>();
+    if (nnz > 0) {
+      split_kernel<<<int(std::min<int64_t>((nnz + KT - 1) / KT, KBLOCKS)), KT, 0, st>>>(
+          val, val2.as<df64>(), nnz);
+      ctx->launches++;
+    }
+  }
+  const int W = split ? pick_w_split(nnz, n) : pick_w<VT>(nnz, n);
   const int ga = std::min(spmv_blocks(n, W), PBLOCKS);
   const int gv = int(std::max<int64_t>(1, std::min<int64_t>((n + KT - 1) / KT, KBLOCKS)));
   minres_init<VT><<<gv, KT, 0, st>>>(m, n);
   if (pc) {
     hx_apply<VT>(*pc, b, m.y, nullptr, st);
-    dot_partials<VT><<<gv, KT, 0, st>>>(b, m.y, m.partB, n, nullptr);
+    dot_partials<VT><<<gv, KT, 0, st>>>(b, m.y, m.partB, n, nullptr, m.y2);
   }
   minres_init_state<<<1, KT, 0, st>>>(S, S + 1, m.partB, gv, rtol, (long long)max_iters);
   ctx->launches += 2;
   SolverState hs{};
+  // (a runtime branch around the constexpr one: a kernel launch that follows an
+  // `if constexpr ... else` in this lambda was dropped from the device code)
   auto iteration = [&](int cur) {
-    switch (W) {
-      case 4:
-        minres_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
-        break;
-      case 8:
-        minres_a<8, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
-        break;
-      case 16:
-        minres_a<16, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
-        break;
-      default:
-        minres_a<32, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
-        break;
+    if (split) {
+      if constexpr (split) {
+        const df64* v2 = val2.as<df64>();
+        switch (W) {
+          case 4:
+            minres_a_split<4><<<ga, KT, 0, st>>>(rp, ci, v2, m, S + cur, n);
+            break;
+          case 8:
+            minres_a_split<8><<<ga, KT, 0, st>>>(rp, ci, v2, m, S + cur, n);
+            break;
+          case 16:
+            minres_a_split<16><<<ga, KT, 0, st>>>(rp, ci, v2, m, S + cur, n);
+            break;
+          default:
+            minres_a_split<32><<<ga, KT, 0, st>>>(rp, ci, v2, m, S + cur, n);
+            break;
+        }
+      }
+    } else {
+      switch (W) {
+        case 4:
+          minres_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+          break;
+        case 8:
+          minres_a<8, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+          break;
+        case 16:
+          minres_a<16, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+          break;
+        default:
+          minres_a<32, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+          break;
+      }
     }
     minres_b<VT><<<gv, KT, 0, st>>>(m, S + cur, ga, n);
     if (pc) {
       const int* done = &(S + cur)->done;
       hx_apply<VT>(*pc, m.r2, m.y, done, st);
-      dot_partials<VT><<<gv, KT, 0, st>>>(m.r2, m.y, m.partB, n, done);
+      dot_partials<VT><<<gv, KT, 0, st>>>(m.r2, m.y, m.partB, n, done, m.y2);
     }
     minres_c<VT><<<gv, KT, 0, st>>>(m, S + cur, S + (1 - cur), ga, gv, rtol, (long long)max_iters, n);
   };
@@ -682,8 +881,24 @@ static fq_status cg_impl(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, cons
   c.partA = parts.as<double>();
   c.partB = parts.as<double>() + PBLOCKS;
   c.partC = parts.as<double>() + 2 * PBLOCKS;
+  c.p2 = nullptr;
   SolverState* S = state.as<SolverState>();
-  const int W = pick_w<VT>(nnz, n);
+  // FP64 CSR operators: the product runs on float-float pairs of the values and of p
+  constexpr bool split_type = std::is_same<VT, double>::value;
+  const bool split = split_type && !hook;
+  DevBuf val2, p2;
+  if constexpr (split_type) {
+    if (split) {
+      FQ_TRY(val2.alloc(ctx, size_t(std::max<int64_t>(nnz, 1)) * sizeof(df64)));
+      FQ_TRY(p2.alloc(ctx, size_t(std::max<int64_t>(n, 1)) * sizeof(df64)));
+      c.p2 = p2.as<df64>();
+      if (nnz > 0) {
+        split_kernel<<<int(std::min<int64_t>((nnz + KT - 1) / KT, KBLOCKS)), KT, 0, st>>>(val, val2.as<df64>(), nnz);
+        ctx->launches++;
+      }
+    }
+  }
+  const int W = split ? pick_w_split(nnz, n) : pick_w<VT>(nnz, n);
   const int ga = std::min(spmv_blocks(n, W), PBLOCKS);
   const int gv = int(std::max<int64_t>(1, std::min<int64_t>((n + KT - 1) / KT, KBLOCKS)));
   cg_init<VT><<<gv, KT, 0, st>>>(c, n);
@@ -700,6 +915,24 @@ static fq_status cg_impl(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, cons
         const int* done = &(S + cur)->done;
         hook->apply(hook->self, c.p, c.ap, done, st);
         dot_partials<VT><<<ga, KT, 0, st>>>(c.p, c.ap, c.partA, n, done);
+      }
+    } else if (split) {
+      if constexpr (split_type) {
+        const df64* v2 = val2.as<df64>();
+        switch (W) {
+          case 4:
+            cg_a_split<4><<<ga, KT, 0, st>>>(rp, ci, v2, c, S + cur, n);
+            break;
+          case 8:
+            cg_a_split<8><<<ga, KT, 0, st>>>(rp, ci, v2, c, S + cur, n);
+            break;
+          case 16:
+            cg_a_split<16><<<ga, KT, 0, st>>>(rp, ci, v2, c, S + cur, n);
+            break;
+          default:
+            cg_a_split<32><<<ga, KT, 0, st>>>(rp, ci, v2, c, S + cur, n);
+            break;
+        }
       }
     } else switch (W) {
       case 4:

@@ -13,6 +13,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "fq_hx.h"
@@ -25,6 +26,28 @@ constexpr int MT = 256;
 
 inline int grid_for_n(int64_t n) { return int(std::max<int64_t>(1, std::min<int64_t>((n + MT - 1) / MT, 152 * 32))); }
 
+// sum_{q in [b, e)} val[q] x[ci[q] * m + c], accumulated in q order (the plain
+// loop's rounding), with the index and value loads of four entries issued
+// before their gathers: the coarse levels have too few rows to hide a load chain
+// per entry, and the sum's order does not change.
+template <typename VT>
+__device__ __forceinline__ VT row_sum4(const int32_t* __restrict__ ci, const VT* __restrict__ val,
+                                       const VT* __restrict__ x, int b, int e, int m, int c, VT a) {
+  int q = b;
+  for (; q + 4 <= e; q += 4) {
+    const int32_t c0 = __ldg(ci + q), c1 = __ldg(ci + q + 1), c2 = __ldg(ci + q + 2), c3 = __ldg(ci + q + 3);
+    const VT v0 = __ldg(val + q), v1 = __ldg(val + q + 1), v2 = __ldg(val + q + 2), v3 = __ldg(val + q + 3);
+    const VT x0 = __ldg(x + int64_t(c0) * m + c), x1 = __ldg(x + int64_t(c1) * m + c);
+    const VT x2 = __ldg(x + int64_t(c2) * m + c), x3 = __ldg(x + int64_t(c3) * m + c);
+    a += v0 * x0;
+    a += v1 * x1;
+    a += v2 * x2;
+    a += v3 * x3;
+  }
+  for (; q < e; ++q) a += __ldg(val + q) * __ldg(x + int64_t(__ldg(ci + q)) * m + c);
+  return a;
+}
+
 // y[out(row)] = (acc ? y[out(row)] : 0) + (s ? s[row] r[row] : 0) + sum_j A[row, j] x[j],
 // out(row) = (row / nI) m + c0 + row % nI.
 template <typename VT>
@@ -36,9 +59,8 @@ __global__ void __launch_bounds__(MT) gen_spmv_kernel(const int32_t* __restrict_
   if (done && *done) return;
   for (int64_t row = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; row < nrows;
        row += int64_t(gridDim.x) * blockDim.x) {
-    VT a = VT(0);
     const int b = rp[row], e = rp[row + 1];
-    for (int t = b; t < e; ++t) a += val[t] * x[ci[t]];
+    VT a = row_sum4<VT>(ci, val, x, b, e, 1, 0, VT(0));
     if (s) a += s[row] * r[row];
     const int64_t o = nI == 1 && m == 1 ? row : (row / nI) * m + c0 + row % nI;
     y[o] = acc ? y[o] + a : a;
@@ -92,9 +114,8 @@ __global__ void __launch_bounds__(MT) mg_sweep(const int32_t* __restrict__ rp, c
   for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += int64_t(gridDim.x) * blockDim.x) {
     const int64_t i = t / m;
     const int c = int(t - i * m);
-    VT ax = VT(0);
     const int b = rp[i], e = rp[i + 1];
-    for (int q = b; q < e; ++q) ax += val[q] * xi[int64_t(ci[q]) * m + c];
+    const VT ax = row_sum4<VT>(ci, val, xi, b, e, m, c, VT(0));
     const VT res = r[t] - ax;
     xo[t] = mode == 0 ? xi[t] + dinv[i] * res : res;
   }
@@ -110,9 +131,8 @@ __global__ void __launch_bounds__(MT) mg_spmm(const int32_t* __restrict__ rp, co
   for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += int64_t(gridDim.x) * blockDim.x) {
     const int64_t i = t / m;
     const int c = int(t - i * m);
-    VT a = VT(0);
     const int b = rp[i], e = rp[i + 1];
-    for (int q = b; q < e; ++q) a += val[q] * x[int64_t(ci[q]) * m + c];
+    const VT a = row_sum4<VT>(ci, val, x, b, e, m, c, VT(0));
     y[t] = acc ? y[t] + a : a;
   }
 }
@@ -226,7 +246,10 @@ void gen_spmv(const DCsr& A, const VT* x, VT* y, const VT* s, const VT* r, int a
   if (A.nrows == 0) return;
   const double avg = double(A.nnz) / double(A.nrows);
   auto blocks = [&](int W) { return grid_for_n(A.nrows * W); };
-  if (avg <= 8) {
+  // FP64 rows stay on one thread longer: a lane split adds FP64 shuffle sums,
+  // and the FP64 pipe, not memory, bounds these products on GB300
+  const double one_thread = std::is_same<VT, double>::value ? 32 : 8;
+  if (avg <= one_thread) {
     gen_spmv_kernel<VT><<<grid_for_n(A.nrows), MT, 0, st>>>(A.rp, A.ci, A.val<VT>(), x, y, A.nrows, s, r, acc, nI, m,
                                                             c0, done);
   } else if (avg <= 24) {

@@ -138,11 +138,18 @@ fq_status fq_source_assemble(fq_ctx* ctx, fq_mesh* m, int grade, fq_bc bc, int d
   std::vector<double> wlam(pts.size());
   for (int q = 0; q < nq; ++q)
     for (int v = 0; v <= n; ++v) wlam[q * (n + 1) + v] = w[q] * pts[q * (n + 1) + v];
-  DevBuf rule, contrib;
-  FQ_TRY(rule.alloc(ctx, wlam.size() * sizeof(double)));
-  FQ_CUDA(ctx, cudaMemcpyAsync(rule.p, wlam.data(), wlam.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (m->source_degree != degree) {
+    m->source_degree = -1;
+    FQ_TRY(m->source_rule.alloc(ctx, wlam.size() * sizeof(double)));
+    FQ_CUDA(ctx, cudaMemcpyAsync(m->source_rule.p, wlam.data(), wlam.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                 st));
+    m->source_degree = degree;
+  }
   const int lf = cbinom(n + 1, grade + 1);
-  FQ_TRY(contrib.alloc(ctx, std::max<int64_t>(m->ncells * lf, 1) * sizeof(df64)));
+  const size_t slot_bytes = size_t(std::max<int64_t>(m->ncells * lf, 1)) * sizeof(df64);
+  if (m->source_slots.bytes < slot_bytes) FQ_TRY(m->source_slots.alloc(ctx, slot_bytes));
+  DevBuf& rule = m->source_rule;
+  DevBuf& contrib = m->source_slots;
 
   SourceArgs a;
   a.ncells = m->ncells;
