@@ -658,6 +658,157 @@ def run_batch(args):
     print(json.dumps(out))
 
 
+def run_next(args):
+    """The rows after the headline path on the 3D 32^3 mesh: the matrix-free
+    operator against the assembled SpMV, the right-hand side (the source load
+    and the de Rham map) and the Maxwell leapfrog. Each is timed with CUDA
+    events on the library's stream around the public call (median of
+    --steps, L2 flushed before each), and the host restatement in oracle/ is
+    timed once on the same input."""
+    import torch
+
+    import formoniq_gb300 as fq
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = fq.Context(0, stream=stream.cuda_stream)
+    peak, peak_src = measured_peaks()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def timed(fn, steps):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        ts = []
+        for _ in range(steps):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.median(ts)
+
+    def host_time(fn):
+        t0 = time.perf_counter()
+        r = fn()
+        return (time.perf_counter() - t0) * 1e3, r
+
+    def lattice(dim, nb, seed):
+        """Vertex coordinates of the Kuhn cube (vertex id = sum_a c_a (N+1)^a,
+        axis 0 fastest) with a seeded uniform +-0.1h jitter of every coordinate."""
+        idx = np.arange((nb + 1) ** dim)
+        c = np.stack([(idx // (nb + 1) ** a) % (nb + 1) for a in range(dim)], 1).astype(np.float64) / nb
+        return c + JITTER / nb * np.random.default_rng(seed).uniform(-1.0, 1.0, c.shape)
+
+    dim, nb = DIM, NBOX
+    coords = lattice(dim, nb, SEED)
+    mesh = fq.Mesh.kuhn_cube(ctx, dim, nb)
+    mesh.lengths_from_coords(coords)
+    lengths = mesh.lengths_sq()
+    cx = oracle.Complex.from_cells(oracle.kuhn_cells(dim, nb))  # the host restatement's complex (CPU baseline)
+    dcoords = torch.tensor(coords, device="cuda")
+    nc, n0, n1 = mesh.ncells(), mesh.nsimplices(0), mesh.nsimplices(1)
+    rng = np.random.default_rng(SEED)
+    steps = max(3, min(args.steps, 50))
+    out = {"metric": "throughput of the rows after the headline path", "workload":
+           f"kuhn 3D {nb}^3 ({nc} tets), coordinates jittered 0.1h seed {SEED}", "data": "synthetic",
+           "timing": "CUDA events on the library stream around the public call, median, L2 flushed before each",
+           "peak_hbm_gbs": peak, "peak_source": peak_src}
+
+    # matrix-free mass (ElementOperator) against the assembled M_1 (SpMV)
+    x = torch.tensor(rng.standard_normal(n1), device="cuda")
+    y = torch.empty_like(x)
+    op = fq.ElementOperator(mesh, fq.FQ_MASS, 1)
+    m1 = fq.WhitneyComplex(mesh).mass(1)
+    ms_op = timed(lambda: op.apply(x.data_ptr(), y.data_ptr()), steps)
+    ms_spmv = timed(lambda: ctx.check(ctx.L.fq_spmv(ctx.h, m1.h, fq._P(x.data_ptr()), fq._P(y.data_ptr()))),
+                    steps)
+    lf_, lr_ = comb(dim + 1, 2), comb(dim + 1, 2)
+    op_bytes = n1 * 8 + nc * (lf_ + lr_) * 4 + n1 * 8 + nc * lr_ * 8 * 2 + nc * lr_ * 4 + (n1 + 1) * 4 + n1 * 8
+    spmv_bytes = m1.nnz * 12 + (n1 + 1) * 4 + 2 * n1 * 8
+    m1_host = m1.to_scipy()
+    xh = x.cpu().numpy()
+    cpu_ms, _ = host_time(lambda: m1_host @ xh)
+    out["matfree_mass_1"] = {
+        "unit": "applies/s", "dofs": n1, "matrix_free": {"ms": ms_op, "per_s": 1e3 / ms_op,
+                                                          "algorithmic_bytes": op_bytes,
+                                                          "GBps": op_bytes / (ms_op * 1e6)},
+        "assembled_spmv": {"ms": ms_spmv, "per_s": 1e3 / ms_spmv, "algorithmic_bytes": spmv_bytes,
+                           "GBps": spmv_bytes / (ms_spmv * 1e6), "frac_of_peak": spmv_bytes / (ms_spmv * 1e6) / peak},
+        "cpu_baseline": {"ms": cpu_ms, "kind": "port", "cores": 1, "sample": "scipy CSR matvec of the same M_1"}}
+    op.close()
+    m1.close()
+
+    # source load: SourceForm, k = 1, degree-3 rule, reference-frame values
+    for k, degree in ((1, 3), (2, 3)):
+        nq = ctx.L.fq_source_npoints(dim, degree)
+        vals_h = rng.standard_normal((nc, nq, comb(dim, k)))
+        vals = torch.tensor(vals_h, device="cuda")
+        ms_src = timed(lambda: fq.source_form(mesh, k, vals, degree), steps)
+        nk = mesh.nsimplices(k)
+        lf = comb(dim + 1, k + 1)
+        src_bytes = vals_h.nbytes + nc * comb(dim + 1, 2) * 4 + n1 * 8 + nc * lf * (8 + 4) + nk * (4 + 8)
+        cpu_ms, _ = host_time(lambda: oracle.source_form(cx, lengths, k, vals_h, degree))
+        out[f"source_load_{k}"] = {"unit": "cells/s", "quadrature_degree": degree, "nodes": nq, "ms": ms_src,
+                                   "per_s": nc / (ms_src * 1e-3), "algorithmic_bytes": src_bytes,
+                                   "GBps": src_bytes / (ms_src * 1e6),
+                                   "cpu_baseline": {"ms": cpu_ms, "per_s": nc / (cpu_ms * 1e-3), "kind": "port",
+                                                    "cores": 1, "sample": "oracle.source_form, numpy, same values"}}
+
+    # de Rham map of a smooth 1-form, degree-3 rule (nodes, field on the device, reduction)
+    def field_t(p):
+        return torch.stack([torch.sin(p[:, 0]) * p[:, 1], p[:, 2] ** 2, torch.cos(p[:, 1]) - p[:, 0]], 1)
+
+    def field_n(p):
+        return np.stack([np.sin(p[:, 0]) * p[:, 1], p[:, 2] ** 2, np.cos(p[:, 1]) - p[:, 0]], 1)
+
+    ms_dr = timed(lambda: fq.derham_map(mesh, dcoords, 1, field_t, 3), steps)
+    cpu_ms, _ = host_time(lambda: oracle.derham_map(cx, coords, 1, field_n, 3))
+    out["derham_map_1"] = {"unit": "edges/s", "edges": n1, "quadrature_degree": 3, "ms": ms_dr,
+                           "per_s": n1 / (ms_dr * 1e-3),
+                           "cpu_baseline": {"ms": cpu_ms, "per_s": n1 / (cpu_ms * 1e-3), "kind": "port", "cores": 1,
+                                            "sample": "oracle.derham_map, numpy, same field"}}
+
+    # Maxwell leapfrog on the full complex of a 16^3 mesh (all grades, CG mass blocks)
+    nbl = 16
+    meshl = fq.Mesh.kuhn_cube(ctx, dim, nbl)
+    meshl.lengths_from_coords(lattice(dim, nbl, SEED + 1))
+    ll = meshl.lengths_sq()
+    cxl = oracle.Complex.from_cells(oracle.kuhn_cells(dim, nbl))
+    dt = 0.05 / nbl
+    lf = fq.Leapfrog(meshl, fq.FQ_ABSOLUTE, dt)
+    off = lf.offsets()
+    y0 = torch.tensor(rng.standard_normal(int(off[-1])), device="cuda")
+    nsteps = 10
+    ms_lf = timed(lambda: lf.step(y0, nsteps), max(3, steps // 10))
+    owc = oracle.WhitneyComplex(cxl, ll)
+    _, _, olf = oracle.leapfrog_for(owc, dt)
+    yh = y0.cpu().numpy()
+
+    def cpu_steps():
+        y = yh
+        for _ in range(2):
+            y = olf.step(y)
+        return y
+
+    cpu_ms, _ = host_time(cpu_steps)
+    out["leapfrog_16"] = {"unit": "steps/s", "mesh": f"kuhn 3D {nbl}^3", "dofs": int(off[-1]), "dt": dt,
+                          "ms_per_step": ms_lf / nsteps, "per_s": nsteps / (ms_lf * 1e-3),
+                          "inner_cg_iterations_last": lf.inner_iters,
+                          "cpu_baseline": {"ms_per_step": cpu_ms / 2, "per_s": 2 / (cpu_ms * 1e-3), "kind": "port",
+                                           "cores": 1, "sample": "oracle.Leapfrog (SuperLU mass factors), 2 steps"}}
+    lf.close()
+    meshl.close()
+    mesh.close()
+    ctx.close()
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -671,9 +822,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-solve", action="store_true", help="skip the solve phase (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer phase (profiling runs)")
-    ap.add_argument("--workload", default="assembly", choices=["assembly", "precision", "serve", "batch"],
+    ap.add_argument("--workload", default="assembly", choices=["assembly", "precision", "serve", "batch", "next"],
                     help="assembly: the headline line; precision: the 4D FP32-with-refinement study; "
-                         "serve: the request stream, served vs plain")
+                         "serve: the request stream, served vs plain; batch: many meshes in one launch set; "
+                         "next: matrix-free operator, source load, de Rham map, leapfrog")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--meshes", type=int, default=512, help="batch: number of meshes")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate (requests/s)")
@@ -689,6 +841,8 @@ def main():
         run_serve(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "next":
+        run_next(args)
     else:
         run_ours(args)
 

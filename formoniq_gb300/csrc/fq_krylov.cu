@@ -70,10 +70,40 @@ __device__ __forceinline__ double reduce_partials(const double* part, int np, do
   return block_sum(v, sh);
 }
 
-// The scalar recurrences (FP64 divisions and square roots, each a sequence of
-// FP64 instructions) run on one thread per block and reach the others through
-// shared memory: repeated by every thread of a full grid they cost more on
-// GB300's narrow FP64 pipe than the vector work of the kernel.
+// Per-iteration scalars of the Krylov loops and the arrival counters of their
+// two grid reductions (device memory next to the two solver states).
+struct IterScalars {
+  double alfa, c2;        // MINRES, after A
+  double ce, cd, cg, cp;  // MINRES, after the (preconditioned) product r2.y
+  double alpha, beta;     // CG
+  unsigned count[2];
+  unsigned pad[2];
+};
+
+// A grid reduction without a second kernel and without every block repeating
+// it: each block leaves its partial (thread 0, before the call), and the block
+// that arrives last - told by a device-scope counter after a fence - reduces all
+// partials and resets the counter for the next iteration. It sums in index
+// order with reduce_partials' per-thread stride, so the total is bit-identical
+// to the one every block used to recompute. The scalar recurrence (FP64
+// divisions and square roots) then runs once, on that block's thread 0:
+// repeated by every thread of a full grid it cost more on GB300's narrow FP64
+// pipe than the vector work.
+__device__ __forceinline__ bool arrive_last(unsigned* counter) {
+  __shared__ unsigned ticket;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    ticket = atomicAdd(counter, 1u);
+  }
+  __syncthreads();
+  return ticket == gridDim.x - 1;
+}
+
+__device__ __forceinline__ double reduce_arrived(const double* part, int np, double* sh) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) v += __ldcg(part + i);
+  return block_sum(v, sh);
+}
 
 // Sub-warp CSR row product: W lanes per row, fixed lane order.
 template <int W, typename VT>
@@ -291,10 +321,83 @@ __global__ void minres_init_state(SolverState* s0, SolverState* s1, const double
   }
 }
 
-// A: v = y / beta, z = A v - (beta/oldb) r1, partial v.z
+// The MINRES rotation (krylov.rs:113-211) on one thread: the next state into
+// *out and the w/x update coefficients into X.
+__device__ void minres_rotate(const SolverState& in, double alfa, double beta_sq, double rtol, long long max_iters,
+                              IterScalars* X, SolverState* out) {
+  SolverState s = in;
+  const double eps = DBL_EPSILON;
+  const double oldb = s.beta;
+  const double beta = sqrt(fmax(beta_sq, 0.0));
+  const double oldeps = s.epsln;
+  const double delta = s.cs * s.dbar + s.sn * alfa;
+  const double gbar = s.sn * s.dbar - s.cs * alfa;
+  const double epsln = s.sn * beta;
+  const double dbar = -s.cs * beta;
+  const double gamma = fmax(sqrt(gbar * gbar + beta * beta), eps);
+  const double cs = gbar / gamma;
+  const double sn = beta / gamma;
+  const double phi = cs * s.phibar;
+  const double phibar = s.phibar * sn;
+  X->ce = -oldeps;
+  X->cd = -delta;
+  X->cg = 1.0 / gamma;
+  X->cp = phi;
+  s.oldb = oldb;
+  s.beta = beta;
+  s.epsln = epsln;
+  s.dbar = dbar;
+  s.cs = cs;
+  s.sn = sn;
+  s.phibar = phibar;
+  s.alfa = alfa;
+  s.rbeta = 1.0 / beta;
+  s.c1 = -beta / oldb;
+  s.iters += 1;
+  s.residual = phibar / s.beta1;
+  if (!isfinite(s.residual)) {
+    s.breakdown = 1;
+    s.done = 1;
+  }
+  if (s.residual <= rtol) {
+    s.converged = 1;
+    s.done = 1;
+  }
+  if (s.iters >= max_iters) s.done = 1;
+  *out = s;
+}
+
+// The last block of A: alfa = v.z and the coefficient of B.
+__device__ __forceinline__ void minres_after_a(double acc, double* partA, const SolverState* S, IterScalars* X,
+                                               double* sh) {
+  if (threadIdx.x == 0) partA[blockIdx.x] = acc;
+  if (arrive_last(&X->count[0])) {
+    const double alfa = reduce_arrived(partA, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      X->alfa = alfa;
+      X->c2 = -alfa / S->beta;
+      X->count[0] = 0u;
+    }
+  }
+}
+
+// The last block of the kernel that forms r2.y: the rotation.
+__device__ __forceinline__ void minres_after_b(double acc, double* partB, const SolverState* S, IterScalars* X,
+                                               SolverState* Sout, double rtol, long long max_iters, double* sh) {
+  if (threadIdx.x == 0) partB[blockIdx.x] = acc;
+  if (arrive_last(&X->count[1])) {
+    const double beta_sq = reduce_arrived(partB, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      minres_rotate(*S, X->alfa, beta_sq, rtol, max_iters, X, Sout);
+      X->count[1] = 0u;
+    }
+  }
+}
+
+// A: v = y / beta, z = A v - (beta/oldb) r1, alfa = v.z
 template <int W, typename VT>
 __global__ void __launch_bounds__(KT) minres_a(const int32_t* rp, const int32_t* ci, const VT* val, MinresVecs<VT> m,
-                                               const SolverState* __restrict__ S, int64_t n) {
+                                               const SolverState* __restrict__ S, IterScalars* X, int64_t n) {
   __shared__ double sh[32];
   if (S->done) return;
   const VT rbt = VT(S->rbeta), c1t = VT(S->c1);
@@ -314,14 +417,14 @@ __global__ void __launch_bounds__(KT) minres_a(const int32_t* rp, const int32_t*
     }
   }
   acc = block_sum(acc, sh);
-  if (threadIdx.x == 0) m.partA[blockIdx.x] = acc;
+  minres_after_a(acc, m.partA, S, X, sh);
 }
 
 // A for an FP64 operator on the FP32 pipe (values and y as float-float pairs).
 template <int W>
 __global__ void __launch_bounds__(KT) minres_a_split(const int32_t* rp, const int32_t* ci, const df64* val,
                                                      MinresVecs<double> m, const SolverState* __restrict__ S,
-                                                     int64_t n) {
+                                                     IterScalars* X, int64_t n) {
   __shared__ double sh[32];
   if (S->done) return;
   const double rbt = S->rbeta, c1t = S->c1;
@@ -341,19 +444,17 @@ __global__ void __launch_bounds__(KT) minres_a_split(const int32_t* rp, const in
     }
   }
   acc = block_sum(acc, sh);
-  if (threadIdx.x == 0) m.partA[blockIdx.x] = acc;
+  minres_after_a(acc, m.partA, S, X, sh);
 }
 
-// B: alfa; z -= (alfa/beta) r2; r1 = r2; r2 = z; y = P r2; partial r2.y
+// B: z -= (alfa/beta) r2; r1 = r2; r2 = z; y = P r2 (diagonal P); r2.y and the rotation
 template <typename VT>
-__global__ void __launch_bounds__(KT) minres_b(MinresVecs<VT> m, SolverState* __restrict__ S, int npa, int64_t n) {
+__global__ void __launch_bounds__(KT) minres_b(MinresVecs<VT> m, const SolverState* __restrict__ S, IterScalars* X,
+                                               SolverState* __restrict__ Sout, double rtol, long long max_iters,
+                                               int64_t n) {
   __shared__ double sh[32];
-  __shared__ double coef;
   if (S->done) return;
-  const double alfa = reduce_partials(m.partA, npa, sh);
-  if (threadIdx.x == 0) coef = -alfa / S->beta;
-  __syncthreads();
-  const VT c2 = VT(coef);
+  const VT c2 = VT(X->c2);
   double acc = 0.0;
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
     const VT r2 = m.r2[i];
@@ -368,9 +469,28 @@ __global__ void __launch_bounds__(KT) minres_b(MinresVecs<VT> m, SolverState* __
       acc += double(zi) * double(yi);
     }
   }
-  if (m.external) return;  // y = P r2 and its partials come from the preconditioner
+  if (m.external) return;  // y = P r2 and r2.y come from the preconditioner and minres_dot
   acc = block_sum(acc, sh);
-  if (threadIdx.x == 0) m.partB[blockIdx.x] = acc;
+  minres_after_b(acc, m.partB, S, X, Sout, rtol, max_iters, sh);
+}
+
+// r2.y after an external preconditioner wrote y = P r2 (and y's float pairs),
+// then the rotation.
+template <typename VT>
+__global__ void __launch_bounds__(KT) minres_dot(MinresVecs<VT> m, const SolverState* __restrict__ S,
+                                                 IterScalars* X, SolverState* __restrict__ Sout, double rtol,
+                                                 long long max_iters, int64_t n) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  double acc = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const VT yi = m.y[i];
+    acc += double(m.r2[i]) * double(yi);
+    if constexpr (std::is_same<VT, double>::value)
+      if (m.y2) m.y2[i] = df64(yi);
+  }
+  acc = block_sum(acc, sh);
+  minres_after_b(acc, m.partB, S, X, Sout, rtol, max_iters, sh);
 }
 
 // Partials of a.b (after an external preconditioner wrote b = P a).
@@ -390,65 +510,17 @@ __global__ void __launch_bounds__(KT) dot_partials(const VT* __restrict__ a, con
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
-// C: rotation (identical in every block), w/x update, state -> the other slot
+// C: the w/x update with the rotation's coefficients; a finished loop carries
+// its state to the other slot
 template <typename VT>
 __global__ void __launch_bounds__(KT) minres_c(MinresVecs<VT> m, const SolverState* __restrict__ Sin,
-                                               SolverState* __restrict__ Sout, int npa, int npb, double rtol,
-                                               long long max_iters, int64_t n) {
-  __shared__ double sh[32];
+                                               SolverState* __restrict__ Sout, const IterScalars* __restrict__ X,
+                                               int64_t n) {
   if (Sin->done) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *Sout = *Sin;
     return;
   }
-  __shared__ double coef[4];
-  const double alfa = reduce_partials(m.partA, npa, sh);
-  const double beta_sq = reduce_partials(m.partB, npb, sh);
-  if (threadIdx.x == 0) {
-    SolverState s = *Sin;
-    const double eps = DBL_EPSILON;
-    const double oldb = s.beta;
-    const double beta = sqrt(fmax(beta_sq, 0.0));
-    const double oldeps = s.epsln;
-    const double delta = s.cs * s.dbar + s.sn * alfa;
-    const double gbar = s.sn * s.dbar - s.cs * alfa;
-    const double epsln = s.sn * beta;
-    const double dbar = -s.cs * beta;
-    const double gamma = fmax(sqrt(gbar * gbar + beta * beta), eps);
-    const double cs = gbar / gamma;
-    const double sn = beta / gamma;
-    const double phi = cs * s.phibar;
-    const double phibar = s.phibar * sn;
-    coef[0] = -oldeps;
-    coef[1] = -delta;
-    coef[2] = 1.0 / gamma;
-    coef[3] = phi;
-    if (blockIdx.x == 0) {
-      s.oldb = oldb;
-      s.beta = beta;
-      s.epsln = epsln;
-      s.dbar = dbar;
-      s.cs = cs;
-      s.sn = sn;
-      s.phibar = phibar;
-      s.alfa = alfa;
-      s.rbeta = 1.0 / beta;
-      s.c1 = -beta / oldb;
-      s.iters += 1;
-      s.residual = phibar / s.beta1;
-      if (!isfinite(s.residual)) {
-        s.breakdown = 1;
-        s.done = 1;
-      }
-      if (s.residual <= rtol) {
-        s.converged = 1;
-        s.done = 1;
-      }
-      if (s.iters >= max_iters) s.done = 1;
-      *Sout = s;
-    }
-  }
-  __syncthreads();
-  const VT ce = VT(coef[0]), cd = VT(coef[1]), cg = VT(coef[2]), cp = VT(coef[3]);
+  const VT ce = VT(X->ce), cd = VT(X->cd), cg = VT(X->cg), cp = VT(X->cp);
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
     const VT w = m.w[i];
     VT wn = m.v[i] + ce * m.w2[i];
@@ -521,10 +593,58 @@ __global__ void cg_init_state(SolverState* s0, SolverState* s1, const double* pa
   }
 }
 
-// A: ap = A p, partial p.ap
+// CG's scalar step on one thread: beta and the next state.
+__device__ void cg_advance(const SolverState& in, double rz_next, double rr, double rtol, long long max_iters,
+                           IterScalars* X, SolverState* out) {
+  SolverState s = in;
+  X->beta = rz_next / in.rz;
+  s.rz = rz_next;
+  s.iters += 1;
+  s.residual = sqrt(rr) / s.bnorm;
+  if (!isfinite(s.residual)) {
+    s.breakdown = 1;
+    s.done = 1;
+  }
+  if (s.residual <= rtol) {
+    s.converged = 1;
+    s.done = 1;
+  }
+  if (s.iters >= max_iters) s.done = 1;
+  *out = s;
+}
+
+// The last block of A: alpha = rz / p.ap.
+__device__ __forceinline__ void cg_after_a(double acc, double* partA, const SolverState* S, IterScalars* X,
+                                           double* sh) {
+  if (threadIdx.x == 0) partA[blockIdx.x] = acc;
+  if (arrive_last(&X->count[0])) {
+    const double pap = reduce_arrived(partA, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      X->alpha = S->rz / pap;
+      X->count[0] = 0u;
+    }
+  }
+}
+
+// The last block of the kernel that forms r.z (r.r from cg_b, npc partials):
+// beta and the next state.
+__device__ __forceinline__ void cg_after_b(const double* partB, const double* partC, int npc, const SolverState* S,
+                                           IterScalars* X, SolverState* Sout, double rtol, long long max_iters,
+                                           double* sh) {
+  if (arrive_last(&X->count[1])) {
+    const double rz_next = reduce_arrived(partB, gridDim.x, sh);
+    const double rr = reduce_arrived(partC, npc, sh);
+    if (threadIdx.x == 0) {
+      cg_advance(*S, rz_next, rr, rtol, max_iters, X, Sout);
+      X->count[1] = 0u;
+    }
+  }
+}
+
+// A: ap = A p, alpha
 template <int W, typename VT>
 __global__ void __launch_bounds__(KT) cg_a(const int32_t* rp, const int32_t* ci, const VT* val, CgVecs<VT> c,
-                                           const SolverState* __restrict__ S, int64_t n) {
+                                           const SolverState* __restrict__ S, IterScalars* X, int64_t n) {
   __shared__ double sh[32];
   if (S->done) return;
   const int lane = threadIdx.x % W;
@@ -540,13 +660,14 @@ __global__ void __launch_bounds__(KT) cg_a(const int32_t* rp, const int32_t* ci,
     }
   }
   acc = block_sum(acc, sh);
-  if (threadIdx.x == 0) c.partA[blockIdx.x] = acc;
+  cg_after_a(acc, c.partA, S, X, sh);
 }
 
 // A for an FP64 operator on the FP32 pipe (values and p as float-float pairs).
 template <int W>
 __global__ void __launch_bounds__(KT) cg_a_split(const int32_t* rp, const int32_t* ci, const df64* val,
-                                                 CgVecs<double> c, const SolverState* __restrict__ S, int64_t n) {
+                                                 CgVecs<double> c, const SolverState* __restrict__ S, IterScalars* X,
+                                                 int64_t n) {
   __shared__ double sh[32];
   if (S->done) return;
   const int lane = threadIdx.x % W;
@@ -563,19 +684,29 @@ __global__ void __launch_bounds__(KT) cg_a_split(const int32_t* rp, const int32_
     }
   }
   acc = block_sum(acc, sh);
-  if (threadIdx.x == 0) c.partA[blockIdx.x] = acc;
+  cg_after_a(acc, c.partA, S, X, sh);
 }
 
-// B: alpha = rz / p.ap; x += alpha p; r -= alpha ap; z = P r; partials r.z, r.r
-template <typename VT>
-__global__ void __launch_bounds__(KT) cg_b(CgVecs<VT> c, const SolverState* __restrict__ S, int npa, int64_t n) {
+// p.ap after an operator hook wrote ap = A p (matrix-free), then alpha.
+__global__ void __launch_bounds__(KT) cg_pap(CgVecs<double> c, const SolverState* __restrict__ S, IterScalars* X,
+                                             int64_t n) {
   __shared__ double sh[32];
-  __shared__ double coef;
   if (S->done) return;
-  const double pap = reduce_partials(c.partA, npa, sh);
-  if (threadIdx.x == 0) coef = S->rz / pap;
-  __syncthreads();
-  const double alpha = coef;
+  double acc = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    acc += c.p[i] * c.ap[i];
+  acc = block_sum(acc, sh);
+  cg_after_a(acc, c.partA, S, X, sh);
+}
+
+// B: x += alpha p; r -= alpha ap; z = P r (diagonal P); r.z, r.r and the scalar step
+template <typename VT>
+__global__ void __launch_bounds__(KT) cg_b(CgVecs<VT> c, const SolverState* __restrict__ S, IterScalars* X,
+                                           SolverState* __restrict__ Sout, double rtol, long long max_iters,
+                                           int64_t n) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  const double alpha = X->alpha;
   const VT at = VT(alpha), mat = VT(-alpha);
   double rz = 0.0, rr = 0.0;
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
@@ -595,6 +726,24 @@ __global__ void __launch_bounds__(KT) cg_b(CgVecs<VT> c, const SolverState* __re
     if (!c.external) c.partB[blockIdx.x] = rz;
     c.partC[blockIdx.x] = rr;
   }
+  if (c.external) return;  // z = P r and r.z come from the preconditioner and cg_dot
+  cg_after_b(c.partB, c.partC, gridDim.x, S, X, Sout, rtol, max_iters, sh);
+}
+
+// r.z after an external preconditioner wrote z = P r, then the scalar step
+// (r.r from cg_b's npc partials).
+template <typename VT>
+__global__ void __launch_bounds__(KT) cg_dot(CgVecs<VT> c, const SolverState* __restrict__ S, IterScalars* X,
+                                             SolverState* __restrict__ Sout, int npc, double rtol,
+                                             long long max_iters, int64_t n) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  double acc = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    acc += double(c.r[i]) * double(c.z[i]);
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) c.partB[blockIdx.x] = acc;
+  cg_after_b(c.partB, c.partC, npc, S, X, Sout, rtol, max_iters, sh);
 }
 
 // External preconditioner, first step: p = z (= P b), partials of b.z.
@@ -613,43 +762,21 @@ __global__ void __launch_bounds__(KT) cg_init_p(CgVecs<VT> c, int64_t n) {
   if (threadIdx.x == 0) c.partB[blockIdx.x] = rz;
 }
 
-// C: beta = rz_next / rz; p = beta p + z; state
+// C: p = beta p + z; a finished loop carries its state to the other slot
 template <typename VT>
 __global__ void __launch_bounds__(KT) cg_c(CgVecs<VT> c, const SolverState* __restrict__ Sin,
-                                           SolverState* __restrict__ Sout, int npb, double rtol, long long max_iters,
+                                           SolverState* __restrict__ Sout, const IterScalars* __restrict__ X,
                                            int64_t n) {
-  __shared__ double sh[32];
   if (Sin->done) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *Sout = *Sin;
     return;
   }
-  __shared__ double coef;
-  const double rz_next = reduce_partials(c.partB, npb, sh);
-  const double rr = reduce_partials(c.partC, npb, sh);
-  if (threadIdx.x == 0) coef = rz_next / Sin->rz;
-  __syncthreads();
-  const VT bt = VT(coef);
+  const VT bt = VT(X->beta);
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
     const VT pi = c.p[i] * bt + c.z[i];
     c.p[i] = pi;
     if constexpr (std::is_same<VT, double>::value)
       if (c.p2) c.p2[i] = df64(pi);
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    SolverState s = *Sin;
-    s.rz = rz_next;
-    s.iters += 1;
-    s.residual = sqrt(rr) / s.bnorm;
-    if (!isfinite(s.residual)) {
-      s.breakdown = 1;
-      s.done = 1;
-    }
-    if (s.residual <= rtol) {
-      s.converged = 1;
-      s.done = 1;
-    }
-    if (s.iters >= max_iters) s.done = 1;
-    *Sout = s;
   }
 }
 
@@ -759,7 +886,7 @@ fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT
   const size_t vb = size_t(std::max<int64_t>(n, 1)) * sizeof(VT);
   FQ_TRY(vecs.alloc(ctx, vb * 7));
   FQ_TRY(parts.alloc(ctx, 2 * PBLOCKS * sizeof(double)));
-  FQ_TRY(state.alloc(ctx, 2 * sizeof(SolverState)));
+  FQ_TRY(state.alloc(ctx, 2 * sizeof(SolverState) + sizeof(IterScalars)));
   MinresVecs<VT> m;
   char* base = vecs.as<char>();
   m.x = x;
@@ -777,6 +904,8 @@ fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT
   m.partB = parts.as<double>() + PBLOCKS;
   m.y2 = nullptr;
   SolverState* S = state.as<SolverState>();
+  IterScalars* X = reinterpret_cast<IterScalars*>(S + 2);  // per-iteration scalars, reduction counters at 0
+  FQ_CUDA(ctx, cudaMemsetAsync(X, 0, sizeof(IterScalars), st));
   // FP64: the product runs on float-float pairs of the values and of y
   constexpr bool split = std::is_same<VT, double>::value;
   DevBuf val2, y2;
@@ -809,42 +938,42 @@ fq_status minres_run(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const VT
         const df64* v2 = val2.as<df64>();
         switch (W) {
           case 4:
-            minres_a_split<4><<<ga, KT, 0, st>>>(rp, ci, v2, m, S + cur, n);
+            minres_a_split<4><<<ga, KT, 0, st>>>(rp, ci, v2, m, S + cur, X, n);
             break;
           case 8:
-            minres_a_split<8><<<ga, KT, 0, st>>>(rp, ci, v2, m, S + cur, n);
+            minres_a_split<8><<<ga, KT, 0, st>>>(rp, ci, v2, m, S + cur, X, n);
             break;
           case 16:
-            minres_a_split<16><<<ga, KT, 0, st>>>(rp, ci, v2, m, S + cur, n);
+            minres_a_split<16><<<ga, KT, 0, st>>>(rp, ci, v2, m, S + cur, X, n);
             break;
           default:
-            minres_a_split<32><<<ga, KT, 0, st>>>(rp, ci, v2, m, S + cur, n);
+            minres_a_split<32><<<ga, KT, 0, st>>>(rp, ci, v2, m, S + cur, X, n);
             break;
         }
       }
     } else {
       switch (W) {
         case 4:
-          minres_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+          minres_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, X, n);
           break;
         case 8:
-          minres_a<8, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+          minres_a<8, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, X, n);
           break;
         case 16:
-          minres_a<16, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+          minres_a<16, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, X, n);
           break;
         default:
-          minres_a<32, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, n);
+          minres_a<32, VT><<<ga, KT, 0, st>>>(rp, ci, val, m, S + cur, X, n);
           break;
       }
     }
-    minres_b<VT><<<gv, KT, 0, st>>>(m, S + cur, ga, n);
+    minres_b<VT><<<gv, KT, 0, st>>>(m, S + cur, X, S + (1 - cur), rtol, (long long)max_iters, n);
     if (pc) {
       const int* done = &(S + cur)->done;
       hx_apply<VT>(*pc, m.r2, m.y, done, st);
-      dot_partials<VT><<<gv, KT, 0, st>>>(m.r2, m.y, m.partB, n, done, m.y2);
+      minres_dot<VT><<<gv, KT, 0, st>>>(m, S + cur, X, S + (1 - cur), rtol, (long long)max_iters, n);
     }
-    minres_c<VT><<<gv, KT, 0, st>>>(m, S + cur, S + (1 - cur), ga, gv, rtol, (long long)max_iters, n);
+    minres_c<VT><<<gv, KT, 0, st>>>(m, S + cur, S + (1 - cur), X, n);
   };
   // a preconditioned iteration costs more: poll more often so fewer finished
   // iterations are queued past convergence
@@ -867,7 +996,7 @@ static fq_status cg_impl(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, cons
   const size_t vb = size_t(std::max<int64_t>(n, 1)) * sizeof(VT);
   FQ_TRY(vecs.alloc(ctx, vb * 4));
   FQ_TRY(parts.alloc(ctx, 3 * PBLOCKS * sizeof(double)));
-  FQ_TRY(state.alloc(ctx, 2 * sizeof(SolverState)));
+  FQ_TRY(state.alloc(ctx, 2 * sizeof(SolverState) + sizeof(IterScalars)));
   CgVecs<VT> c;
   char* base = vecs.as<char>();
   c.x = x;
@@ -883,6 +1012,8 @@ static fq_status cg_impl(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, cons
   c.partC = parts.as<double>() + 2 * PBLOCKS;
   c.p2 = nullptr;
   SolverState* S = state.as<SolverState>();
+  IterScalars* X = reinterpret_cast<IterScalars*>(S + 2);  // per-iteration scalars, reduction counters at 0
+  FQ_CUDA(ctx, cudaMemsetAsync(X, 0, sizeof(IterScalars), st));
   // FP64 CSR operators: the product runs on float-float pairs of the values and of p
   constexpr bool split_type = std::is_same<VT, double>::value;
   const bool split = split_type && !hook;
@@ -914,47 +1045,47 @@ static fq_status cg_impl(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, cons
       if constexpr (std::is_same<VT, double>::value) {
         const int* done = &(S + cur)->done;
         hook->apply(hook->self, c.p, c.ap, done, st);
-        dot_partials<VT><<<ga, KT, 0, st>>>(c.p, c.ap, c.partA, n, done);
+        cg_pap<<<ga, KT, 0, st>>>(c, S + cur, X, n);
       }
     } else if (split) {
       if constexpr (split_type) {
         const df64* v2 = val2.as<df64>();
         switch (W) {
           case 4:
-            cg_a_split<4><<<ga, KT, 0, st>>>(rp, ci, v2, c, S + cur, n);
+            cg_a_split<4><<<ga, KT, 0, st>>>(rp, ci, v2, c, S + cur, X, n);
             break;
           case 8:
-            cg_a_split<8><<<ga, KT, 0, st>>>(rp, ci, v2, c, S + cur, n);
+            cg_a_split<8><<<ga, KT, 0, st>>>(rp, ci, v2, c, S + cur, X, n);
             break;
           case 16:
-            cg_a_split<16><<<ga, KT, 0, st>>>(rp, ci, v2, c, S + cur, n);
+            cg_a_split<16><<<ga, KT, 0, st>>>(rp, ci, v2, c, S + cur, X, n);
             break;
           default:
-            cg_a_split<32><<<ga, KT, 0, st>>>(rp, ci, v2, c, S + cur, n);
+            cg_a_split<32><<<ga, KT, 0, st>>>(rp, ci, v2, c, S + cur, X, n);
             break;
         }
       }
     } else switch (W) {
       case 4:
-        cg_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
+        cg_a<4, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, X, n);
         break;
       case 8:
-        cg_a<8, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
+        cg_a<8, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, X, n);
         break;
       case 16:
-        cg_a<16, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
+        cg_a<16, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, X, n);
         break;
       default:
-        cg_a<32, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, n);
+        cg_a<32, VT><<<ga, KT, 0, st>>>(rp, ci, val, c, S + cur, X, n);
         break;
     }
-    cg_b<VT><<<gv, KT, 0, st>>>(c, S + cur, ga, n);
+    cg_b<VT><<<gv, KT, 0, st>>>(c, S + cur, X, S + (1 - cur), rtol, (long long)max_iters, n);
     if (pc) {
       const int* done = &(S + cur)->done;
       hx_apply<VT>(*pc, c.r, c.z, done, st);
-      dot_partials<VT><<<gv, KT, 0, st>>>(c.r, c.z, c.partB, n, done);
+      cg_dot<VT><<<gv, KT, 0, st>>>(c, S + cur, X, S + (1 - cur), gv, rtol, (long long)max_iters, n);
     }
-    cg_c<VT><<<gv, KT, 0, st>>>(c, S + cur, S + (1 - cur), gv, rtol, (long long)max_iters, n);
+    cg_c<VT><<<gv, KT, 0, st>>>(c, S + cur, S + (1 - cur), X, n);
   };
   FQ_TRY(run_graph_loop(ctx, S, max_iters, iteration, &hs, pc ? 4 : 64));
   rep->iters = hs.iters;
