@@ -108,13 +108,30 @@ FQ_HDI float float_of(uint32_t u) {
 // 2^k for -126 <= k <= 127
 FQ_HDI float pow2f(int k) { return float_of(uint32_t(k + 127) << 23); }
 
+// The rare ranges of the conversions below (|exponent| > 60, subnormals, inf,
+// nan) take the conversion instructions, which run on the FP64 pipe. They stay
+// out of line: inlined, the compiler if-converts the short fallback and issues
+// its conversions for every value.
+#if defined(__CUDACC__)
+#define FQ_NOINLINE __noinline__
+#else
+#define FQ_NOINLINE __attribute__((noinline))
+#endif
+// (hi, lo) packed into one 64-bit word: returned in registers, no stack
+static FQ_HD FQ_NOINLINE uint64_t split_rare(double d) {
+  const float hi = f_from_double(d);
+  const float lo = f_from_double(d - double(hi));
+  return (uint64_t(bits_of(lo)) << 32) | bits_of(hi);
+}
+static FQ_HD FQ_NOINLINE double widen_rare(float f) { return double(f); }
+
 // float -> double, exact.
 FQ_HDI double widen(float f) {
   const uint32_t u = bits_of(f);
   const uint32_t ex = (u >> 23) & 0xffu;
   if (ex == 0u || ex == 0xffu) {
     if ((u & 0x7fffffffu) == 0u) return double_of(uint64_t(u) << 32);  // signed zero
-    return double(f);                                                 // subnormal, inf, nan
+    return widen_rare(f);                                             // subnormal, inf, nan
   }
   return double_of((uint64_t(u & 0x80000000u) << 32) | (uint64_t(ex + 896u) << 52) |
                    (uint64_t(u & 0x7fffffu) << 29));
@@ -130,10 +147,16 @@ struct df64 {
   // into its leading 24 bits (rounded) and a signed remainder of at most 29 bits.
   FQ_HDI explicit df64(double d) {
     const uint64_t u = bits_of(d);
+    if ((u << 1) == 0u) {  // signed zero
+      hi = float_of(uint32_t(u >> 32));
+      lo = 0.f;
+      return;
+    }
     const int e = int((u >> 52) & 0x7ffu) - 1023;  // unbiased exponent
     if (e < -60 || e > 60) {
-      hi = f_from_double(d);
-      lo = f_from_double(d - double(hi));
+      const uint64_t p = split_rare(d);
+      hi = float_of(uint32_t(p));
+      lo = float_of(uint32_t(p >> 32));
       return;
     }
     const uint64_t m = (u & 0xfffffffffffffull) | (1ull << 52);  // d = +-m 2^(e-52)

@@ -30,9 +30,11 @@ namespace fq {
 template <int N, typename T>
 FQ_HD T cell_bary(const double* s, Bary<N, T>& B, bool& bad) {
   constexpr int NE = cbinom(N + 1, 2);
+  // every squared length positive, tested on the bits (positive doubles are the
+  // positive 64-bit integers): a double compare would issue on the FP64 pipe
   bool riemannian = true;
 #pragma unroll
-  for (int e = 0; e < NE; ++e) riemannian = riemannian && s[e] > 0.0;
+  for (int e = 0; e < NE; ++e) riemannian = riemannian && int64_t(bits_of(s[e])) > 0;
   if (std::is_same<T, df64>::value && N <= 3 && riemannian) {
     if constexpr (std::is_same<T, df64>::value && N <= 3) {
       df64 sd[NE > 0 ? NE : 1];
