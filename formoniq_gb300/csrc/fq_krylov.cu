@@ -783,11 +783,6 @@ __global__ void __launch_bounds__(KT) cg_c(CgVecs<VT> c, const SolverState* __re
 // ---------------------------------------------------------------------------
 // Host drivers
 // ---------------------------------------------------------------------------
-struct Workspace {
-  DevBuf vecs, parts, state;
-  SolverState* host_state = nullptr;
-};
-
 
 // Runs `one_iteration(parity)` (the three kernels of one iteration, reading
 // state slot `parity` and writing slot 1 - parity) as a CUDA graph of two
