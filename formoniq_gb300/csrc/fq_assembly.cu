@@ -570,16 +570,19 @@ __global__ void __launch_bounds__(256) scatter_sym_kernel(const int2* __restrict
                                                           const int32_t* __restrict__ perm,
                                                           const E* __restrict__ elem, V* __restrict__ values,
                                                           uint8_t* __restrict__ zflag, int* status, int64_t nup) {
+  // The plan arrays are read once and the values written once per assembly:
+  // streaming (evict-first) accesses, so that L2 keeps the element buffer the
+  // element kernel has just written, which every gather reads.
   const int64_t u = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (u >= nup) return;
-  const int2 sm = __ldg(pair + u);
-  const int b = __ldg(up_ptr + u), e = __ldg(up_ptr + u + 1);
+  const int2 sm = __ldcs(pair + u);
+  const int b = __ldcs(up_ptr + u), e = __ldcs(up_ptr + u + 1);
   E acc = E(0);
   bool nz = false;
   for (int t = b; t < e; t += kScatterUnroll) {
     int p[kScatterUnroll];
 #pragma unroll
-    for (int k = 0; k < kScatterUnroll; ++k) p[k] = t + k < e ? __ldg(perm + t + k) : 0;
+    for (int k = 0; k < kScatterUnroll; ++k) p[k] = t + k < e ? __ldcs(perm + t + k) : 0;
     E v[kScatterUnroll];
 #pragma unroll
     for (int k = 0; k < kScatterUnroll; ++k) v[k] = t + k < e ? elem[p[k]] : E(0);
@@ -592,12 +595,12 @@ __global__ void __launch_bounds__(256) scatter_sym_kernel(const int2* __restrict
   }
   const V out = store_value(acc);
   const uint8_t z = nz ? 0 : 1;
-  values[sm.x] = out;
+  __stcs(values + sm.x, out);
   if (zflag) zflag[sm.x] = z;
   int nzero = nz ? 0 : 1;
   if (sm.y != sm.x) {
     if (sm.y >= 0) {
-      values[sm.y] = out;
+      __stcs(values + sm.y, out);
       if (zflag) zflag[sm.y] = z;
       nzero += nz ? 0 : 1;
     } else {
