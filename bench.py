@@ -1,6 +1,6 @@
 """Benchmark of the Galerkin assembly + Krylov solve path on GB300.
 
-Workload (BASELINE config "3D unit cube"): the Kuhn subdivision of a 32^3 grid
+Workload (the 3D unit cube): the Kuhn subdivision of a 32^3 grid
 (196,608 tets), every vertex coordinate jittered by seeded uniform +-0.1h,
 FP64 signed squared edge lengths. A step assembles the k=1 and k=2 Hodge masses
 and exterior-derivative stiffnesses (M_1, M_2, dif_both(2), dif_both(3)) from
@@ -10,6 +10,11 @@ The same run times the mixed k=1 Hodge-Laplace solve by preconditioned MINRES to
 with host buffers.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py --workload precision|serve|batch|next
+
+The other workloads: the 4D FP32-with-refinement study, the served request
+stream, many meshes assembled in one launch set, and the rows after the headline
+path (matrix-free operator, source load, de Rham map, leapfrog).
 
 Multi-GPU: the path does not shard (one mesh per solve), so N > 1 runs N
 independent replicas, one per rank, with no collective on the data path.
