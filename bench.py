@@ -275,14 +275,12 @@ def roofline_record(ctx, mesh, mats, ncells, ms, el_ms, sc_ms, el_n, sc_n):
         nent = lr * (lr + 1) // 2 if sym else lr * lc
         nnz = m.nnz
         el_bytes += n1 * 8 + ncells * comb(n + 1, 2) * 4 + ncells * nent * 8
-        if sym:
-            # symmetric plan: every packed element entry gathered once with its
-            # plan index, one (slot, mirror) pair and pointer per upper slot, every
-            # slot's value written
-            nup = (nnz + m.shape[0]) // 2
-            sc_bytes += ncells * nent * (8 + 4) + nup * (8 + 4) + 4 + nnz * 8
-        else:
-            sc_bytes += ncells * lr * lc * (8 + 4) + (nnz + 1) * 4 + nnz * 8
+        # the scatter's compulsory bytes for this plan (the library's count):
+        # symmetric plans gather every packed element entry once, read one
+        # 16-byte record per upper slot (slot, mirror, first two contributions)
+        # and the plan indices of the slots with more than two, and write every
+        # slot's value
+        sc_bytes += m.scatter_bytes()
         tg = k - 1 if name == "dif_both" else k
         fused_bytes += n1 * 8 + ncells * (n + 1) * 4 + ncells * 2 * comb(n + 1, tg + 1) * 4 + nnz * 8
     el_avg = el_ms / max(el_n, 1) * len(FORMS)  # per step, all forms

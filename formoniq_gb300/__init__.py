@@ -186,6 +186,7 @@ _SIGNATURES = {
     "fq_assemble_host_many": (ctypes.c_int, [_P, _P, _DP, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.c_int]),
     "fq_reassemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P]),
     "fq_matrix_info": (ctypes.c_int, [_P, _I64P, _I64P, _I64P, ctypes.POINTER(ctypes.c_int)]),
+    "fq_matrix_scatter_bytes": (ctypes.c_int, [_P, _I64P]),
     "fq_matrix_device_arrays": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     "fq_matrix_copy_to_host": (ctypes.c_int, [_P, _P, _I32P, _I32P, _P]),
     "fq_matrix_destroy": (None, [_P]),
@@ -344,6 +345,12 @@ class Matrix:
     @property
     def nnz(self) -> int:
         return self.info()[2]
+
+    def scatter_bytes(self) -> int:
+        """Bytes one re-assembly's scatter reads and writes for this matrix (fq_matrix_scatter_bytes)."""
+        b = ctypes.c_int64()
+        self.ctx.check(self.ctx.L.fq_matrix_scatter_bytes(self.h, ctypes.byref(b)), "fq_matrix_scatter_bytes")
+        return b.value
 
     def host_arrays(self):
         nr, nc, nnz, pr = self.info()

@@ -880,6 +880,21 @@ fq_status fq_matrix_info(const fq_matrix* a, int64_t* nrows, int64_t* ncols, int
   return FQ_OK;
 }
 
+fq_status fq_matrix_scatter_bytes(const fq_matrix* a, int64_t* bytes) {
+  if (!a || !bytes) return FQ_INVALID_ARG;
+  *bytes = 0;
+  const Plan* p = a->plan;
+  if (!p) return FQ_OK;
+  const int64_t we = a->precision == FQ_FP32 ? 4 : 8;  // element values (float pairs in FQ_FP64)
+  const int64_t wv = a->precision == FQ_FP32 ? 4 : 8;  // assembled values
+  if (p->nup > 0)
+    *bytes = a->mesh->ncells * int64_t(p->nent) * we + p->nup * 16 + p->ntail_slots * 4 + p->ntail * 4 +
+             p->nslots * wv;
+  else
+    *bytes = p->ntrip * (we + 4) + (p->nslots + 1) * 4 + p->nslots * wv;
+  return FQ_OK;
+}
+
 fq_status fq_matrix_device_arrays(const fq_matrix* a, const int32_t** rp, const int32_t** ci, const void** val) {
   if (!a) return FQ_INVALID_ARG;
   if (rp) *rp = a->rp;

@@ -228,6 +228,41 @@ __global__ void upper_list_kernel(const int32_t* __restrict__ row_ptr, const int
     }
 }
 
+// One 16-byte record per upper slot with its first two contributions inline: the
+// scatter then reaches the element values of most slots in two dependent loads
+// (record, values) instead of three (pair and pointer, plan index, values).
+__global__ void upper_rec_kernel(const int2* __restrict__ pair, const int32_t* __restrict__ up_ptr,
+                                 const int32_t* __restrict__ up_perm, int64_t nup, int4* __restrict__ rec) {
+  for (int64_t u = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; u < nup; u += int64_t(gridDim.x) * blockDim.x) {
+    const int2 sm = pair[u];
+    const int32_t b = up_ptr[u], e = up_ptr[u + 1];
+    const int32_t p0 = e > b ? up_perm[b] : -1;
+    const int32_t p1 = e - b == 2 ? up_perm[b + 1] : (e - b > 2 ? -(2 + (b + 1)) : -1);
+    rec[u] = make_int4(sm.x, sm.y, p0, p1);
+  }
+}
+
+// Slots with more than two contributions and their contributions past the first.
+__global__ void upper_tail_kernel(const int32_t* __restrict__ up_ptr, int64_t nup,
+                                  unsigned long long* __restrict__ out) {
+  unsigned long long slots = 0, tail = 0;
+  for (int64_t u = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; u < nup; u += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t c = up_ptr[u + 1] - up_ptr[u];
+    if (c > 2) {
+      slots += 1;
+      tail += unsigned(c - 1);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    slots += __shfl_down_sync(0xffffffffu, slots, o);
+    tail += __shfl_down_sync(0xffffffffu, tail, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(out, slots);
+    atomicAdd(out + 1, tail);
+  }
+}
+
 __global__ void upper_perm_kernel(const int2* __restrict__ pair, const int32_t* __restrict__ up_ptr,
                                   const int32_t* __restrict__ slot_ptr, const int32_t* __restrict__ perm, int64_t nup,
                                   int32_t* up_perm) {
@@ -473,7 +508,20 @@ fq_status build_plan(fq_ctx* ctx, fq_mesh* m, Plan& plan, const Layout& lay) {
     upper_perm_kernel<<<grid_for(nup, 256), 256, 0, st>>>(plan.up_pair.as<int2>(), plan.up_ptr.as<int32_t>(),
                                                          plan.slot_ptr.as<int32_t>(), plan.perm.as<int32_t>(), nup,
                                                          plan.up_perm.as<int32_t>());
-    ctx->launches += 3;
+    FQ_TRY(plan.up_rec.alloc(ctx, std::max<int64_t>(nup, 1) * 16));
+    upper_rec_kernel<<<grid_for(nup, 256), 256, 0, st>>>(plan.up_pair.as<int2>(), plan.up_ptr.as<int32_t>(),
+                                                        plan.up_perm.as<int32_t>(), nup, plan.up_rec.as<int4>());
+    DevBuf tails;
+    FQ_TRY(tails.alloc(ctx, 16));
+    FQ_CUDA(ctx, cudaMemsetAsync(tails.p, 0, 16, st));
+    upper_tail_kernel<<<grid_for(nup, 256), 256, 0, st>>>(plan.up_ptr.as<int32_t>(), nup,
+                                                         tails.as<unsigned long long>());
+    unsigned long long th[2] = {0, 0};
+    FQ_CUDA(ctx, cudaMemcpyAsync(th, tails.p, 16, cudaMemcpyDeviceToHost, st));
+    FQ_CUDA(ctx, cudaStreamSynchronize(st));
+    plan.ntail_slots = int64_t(th[0]);
+    plan.ntail = int64_t(th[1]);
+    ctx->launches += 5;
   }
 
   // diagonal plan (preconditioner of the mixed system)
@@ -565,43 +613,53 @@ __global__ void __launch_bounds__(256) scatter_kernel(const int32_t* __restrict_
 // A mirror the pattern lacks (never, for a structurally symmetric program) sets
 // status bit 2.
 template <typename E, typename V>
-__global__ void __launch_bounds__(256) scatter_sym_kernel(const int2* __restrict__ pair,
+__global__ void __launch_bounds__(256) scatter_sym_kernel(const int4* __restrict__ rec,
                                                           const int32_t* __restrict__ up_ptr,
                                                           const int32_t* __restrict__ perm,
                                                           const E* __restrict__ elem, V* __restrict__ values,
                                                           uint8_t* __restrict__ zflag, int* status, int64_t nup) {
-  // The plan arrays are read once and the values written once per assembly:
+  // The plan records are read once and the values written once per assembly:
   // streaming (evict-first) accesses, so that L2 keeps the element buffer the
-  // element kernel has just written, which every gather reads.
+  // element kernel has just written, which every gather reads. A record holds
+  // the slot's first two contributions, so most slots need no plan index load.
   const int64_t u = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (u >= nup) return;
-  const int2 sm = __ldcs(pair + u);
-  const int b = __ldcs(up_ptr + u), e = __ldcs(up_ptr + u + 1);
+  const int4 r = __ldcs(rec + u);
+  const E v0 = r.z >= 0 ? elem[r.z] : E(0);  // every slot has a contribution; guarded all the same
+  const E v1 = r.w >= 0 ? elem[r.w] : E(0);
   E acc = E(0);
-  bool nz = false;
-  for (int t = b; t < e; t += kScatterUnroll) {
-    int p[kScatterUnroll];
+  acc += v0;
+  bool nz = nonzero_bits(v0);
+  if (r.w >= 0) {
+    acc += v1;
+    nz |= nonzero_bits(v1);
+  } else if (r.w < -1) {
+    // more than two contributions: the rest, in order, from the plan
+    const int e = __ldcs(up_ptr + u + 1);
+    for (int t = -(r.w + 2); t < e; t += kScatterUnroll) {
+      int p[kScatterUnroll];
 #pragma unroll
-    for (int k = 0; k < kScatterUnroll; ++k) p[k] = t + k < e ? __ldcs(perm + t + k) : 0;
-    E v[kScatterUnroll];
+      for (int k = 0; k < kScatterUnroll; ++k) p[k] = t + k < e ? __ldcs(perm + t + k) : 0;
+      E v[kScatterUnroll];
 #pragma unroll
-    for (int k = 0; k < kScatterUnroll; ++k) v[k] = t + k < e ? elem[p[k]] : E(0);
+      for (int k = 0; k < kScatterUnroll; ++k) v[k] = t + k < e ? elem[p[k]] : E(0);
 #pragma unroll
-    for (int k = 0; k < kScatterUnroll; ++k)
-      if (t + k < e) {
-        acc += v[k];
-        nz |= nonzero_bits(v[k]);
-      }
+      for (int k = 0; k < kScatterUnroll; ++k)
+        if (t + k < e) {
+          acc += v[k];
+          nz |= nonzero_bits(v[k]);
+        }
+    }
   }
   const V out = store_value(acc);
   const uint8_t z = nz ? 0 : 1;
-  __stcs(values + sm.x, out);
-  if (zflag) zflag[sm.x] = z;
+  __stcs(values + r.x, out);
+  if (zflag) zflag[r.x] = z;
   int nzero = nz ? 0 : 1;
-  if (sm.y != sm.x) {
-    if (sm.y >= 0) {
-      __stcs(values + sm.y, out);
-      if (zflag) zflag[sm.y] = z;
+  if (r.y != r.x) {
+    if (r.y >= 0) {
+      __stcs(values + r.y, out);
+      if (zflag) zflag[r.y] = z;
       nzero += nz ? 0 : 1;
     } else {
       atomicOr(status, 4);
@@ -640,7 +698,7 @@ void launch_scatter(const Plan& plan, const void* elem, void* values, uint8_t* z
   int* zero_count = status + 1;
   if (plan.nup > 0) {
     const unsigned blocks = unsigned((plan.nup + 255) / 256);
-    const int2* pr = plan.up_pair.as<int2>();
+    const int4* pr = plan.up_rec.as<int4>();
     const int32_t* up = plan.up_ptr.as<int32_t>();
     const int32_t* pm = plan.up_perm.as<int32_t>();
     if (mode == 1)

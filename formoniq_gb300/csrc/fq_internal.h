@@ -61,6 +61,10 @@ struct Plan {
   DevBuf up_pair;       // int2 [nup]: (slot, mirror slot)
   DevBuf up_ptr;        // int32 [nup+1]
   DevBuf up_perm;       // int32 [ntrip_up]
+  DevBuf up_rec;        // int4 [nup]: slot, mirror, first contribution, then the second one,
+                        // -1 (only one) or -(2 + its position in up_perm) (more than two)
+  int64_t ntail_slots = 0, ntail = 0;  // upper slots with more than two contributions; their contributions
+                                       // past the first (read from up_perm)
   // Diagonal plan (EK_KKT preconditioner): slots = rows.
   int64_t ndiag_trip = 0;
   DevBuf diag_ptr;      // int32 [nrows+1]

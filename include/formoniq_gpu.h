@@ -226,6 +226,10 @@ fq_status fq_assemble_host_many(fq_ctx* ctx, fq_mesh* mesh, const double* length
 fq_status fq_reassemble_noalloc(fq_ctx* ctx, fq_mesh* mesh, const fq_matrix* pattern, void* values_out);
 
 fq_status fq_matrix_info(const fq_matrix* m, int64_t* nrows, int64_t* ncols, int64_t* nnz, int* precision);
+/* The bytes one re-assembly's scatter reads and writes for this matrix: every
+ * element value once, the plan's records and the indices it still reads, every
+ * assembled value once (the roofline accounting of the scatter). 0 without a plan. */
+fq_status fq_matrix_scatter_bytes(const fq_matrix* m, int64_t* bytes);
 fq_status fq_matrix_device_arrays(const fq_matrix* m, const int32_t** row_ptr, const int32_t** col_idx,
                                   const void** values);
 /* Host copies: row_ptr [nrows+1], col_idx [nnz], values [nnz] (double or float). */

@@ -513,3 +513,22 @@ def test_budget_is_enforced():
         fq.WhitneyComplex(m).mass(1)
     assert e.value.name == "FQ_OOM_BUDGET"
     small.close()
+
+
+def test_scatter_bytes_accounting(oracle, ctx):
+    """fq_matrix_scatter_bytes counts every packed element entry once, one
+    16-byte record per upper slot, the plan indices of slots with more than two
+    contributions, and every assembled value once."""
+    cx, coords = oracle.cartesian_unit(3, 4)
+    coords = oracle.jitter_coords(coords, 4, seed=3, amplitude=0.1)
+    mesh = fq.Mesh.from_cells(ctx, oracle.kuhn_cells(3, 4))
+    mesh.set_lengths_sq(cx.edge_lengths_sq(coords))
+    m1 = fq.WhitneyComplex(mesh).mass(1)
+    nr, nc, nnz, _ = m1.info()
+    nent = 6 * 7 // 2
+    nup = (nnz + nr) // 2
+    base = cx.ncells() * nent * 8 + nup * 16 + nnz * 8
+    b = m1.scatter_bytes()
+    assert base <= b <= base + cx.ncells() * nent * 8, (b, base)
+    m1.close()
+    mesh.close()
