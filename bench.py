@@ -534,9 +534,15 @@ def stream_summary(reqs, res, wall, kind=None):
     def pct(p):
         return lat[min(len(lat) - 1, int(math.ceil(p / 100 * len(lat))) - 1)]
 
+    statuses = collections.Counter(int(r["status"]) for _, r in pairs)
     return {"solves_per_s": len(ok) / (span_ms * 1e-3), "p50_ms": pct(50), "p99_ms": pct(99),
             "mean_run_ms": sum(r["run_ms"] for _, r in pairs) / len(pairs), "converged": len(ok), "n": len(pairs),
-            "wall_s": wall, "cache_hits": sum(r["cache_hit"] for _, r in pairs)}
+            "wall_s": wall, "cache_hits": sum(r["cache_hit"] for _, r in pairs),
+            "statuses": {str(k): v for k, v in sorted(statuses.items())},
+            "unconverged": [{"dim": q.get("dim"), "nbox": q.get("nbox"), "grade": q.get("grade"),
+                             "status": int(r["status"]),
+                             "iters": int(r["report"].iters), "true_residual": float(r["report"].true_residual)}
+                            for q, r in pairs if not (r["status"] == 0 and r["report"].converged)][:8]}
 
 
 def run_serve(args):

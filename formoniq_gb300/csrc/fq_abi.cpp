@@ -399,6 +399,12 @@ static fq_status mixed_krylov(fq_mixed* P, const double* rhs, double* x, const f
   if (P->precision != FQ_FP32 || !P->kkt32) {
     FQ_TRY(minres_run<double>(ctx, P->rp, P->ci, P->val, n, P->nnz, P->dinv.as<double>(), pc, rhs, x, o->rtol,
                               o->max_iters, rep));
+    // LU catches the rare non-convergence of the iterative path (elliptic.rs:147-159), here for
+    // systems small enough for a dense factorization
+    if (!rep->converged && ctx->dense_fallback && n <= kDenseMax && dense_fallback_available()) {
+      FQ_TRY(dense_lu_solve(ctx, P->rp, P->ci, P->val, n, rhs, x));
+      rep->converged = 1;
+    }
   } else {
     // FP64 residual and update around an FP32 MINRES (iterative refinement).
     DevBuf r, r32, d32;
@@ -1378,6 +1384,11 @@ fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* m, double mass_term, const
   FQ_TRY(minres_run<double>(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, sii->nnz, pc_diag,
                             dp && dp->use_hx ? &dp->hx : nullptr, rhs.as<double>(), x.as<double>(), o->rtol,
                             o->max_iters, &r));
+  // the reference solves this system by LU: a small one MINRES left unconverged is finished that way
+  if (!r.converged && ctx->dense_fallback && nrel <= kDenseMax && dense_fallback_available()) {
+    FQ_TRY(dense_lu_solve(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, rhs.as<double>(), x.as<double>()));
+    r.converged = 1;
+  }
   {
     DevBuf rr;
     FQ_TRY(rr.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));

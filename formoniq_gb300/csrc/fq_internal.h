@@ -148,6 +148,9 @@ struct fq_ctx {
   fq::DevBuf scratch;      // reusable temporary storage
   // instrumentation: CUDA events on `stream` around element passes (slot 0) and
   // scatters (slot 1) of every assembly while `profiling` is set
+  // the dense direct fallback of unconverged MINRES solves (fq_direct.cu); server
+  // lanes leave it off (see fq_server.cpp)
+  bool dense_fallback = true;
   bool profiling = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<cudaEvent_t> prof_events;  // four per matrix of a multi-matrix assembly
@@ -160,6 +163,14 @@ struct fq_ctx {
 namespace fq {
 
 fq_status set_error(fq_ctx* ctx, fq_status s, const std::string& msg);
+
+// The direct fallback (fq_direct.cu): A x = b by a dense LU with partial
+// pivoting on the device, for systems of at most kDenseMax unknowns (A as CSR,
+// b and x device vectors). FQ_UNSUPPORTED without cuSOLVER or above the size.
+constexpr int64_t kDenseMax = 8192;
+bool dense_fallback_available();
+fq_status dense_lu_solve(fq_ctx* ctx, const int32_t* rp, const int32_t* ci, const double* val, int64_t n,
+                         const double* b, double* x);
 
 // The simplices of grade k on the device, [N_k][k+1] vertex ids (uploaded once
 // per mesh, kept by the mesh).

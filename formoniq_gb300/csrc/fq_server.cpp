@@ -259,6 +259,12 @@ void run_job(fq_server* S, fq_server::Lane& L, Job& J) {
 
 void lane_main(fq_server* S, fq_server::Lane* L) {
   fq_status s = fq_ctx_create(S->device, nullptr, S->budget, &L->ctx);
+  // No dense direct fallback in lanes: cuSOLVER's handle set-up and tear-down
+  // allocate and free device memory synchronously, which invalidates the graph
+  // captures other lanes run concurrently (their requests then fail with CUDA
+  // errors). Lanes keep the MINRES result, as the serving stream's iteration
+  // caps intend.
+  if (s == FQ_OK) L->ctx->dense_fallback = false;
   {
     std::lock_guard<std::mutex> lk(S->mu);
     if (s != FQ_OK && S->init_status == FQ_OK) S->init_status = s;

@@ -365,6 +365,16 @@ fq_status fq_source_nodes(fq_ctx* ctx, fq_mesh* mesh, const double* coords, int 
 fq_status fq_source_assemble(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, int degree, const double* coords,
                              int adim, const double* values, double* out);
 
+/* Direct fallback: the reference finishes a MINRES that did not converge with a
+ * sparse LU (problems/elliptic.rs:147-159) and solves the Dirac source problem by
+ * LU. Here the mixed FP64 solve and the Dirac solve finish an unconverged MINRES
+ * on a system of at most 8,192 unknowns by a dense LU with partial pivoting on
+ * the device (cuSOLVER, loaded at run time); report.converged is then 1 with
+ * report.iters the MINRES iterations spent, and report.true_residual that of the
+ * direct solution. Larger systems keep the MINRES result (FQ_NOT_CONVERGED), and
+ * so do the server's lanes (the factorization's synchronous allocations would
+ * break the graph captures of the other lanes). */
+
 /* ---- the covariant Hodge-Dirac source problem ---------------------------- */
 /* dirac::solve_dirac_source (problems/dirac.rs:473-531) with MINRES in place of
  * the reference's sparse LU: S = A + m M of HodgeDirac::assemble_selfadjoint
