@@ -1,0 +1,46 @@
+"""The symmetric scatter's 16-byte slot records, replayed on the CPU.
+
+formoniq_gb300/csrc/fq_assembly.cu encodes, per upper slot u with contributions
+up_perm[up_ptr[u] .. up_ptr[u+1]), a record (slot, mirror, p0, p1): p0 the first
+contribution, p1 the second when there are exactly two, -1 when there is one,
+-(2 + up_ptr[u] + 1) when there are more (the rest read from up_perm up to
+up_ptr[u+1]). The scatter decodes it. This replays both and checks that every
+slot sums exactly its contributions, in plan order.
+"""
+import random
+
+
+def encode(up_ptr, up_perm, u):
+    b, e = up_ptr[u], up_ptr[u + 1]
+    p0 = up_perm[b] if e > b else -1
+    p1 = up_perm[b + 1] if e - b == 2 else (-(2 + (b + 1)) if e - b > 2 else -1)
+    return p0, p1
+
+
+def decode(rec, up_ptr, up_perm, u, unroll=4):
+    p0, p1 = rec
+    seen = [p0] if p0 >= 0 else []
+    if p1 >= 0:
+        seen.append(p1)
+    elif p1 < -1:
+        e = up_ptr[u + 1]
+        t = -(p1 + 2)
+        while t < e:
+            for k in range(unroll):
+                if t + k < e:
+                    seen.append(up_perm[t + k])
+            t += unroll
+    return seen
+
+
+def test_records_visit_every_contribution_in_order():
+    rng = random.Random(7)
+    for _ in range(200):
+        counts = [rng.choice([1, 1, 1, 2, 2, 3, 4, 5, 6, 9]) for _ in range(rng.randint(1, 60))]
+        up_ptr = [0]
+        for c in counts:
+            up_ptr.append(up_ptr[-1] + c)
+        up_perm = [rng.randrange(10 ** 6) for _ in range(up_ptr[-1])]
+        for u in range(len(counts)):
+            rec = encode(up_ptr, up_perm, u)
+            assert decode(rec, up_ptr, up_perm, u) == up_perm[up_ptr[u]:up_ptr[u + 1]]
