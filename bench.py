@@ -114,6 +114,18 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(ms: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's step time (all ranks call it; one all-reduce MAX)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -218,10 +230,7 @@ def run_ours(args):
         launches = ctx.kernel_launches - launches0
         step_ms = [a.elapsed_time(b) for a, b in evs]
         ms = sum(step_ms) / len(step_ms)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms, world)
         value = world * ncells / (ms * 1e-3)
         # the element / scatter split from a separate pass of the same steps with
         # CUDA events around every kernel (events inside the timed steps would
