@@ -140,6 +140,9 @@ def measured_peaks():
 # ---------------------------------------------------------------------------
 
 def cpu_assembly(nbox: int, steps: int = 1):
+    """The oracle's C++/OpenMP assembly of the step's four forms on the same
+    mesh and lengths; returns the cell count, the per-step times, the host
+    threads used and the last step's matrices (the parity reference)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
@@ -147,20 +150,50 @@ def cpu_assembly(nbox: int, steps: int = 1):
     coords = oracle.jitter_coords(coords, nbox, SEED, JITTER)
     lengths = cx.edge_lengths_sq(coords)
     wc = oracle.WhitneyComplex(cx, lengths)
-    times = []
+    times, mats = [], None
     for _ in range(steps):
         t0 = time.perf_counter()
-        for name, k in FORMS:
-            getattr(wc, name)(k)
+        mats = [getattr(wc, name)(k) for name, k in FORMS]
         times.append(time.perf_counter() - t0)
-    return cx.ncells(), times, oracle.num_threads()
+    return cx.ncells(), times, oracle.num_threads(), mats
+
+
+def parity_record(gpu_mats, ref_mats):
+    """Parity of the timed step's matrices with the oracle's: CSR row_ptr and
+    col_idx bit-exact, values by relative Frobenius norm (bar 1e-12)."""
+    import scipy.sparse as sp
+
+    exact, worst, per = True, 0.0, {}
+    for (name, k), g, r in zip(FORMS, gpu_mats, ref_mats):
+        g = g.to_scipy()
+        pat = g.shape == r.shape and np.array_equal(g.indptr.astype(np.int64), r.indptr.astype(np.int64)) and \
+            np.array_equal(g.indices.astype(np.int64), r.indices.astype(np.int64))
+        if pat:
+            err = float(np.linalg.norm(g.data - r.data) / max(np.linalg.norm(r.data), 1e-300))
+        else:
+            d = (sp.csr_matrix(g) - r).tocsr()
+            err = float(sp.linalg.norm(d) / max(sp.linalg.norm(r), 1e-300))
+        exact &= bool(pat)
+        worst = max(worst, err)
+        per[f"{name}({k})"] = {"pattern_exact": bool(pat), "rel_frob": err}
+    return {"pattern_exact": exact, "max_rel_frob": worst, "bar_rel_frob": 1e-12, "pass": exact and worst <= 1e-12,
+            "against": "oracle C++ restatement of the reference assembly, same mesh and lengths", "forms": per}
+
+
+def workload_name(ncells: int) -> str:
+    """The headline workload, worded identically in both arms."""
+    return (f"kuhn {DIM}D {NBOX}^3 ({ncells} tets), jitter 0.1h seed {SEED}; step = M_1, M_2, dif_both(2), "
+            f"dif_both(3) assembled from resident lengths")
+
+
+DTYPE_FP64 = "f64 (float-float compute, 48-bit significand; f64 storage)"
 
 
 def run_reference(args):
     rank, _, world = env_rank()
     if rank != 0:
         return
-    ncells, times, cores = cpu_assembly(NBOX, args.warmup + args.steps)
+    ncells, times, cores, _ = cpu_assembly(NBOX, args.warmup + args.steps)
     t = times[args.warmup:]
     mean = sum(t) / len(t)
     value = ncells / mean
@@ -168,7 +201,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"kuhn {DIM}D {NBOX}^3 ({ncells} tets), forms M_1 M_2 dif_both(2) dif_both(3)",
+        "config": {"workload": workload_name(ncells),
                    "parallelism": "host threads (OpenMP cell-parallel, rayon-style per-thread triplets)"},
         "cpu_baseline": {"value": value, "unit": "cells/s", "cores": cores, "kind": "port",
                          "sample": f"full workload, {args.steps} timed steps"},
@@ -180,6 +213,47 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
+
+def timed_assembly(ctx, mats, flush, stream, steps, warmup, world):
+    """W untimed steps, then K steps each bracketed by CUDA events on the
+    library's stream (L2 flushed before each, outside the events), then a second
+    pass of the same steps with CUDA events around every kernel for the element
+    / scatter split (events inside the timed steps would perturb them)."""
+    import torch
+
+    import formoniq_gb300 as fq
+
+    def step():
+        fq.Matrix.reassemble_many(mats)  # the forms queued back to back, one status read
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    launches0 = ctx.kernel_launches
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for i in range(steps):
+        flush.fill_(float(i))
+        evs[i][0].record(stream)
+        step()
+        evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = ctx.kernel_launches - launches0
+    ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / steps, world)
+    ctx.profile(reset=True)
+    ctx.set_profiling(True)
+    for i in range(steps):
+        flush.fill_(float(i))
+        step()
+    torch.cuda.synchronize()
+    ctx.set_profiling(False)
+    (el_ms, sc_ms), (el_n, sc_n) = ctx.profile(reset=True)
+    return dict(ms=ms, wall=wall, launches=launches, el_ms=el_ms, sc_ms=sc_ms, el_n=el_n, sc_n=sc_n)
+
 
 def run_ours(args):
     import torch
@@ -198,73 +272,53 @@ def run_ours(args):
     mesh = fq.Mesh.kuhn_cube(ctx, DIM, NBOX)
     mesh.kuhn_lengths(jitter=JITTER, seed=SEED + rank)
     ncells = mesh.ncells()
-    wc = fq.WhitneyComplex(mesh)
     t0 = time.perf_counter()
-    mats = [getattr(wc, name)(k) for name, k in FORMS]  # patterns and permutations built here (set-up)
+    mats = [getattr(fq.WhitneyComplex(mesh), name)(k) for name, k in FORMS]  # patterns and plans built here
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t0
+    mats_ieee = [getattr(fq.WhitneyComplex(mesh, precision=fq.FQ_FP64_IEEE), name)(k) for name, k in FORMS]
+    torch.cuda.synchronize()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
 
-    def step():
-        fq.Matrix.reassemble_many(mats)  # the four forms queued back to back, one status read
-
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     # the clock sampler starts before the warm-up: its process start-up stays out of the timed steps
     with ClockSampler(local_rank) as clocks:
         time.sleep(0.5)
-        for _ in range(args.warmup):
-            step()
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
-        launches0 = ctx.kernel_launches
-        torch.cuda.synchronize()
-        wall0 = time.perf_counter()
-        for i in range(args.steps):
-            flush.fill_(float(i))  # L2 flush between timed steps (outside the events)
-            evs[i][0].record(stream)
-            step()
-            evs[i][1].record(stream)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - wall0
-        launches = ctx.kernel_launches - launches0
-        step_ms = [a.elapsed_time(b) for a, b in evs]
-        ms = sum(step_ms) / len(step_ms)
-        ms = max_over_ranks(ms, world)
-        value = world * ncells / (ms * 1e-3)
-        # the element / scatter split from a separate pass of the same steps with
-        # CUDA events around every kernel (events inside the timed steps would
-        # perturb them)
-        ctx.profile(reset=True)
-        ctx.set_profiling(True)
-        for i in range(args.steps):
-            flush.fill_(float(i))
-            step()
-        torch.cuda.synchronize()
-        ctx.set_profiling(False)
-        (el_ms, sc_ms), (el_n, sc_n) = ctx.profile(reset=True)
+        main = timed_assembly(ctx, mats, flush, stream, args.steps, args.warmup, world)
+        ieee = timed_assembly(ctx, mats_ieee, flush, stream, args.steps, args.warmup, world)
         solve = None if args.no_solve else solve_phase(fq, torch, mesh, stream, args)
-    roofline = roofline_record(ctx, mesh, mats, ncells, ms, el_ms, sc_ms, el_n, sc_n)
+    ms = main["ms"]
+    value = world * ncells / (ms * 1e-3)
+    roofline = roofline_record(ctx, mesh, mats, ncells, ms, main)
+    ieee_roof = roofline_record(ctx, mesh, mats_ieee, ncells, ieee["ms"], ieee)
+    ieee_rec = {"value": world * ncells / (ieee["ms"] * 1e-3), "unit": "cells/s", "ms_per_step": ieee["ms"],
+                "dtype": "f64 (IEEE binary64 throughout)", "element_ms_per_step": ieee_roof["element_ms_per_step"],
+                "scatter_ms_per_step": ieee_roof["scatter_ms_per_step"],
+                "scatter_frac": ieee_roof["scatter_GBps"] / ieee_roof["peak"],
+                "fused_assembly_frac": ieee_roof["fused_assembly_frac"]}
     e2e = None if args.no_e2e else e2e_phase(ctx, mesh, mats, flush, args, ncells, world)
-    cpu = None
+    cpu = parity = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cnc, ct, cores = cpu_assembly(NBOX, 1)
+        cnc, ct, cores, omats = cpu_assembly(NBOX, 1)
         cpu = {"value": cnc / ct[0], "unit": "cells/s", "cores": cores, "kind": "port",
                "sample": f"one full step ({cnc} tets, 4 forms), oracle C++/OpenMP assembly"}
+        fq.Matrix.reassemble_many(mats)
+        fq.Matrix.reassemble_many(mats_ieee)
+        parity = {"fp64_float_float": parity_record(mats, omats), "fp64_ieee": parity_record(mats_ieee, omats)}
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"kuhn {DIM}D {NBOX}^3 ({ncells} tets), jitter 0.1h seed {SEED}; step = M_1, M_2, "
-                               f"dif_both(2), dif_both(3) assembled from resident lengths",
+        "vs_baseline": None, "dtype": DTYPE_FP64, "precision_mode": "FQ_FP64", "data": "synthetic",
+        "config": {"workload": workload_name(ncells),
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
                    "setup_s_pattern_and_permutation": round(setup_s, 3)},
         "roofline": roofline,
         "e2e": e2e,
         "cpu_baseline": cpu,
-        "gpu_launches": launches,
+        "gpu_launches": main["launches"],
         "clocks": clocks.summary(),
-        "wall_s_timed": wall,
+        "wall_s_timed": main["wall"],
+        "ieee_fp64": ieee_rec,
+        "parity": parity,
         "solve": solve,
     }
     if rank == 0:
@@ -273,7 +327,7 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def roofline_record(ctx, mesh, mats, ncells, ms, el_ms, sc_ms, el_n, sc_n):
+def roofline_record(ctx, mesh, mats, ncells, ms, t):
     """Algorithmic bytes per launch of each kernel (per form, summed over the
     step's forms) over its CUDA-event time on the launching stream."""
     n = DIM
@@ -282,8 +336,9 @@ def roofline_record(ctx, mesh, mats, ncells, ms, el_ms, sc_ms, el_n, sc_n):
     for (name, k), m in zip(FORMS, mats):
         lr, lc, sym = local_shape(n, name, k)
         nent = lr * (lr + 1) // 2 if sym else lr * lc
-        nnz = m.nnz
-        el_bytes += n1 * 8 + ncells * comb(n + 1, 2) * 4 + ncells * nent * 8
+        _, _, nnz, prec = m.info()
+        w = 4 if prec == 1 else 8
+        el_bytes += n1 * 8 + ncells * comb(n + 1, 2) * 4 + ncells * nent * w
         # the scatter's compulsory bytes for this plan (the library's count):
         # symmetric plans gather every packed element entry once, read one
         # 16-byte record per upper slot (slot, mirror, first two contributions)
@@ -291,13 +346,14 @@ def roofline_record(ctx, mesh, mats, ncells, ms, el_ms, sc_ms, el_n, sc_n):
         # slot's value
         sc_bytes += m.scatter_bytes()
         tg = k - 1 if name == "dif_both" else k
-        fused_bytes += n1 * 8 + ncells * (n + 1) * 4 + ncells * 2 * comb(n + 1, tg + 1) * 4 + nnz * 8
-    el_avg = el_ms / max(el_n, 1) * len(FORMS)  # per step, all forms
-    sc_avg = sc_ms / max(sc_n, 1) * len(FORMS)
+        fused_bytes += n1 * 8 + ncells * (n + 1) * 4 + ncells * 2 * comb(n + 1, tg + 1) * 4 + nnz * w
+    el_avg = t["el_ms"] / max(t["el_n"], 1) * len(FORMS)  # per step, all forms
+    sc_avg = t["sc_ms"] / max(t["sc_n"], 1) * len(FORMS)
     hbm_peak, peak_src = measured_peaks()
     dominant = "element" if el_avg >= sc_avg else "scatter"
     dom_bytes, dom_ms = (el_bytes, el_avg) if dominant == "element" else (sc_bytes, sc_avg)
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    fused_gbps = fused_bytes / (ms * 1e-3) / 1e9
     return {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
             "algorithmic_bytes_per_step": dom_bytes, "kernel_ms_per_step": dom_ms,
@@ -306,8 +362,8 @@ def roofline_record(ctx, mesh, mats, ncells, ms, el_ms, sc_ms, el_n, sc_n):
             "scatter_GBps": sc_bytes / (sc_avg * 1e-3) / 1e9,
             "fp64_fma_peak_tflops_measured": ctx.fma_peak_tflops(True),
             "fp32_fma_peak_tflops_measured": ctx.fma_peak_tflops(False),
-            "fused_assembly_bytes_per_step": fused_bytes,
-            "fused_assembly_GBps": fused_bytes / (ms * 1e-3) / 1e9}
+            "fused_assembly_bytes_per_step": fused_bytes, "fused_assembly_GBps": fused_gbps,
+            "fused_assembly_frac": fused_gbps / hbm_peak}
 
 
 def solve_phase(fq, torch, mesh, stream, args):

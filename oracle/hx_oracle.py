@@ -133,17 +133,20 @@ class NodalMultigrid:
 
 
 def lattice_spacing(cx, lengths: np.ndarray, n: int, nbox: int) -> np.ndarray:
-    edges = cx.simplices(1)
-    index = {(int(e[0]), int(e[1])): i for i, e in enumerate(edges)}
+    """Per axis, the root mean squared length of the single-axis edges
+    (v, v + (N+1)^a), averaged in increasing v."""
+    edges = np.asarray(cx.simplices(1), np.int64)
+    nv = (nbox + 1) ** n
+    keys = edges[:, 0] * nv + edges[:, 1]
+    order = np.argsort(keys, kind="stable")
+    v = np.arange(nv, dtype=np.int64)
     h = np.zeros(n)
     for a in range(n):
         stride = (nbox + 1) ** a
-        vals = []
-        for v in range((nbox + 1) ** n):
-            if lattice_coords(v, n, nbox)[a] >= nbox:
-                continue
-            vals.append(lengths[index[(v, v + stride)]])
-        h[a] = math.sqrt(float(np.mean(vals)))
+        vv = v[(v // stride) % (nbox + 1) < nbox]
+        want = vv * nv + vv + stride
+        idx = order[np.searchsorted(keys, want, sorter=order)]
+        h[a] = math.sqrt(float(np.mean(lengths[idx])))
     return h
 
 
@@ -153,30 +156,37 @@ def colex_subsets(n: int, j: int):
 
 
 def vector_nodal(cx, j: int, n: int, nbox: int, relative: bool, h: np.ndarray) -> sp.csr_matrix:
-    """Pi_j: rows the grade-j unknowns, columns (node, I) node-major."""
+    """Pi_j: rows the grade-j unknowns, columns (node, I) node-major. Entry
+    (s, (node(v), I)) = det(E_s[I, :]) / (j+1)! for every vertex v of s, with E_s
+    the lattice edge vectors (scaled per axis by h) from the first vertex of s."""
     ncomp = 1 if j == 0 else math.comb(n, j)
     n0 = level_nodes(n, nbox, relative)
-    simp = cx.simplices(j)
-    keep = np.arange(len(simp)) if not relative else cx.interior(j)
-    subs = colex_subsets(n, j)
+    simp = np.asarray(cx.simplices(j), np.int64)
+    keep = np.arange(len(simp)) if not relative else np.asarray(cx.interior(j), np.int64)
+    verts = simp[keep]                                       # [m, j+1]
+    m = len(keep)
+    lat = np.stack([(verts // (nbox + 1) ** a) % (nbox + 1) for a in range(n)], -1)  # [m, j+1, n]
     factor = 1.0 / math.factorial(j + 1)
-    rows, cols, vals = [], [], []
-    for row, s in enumerate(keep):
-        vs = [int(v) for v in simp[s]]
-        c0 = np.array(lattice_coords(vs[0], n, nbox))
-        E = np.array([(np.array(lattice_coords(v, n, nbox)) - c0) * h for v in vs[1:]]).T.reshape(n, j)
-        comp = [1.0] if j == 0 else [np.linalg.det(E[sub, :]) for sub in subs]
-        for v in vs:
-            node = node_index(lattice_coords(v, n, nbox), n, nbox, relative)
-            if node < 0:
-                continue
-            for q in range(ncomp):
-                val = factor * comp[q]
-                if val != 0.0:
-                    rows.append(row)
-                    cols.append(node * ncomp + q)
-                    vals.append(val)
-    return sp.csr_matrix((vals, (rows, cols)), shape=(len(keep), n0 * ncomp))
+    if j == 0:
+        comp = np.ones((m, 1))
+    else:
+        E = np.transpose((lat[:, 1:, :] - lat[:, :1, :]) * h, (0, 2, 1))  # [m, n, j]
+        comp = np.stack([np.linalg.det(E[:, sub, :]) for sub in colex_subsets(n, j)], 1)  # [m, ncomp]
+    if relative:
+        inside = np.all((lat > 0) & (lat < nbox), -1)            # [m, j+1]
+        node = np.zeros(lat.shape[:2], np.int64)
+        stride = 1
+        for a in range(n):
+            node += (lat[:, :, a] - 1) * stride
+            stride *= nbox - 1
+        node[~inside] = -1
+    else:
+        node = verts
+    rows = np.repeat(np.arange(m), (j + 1) * ncomp).reshape(m, j + 1, ncomp)
+    cols = node[:, :, None] * ncomp + np.arange(ncomp)[None, None, :]
+    vals = np.broadcast_to((factor * comp)[:, None, :], (m, j + 1, ncomp))
+    ok = (node[:, :, None] >= 0) & (vals != 0.0)
+    return sp.csr_matrix((vals[ok], (rows[ok], cols[ok])), shape=(m, n0 * ncomp))
 
 
 class HxPreconditioner:
@@ -189,6 +199,7 @@ class HxPreconditioner:
         self.cx = cx
         self._pi = {}
         self._s = {}
+        self._d = {}
 
     def smoother(self, j: int) -> np.ndarray:
         if j not in self._s:
@@ -210,6 +221,8 @@ class HxPreconditioner:
     def apply(self, j: int, r: np.ndarray) -> np.ndarray:
         y = self.smoother(j) * r + self.nodal(j, r)
         if j >= 1:
-            D = self.wc.dif(j - 1)
+            if j - 1 not in self._d:
+                self._d[j - 1] = self.wc.dif(j - 1)
+            D = self._d[j - 1]
             y = y + D @ self.apply(j - 1, D.T @ r)
         return y

@@ -6,6 +6,10 @@ or warp-staged) must skip the padding, keep every slot_ptr / perm / value
 access inside its mesh and write every real slot exactly once. This replays the
 kernels' index computations (grid-stride loops, binary search over the
 entries, the padding test) for random batches and grid sizes.
+
+This checks the index scheme, written out again in Python, not the compiled
+kernels; the GPU batch tests (every member against fq_assemble and the oracle)
+pin the kernels themselves.
 """
 import random
 

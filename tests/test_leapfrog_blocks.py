@@ -5,6 +5,9 @@ parity on the diagonal of one block CSR: row pointers shifted by the block's
 entry offset, column indices by its row offset (lf_block_csr, one thread per
 index up to max(nrows + 1, nnz)). This replays that kernel on random CSRs and
 checks the block equals scipy's block_diag of the grades' matrices.
+
+This checks the index scheme, written out again in Python, not the compiled
+kernel; the GPU leapfrog tests against the oracle pin the kernel itself.
 """
 import random
 

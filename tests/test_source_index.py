@@ -8,6 +8,9 @@ loops (grid-stride over 128-cell blocks, the chunk loop, the cooperative copy
 and each thread's reads) and checks every global read is inside the values
 array, every shared-memory index inside 128 * stride doubles, and that each
 thread reads exactly its own cell's values, each once, in node order.
+
+This checks the index scheme, written out again in Python, not the compiled
+kernel; the GPU source-load tests against the oracle pin the kernel itself.
 """
 import random
 
