@@ -15,7 +15,6 @@
 // overlaps on the GPU (two streams, or two host threads) race on it.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "fq_element_kernel.cuh"
@@ -23,35 +22,26 @@
 
 namespace fq {
 
-// 32 MiB: the element buffer of up to 4 Mi FP64 entries (e.g. M_1 of a
-// 199,728-cell 3D mesh, 21 entries per cell); the size rule also keeps one
-// byte per CSR slot of headroom.
+// 32 MiB: the element buffer of up to 4 Mi FP64 (8 Mi FP32) entries, e.g. M_1
+// of a 199,728-cell 3D mesh at 21 entries per cell.
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-void* g_scratch_addr[kMaxDevices] = {};
-}  // namespace
-
-// Set-up, once per device, with that device current: the host-side name of a
-// __device__ array is only a stand-in, so its device address is looked up here.
+// Set-up, with the context's device current: the host-side name of a
+// __device__ array is only a stand-in, so its device address is looked up. It
+// is looked up on every call (a cheap table lookup next to the status read the
+// call ends with), so an address never outlives the module instance it came
+// from, e.g. across a device reset.
 static fq_status noalloc_scratch(fq_ctx* ctx, void** out) {
-  if (ctx->device < 0 || ctx->device >= kMaxDevices) return set_error(ctx, FQ_UNSUPPORTED, "device index too large");
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[ctx->device]) {
-    int prev = 0;
-    FQ_CUDA(ctx, cudaGetDevice(&prev));
-    FQ_CUDA(ctx, cudaSetDevice(ctx->device));
-    void* ptr = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    cudaSetDevice(prev);
-    if (e != cudaSuccess) return cuda_check(ctx, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-    g_scratch_addr[ctx->device] = ptr;
-  }
-  *out = g_scratch_addr[ctx->device];
+  int prev = 0;
+  FQ_CUDA(ctx, cudaGetDevice(&prev));
+  if (prev != ctx->device) FQ_CUDA(ctx, cudaSetDevice(ctx->device));
+  void* ptr = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (prev != ctx->device) cudaSetDevice(prev);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+  *out = ptr;
   return FQ_OK;
 }
 
@@ -69,12 +59,11 @@ extern "C" fq_status fq_reassemble_noalloc(fq_ctx* ctx, fq_mesh* mesh, const fq_
   const Plan& p = *pattern->plan;
   const int mode = pattern->precision;
   const size_t w = mode == FQ_FP32 ? 4 : 8;
-  const size_t elem_bytes = (size_t(p.nent) * size_t(mesh->ncells) * w + 255) & ~size_t(255);
-  const size_t need = elem_bytes + size_t(p.nslots);
+  const size_t need = size_t(p.nent) * size_t(mesh->ncells) * w;
   if (need > kNoAllocScratchBytes)
     return set_error(ctx, FQ_INVALID_ARG,
                      "fq_reassemble_noalloc: needs " + std::to_string(need) + " bytes of scratch, the static maximum is " +
-                         std::to_string(kNoAllocScratchBytes) + " bytes (element entries x cells x width + slots)");
+                         std::to_string(kNoAllocScratchBytes) + " bytes (element entries x cells x value width)");
   void* scratch = nullptr;
   FQ_TRY(noalloc_scratch(ctx, &scratch));
   unsigned char* base = static_cast<unsigned char*>(scratch);

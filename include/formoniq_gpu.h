@@ -218,11 +218,12 @@ fq_status fq_assemble_host_many(fq_ctx* ctx, fq_mesh* mesh, const double* length
  * library holds until exit, and the values (nnz of `pattern`, its precision)
  * are written to the caller's device buffer `values_out` in the CSR order of
  * `pattern`, a matrix fq_assemble made on this mesh. Rejects, with
- * FQ_INVALID_ARG and a message, a mesh whose element buffer plus one byte per
- * slot exceeds the array; returns FQ_UNSUPPORTED when the exact-zero rule
- * would change the pattern. The first call on a device looks up the array's
- * device address and should come before any stream capture. All calls share
- * the array: calls whose work overlaps on the GPU race. */
+ * FQ_INVALID_ARG and a message, a mesh whose element buffer (entries x cells x
+ * value width) exceeds the array; returns FQ_UNSUPPORTED when the exact-zero
+ * rule would change the pattern. Every call looks up the array's device address
+ * with the context's device current, and synchronises ctx->stream before it
+ * returns (it reads the status words back). All calls share the array: calls
+ * whose work overlaps on the GPU race. */
 fq_status fq_reassemble_noalloc(fq_ctx* ctx, fq_mesh* mesh, const fq_matrix* pattern, void* values_out);
 
 fq_status fq_matrix_info(const fq_matrix* m, int64_t* nrows, int64_t* ncols, int64_t* nnz, int* precision);

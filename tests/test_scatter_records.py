@@ -6,6 +6,10 @@ contribution, p1 the second when there are exactly two, -1 when there is one,
 -(2 + up_ptr[u] + 1) when there are more (the rest read from up_perm up to
 up_ptr[u+1]). The scatter decodes it. This replays both and checks that every
 slot sums exactly its contributions, in plan order.
+
+This checks the encoding scheme, written out again in Python, not the compiled
+kernel: a change to the kernel alone would still pass here. The GPU parity
+tests (every assembled matrix against the oracle) pin the kernel itself.
 """
 import random
 

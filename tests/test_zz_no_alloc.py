@@ -15,24 +15,28 @@ import formoniq_gb300 as fq
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_reassembly_matches_fq_assemble_on_two_calls():
+@pytest.mark.parametrize("precision,tol", [(fq.FQ_FP64, 1e-12), (fq.FQ_FP64_IEEE, 1e-12), (fq.FQ_FP32, 1e-6)])
+def test_noalloc_reassembly_matches_fq_assemble_on_two_calls(precision, tol):
+    """Every precision mode (float-float, IEEE double, FP32 values into a
+    float32 buffer), two calls in a row on new lengths, each against the
+    ordinary entry point in the same precision."""
     import torch
 
     ctx = fq.Context(0)
     mesh = fq.Mesh.kuhn_cube(ctx, 3, 6)
-    wc = fq.WhitneyComplex(mesh)
-    out = None
+    wc = fq.WhitneyComplex(mesh, precision=precision)
+    dtype = torch.float32 if precision == fq.FQ_FP32 else torch.float64
     for call, seed in enumerate((3, 4)):
         mesh.kuhn_lengths(jitter=0.1, seed=seed)
         for name, k in (("mass", 1), ("dif_both", 2), ("dif_test", 2)):
             m = getattr(wc, name)(k)  # the existing entry point on the new lengths
-            expect = m.to_scipy().data
-            out = torch.full((m.nnz,), float("nan"), dtype=torch.float64, device="cuda")
+            expect = m.to_scipy().data.astype(np.float64)
+            out = torch.full((m.nnz,), float("nan"), dtype=dtype, device="cuda")
             torch.cuda.synchronize()
             m.reassemble_noalloc(mesh, out.data_ptr())
-            got = out.cpu().numpy()
+            got = out.cpu().numpy().astype(np.float64)
             err = np.linalg.norm(got - expect) / np.linalg.norm(expect)
-            assert err <= 1e-12, (call, name, k, err)
+            assert err <= tol, (precision, call, name, k, err)
     ctx.close()
 
 
