@@ -140,6 +140,7 @@ _SIGNATURES = {
     "fq_ctx_kernel_launches": (ctypes.c_uint64, [_P]),
     "fq_default_solve_opts": (None, [ctypes.POINTER(SolveOpts)]),
     "fq_ctx_set_profiling": (ctypes.c_int, [_P, ctypes.c_int]),
+    "fq_ctx_set_scatter_shape": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     "fq_ctx_profile": (ctypes.c_int, [_P, _DP, _I64P, ctypes.c_int, ctypes.c_int]),
     "fq_measure_fma_peak": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
     "fq_mesh_from_cells": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64, _I32P, ctypes.POINTER(_P)]),
@@ -292,6 +293,11 @@ class Context:
 
     def set_profiling(self, enable: bool):
         self.check(self.L.fq_ctx_set_profiling(self.h, int(enable)), "fq_ctx_set_profiling")
+
+    def set_scatter_shape(self, slots_per_thread: int, blocks_per_sm: int = 0):
+        """Launch shape of the symmetric scatter (fq_ctx_set_scatter_shape)."""
+        self.check(self.L.fq_ctx_set_scatter_shape(self.h, int(slots_per_thread), int(blocks_per_sm)),
+                   "fq_ctx_set_scatter_shape")
 
     def profile(self, reset: bool = False):
         """(element_ms, scatter_ms), (element_launches, scatter_launches)."""

@@ -583,6 +583,17 @@ fq_status fq_ctx_profile(fq_ctx* ctx, double* ms, int64_t* launches, int nslots,
 }
 uint64_t fq_ctx_kernel_launches(const fq_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+fq_status fq_ctx_set_scatter_shape(fq_ctx* ctx, int slots_per_thread, int blocks_per_sm) {
+  if (!ctx) return FQ_INVALID_ARG;
+  if (!(slots_per_thread == -1 || slots_per_thread == 0 || slots_per_thread == 1 || slots_per_thread == 2 ||
+        slots_per_thread == 4 || slots_per_thread == 8) ||
+      blocks_per_sm < 0 || blocks_per_sm > 8)
+    return set_error(ctx, FQ_INVALID_ARG, "scatter shape: slots per thread in {-1,0,1,2,4,8}, blocks per SM in 0..8");
+  ctx->scatter_shape.slots_per_thread = slots_per_thread;
+  ctx->scatter_shape.blocks_per_sm = blocks_per_sm;
+  return FQ_OK;
+}
+
 // ---- meshes -----------------------------------------------------------------
 fq_status fq_mesh_from_cells(fq_ctx* ctx, int dim, int64_t ncells, const int32_t* cells, fq_mesh** out) {
   if (!ctx || !out) return FQ_INVALID_ARG;

@@ -668,6 +668,92 @@ __global__ void __launch_bounds__(256) scatter_sym_kernel(const int4* __restrict
   if (nzero) atomicAdd(status + 1, nzero);
 }
 
+// Symmetric plans, U upper slots per thread: a persistent grid walks the
+// records in rounds of U * (grid threads); in a round, thread t handles the
+// slots t, t + T, ..., t + (U-1) T (T = grid threads), so each of its U record
+// loads is one coalesced warp transaction. All U records are loaded before any
+// element value, and the next round's records are loaded before this round's
+// gathers, so a thread keeps up to 2U record loads and 2U element gathers in
+// flight where scatter_sym_kernel keeps one record, then two gathers. Every
+// slot sums the same contributions in the same order as scatter_sym_kernel:
+// the results are bit-identical.
+template <typename E, typename V, int U>
+__global__ void __launch_bounds__(256) scatter_sym_multi_kernel(const int4* __restrict__ rec,
+                                                                const int32_t* __restrict__ up_ptr,
+                                                                const int32_t* __restrict__ perm,
+                                                                const E* __restrict__ elem, V* __restrict__ values,
+                                                                uint8_t* __restrict__ zflag, int* status, int64_t nup) {
+  const int64_t T = int64_t(gridDim.x) * blockDim.x;
+  int nzero = 0;
+  int4 nxt[U];
+#pragma unroll
+  for (int i = 0; i < U; ++i) {
+    const int64_t u = int64_t(blockIdx.x) * blockDim.x + threadIdx.x + i * T;
+    nxt[i] = u < nup ? __ldcs(rec + u) : make_int4(-1, -1, -1, -1);
+  }
+  for (int64_t t0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t0 < nup; t0 += U * T) {
+    int4 r[U];
+#pragma unroll
+    for (int i = 0; i < U; ++i) r[i] = nxt[i];
+    const int64_t t1 = t0 + U * T;
+    if (t1 < nup) {
+#pragma unroll
+      for (int i = 0; i < U; ++i) {
+        const int64_t u = t1 + i * T;
+        nxt[i] = u < nup ? __ldcs(rec + u) : make_int4(-1, -1, -1, -1);
+      }
+    }
+    E v0[U], v1[U];
+#pragma unroll
+    for (int i = 0; i < U; ++i) {
+      v0[i] = r[i].z >= 0 ? elem[r[i].z] : E(0);
+      v1[i] = r[i].w >= 0 ? elem[r[i].w] : E(0);
+    }
+#pragma unroll
+    for (int i = 0; i < U; ++i) {
+      if (r[i].x < 0) continue;  // past the end
+      E acc = E(0);
+      acc += v0[i];
+      bool nz = nonzero_bits(v0[i]);
+      if (r[i].w >= 0) {
+        acc += v1[i];
+        nz |= nonzero_bits(v1[i]);
+      } else if (r[i].w < -1) {
+        const int e = __ldcs(up_ptr + (t0 + i * T) + 1);
+        for (int t = -(r[i].w + 2); t < e; t += kScatterUnroll) {
+          int p[kScatterUnroll];
+#pragma unroll
+          for (int k = 0; k < kScatterUnroll; ++k) p[k] = t + k < e ? __ldcs(perm + t + k) : 0;
+          E v[kScatterUnroll];
+#pragma unroll
+          for (int k = 0; k < kScatterUnroll; ++k) v[k] = t + k < e ? elem[p[k]] : E(0);
+#pragma unroll
+          for (int k = 0; k < kScatterUnroll; ++k)
+            if (t + k < e) {
+              acc += v[k];
+              nz |= nonzero_bits(v[k]);
+            }
+        }
+      }
+      const V out = store_value(acc);
+      const uint8_t z = nz ? 0 : 1;
+      __stcs(values + r[i].x, out);
+      if (zflag) zflag[r[i].x] = z;
+      nzero += nz ? 0 : 1;
+      if (r[i].y != r[i].x) {
+        if (r[i].y >= 0) {
+          __stcs(values + r[i].y, out);
+          if (zflag) zflag[r[i].y] = z;
+          nzero += nz ? 0 : 1;
+        } else {
+          atomicOr(status, 4);
+        }
+      }
+    }
+  }
+  if (nzero) atomicAdd(status + 1, nzero);
+}
+
 template <typename E>
 __global__ void __launch_bounds__(256) scatter_diag_kernel(const int32_t* __restrict__ ptr,
                                                            const int32_t* __restrict__ perm,
@@ -692,11 +778,61 @@ void launch_df64_to_double(const void* in, double* out, int64_t n, cudaStream_t 
   df64_to_double_kernel<<<g, 256, 0, st>>>(static_cast<const df64*>(in), out, n);
 }
 
+// The symmetric scatter with U slots per thread on a persistent grid of
+// `bps` blocks of 256 threads per SM (bps 0: as many as are resident at once),
+// at most enough blocks to give every thread one round.
+template <typename E, typename V, int U>
+static void launch_sym_multi(const Plan& plan, const E* elem, V* values, uint8_t* zero_flags, int* status, int bps,
+                             cudaStream_t st) {
+  static int sms = 0, resident = 0;  // per instantiation: the device's SMs and resident blocks of this kernel
+  if (sms == 0) {
+    int dev = 0, n = 152, r = 1;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, scatter_sym_multi_kernel<E, V, U>, 256, 0) != cudaSuccess)
+      r = 1;
+    resident = std::max(r, 1);
+    sms = n;
+  }
+  const int per_sm = bps > 0 ? bps : resident;
+  const int64_t need = (plan.nup + int64_t(256) * U - 1) / (int64_t(256) * U);
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm));
+  scatter_sym_multi_kernel<E, V, U><<<unsigned(blocks), 256, 0, st>>>(plan.up_rec.as<int4>(), plan.up_ptr.as<int32_t>(),
+                                                                        plan.up_perm.as<int32_t>(), elem, values,
+                                                                        zero_flags, status, plan.nup);
+}
+
+template <typename E, typename V>
+static bool launch_sym_shape(const Plan& plan, const E* elem, V* values, uint8_t* zero_flags, int* status,
+                             ScatterShape shape, cudaStream_t st) {
+  const int bps = shape.blocks_per_sm;
+  switch (shape.slots_per_thread) {
+    case 1: launch_sym_multi<E, V, 1>(plan, elem, values, zero_flags, status, bps, st); return true;
+    case 2: launch_sym_multi<E, V, 2>(plan, elem, values, zero_flags, status, bps, st); return true;
+    case 4: launch_sym_multi<E, V, 4>(plan, elem, values, zero_flags, status, bps, st); return true;
+    case 8: launch_sym_multi<E, V, 8>(plan, elem, values, zero_flags, status, bps, st); return true;
+    default: return false;
+  }
+}
+
 void launch_scatter(const Plan& plan, const void* elem, void* values, uint8_t* zero_flags, int* status, int mode,
-                    cudaStream_t st) {
+                    cudaStream_t st, ScatterShape shape) {
   if (plan.nslots == 0) return;
   int* zero_count = status + 1;
   if (plan.nup > 0) {
+    if (shape.slots_per_thread < 0) shape.slots_per_thread = mode == FQ_FP64 ? 0 : 1;
+    if (shape.slots_per_thread > 0) {
+      bool done = false;
+      if (mode == 1)
+        done = launch_sym_shape(plan, static_cast<const float*>(elem), static_cast<float*>(values), zero_flags, status,
+                                shape, st);
+      else if (mode == 2)
+        done = launch_sym_shape(plan, static_cast<const double*>(elem), static_cast<double*>(values), zero_flags,
+                                status, shape, st);
+      else
+        done = launch_sym_shape(plan, static_cast<const df64*>(elem), static_cast<double*>(values), zero_flags,
+                                status, shape, st);
+      if (done) return;
+    }
     const unsigned blocks = unsigned((plan.nup + 255) / 256);
     const int4* pr = plan.up_rec.as<int4>();
     const int32_t* up = plan.up_ptr.as<int32_t>();
@@ -897,7 +1033,7 @@ static fq_status assemble_launch(fq_ctx* ctx, fq_matrix* m, cudaEvent_t* ev, boo
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[1], ctx->stream));
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[2], ctx->stream));
   launch_scatter(p, mesh->elem.p, m->full_values.p, with_flags ? m->zero_flags.as<uint8_t>() : nullptr, zc, mode,
-                 ctx->stream);
+                 ctx->stream, ctx->scatter_shape);
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[3], ctx->stream));
   if (p.nslots > 0) ctx->launches++;
   return FQ_OK;

@@ -20,6 +20,17 @@ struct fq_ctx;
 
 namespace fq {
 
+// Launch shape of the symmetric scatter: slots_per_thread -1 = by precision
+// (measured on the 3D 32^3 step: one thread per upper slot for float-float
+// values, one slot per thread on a persistent grid for FP32 and IEEE FP64),
+// 0 = one thread per upper slot (scatter_sym_kernel), 1/2/4/8 = that many slots
+// per thread on a persistent grid of blocks_per_sm 256-thread blocks per SM
+// (0 = as many as are resident at once).
+struct ScatterShape {
+  int slots_per_thread = -1;
+  int blocks_per_sm = 0;
+};
+
 // Owned device allocation, charged against the context's HBM budget.
 struct DevBuf {
   fq_ctx* ctx = nullptr;
@@ -151,6 +162,7 @@ struct fq_ctx {
   // the dense direct fallback of unconverged MINRES solves (fq_direct.cu); server
   // lanes leave it off (see fq_server.cpp)
   bool dense_fallback = true;
+  fq::ScatterShape scatter_shape;  // launch shape of the symmetric scatter (fq_ctx_set_scatter_shape)
   bool profiling = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<cudaEvent_t> prof_events;  // four per matrix of a multi-matrix assembly
@@ -213,7 +225,7 @@ fq_status build_plan(fq_ctx* ctx, fq_mesh* mesh, Plan& plan, const Layout& lay);
 // = 1 when every contribution was exactly 0.0; status[1] += count of such
 // slots; status[0] |= 4 if a symmetric plan misses a mirror slot.
 void launch_scatter(const Plan& plan, const void* elem, void* values, uint8_t* zero_flags, int* status, int mode,
-                    cudaStream_t st);
+                    cudaStream_t st, ScatterShape shape = ScatterShape());
 void launch_scatter_diag(const Plan& plan, const void* elem, double* out, int mode, cudaStream_t st);
 void launch_df64_to_double(const void* in, double* out, int64_t n, cudaStream_t st);
 

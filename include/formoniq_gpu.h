@@ -122,6 +122,15 @@ fq_status fq_ctx_profile(fq_ctx* ctx, double* ms, int64_t* launches, int nslots,
  * this device's FP64 (fp64 != 0) or FP32 pipe, in TFLOP/s (2 flops per FMA),
  * from a register-resident FMA-chain kernel timed with CUDA events. */
 fq_status fq_measure_fma_peak(fq_ctx* ctx, int fp64, double* tflops);
+/* Launch shape of the symmetric scatter of this context's assemblies, no
+ * counterpart in the reference: slots_per_thread -1 = by precision (the
+ * default: one thread per upper slot for FQ_FP64, one slot per thread on a
+ * persistent grid for FQ_FP32 and FQ_FP64_IEEE), 0 = one thread per upper slot,
+ * 1/2/4/8 = that many upper slots per thread on a persistent grid of
+ * blocks_per_sm 256-thread blocks per SM (0 = as many as are resident at once).
+ * Every shape sums each slot's contributions in the same order: the values are
+ * bit-identical. */
+fq_status fq_ctx_set_scatter_shape(fq_ctx* ctx, int slots_per_thread, int blocks_per_sm);
 
 /* ---- topology: Complex -------------------------------------------------- */
 /* Complex::from_cells (crates/simplicial/src/topology/complex.rs:278-336):

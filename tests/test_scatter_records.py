@@ -48,3 +48,38 @@ def test_records_visit_every_contribution_in_order():
         for u in range(len(counts)):
             rec = encode(up_ptr, up_perm, u)
             assert decode(rec, up_ptr, up_perm, u) == up_perm[up_ptr[u]:up_ptr[u + 1]]
+
+
+def multi_slot_rounds(nup, grid_threads, U):
+    """The slots each thread of scatter_sym_multi_kernel handles, round by
+    round, and the record loads it issues (current and prefetched): the
+    kernel's index scheme, written out again in Python."""
+    handled, loads = [], []
+    T = grid_threads
+    for tid in range(T):
+        nxt = [tid + i * T for i in range(U)]
+        loads += [u for u in nxt if u < nup]
+        t0 = tid
+        while t0 < nup:
+            cur = nxt
+            t1 = t0 + U * T
+            if t1 < nup:
+                nxt = [t1 + i * T for i in range(U)]
+                loads += [u for u in nxt if u < nup]
+            handled += [u for u in cur if u < nup]
+            t0 = t1
+    return handled, loads
+
+
+def test_multi_slot_rounds_cover_every_slot_once():
+    """Every upper slot is handled exactly once, every record load is in
+    bounds, and no record is loaded twice, for U in 1, 2, 4, 8 over grids
+    smaller and larger than one round."""
+    rng = random.Random(7)
+    for _ in range(300):
+        U = rng.choice([1, 2, 4, 8])
+        nup = rng.randint(0, 3000)
+        T = 256 * rng.randint(1, 6)
+        handled, loads = multi_slot_rounds(nup, T, U)
+        assert sorted(handled) == list(range(nup))
+        assert sorted(loads) == list(range(nup))
