@@ -30,15 +30,15 @@ __all__ = [
     "FQ_MASS", "FQ_DIF_TRIAL", "FQ_DIF_TEST", "FQ_DIF_BOTH", "FQ_ABSOLUTE", "FQ_RELATIVE", "FQ_FP64", "FQ_FP32", "FQ_FP64_IEEE",
     "FqError", "FqUnavailable", "Context", "Mesh", "Matrix", "WhitneyComplex", "MixedProblem", "SolveOpts",
     "Report", "solve_source", "solve_dirac_source", "dirac_system", "minres", "cg", "hx_cg", "hx_apply", "lib_path",
-    "load", "exported_symbols", "FQ_PC_AUTO", "FQ_PC_JACOBI", "FQ_PC_HX", "Server", "FQ_REQ_HODGE", "FQ_REQ_DIRAC",
+    "load", "exported_symbols", "FQ_PC_AUTO", "FQ_PC_JACOBI", "FQ_PC_HX", "FQ_PC_DIRECT", "FQ_PC_COMPARISON", "Server", "FQ_REQ_HODGE", "FQ_REQ_DIRAC",
     "Batch", "FQ_BATCH_MASS", "FQ_BATCH_HDIF", "ElementOperator", "derham_map", "Leapfrog",
-    "source_nodes", "source_form",
+    "source_nodes", "source_form", "SparseLu",
 ]
 
 FQ_MASS, FQ_DIF_TRIAL, FQ_DIF_TEST, FQ_DIF_BOTH = 0, 1, 2, 3
 FQ_ABSOLUTE, FQ_RELATIVE = 0, 1
 FQ_FP64, FQ_FP32, FQ_FP64_IEEE = 0, 1, 2
-FQ_PC_AUTO, FQ_PC_JACOBI, FQ_PC_HX = 0, 1, 2
+FQ_PC_AUTO, FQ_PC_JACOBI, FQ_PC_HX, FQ_PC_DIRECT, FQ_PC_COMPARISON = 0, 1, 2, 3, 4
 FQ_REQ_HODGE, FQ_REQ_DIRAC = 0, 1
 FQ_BATCH_MASS, FQ_BATCH_HDIF = 0, 1
 
@@ -227,6 +227,12 @@ _SIGNATURES = {
     "fq_solve_dirac_source": (ctypes.c_int, [_P, _P, ctypes.c_double, _DP, _DP, _DP, ctypes.POINTER(SolveOpts),
                                              ctypes.POINTER(_Report)]),
     "fq_dirac_system": (ctypes.c_int, [_P, _P, ctypes.c_double, ctypes.POINTER(_P)]),
+    "fq_sparse_lu_create": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(_P)]),
+    "fq_sparse_lu_factor": (ctypes.c_int, [_P, _P]),
+    "fq_sparse_lu_solve": (ctypes.c_int, [_P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
+    "fq_sparse_lu_info": (ctypes.c_int, [_P, _I64P, _I64P, _DP, _I64P, _I64P]),
+    "fq_sparse_lu_destroy": (None, [_P]),
+    "fq_sparse_lu_analyse_host": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int64, _I32P, _I32P, _I32P, _DP]),
 }
 
 
@@ -826,6 +832,60 @@ def dirac_system(mesh: Mesh, mass_term: float) -> Matrix:
     mesh.ctx.check(mesh.ctx.L.fq_dirac_system(mesh.ctx.h, mesh.h, float(mass_term), ctypes.byref(h)),
                    "fq_dirac_system")
     return Matrix(mesh.ctx, h)
+
+
+class SparseLu:
+    """The sparse direct solver (fq_sparse_lu_*), the stand-in for FaerLu
+    (formoniq/src/linalg/faer.rs:51-74): multifrontal LU on a nested-dissection
+    ordering of the Kuhn lattice, its factors preconditioning FP64 GMRES.
+    ``a`` is an assembled square FP64 matrix of a Kuhn cube mesh."""
+
+    def __init__(self, mesh: Mesh, a: Matrix):
+        self.ctx, self.mesh, self.a = mesh.ctx, mesh, a
+        h = _P()
+        self.ctx.check(self.ctx.L.fq_sparse_lu_create(self.ctx.h, mesh.h, a.h, ctypes.byref(h)), "fq_sparse_lu_create")
+        self.h = h
+        self.ctx._adopt(self)
+
+    def factor(self):
+        self.ctx.check(self.ctx.L.fq_sparse_lu_factor(self.h, self.a.h), "fq_sparse_lu_factor")
+        return self
+
+    def solve_device(self, b_ptr: int, x_ptr: int, opts: Optional[SolveOpts] = None) -> "Report":
+        rep = _Report()
+        opts = opts or SolveOpts.default()
+        s = self.ctx.L.fq_sparse_lu_solve(self.h, self.a.h, _P(b_ptr), _P(x_ptr), ctypes.byref(opts), ctypes.byref(rep))
+        if s not in (0, 3):
+            self.ctx.check(s, "fq_sparse_lu_solve")
+        return Report.of(rep)
+
+    def solve(self, b: np.ndarray, opts: Optional[SolveOpts] = None):
+        import torch
+
+        bd = torch.tensor(np.ascontiguousarray(b, np.float64), device="cuda")
+        xd = torch.empty_like(bd)
+        torch.cuda.synchronize()
+        rep = self.solve_device(bd.data_ptr(), xd.data_ptr(), opts)
+        return xd.cpu().numpy(), rep
+
+    def info(self) -> dict:
+        fr, lv, fb, pp = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        fl = ctypes.c_double()
+        self.ctx.check(self.ctx.L.fq_sparse_lu_info(self.h, ctypes.byref(fr), ctypes.byref(lv), ctypes.byref(fl),
+                                                    ctypes.byref(fb), ctypes.byref(pp)))
+        return {"fronts": fr.value, "levels": lv.value, "flops": fl.value, "factor_bytes": fb.value,
+                "perturbed_pivots": pp.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.fq_sparse_lu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def _krylov(fn: str, a: Matrix, b_ptr: int, x_ptr: int, inv_diag_ptr: int = 0, opts=None) -> Report:

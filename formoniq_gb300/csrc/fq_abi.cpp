@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "fq_hx.h"
+#include "fq_sparse_lu.h"
 #include "fq_internal.h"
 
 namespace fq {
@@ -340,6 +341,9 @@ static fq_status mixed_assemble(fq_mixed* P) {
   }
   P->sysview.ctx = ctx;
   P->sysview.mesh = m;
+  P->sysview.kind = EK_KKT;  // the layout of its unknowns (a border row last)
+  P->sysview.grade = P->grade;
+  P->sysview.bc = P->bc;
   P->sysview.nrows = P->sysview.ncols = P->n;
   P->sysview.nnz = P->nnz;
   P->sysview.precision = FQ_FP64;
@@ -1273,7 +1277,7 @@ static fq_status comparison_lengths(fq_ctx* ctx, const fq_mesh* m, std::vector<d
 // SPD preconditioners of the relative Dirac system on a Kuhn mesh, both from
 // the Euclidean comparison geometry (the operator's Lorentzian mass is
 // indefinite, so |diag(S)| = m |diag(M)| weighs time-like faces badly):
-//   FQ_PC_AUTO: the inverse diagonal of the comparison masses M_j, j = 0..n
+//   FQ_PC_COMPARISON: the inverse diagonal of the comparison masses M_j, j = 0..n
 //     (the L^2 Riesz map's diagonal; as cheap per iteration as Jacobi);
 //   FQ_PC_HX:   diag(hdif_gram(j)) of the comparison geometry, each block an HX
 //     multigrid (the H Lambda Riesz map; fewer iterations on small meshes, a
@@ -1316,16 +1320,123 @@ static fq_status dirac_comparison(fq_ctx* ctx, fq_mesh* m, bool hx, DiracPrecond
   return FQ_OK;
 }
 
+// The relative harmonic field of the massless Dirac operator in the flat
+// relative layout (top_harmonic, problems/dirac.rs:552-570): zero below the top
+// grade, h_n = M_n^-1 z on the cells, z the coherent orientation. The relative
+// top-grade mass is diagonal (one Whitney n-form per cell).
+static fq_status top_harmonic(fq_ctx* ctx, fq_mesh* m, int64_t nrel, DevBuf& h, int64_t* top_off) {
+  const int n = m->dim;
+  if (m->orientation.empty()) {
+    std::vector<int8_t> tmp(static_cast<size_t>(m->ncells));
+    FQ_TRY(fq_mesh_orientation(m, tmp.data()));
+  }
+  fq_matrix* mn = nullptr;
+  FQ_TRY(make_matrix(ctx, m, EK_MASS, n, FQ_RELATIVE, FQ_FP64, 0.0, &mn));
+  std::unique_ptr<fq_matrix> g(mn);
+  const int64_t nt = m->ninterior[n];
+  DevBuf d;
+  FQ_TRY(d.alloc(ctx, std::max<int64_t>(nt, 1) * 8));
+  vec_diag(mn, d.as<double>(), ctx->stream);
+  ctx->launches++;
+  std::vector<double> dh(static_cast<size_t>(std::max<int64_t>(nt, 1))),
+      hh(static_cast<size_t>(std::max<int64_t>(nrel, 1)), 0.0);
+  FQ_CUDA(ctx, cudaMemcpyAsync(dh.data(), d.p, nt * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  int64_t off = 0;
+  for (int k = 0; k < n; ++k) off += m->ninterior[k];
+  for (int64_t c = 0; c < nt; ++c) hh[off + c] = double(m->orientation[c]) / dh[c];
+  FQ_TRY(h.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));
+  FQ_CUDA(ctx, cudaMemcpyAsync(h.p, hh.data(), nrel * 8, cudaMemcpyHostToDevice, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *top_off = off;
+  return FQ_OK;
+}
+
+// The direct route of the Dirac source problem: the relative system (bordered
+// with the top harmonic at m = 0 when it spans the kernel, as solve_bordered,
+// problems/dirac.rs:525-531, 578-598) factored by the sparse direct solver,
+// GMRES in FP64 to opts->rtol.
+static fq_status dirac_direct(fq_ctx* ctx, fq_mesh* m, fq_matrix* sii, double mass_term, int64_t nrel,
+                              const double* rhs, double* x, const fq_solve_opts* o, fq_report* r) {
+  std::vector<int32_t> dofv;
+  FQ_TRY(layout_dof_vertices(ctx, m, EK_DIRAC, 0, FQ_RELATIVE, nrel, dofv));
+  const int32_t* rp = sii->rp;
+  const int32_t* ci = sii->ci;
+  const double* val = sii->values.as<double>();
+  int64_t nsys = nrel;
+  DevBuf brp, bci, bval, bb, bx, h;
+  bool bordered = false;
+  if (mass_term == 0.0 && nrel > 0) {
+    DevBuf sh;
+    int64_t off = 0;
+    FQ_TRY(top_harmonic(ctx, m, nrel, h, &off));
+    FQ_TRY(sh.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));
+    launch_spmv(sii, h.p, sh.p, ctx->stream);
+    ctx->launches++;
+    std::vector<double> hv(static_cast<size_t>(nrel)), sv(static_cast<size_t>(nrel));
+    FQ_CUDA(ctx, cudaMemcpyAsync(hv.data(), h.p, nrel * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    FQ_CUDA(ctx, cudaMemcpyAsync(sv.data(), sh.p, nrel * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double hn = 0, sn = 0;
+    for (int64_t i = 0; i < nrel; ++i) {
+      hn += hv[i] * hv[i];
+      sn += sv[i] * sv[i];
+    }
+    if (std::sqrt(sn) <= 1e-8 * std::sqrt(hn)) {
+      // the top harmonic spans the kernel: border the system with it
+      FQ_TRY(border_csr(ctx, sii, h.as<double>() + off, off, m->ninterior[m->dim], brp, bci, bval));
+      rp = brp.as<int32_t>();
+      ci = bci.as<int32_t>();
+      val = bval.as<double>();
+      nsys = nrel + 1;
+      dofv.resize(size_t(nsys) * 5, -1);
+      FQ_TRY(bb.alloc(ctx, nsys * 8));
+      FQ_TRY(bx.alloc(ctx, nsys * 8));
+      FQ_CUDA(ctx, cudaMemsetAsync(bb.p, 0, nsys * 8, ctx->stream));
+      FQ_CUDA(ctx, cudaMemcpyAsync(bb.p, rhs, nrel * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+      bordered = true;
+    }
+  }
+  // the analysis depends on the pattern only: kept on the mesh for the next
+  // solve (new lengths or load), redone when the pattern changed
+  std::shared_ptr<SparseLu>& cached = m->dirac_lu[bordered ? 1 : 0];
+  int32_t nnz32 = 0;
+  FQ_CUDA(ctx, cudaMemcpyAsync(&nnz32, rp + nsys, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const int64_t nnz = nnz32;
+  if (!cached || cached->n != nsys || cached->nnz != nnz) {
+    cached.reset();
+    auto lu = std::make_shared<SparseLu>();
+    FQ_TRY(sparse_lu_build(ctx, m, nsys, rp, ci, dofv, *lu));
+    cached = lu;
+  }
+  SparseLu& lu = *cached;
+  FQ_TRY(sparse_lu_factor(ctx, lu, rp, ci, val, FQ_FP32));
+  const fq_status gs = sparse_lu_solve(ctx, lu, rp, ci, val, bordered ? bb.as<double>() : rhs,
+                                       bordered ? bx.as<double>() : x, o->rtol, o->max_iters, r);
+  if (gs != FQ_OK && gs != FQ_NOT_CONVERGED) return gs;
+  if (bordered) FQ_CUDA(ctx, cudaMemcpyAsync(x, bx.p, nrel * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+  return FQ_OK;
+}
+
 fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* m, double mass_term, const double* load_h,
                                 const double* lift_h, double* x_h, const fq_solve_opts* o, fq_report* rep) {
   if (!ctx || !m || !load_h || !x_h) return FQ_INVALID_ARG;
-  if (mass_term == 0.0)
-    return set_error(ctx, FQ_UNSUPPORTED, "massless Dirac needs the bordered direct solve; pass a nonzero mass term");
   FQ_GUARD_BEGIN
   fq_solve_opts d;
   fq_default_solve_opts(&d);
   if (!o) o = &d;
   const int n = m->dim;
+  const int pcsel = o->preconditioner;
+  const bool kuhn = m->kuhn_nbox > 0;
+  if (pcsel == FQ_PC_DIRECT && !kuhn)
+    return set_error(ctx, FQ_UNSUPPORTED, "the direct Dirac solve needs a Kuhn cube mesh (fq_mesh_kuhn_cube)");
+  if ((pcsel == FQ_PC_HX || pcsel == FQ_PC_COMPARISON) && !kuhn)
+    return set_error(ctx, FQ_UNSUPPORTED, "the comparison-lattice Dirac preconditioners need a Kuhn cube mesh");
+  const bool direct = pcsel == FQ_PC_DIRECT || (pcsel == FQ_PC_AUTO && kuhn);
+  if (mass_term == 0.0 && !direct)
+    return set_error(ctx, FQ_UNSUPPORTED, "the massless Dirac system is singular: it needs the bordered direct solve "
+                                          "(FQ_PC_AUTO or FQ_PC_DIRECT on a Kuhn cube mesh)");
   int64_t nfull = 0, nrel = 0;
   for (int k = 0; k <= n; ++k) {
     nfull += m->nsimp[k];
@@ -1378,29 +1489,30 @@ fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* m, double mass_term, const
   vec_gather(load.as<double>(), dmap.as<int32_t>(), rhs.as<double>(), nrel, st);
   launch_spmv(sib.get(), lift.p, tmp.p, st);
   vec_sub(rhs.as<double>(), tmp.as<double>(), nrel, st);
-  vec_diag(sii, diag.as<double>(), st);
-  vec_recip(diag.as<double>(), dinv.as<double>(), nullptr, nrel, 1, st);
-  ctx->launches += 5;
-  // preconditioner: HX blocks of the comparison geometry on Kuhn meshes, else |diag(S)|
-  const int pcsel = o->preconditioner;
-  if (pcsel == FQ_PC_HX && m->kuhn_nbox <= 0)
-    return set_error(ctx, FQ_UNSUPPORTED, "the HX Dirac preconditioner needs a Kuhn cube mesh");
-  std::unique_ptr<DiracPrecond> dp;
-  if (pcsel != FQ_PC_JACOBI && m->kuhn_nbox > 0 && nrel > 0) {
-    dp = std::make_unique<DiracPrecond>();
-    FQ_TRY(dirac_comparison(ctx, m, pcsel == FQ_PC_HX, *dp));
-  }
-  const double* pc_diag = !dp ? dinv.as<double>() : (dp->use_hx ? nullptr : dp->dinv.as<double>());
+  ctx->launches += 3;
   fq_report r{};
-  FQ_TRY(minres_run<double>(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, sii->nnz, pc_diag,
-                            dp && dp->use_hx ? &dp->hx : nullptr, rhs.as<double>(), x.as<double>(), o->rtol,
-                            o->max_iters, &r));
-  // the reference solves this system by LU: a small one MINRES left unconverged is finished that way
-  if (!r.converged && ctx->dense_fallback && nrel <= kDenseMax && dense_fallback_available()) {
-    FQ_TRY(dense_lu_solve(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, rhs.as<double>(), x.as<double>()));
-    r.converged = 1;
-  }
-  {
+  if (direct) {
+    FQ_TRY(dirac_direct(ctx, m, sii, mass_term, nrel, rhs.as<double>(), x.as<double>(), o, &r));
+  } else {
+    vec_diag(sii, diag.as<double>(), st);
+    vec_recip(diag.as<double>(), dinv.as<double>(), nullptr, nrel, 1, st);
+    ctx->launches += 2;
+    // preconditioner: from the comparison lattice on Kuhn meshes (its mass
+    // diagonal, or HX blocks of its hdif_gram), else |diag(S)|
+    std::unique_ptr<DiracPrecond> dp;
+    if ((pcsel == FQ_PC_COMPARISON || pcsel == FQ_PC_HX) && nrel > 0) {
+      dp = std::make_unique<DiracPrecond>();
+      FQ_TRY(dirac_comparison(ctx, m, pcsel == FQ_PC_HX, *dp));
+    }
+    const double* pc_diag = !dp ? dinv.as<double>() : (dp->use_hx ? nullptr : dp->dinv.as<double>());
+    FQ_TRY(minres_run<double>(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, sii->nnz, pc_diag,
+                              dp && dp->use_hx ? &dp->hx : nullptr, rhs.as<double>(), x.as<double>(), o->rtol,
+                              o->max_iters, &r));
+    // the reference solves this system by LU: a small one MINRES left unconverged is finished that way
+    if (!r.converged && ctx->dense_fallback && nrel <= kDenseMax && dense_fallback_available()) {
+      FQ_TRY(dense_lu_solve(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, rhs.as<double>(), x.as<double>()));
+      r.converged = 1;
+    }
     DevBuf rr;
     FQ_TRY(rr.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));
     double rn = 0, bn = 0;
@@ -1414,6 +1526,7 @@ fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* m, double mass_term, const
   FQ_CUDA(ctx, cudaMemsetAsync(ext.p, 0, nfull * 8, st));
   vec_scatter_map(x.as<double>(), dmap.as<int32_t>(), ext.as<double>(), nrel, st);
   vec_add(ext.as<double>(), lift.as<double>(), nfull, st);
+  ctx->launches += 2;
   FQ_CUDA(ctx, cudaMemcpyAsync(x_h, ext.p, nfull * 8, cudaMemcpyDeviceToHost, st));
   FQ_CUDA(ctx, cudaStreamSynchronize(st));
   if (rep) *rep = r;

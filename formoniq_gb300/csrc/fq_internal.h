@@ -19,6 +19,7 @@
 struct fq_ctx;
 
 namespace fq {
+struct SparseLu;
 
 // Launch shape of the symmetric scatter: slots_per_thread -1 = by precision
 // (measured on the 3D 32^3 step: one thread per upper slot for float-float
@@ -128,6 +129,9 @@ struct fq_mesh {
   // per-cell slot buffer, kept across calls
   int source_degree = -1;
   fq::DevBuf source_rule, source_slots;
+  // the sparse direct solver's analysis of the relative Dirac system (plain,
+  // and bordered for the massless case), kept for the next solve on this mesh
+  std::shared_ptr<fq::SparseLu> dirac_lu[2];
 };
 
 struct fq_matrix {

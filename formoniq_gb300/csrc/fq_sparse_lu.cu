@@ -1,0 +1,1117 @@
+// Numeric phase of the sparse direct solver (fq_sparse_lu.h): batched front
+// assembly, partial LU in tiles with tournament pivoting, triangular solves,
+// and the FP64 GMRES that the factors precondition. The factorization runs in
+// FP32 (tiles of 128 columns) or FP64 (tiles of 64 columns).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fq_sparse_lu.h"
+
+namespace fq {
+
+namespace {
+
+template <typename T>
+struct SlCfg;
+template <>
+struct SlCfg<float> {
+  static constexpr int TILE = 128;    // columns per tile step
+  static constexpr int ROWS = 256;    // rows of a tournament leaf or merge
+  static constexpr int BM = 128;      // product tile (BM x BM outputs per CTA)
+  static constexpr int TM = 8;        // outputs per thread and dimension
+  static constexpr int MAXM = 46000;  // front rows a solve CTA holds in shared memory
+};
+template <>
+struct SlCfg<double> {
+  static constexpr int TILE = 64;
+  static constexpr int ROWS = 128;
+  static constexpr int BM = 64;
+  static constexpr int TM = 4;
+  static constexpr int MAXM = 26000;
+};
+static_assert(SlCfg<float>::TILE <= kTile && SlCfg<double>::TILE <= kTile, "tile store sized for kTile");
+
+constexpr int kBK = 32;  // K chunk of the products
+constexpr int kThreads = 256;
+
+// ---------------------------------------------------------------------------
+// assembly
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void sl_assemble_kernel(const int32_t* __restrict__ slot, const int32_t* __restrict__ row,
+                                   const int64_t* __restrict__ off, int64_t b, int64_t e,
+                                   const int32_t* __restrict__ ci, const double* __restrict__ val,
+                                   const double* __restrict__ d, T* __restrict__ pool) {
+  for (int64_t q = b + int64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < e; q += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t s = slot[q];
+    pool[off[q]] = T(d[row[q]] * val[s] * d[ci[s]]);
+  }
+}
+
+// d_i = 1 / sqrt(max_j |a_ij|) (1 for an empty or zero row)
+__global__ void sl_row_scale_kernel(const int32_t* __restrict__ rp, const double* __restrict__ val, int64_t n,
+                                    double* __restrict__ d) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    double mx = 0.0;
+    for (int32_t t = rp[i]; t < rp[i + 1]; ++t) mx = fmax(mx, fabs(val[t]));
+    d[i] = mx > 0.0 && isfinite(mx) ? 1.0 / sqrt(mx) : 1.0;
+  }
+}
+
+// The Schur complement of child `which` (0 or 1) of every front of the list
+// added into the front at its parent-local rows and columns.
+template <typename T>
+__global__ void sl_extend_add_kernel(const FrontDesc* __restrict__ fd, const int32_t* __restrict__ list, int which,
+                                     const int32_t* __restrict__ ea, T* __restrict__ pool) {
+  const FrontDesc X = fd[list[blockIdx.y]];
+  const int c = which == 0 ? X.child0 : X.child1;
+  if (c < 0) return;
+  const FrontDesc C = fd[c];
+  const int64_t u = C.m - C.f;
+  const int64_t total = u * u;
+  const int32_t* map = ea + C.ea_off;
+  for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t bcol = t / u, arow = t - bcol * u;
+    const T v = pool[C.off + (C.f + bcol) * C.m + (C.f + arow)];
+    pool[X.off + int64_t(map[bcol]) * X.m + map[arow]] += v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pivot selection over the whole fully summed panel (tournament pivoting):
+// the panel of a step is the front's fully summed rows k..f-1 in the step's
+// columns k..k+b-1. Leaves of ROWS rows each pick b candidate rows by Gaussian
+// elimination with partial pivoting (GEPP); pairs of candidate sets are merged
+// by GEPP on their original rows, up a binary tree, until b winners remain, in
+// GEPP's pivot order. Moving them to the top rows and factoring the tile
+// without further interchanges reproduces the final GEPP (communication-
+// avoiding LU, Grigori, Demmel and Xiang, SIAM J. Matrix Anal. Appl. 32,
+// 2011): a pivoting as wide as partial pivoting restricted to the front's
+// fully summed rows.
+// ---------------------------------------------------------------------------
+// GEPP on the rows x b block held column-major in blk (column stride ld);
+// idx[i] names row i. On return idx[0..min(rows, b)) are the pivot rows in
+// pivot order.
+template <typename T>
+__device__ void gepp_select(T* blk, int ld, int* idx, int rows, int b) {
+  __shared__ int s_p;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int steps = min(rows, b);
+  for (int j = 0; j < steps; ++j) {
+    if (tid < 32) {
+      T best = T(-1);
+      int bi = j;
+      for (int i = j + tid; i < rows; i += 32) {
+        const T a = fabs(blk[j * ld + i]);
+        if (a > best || (a == best && i < bi)) {
+          best = a;
+          bi = i;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const T ob = __shfl_down_sync(0xffffffffu, best, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (tid == 0) s_p = bi;
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (p != j) {
+      for (int l = tid; l < b; l += nt) {
+        const T t = blk[l * ld + j];
+        blk[l * ld + j] = blk[l * ld + p];
+        blk[l * ld + p] = t;
+      }
+      if (tid == 0) {
+        const int t = idx[j];
+        idx[j] = idx[p];
+        idx[p] = t;
+      }
+    }
+    __syncthreads();
+    const T d = blk[j * ld + j];
+    if (d != T(0) && isfinite(d)) {
+      const T rinv = T(1) / d;
+      for (int i = j + 1 + tid; i < rows; i += nt) blk[j * ld + i] *= rinv;
+      __syncthreads();
+      const int w = rows - j - 1, c = b - j - 1;
+      for (int t = tid; t < w * c; t += nt) {
+        const int l = j + 1 + t / w, i = j + 1 + t % w;
+        blk[l * ld + i] -= blk[j * ld + i] * blk[l * ld + j];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Leaves: block q of every front's panel; candidate set q = its b GEPP winners.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) sl_tourn_leaf_kernel(const FrontDesc* __restrict__ fd,
+                                                                 const int32_t* __restrict__ list, int k,
+                                                                 const T* __restrict__ pool, int maxsets,
+                                                                 int32_t* __restrict__ cand,
+                                                                 int32_t* __restrict__ ccount) {
+  using C = SlCfg<T>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* blk = reinterpret_cast<T*>(smraw);
+  __shared__ int idx[C::ROWS];
+  const FrontDesc F = fd[list[blockIdx.y]];
+  if (F.f <= k) return;
+  const int b = min(C::TILE, F.f - k);
+  const int q = blockIdx.x;
+  const int r0 = k + q * C::ROWS;
+  if (r0 >= F.f) return;
+  const int rows = min(C::ROWS, F.f - r0);
+  const int64_t m = F.m;
+  const T* A = pool + F.off;
+  for (int t = threadIdx.x; t < rows * b; t += blockDim.x) {
+    const int col = t / rows, row = t - col * rows;
+    blk[col * (C::ROWS + 1) + row] = A[(k + col) * m + (r0 + row)];
+  }
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) idx[i] = r0 + i;
+  __syncthreads();
+  gepp_select<T>(blk, C::ROWS + 1, idx, rows, b);
+  const int64_t set = int64_t(blockIdx.y) * maxsets + q;
+  const int nw = min(rows, b);
+  for (int i = threadIdx.x; i < nw; i += blockDim.x) cand[set * kTile + i] = idx[i];
+  if (threadIdx.x == 0) ccount[set] = nw;
+}
+
+// One tournament round: set q of the output = GEPP winners of sets 2q and
+// 2q+1 of the input, or set 2q copied when 2q+1 is empty. Sets beyond a
+// front's own count are empty (count 0).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) sl_tourn_merge_kernel(const FrontDesc* __restrict__ fd,
+                                                                  const int32_t* __restrict__ list, int k,
+                                                                  const T* __restrict__ pool, int maxsets,
+                                                                  int nsets_in, const int32_t* __restrict__ cin,
+                                                                  const int32_t* __restrict__ nin,
+                                                                  int32_t* __restrict__ cout,
+                                                                  int32_t* __restrict__ nout) {
+  using C = SlCfg<T>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* blk = reinterpret_cast<T*>(smraw);
+  __shared__ int idx[C::ROWS];
+  const FrontDesc F = fd[list[blockIdx.y]];
+  const int q = blockIdx.x;
+  const int64_t base = int64_t(blockIdx.y) * maxsets;
+  if (F.f <= k) {
+    if (threadIdx.x == 0) nout[base + q] = 0;
+    return;
+  }
+  const int b = min(C::TILE, F.f - k);
+  const int64_t a0 = base + 2 * q, a1 = base + 2 * q + 1;
+  const int na = 2 * q < nsets_in ? nin[a0] : 0;
+  const int nb = 2 * q + 1 < nsets_in ? nin[a1] : 0;
+  if (nb == 0) {
+    for (int i = threadIdx.x; i < na; i += blockDim.x) cout[(base + q) * kTile + i] = cin[a0 * kTile + i];
+    if (threadIdx.x == 0) nout[base + q] = na;
+    return;
+  }
+  const int rows = na + nb;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) idx[i] = i < na ? cin[a0 * kTile + i] : cin[a1 * kTile + i - na];
+  __syncthreads();
+  const int64_t m = F.m;
+  const T* A = pool + F.off;
+  for (int t = threadIdx.x; t < rows * b; t += blockDim.x) {
+    const int col = t / rows, row = t - col * rows;
+    blk[col * (C::ROWS + 1) + row] = A[(k + col) * m + idx[row]];
+  }
+  __syncthreads();
+  gepp_select<T>(blk, C::ROWS + 1, idx, rows, b);
+  const int nw = min(rows, b);
+  for (int i = threadIdx.x; i < nw; i += blockDim.x) cout[(base + q) * kTile + i] = idx[i];
+  if (threadIdx.x == 0) nout[base + q] = nw;
+}
+
+// The winners (set 0) as a sequence of row interchanges: for j = 0..b-1, row
+// k+j is swapped with row piv[start + k + j] (front-local), applied in order,
+// which leaves winner j at row k+j. Positions k+j not yet filled hold rows of
+// the top block k..k+b-1 (an interchange only ever moves a top row down), so
+// tracking where those rows are suffices.
+__global__ void sl_swap_sequence_kernel(const FrontDesc* __restrict__ fd, const int32_t* __restrict__ list, int k,
+                                        int tile, int maxsets, const int32_t* __restrict__ cand,
+                                        int32_t* __restrict__ piv) {
+  __shared__ int at_top[kTile];  // original top row now at position k+i (i not yet filled)
+  __shared__ int where[kTile];   // position of original top row k+i
+  const FrontDesc F = fd[list[blockIdx.x]];
+  if (F.f <= k || threadIdx.x != 0) return;
+  const int b = min(tile, F.f - k);
+  const int32_t* w = cand + int64_t(blockIdx.x) * maxsets * kTile;
+  for (int i = 0; i < b; ++i) {
+    at_top[i] = k + i;
+    where[i] = k + i;
+  }
+  for (int j = 0; j < b; ++j) {
+    const int r = w[j];
+    const bool top = r >= k && r < k + b;
+    const int t = top ? where[r - k] : r;
+    piv[F.start + k + j] = t;
+    if (t != k + j) {
+      const int x = at_top[j];  // the top row at k+j moves to t
+      where[x - k] = t;
+      if (t < k + b) at_top[t - k] = x;
+    }
+    if (top) where[r - k] = k + j;
+    at_top[j] = r;
+  }
+}
+
+// The step's interchanges on every column of the front (fully summed rows only).
+template <typename T>
+__global__ void sl_apply_swaps_kernel(const FrontDesc* __restrict__ fd, const int32_t* __restrict__ list, int k,
+                                      int tile, const int32_t* __restrict__ piv, T* __restrict__ pool) {
+  const FrontDesc F = fd[list[blockIdx.y]];
+  if (F.f <= k) return;
+  const int b = min(tile, F.f - k);
+  const int64_t m = F.m;
+  T* A = pool + F.off;
+  for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < m; c += int64_t(gridDim.x) * blockDim.x) {
+    T* col = A + c * m;
+    for (int j = 0; j < b; ++j) {
+      const int t = piv[F.start + k + j];
+      if (t != k + j) {
+        const T v = col[k + j];
+        col[k + j] = col[t];
+        col[t] = v;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// the tile of the partial factorization (its rows already in pivot order): LU
+// without interchanges, a pivot below the floor perturbed, and the tile's
+// triangular inverses
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kThreads) sl_tile_kernel(const FrontDesc* __restrict__ fd,
+                                                           const int32_t* __restrict__ list, int k,
+                                                           T* __restrict__ pool, T* __restrict__ tiles,
+                                                           int* __restrict__ status, T thresh) {
+  using C = SlCfg<T>;
+  constexpr int TL = C::TILE, LD = C::TILE + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* Tt = reinterpret_cast<T*>(smraw);  // [TL][LD], column-major Tt[col * LD + row]
+  T* Xs = Tt + TL * LD;                 // inverse under construction
+  __shared__ T s_val;
+  const FrontDesc F = fd[list[blockIdx.x]];
+  if (F.f <= k) return;
+  const int b = min(TL, F.f - k);
+  const int64_t m = F.m;
+  T* A = pool + F.off;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int t = tid; t < b * b; t += nt) {
+    const int col = t / b, row = t - col * b;
+    Tt[col * LD + row] = A[(k + col) * m + (k + row)];
+  }
+  __syncthreads();
+  int npert = 0, nbad = 0;
+  for (int j = 0; j < b; ++j) {
+    if (tid == 0) {
+      T d = Tt[j * LD + j];
+      if (!isfinite(d)) {
+        ++nbad;
+        d = thresh;
+      } else if (fabs(d) < thresh) {
+        ++npert;
+        d = d < T(0) ? -thresh : thresh;
+      }
+      Tt[j * LD + j] = d;
+      s_val = T(1) / d;
+    }
+    __syncthreads();
+    const T rinv = s_val;
+    for (int i = j + 1 + tid; i < b; i += nt) Tt[j * LD + i] *= rinv;
+    __syncthreads();
+    const int w = b - j - 1;
+    for (int t = tid; t < w * w; t += nt) {
+      const int l = j + 1 + t / w, i = j + 1 + t % w;
+      Tt[l * LD + i] -= Tt[j * LD + i] * Tt[l * LD + j];
+    }
+    __syncthreads();
+  }
+  if (tid == 0 && (npert || nbad)) {
+    atomicAdd(status, npert);
+    atomicAdd(status + 1, nbad);
+  }
+  for (int t = tid; t < b * b; t += nt) {
+    const int col = t / b, row = t - col * b;
+    A[(k + col) * m + (k + row)] = Tt[col * LD + row];
+  }
+  // inverses: unit lower L^-1, then U^-1; one thread per column
+  T* out = tiles + F.tile_off + int64_t(k / TL) * 2 * TL * TL;
+  if (tid < b) {
+    const int j = tid;
+    for (int i = 0; i < b; ++i) Xs[j * LD + i] = T(0);
+    Xs[j * LD + j] = T(1);
+    for (int i = j + 1; i < b; ++i) {
+      T s = T(0);
+      for (int l = j; l < i; ++l) s += Tt[l * LD + i] * Xs[j * LD + l];
+      Xs[j * LD + i] = -s;
+    }
+  }
+  __syncthreads();
+  for (int t = tid; t < TL * TL; t += nt) {
+    const int col = t / TL, row = t - col * TL;
+    out[t] = (col < b && row < b) ? Xs[col * LD + row] : T(0);
+  }
+  __syncthreads();
+  if (tid < b) {
+    const int j = tid;
+    for (int i = 0; i < b; ++i) Xs[j * LD + i] = T(0);
+    Xs[j * LD + j] = T(1) / Tt[j * LD + j];
+    for (int i = j - 1; i >= 0; --i) {
+      T s = T(0);
+      for (int l = i + 1; l <= j; ++l) s += Tt[l * LD + i] * Xs[j * LD + l];
+      Xs[j * LD + i] = -s / Tt[i * LD + i];
+    }
+  }
+  __syncthreads();
+  for (int t = tid; t < TL * TL; t += nt) {
+    const int col = t / TL, row = t - col * TL;
+    out[TL * TL + t] = (col < b && row < b) ? Xs[col * LD + row] : T(0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// the three products of a tile step, one kernel: a BM x BM output tile per CTA,
+// K <= TILE in chunks of kBK, TM x TM outputs per thread.
+//   mode 0 (L panel):  A[k+b+r, k+c]   = sum_q A[k+b+r, k+q] invU[q, c]        (rows below the tile)
+//   mode 1 (U panel):  A[k+r, k+b+c]   = sum_q invL[r, q] A[k+q, k+b+c]        (columns right of it)
+//   mode 2 (trailing): A[k+b+r, k+b+c] -= sum_q A[k+b+r, k+q] A[k+q, k+b+c]
+// In modes 0 and 1 the output overwrites an operand; each CTA owns whole rows
+// (mode 0) or whole columns (mode 1) of it and writes after its last read.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Vec16;  // TM/2 consecutive values in one 16-byte load
+template <>
+struct Vec16<float> {
+  static __device__ __forceinline__ void load(const float* p, float* o) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    o[0] = v.x;
+    o[1] = v.y;
+    o[2] = v.z;
+    o[3] = v.w;
+  }
+};
+template <>
+struct Vec16<double> {
+  static __device__ __forceinline__ void load(const double* p, double* o) {
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    o[0] = v.x;
+    o[1] = v.y;
+  }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) sl_gemm_kernel(const FrontDesc* __restrict__ fd,
+                                                           const int32_t* __restrict__ list, int k, int mode,
+                                                           T* __restrict__ pool, const T* __restrict__ tiles) {
+  using C = SlCfg<T>;
+  constexpr int BM = C::BM, TM = C::TM, H = TM / 2, TL = C::TILE;
+  constexpr int BP = BM + 16 / int(sizeof(T));  // padded row of the B chunk, 16-byte aligned
+  __shared__ __align__(16) T As[kBK][BM];
+  __shared__ __align__(16) T Bs[kBK][BP];
+  const FrontDesc F = fd[list[blockIdx.y]];
+  if (F.f <= k) return;
+  const int b = min(TL, F.f - k);
+  const int64_t m = F.m;
+  const int64_t rest = m - k - b;
+  int64_t rows, cols;
+  if (mode == 0) {
+    rows = rest;
+    cols = b;
+  } else if (mode == 1) {
+    rows = b;
+    cols = rest;
+  } else {
+    rows = rest;
+    cols = rest;
+  }
+  if (rows <= 0 || cols <= 0) return;
+  const int64_t tr = (rows + BM - 1) / BM, tc = (cols + BM - 1) / BM;
+  const int64_t tile = blockIdx.x;
+  if (tile >= tr * tc) return;
+  const int64_t r0 = (tile % tr) * BM, c0 = (tile / tr) * BM;
+  T* P = pool + F.off;
+  const T* inv = tiles + F.tile_off + int64_t(k / TL) * 2 * TL * TL;
+  const T* Xp;
+  int64_t ldx;
+  const T* Yp;
+  int64_t ldy;
+  T* Cp;
+  if (mode == 0) {
+    Xp = P + int64_t(k) * m + (k + b + r0);
+    ldx = m;
+    Yp = inv + TL * TL + c0 * TL;  // invU, ld TL
+    ldy = TL;
+    Cp = P + int64_t(k + c0) * m + (k + b + r0);
+  } else if (mode == 1) {
+    Xp = inv + r0;  // invL, ld TL
+    ldx = TL;
+    Yp = P + (k + b + c0) * m + k;
+    ldy = m;
+    Cp = P + (k + b + c0) * m + (k + r0);
+  } else {
+    Xp = P + int64_t(k) * m + (k + b + r0);
+    ldx = m;
+    Yp = P + (k + b + c0) * m + k;
+    ldy = m;
+    Cp = P + (k + b + c0) * m + (k + b + r0);
+  }
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  T acc[TM][TM];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TM; ++j) acc[i][j] = T(0);
+  const int64_t rlim = rows - r0, clim = cols - c0;
+  for (int q0 = 0; q0 < b; q0 += kBK) {
+    for (int t = tid; t < BM * kBK; t += kThreads) {
+      const int q = t / BM, r = t - q * BM;
+      As[q][r] = (r < rlim && q0 + q < b) ? Xp[int64_t(q0 + q) * ldx + r] : T(0);
+    }
+    for (int t = tid; t < BM * kBK; t += kThreads) {
+      const int c = t / kBK, q = t - c * kBK;
+      Bs[q][c] = (c < clim && q0 + q < b) ? Yp[int64_t(c) * ldy + q0 + q] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int q = 0; q < kBK; ++q) {
+      T av[TM], bv[TM];
+      Vec16<T>::load(&As[q][ty * H], av);
+      Vec16<T>::load(&As[q][BM / 2 + ty * H], av + H);
+      Vec16<T>::load(&Bs[q][tx * H], bv);
+      Vec16<T>::load(&Bs[q][BM / 2 + tx * H], bv + H);
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TM; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < TM; ++j) {
+    const int c = (j < H ? tx * H + j : BM / 2 + tx * H + (j - H));
+    if (c >= clim) continue;
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      const int r = (i < H ? ty * H + i : BM / 2 + ty * H + (i - H));
+      if (r >= rlim) continue;
+      T* dst = Cp + int64_t(c) * m + r;
+      if (mode == 2)
+        *dst -= acc[i][j];
+      else
+        *dst = acc[i][j];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// solves: one CTA per front, the front's right-hand side in shared memory
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kThreads) sl_forward_kernel(const FrontDesc* __restrict__ fd,
+                                                              const int32_t* __restrict__ list,
+                                                              const T* __restrict__ pool,
+                                                              const T* __restrict__ tiles,
+                                                              const int32_t* __restrict__ piv,
+                                                              const int32_t* __restrict__ ea, T* __restrict__ work,
+                                                              T* __restrict__ uvec) {
+  using C = SlCfg<T>;
+  constexpr int TL = C::TILE;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* r = reinterpret_cast<T*>(smraw);
+  __shared__ T y[TL];
+  const FrontDesc F = fd[list[blockIdx.x]];
+  const int m = F.m, f = F.f, tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < m; i += nt) r[i] = i < f ? work[F.start + i] : T(0);
+  __syncthreads();
+  for (int which = 0; which < 2; ++which) {
+    const int c = which == 0 ? F.child0 : F.child1;
+    if (c < 0) continue;
+    const FrontDesc Cd = fd[c];
+    const int u = Cd.m - Cd.f;
+    for (int t = tid; t < u; t += nt) r[ea[Cd.ea_off + t]] += uvec[Cd.uvec_off + t];
+    __syncthreads();
+  }
+  // the front's row interchanges, in the order the factorization made them
+  if (tid == 0)
+    for (int p = 0; p < f; ++p) {
+      const int t = piv[F.start + p];
+      if (t != p) {
+        const T a = r[p];
+        r[p] = r[t];
+        r[t] = a;
+      }
+    }
+  __syncthreads();
+  const T* P = pool + F.off;
+  for (int k = 0; k < f; k += TL) {
+    const int b = min(TL, f - k);
+    const T* iL = tiles + F.tile_off + int64_t(k / TL) * 2 * TL * TL;
+    if (tid < b) {
+      T s = T(0);
+      for (int l = 0; l <= tid; ++l) s += iL[l * TL + tid] * r[k + l];
+      y[tid] = s;
+    }
+    __syncthreads();
+    if (tid < b) r[k + tid] = y[tid];
+    for (int i = k + b + tid; i < m; i += nt) {
+      T s = T(0);
+      for (int l = 0; l < b; ++l) s += P[int64_t(k + l) * m + i] * y[l];
+      r[i] -= s;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < m; i += nt) {
+    if (i < f)
+      work[F.start + i] = r[i];
+    else
+      uvec[F.uvec_off + (i - f)] = r[i];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) sl_backward_kernel(const FrontDesc* __restrict__ fd,
+                                                               const int32_t* __restrict__ list,
+                                                               const T* __restrict__ pool,
+                                                               const T* __restrict__ tiles,
+                                                               const int32_t* __restrict__ urows,
+                                                               T* __restrict__ work) {
+  using C = SlCfg<T>;
+  constexpr int TL = C::TILE;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* x = reinterpret_cast<T*>(smraw);
+  __shared__ T z[TL];
+  __shared__ T part[kThreads / 32][TL];
+  const FrontDesc F = fd[list[blockIdx.x]];
+  const int m = F.m, f = F.f, tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < m; i += nt) x[i] = i < f ? work[F.start + i] : work[urows[F.ea_off + (i - f)]];
+  __syncthreads();
+  const T* P = pool + F.off;
+  const int ntiles = (f + TL - 1) / TL;
+  const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  for (int t = ntiles - 1; t >= 0; --t) {
+    const int k = t * TL, b = min(TL, f - k);
+    // z = y_t - U[t rows, columns after the tile] x: warps split the columns,
+    // lanes the tile rows
+    for (int i0 = 0; i0 < b; i0 += 32) {
+      const int i = i0 + lane;
+      T s = T(0);
+      if (i < b)
+        for (int c = k + b + warp; c < m; c += nw) s += P[int64_t(c) * m + k + i] * x[c];
+      if (i < TL) part[warp][i] = s;
+    }
+    __syncthreads();
+    if (tid < b) {
+      T s = x[k + tid];
+      for (int w = 0; w < nw; ++w) s -= part[w][tid];
+      z[tid] = s;
+    }
+    __syncthreads();
+    const T* iU = tiles + F.tile_off + int64_t(t) * 2 * TL * TL + TL * TL;
+    if (tid < b) {
+      T s = T(0);
+      for (int l = tid; l < b; ++l) s += iU[l * TL + tid] * z[l];
+      x[k + tid] = s;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < f; i += nt) work[F.start + i] = x[i];
+}
+
+// (D A D)^-1 = D^-1 A^-1 D^-1, so A^-1 r = D (D A D)^-1 D r
+template <typename T>
+__global__ void sl_permute_in_kernel(const double* __restrict__ r, const int32_t* __restrict__ perm,
+                                     const double* __restrict__ d, int64_t n, T* __restrict__ w) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    w[perm[i]] = T(d[i] * r[i]);
+}
+
+template <typename T>
+__global__ void sl_permute_out_kernel(const T* __restrict__ w, const int32_t* __restrict__ perm,
+                                      const double* __restrict__ d, int64_t n, double* __restrict__ z) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    z[i] = d[i] * double(w[perm[i]]);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 vector kernels of the GMRES
+// ---------------------------------------------------------------------------
+__global__ void sl_spmv_kernel(const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                               const double* __restrict__ val, const double* __restrict__ x, int64_t n,
+                               double* __restrict__ y) {
+  // four lanes per row
+  const int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t row = g >> 2;
+  const int lane = int(g & 3);
+  double s = 0.0;
+  if (row < n)
+    for (int32_t t = rp[row] + lane; t < rp[row + 1]; t += 4) s += val[t] * x[ci[t]];
+  s += __shfl_down_sync(0xffffffffu, s, 2, 4);
+  s += __shfl_down_sync(0xffffffffu, s, 1, 4);
+  if (row < n && lane == 0) y[row] = s;
+}
+
+// partial[j * nblocks + block] = sum over the block's range of V[j] . w, j < nv
+__global__ void sl_multidot_kernel(const double* __restrict__ V, int64_t ldv, int nv, const double* __restrict__ w,
+                                   int64_t n, double* __restrict__ partial) {
+  __shared__ double red[8][33];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int j0 = 0; j0 < nv; j0 += 32) {
+    const int jn = min(32, nv - j0);
+    double s[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) s[j] = 0.0;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + tid; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+      const double wi = w[i];
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        if (j < jn) s[j] += V[int64_t(j0 + j) * ldv + i] * wi;
+    }
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      double v = s[j];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp][j] = v;
+    }
+    __syncthreads();
+    if (tid < jn) {
+      double v = 0.0;
+      for (int w2 = 0; w2 < int(blockDim.x >> 5); ++w2) v += red[w2][tid];
+      partial[int64_t(j0 + tid) * gridDim.x + blockIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void sl_sum_partials_kernel(const double* __restrict__ partial, int nblocks, int nv,
+                                       double* __restrict__ out) {
+  const int j = blockIdx.x;
+  if (j >= nv) return;
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partial[int64_t(j) * nblocks + b];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (int(threadIdx.x) < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[j] = red[0];
+}
+
+// w += sign * sum_j h[j] V[j]
+__global__ void sl_multiaxpy_kernel(const double* __restrict__ V, int64_t ldv, int nv, const double* __restrict__ h,
+                                    double sign, int64_t n, double* __restrict__ w) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < nv; ++j) s += h[j] * V[int64_t(j) * ldv + i];
+    w[i] += sign * s;
+  }
+}
+
+__global__ void sl_residual_kernel(const double* __restrict__ b, const double* __restrict__ ax, int64_t n,
+                                   double* __restrict__ r) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    r[i] = b[i] - ax[i];
+}
+
+__global__ void sl_scale_into_kernel(const double* __restrict__ a, double s, int64_t n, double* __restrict__ out) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    out[i] = a[i] * s;
+}
+
+int grid_of(int64_t n, int threads) {
+  return int(std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, 152 * 16)));
+}
+
+// shared memory sizes of the kernels that take more than 48 KiB (a host-side
+// setting of each kernel, set before its launches)
+template <typename T>
+fq_status set_attributes(fq_ctx* ctx) {
+  using C = SlCfg<T>;
+  const int tile_smem = 2 * C::TILE * (C::TILE + 1) * int(sizeof(T));
+  const int blk_smem = C::TILE * (C::ROWS + 1) * int(sizeof(T));
+  const int solve_smem = C::MAXM * int(sizeof(T));
+  FQ_CUDA(ctx, cudaFuncSetAttribute(sl_tile_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem));
+  FQ_CUDA(ctx, cudaFuncSetAttribute(sl_tourn_leaf_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, blk_smem));
+  FQ_CUDA(ctx, cudaFuncSetAttribute(sl_tourn_merge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, blk_smem));
+  FQ_CUDA(ctx, cudaFuncSetAttribute(sl_forward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, solve_smem));
+  FQ_CUDA(ctx, cudaFuncSetAttribute(sl_backward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, solve_smem));
+  return FQ_OK;
+}
+
+template <typename T>
+fq_status factor_impl(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_t* ci, const double* val) {
+  using C = SlCfg<T>;
+  cudaStream_t st = ctx->stream;
+  int64_t maxm_all = 0;
+  for (int x = 0; x < lu.nfronts; ++x) maxm_all = std::max<int64_t>(maxm_all, lu.front_m[x]);
+  if (maxm_all > C::MAXM)
+    return set_error(ctx, FQ_UNSUPPORTED, "sparse LU: a front too large for this precision's solve");
+  const int prec = sizeof(T) == 4 ? FQ_FP32 : FQ_FP64;
+  if (lu.precision != prec) {
+    lu.pool.release();
+    lu.tiles.release();
+    lu.uvec.release();
+    lu.work.release();
+    lu.precision = prec;
+  }
+  if (!lu.pool.p) {
+    FQ_TRY(lu.pool.alloc(ctx, size_t(lu.pool_elems) * sizeof(T)));
+    FQ_TRY(lu.tiles.alloc(ctx, size_t(lu.tile_elems) * sizeof(T)));
+    FQ_TRY(lu.uvec.alloc(ctx, size_t(lu.uvec_elems) * sizeof(T)));
+    FQ_TRY(lu.work.alloc(ctx, size_t(std::max<int64_t>(lu.n, 1)) * sizeof(T)));
+  }
+  const int64_t half_sets = std::max<int64_t>(lu.tourn_sets, 1) * 2;  // FP64 leaves are half as tall
+  if (!lu.piv.p) {
+    FQ_TRY(lu.piv.alloc(ctx, size_t(std::max<int64_t>(lu.n, 1)) * 4));
+    FQ_TRY(lu.status.alloc(ctx, 4 * sizeof(int)));
+    FQ_TRY(lu.scale.alloc(ctx, size_t(std::max<int64_t>(lu.n, 1)) * 8));
+    FQ_TRY(lu.tourn_cand.alloc(ctx, size_t(half_sets) * 2 * kTile * 4));
+    FQ_TRY(lu.tourn_count.alloc(ctx, size_t(half_sets) * 2 * 4));
+  }
+  FQ_TRY(set_attributes<T>(ctx));
+  // the symmetric scaling; every entry of D A D is then at most 1 in magnitude,
+  // and a pivot below 1e-6 is perturbed
+  sl_row_scale_kernel<<<grid_of(lu.n, 256), 256, 0, st>>>(rp, val, lu.n, lu.scale.as<double>());
+  ctx->launches++;
+  const T thresh = T(1e-6);
+  FQ_CUDA(ctx, cudaMemsetAsync(lu.status.p, 0, 4 * sizeof(int), st));
+  FQ_CUDA(ctx, cudaMemsetAsync(lu.piv.p, 0, size_t(std::max<int64_t>(lu.n, 1)) * 4, st));
+  const int tile_smem = 2 * C::TILE * (C::TILE + 1) * int(sizeof(T));
+  const int blk_smem = C::TILE * (C::ROWS + 1) * int(sizeof(T));
+  const FrontDesc* fd = lu.fronts.as<FrontDesc>();
+  const int32_t* lists = lu.level_list.as<int32_t>();
+  T* pool = lu.pool.as<T>();
+  T* tiles = lu.tiles.as<T>();
+  for (int l = 0; l < lu.nlevels; ++l) {
+    const int32_t q0 = lu.level_ptr[l], q1 = lu.level_ptr[l + 1];
+    const int nl = q1 - q0;
+    if (nl <= 0) continue;
+    if (nl > 65535) return set_error(ctx, FQ_UNSUPPORTED, "sparse LU: more than 65,535 fronts in one level");
+    const int32_t* list = lists + q0;
+    // zero the level's fronts (contiguous in the pool)
+    const int first = lu.level_fronts[q0], last = lu.level_fronts[q1 - 1];
+    const int64_t zb = lu.front_off[first];
+    const int64_t ze = lu.front_off[last] + int64_t(lu.front_m[last]) * lu.front_m[last];
+    if (ze > zb) FQ_CUDA(ctx, cudaMemsetAsync(pool + zb, 0, size_t(ze - zb) * sizeof(T), st));
+    const int64_t ab = lu.asm_ptr_h[l], ae = lu.asm_ptr_h[l + 1];
+    if (ae > ab) {
+      sl_assemble_kernel<T><<<grid_of(ae - ab, 256), 256, 0, st>>>(lu.asm_slot.as<int32_t>(), lu.asm_row.as<int32_t>(),
+                                                                  lu.asm_off.as<int64_t>(), ab, ae, ci, val,
+                                                                  lu.scale.as<double>(), pool);
+      ctx->launches++;
+    }
+    if (l > 0) {
+      // the children's update sizes bound the grid
+      int64_t maxu2 = 0;
+      for (int32_t q = q0; q < q1; ++q) {
+        const int x = lu.level_fronts[q];
+        for (int c : {lu.child0[x], lu.child1[x]})
+          if (c >= 0) {
+            const int64_t u = lu.front_m[c] - lu.front_f[c];
+            maxu2 = std::max(maxu2, u * u);
+          }
+      }
+      const int64_t want = (maxu2 + 255) / 256;
+      const unsigned gx = unsigned(std::max<int64_t>(1, std::min<int64_t>(want, std::max<int64_t>(1, 152 * 16 / nl))));
+      for (int which = 0; which < 2; ++which) {
+        sl_extend_add_kernel<T><<<dim3(gx, unsigned(nl)), 256, 0, st>>>(fd, list, which, lu.ea_map.as<int32_t>(), pool);
+        ctx->launches++;
+      }
+    }
+    // partial factorization, tile by tile
+    int maxf = 0;
+    int64_t maxm = 0;
+    for (int32_t q = q0; q < q1; ++q) {
+      maxf = std::max(maxf, lu.front_f[lu.level_fronts[q]]);
+      maxm = std::max<int64_t>(maxm, lu.front_m[lu.level_fronts[q]]);
+    }
+    for (int k = 0; k < maxf; k += C::TILE) {
+      // pivot rows over the whole fully summed panel (tournament), moved to the top
+      const int sets = (maxf - k + C::ROWS - 1) / C::ROWS;
+      if (int64_t(nl) * sets > half_sets) return set_error(ctx, FQ_CUDA_ERROR, "sparse LU: tournament buffer too small");
+      int32_t* cand[2] = {lu.tourn_cand.as<int32_t>(), lu.tourn_cand.as<int32_t>() + half_sets * kTile};
+      int32_t* cnt[2] = {lu.tourn_count.as<int32_t>(), lu.tourn_count.as<int32_t>() + half_sets};
+      FQ_CUDA(ctx, cudaMemsetAsync(cnt[0], 0, size_t(nl) * sets * 4, st));
+      sl_tourn_leaf_kernel<T><<<dim3(unsigned(sets), unsigned(nl)), kThreads, blk_smem, st>>>(fd, list, k, pool, sets,
+                                                                                             cand[0], cnt[0]);
+      ctx->launches++;
+      int cur = 0;
+      for (int nsets = sets; nsets > 1; nsets = (nsets + 1) / 2) {
+        sl_tourn_merge_kernel<T><<<dim3(unsigned((nsets + 1) / 2), unsigned(nl)), kThreads, blk_smem, st>>>(
+            fd, list, k, pool, sets, nsets, cand[cur], cnt[cur], cand[cur ^ 1], cnt[cur ^ 1]);
+        ctx->launches++;
+        cur ^= 1;
+      }
+      sl_swap_sequence_kernel<<<unsigned(nl), 32, 0, st>>>(fd, list, k, C::TILE, sets, cand[cur],
+                                                            lu.piv.as<int32_t>());
+      const unsigned gcols = unsigned(std::max<int64_t>(1, std::min<int64_t>((maxm + 255) / 256, 64)));
+      sl_apply_swaps_kernel<T><<<dim3(gcols, unsigned(nl)), 256, 0, st>>>(fd, list, k, C::TILE, lu.piv.as<int32_t>(),
+                                                                         pool);
+      sl_tile_kernel<T><<<unsigned(nl), kThreads, tile_smem, st>>>(fd, list, k, pool, tiles, lu.status.as<int>(),
+                                                                   thresh);
+      ctx->launches += 3;
+      const int64_t rest = std::max<int64_t>(0, maxm - k);
+      const int64_t tl = (rest + C::BM - 1) / C::BM;
+      if (tl > 0) {
+        sl_gemm_kernel<T><<<dim3(unsigned(tl), unsigned(nl)), kThreads, 0, st>>>(fd, list, k, 0, pool, tiles);
+        sl_gemm_kernel<T><<<dim3(unsigned(tl), unsigned(nl)), kThreads, 0, st>>>(fd, list, k, 1, pool, tiles);
+        sl_gemm_kernel<T><<<dim3(unsigned(tl * tl), unsigned(nl)), kThreads, 0, st>>>(fd, list, k, 2, pool, tiles);
+        ctx->launches += 3;
+      }
+    }
+  }
+  FQ_CUDA(ctx, cudaGetLastError());
+  int hs[4] = {0, 0, 0, 0};
+  FQ_CUDA(ctx, cudaMemcpyAsync(hs, lu.status.p, sizeof hs, cudaMemcpyDeviceToHost, st));
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  lu.perturbed = hs[0];
+  lu.nonfinite = hs[1];
+  lu.factored = hs[1] == 0;
+  if (hs[1] > 0) return set_error(ctx, FQ_BREAKDOWN, "sparse LU: non-finite pivot");
+  return FQ_OK;
+}
+
+template <typename T>
+fq_status apply_impl(fq_ctx* ctx, SparseLu& lu, const double* r, double* z) {
+  cudaStream_t st = ctx->stream;
+  const FrontDesc* fd = lu.fronts.as<FrontDesc>();
+  const int32_t* lists = lu.level_list.as<int32_t>();
+  T* work = lu.work.as<T>();
+  sl_permute_in_kernel<T><<<grid_of(lu.n, 256), 256, 0, st>>>(r, lu.perm.as<int32_t>(), lu.scale.as<double>(), lu.n,
+                                                              work);
+  ctx->launches++;
+  for (int l = 0; l < lu.nlevels; ++l) {
+    const int32_t q0 = lu.level_ptr[l], q1 = lu.level_ptr[l + 1];
+    if (q1 <= q0) continue;
+    int64_t maxm = 0;
+    for (int32_t q = q0; q < q1; ++q) maxm = std::max<int64_t>(maxm, lu.front_m[lu.level_fronts[q]]);
+    const size_t smem = size_t(std::max<int64_t>(maxm, 1)) * sizeof(T);
+    sl_forward_kernel<T><<<unsigned(q1 - q0), kThreads, smem, st>>>(fd, lists + q0, lu.pool.as<T>(), lu.tiles.as<T>(),
+                                                                    lu.piv.as<int32_t>(), lu.ea_map.as<int32_t>(), work,
+                                                                    lu.uvec.as<T>());
+    ctx->launches++;
+  }
+  for (int l = lu.nlevels - 1; l >= 0; --l) {
+    const int32_t q0 = lu.level_ptr[l], q1 = lu.level_ptr[l + 1];
+    if (q1 <= q0) continue;
+    int64_t maxm = 0;
+    for (int32_t q = q0; q < q1; ++q) maxm = std::max<int64_t>(maxm, lu.front_m[lu.level_fronts[q]]);
+    const size_t smem = size_t(std::max<int64_t>(maxm, 1)) * sizeof(T);
+    sl_backward_kernel<T><<<unsigned(q1 - q0), kThreads, smem, st>>>(fd, lists + q0, lu.pool.as<T>(), lu.tiles.as<T>(),
+                                                                     lu.urows.as<int32_t>(), work);
+    ctx->launches++;
+  }
+  sl_permute_out_kernel<T><<<grid_of(lu.n, 256), 256, 0, st>>>(work, lu.perm.as<int32_t>(), lu.scale.as<double>(),
+                                                               lu.n, z);
+  ctx->launches++;
+  FQ_CUDA(ctx, cudaGetLastError());
+  return FQ_OK;
+}
+
+struct GmresSpace {
+  DevBuf V, Z, w, partial, h;
+  int nblocks = 0;
+};
+
+fq_status multidot(fq_ctx* ctx, GmresSpace& g, int64_t n, int nv, const double* w, std::vector<double>& out) {
+  cudaStream_t st = ctx->stream;
+  sl_multidot_kernel<<<g.nblocks, 256, 0, st>>>(g.V.as<double>(), n, nv, w, n, g.partial.as<double>());
+  sl_sum_partials_kernel<<<nv, 256, 0, st>>>(g.partial.as<double>(), g.nblocks, nv, g.h.as<double>());
+  ctx->launches += 2;
+  out.assign(nv, 0.0);
+  FQ_CUDA(ctx, cudaMemcpyAsync(out.data(), g.h.p, nv * 8, cudaMemcpyDeviceToHost, st));
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  return FQ_OK;
+}
+
+fq_status self_dot(fq_ctx* ctx, GmresSpace& g, int64_t n, const double* w, double* out) {
+  cudaStream_t st = ctx->stream;
+  // the vector against itself through the same two-stage reduction
+  sl_multidot_kernel<<<g.nblocks, 256, 0, st>>>(w, n, 1, w, n, g.partial.as<double>());
+  sl_sum_partials_kernel<<<1, 256, 0, st>>>(g.partial.as<double>(), g.nblocks, 1, g.h.as<double>());
+  ctx->launches += 2;
+  FQ_CUDA(ctx, cudaMemcpyAsync(out, g.h.p, 8, cudaMemcpyDeviceToHost, st));
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  return FQ_OK;
+}
+
+fq_status axpy_h(fq_ctx* ctx, GmresSpace& g, const double* V, int64_t n, int nv, const std::vector<double>& h,
+                 double sign, double* w) {
+  cudaStream_t st = ctx->stream;
+  FQ_CUDA(ctx, cudaMemcpyAsync(g.h.p, h.data(), nv * 8, cudaMemcpyHostToDevice, st));
+  sl_multiaxpy_kernel<<<grid_of(n, 256), 256, 0, st>>>(V, n, nv, g.h.as<double>(), sign, n, w);
+  ctx->launches++;
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));  // h is a host vector reused by the caller
+  return FQ_OK;
+}
+
+}  // namespace
+
+fq_status sparse_lu_factor(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_t* ci, const double* val,
+                           int precision) {
+  lu.factored = false;
+  if (precision == FQ_FP32) return factor_impl<float>(ctx, lu, rp, ci, val);
+  return factor_impl<double>(ctx, lu, rp, ci, val);
+}
+
+fq_status sparse_lu_apply(fq_ctx* ctx, SparseLu& lu, const double* r, double* z) {
+  if (!lu.factored) return set_error(ctx, FQ_INVALID_ARG, "sparse LU: not factored");
+  if (lu.precision == FQ_FP32) return apply_impl<float>(ctx, lu, r, z);
+  return apply_impl<double>(ctx, lu, r, z);
+}
+
+fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_t* ci, const double* val,
+                          const double* b, double* x, double rtol, int64_t max_iters, fq_report* rep) {
+  const int64_t n = lu.n;
+  const int restart = 30;
+  cudaStream_t st = ctx->stream;
+  GmresSpace g;
+  g.nblocks = std::min<int>(int((n + 255) / 256), 152 * 4);
+  FQ_TRY(g.V.alloc(ctx, size_t(restart + 1) * n * 8));
+  FQ_TRY(g.Z.alloc(ctx, size_t(restart) * n * 8));
+  FQ_TRY(g.w.alloc(ctx, size_t(n) * 8));
+  FQ_TRY(g.partial.alloc(ctx, size_t(g.nblocks) * (restart + 2) * 8));
+  FQ_TRY(g.h.alloc(ctx, size_t(restart + 2) * 8));
+  double* V = g.V.as<double>();
+  double* Z = g.Z.as<double>();
+  double* w = g.w.as<double>();
+  const unsigned spmv_blocks = unsigned((n * 4 + 255) / 256);
+  FQ_CUDA(ctx, cudaMemsetAsync(x, 0, size_t(n) * 8, st));
+  double bnorm2 = 0.0;
+  FQ_TRY(self_dot(ctx, g, n, b, &bnorm2));
+  const double bnorm = std::sqrt(bnorm2);
+  fq_report r{};
+  if (!(bnorm > 0.0)) {
+    r.converged = 1;
+    if (rep) *rep = r;
+    return FQ_OK;
+  }
+  int64_t it = 0;
+  double relres = 1.0;
+  bool done = false;
+  std::vector<double> h, h2;
+  while (!done && it < max_iters) {
+    // r = b - A x into V[0]
+    sl_spmv_kernel<<<spmv_blocks, 256, 0, st>>>(rp, ci, val, x, n, w);
+    sl_residual_kernel<<<grid_of(n, 256), 256, 0, st>>>(b, w, n, V);
+    ctx->launches += 2;
+    double beta2 = 0.0;
+    FQ_TRY(self_dot(ctx, g, n, V, &beta2));
+    const double beta = std::sqrt(beta2);
+    relres = beta / bnorm;
+    if (relres <= rtol) break;
+    sl_scale_into_kernel<<<grid_of(n, 256), 256, 0, st>>>(V, 1.0 / beta, n, V);
+    ctx->launches++;
+    std::vector<std::vector<double>> H(restart + 1, std::vector<double>(restart, 0.0));
+    std::vector<double> cs(restart, 0.0), sn(restart, 0.0), gv(restart + 1, 0.0);
+    gv[0] = beta;
+    int j = 0;
+    for (; j < restart && it < max_iters; ++j, ++it) {
+      FQ_TRY(sparse_lu_apply(ctx, lu, V + int64_t(j) * n, Z + int64_t(j) * n));
+      sl_spmv_kernel<<<spmv_blocks, 256, 0, st>>>(rp, ci, val, Z + int64_t(j) * n, n, w);
+      ctx->launches++;
+      // classical Gram-Schmidt, twice
+      FQ_TRY(multidot(ctx, g, n, j + 1, w, h));
+      FQ_TRY(axpy_h(ctx, g, V, n, j + 1, h, -1.0, w));
+      FQ_TRY(multidot(ctx, g, n, j + 1, w, h2));
+      FQ_TRY(axpy_h(ctx, g, V, n, j + 1, h2, -1.0, w));
+      for (int i = 0; i <= j; ++i) H[i][j] = h[i] + h2[i];
+      double hn2 = 0.0;
+      FQ_TRY(self_dot(ctx, g, n, w, &hn2));
+      const double hn = std::sqrt(hn2);
+      H[j + 1][j] = hn;
+      if (hn > 0.0) {
+        sl_scale_into_kernel<<<grid_of(n, 256), 256, 0, st>>>(w, 1.0 / hn, n, V + int64_t(j + 1) * n);
+        ctx->launches++;
+      }
+      for (int i = 0; i < j; ++i) {
+        const double a = H[i][j], c = H[i + 1][j];
+        H[i][j] = cs[i] * a + sn[i] * c;
+        H[i + 1][j] = -sn[i] * a + cs[i] * c;
+      }
+      const double a = H[j][j], c = H[j + 1][j];
+      const double d = std::hypot(a, c);
+      cs[j] = d > 0 ? a / d : 1.0;
+      sn[j] = d > 0 ? c / d : 0.0;
+      H[j][j] = d;
+      H[j + 1][j] = 0.0;
+      gv[j + 1] = -sn[j] * gv[j];
+      gv[j] = cs[j] * gv[j];
+      relres = std::fabs(gv[j + 1]) / bnorm;
+      if (relres <= rtol || hn == 0.0) {
+        ++j;
+        ++it;
+        break;
+      }
+    }
+    // x += Z y, y = H^-1 g (upper triangular j x j)
+    std::vector<double> y(j, 0.0);
+    for (int i = j - 1; i >= 0; --i) {
+      double s = gv[i];
+      for (int l = i + 1; l < j; ++l) s -= H[i][l] * y[l];
+      y[i] = H[i][i] != 0.0 ? s / H[i][i] : 0.0;
+    }
+    if (j > 0) FQ_TRY(axpy_h(ctx, g, Z, n, j, y, 1.0, x));
+    if (relres <= rtol) {
+      // confirm on the true residual
+      sl_spmv_kernel<<<spmv_blocks, 256, 0, st>>>(rp, ci, val, x, n, w);
+      sl_residual_kernel<<<grid_of(n, 256), 256, 0, st>>>(b, w, n, w);
+      ctx->launches += 2;
+      double t2 = 0.0;
+      FQ_TRY(self_dot(ctx, g, n, w, &t2));
+      relres = std::sqrt(t2) / bnorm;
+      done = relres <= rtol;
+    }
+  }
+  r.iters = it;
+  r.residual = relres;
+  r.true_residual = relres;
+  r.converged = relres <= rtol ? 1 : 0;
+  if (rep) *rep = r;
+  return r.converged ? FQ_OK : FQ_NOT_CONVERGED;
+}
+
+fq_status sparse_lu_solve(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_t* ci, const double* val,
+                          const double* b, double* x, double rtol, int64_t max_iters, fq_report* rep) {
+  fq_report r{};
+  fq_status s = FQ_NOT_CONVERGED;
+  fq_status fs = (lu.factored && lu.precision == FQ_FP32) ? FQ_OK : sparse_lu_factor(ctx, lu, rp, ci, val, FQ_FP32);
+  if (fs == FQ_OK) {
+    s = sparse_lu_gmres(ctx, lu, rp, ci, val, b, x, rtol, std::min<int64_t>(max_iters, kFp32Iterations), &r);
+    if (s != FQ_OK && s != FQ_NOT_CONVERGED) return s;
+  } else if (fs != FQ_BREAKDOWN && fs != FQ_UNSUPPORTED) {
+    return fs;
+  }
+  if (s == FQ_OK) {
+    r.refinements = 0;
+    if (rep) *rep = r;
+    return FQ_OK;
+  }
+  // the FP32 factors were not enough: FP64 factors, GMRES from zero
+  fs = sparse_lu_factor(ctx, lu, rp, ci, val, FQ_FP64);
+  if (fs == FQ_UNSUPPORTED || fs == FQ_BREAKDOWN) {
+    if (rep) *rep = r;
+    return FQ_NOT_CONVERGED;
+  }
+  FQ_TRY(fs);
+  fq_report r2{};
+  s = sparse_lu_gmres(ctx, lu, rp, ci, val, b, x, rtol, std::max<int64_t>(1, max_iters - r.iters), &r2);
+  r2.iters += r.iters;
+  r2.refinements = 1;
+  if (rep) *rep = r2;
+  return s;
+}
+
+}  // namespace fq

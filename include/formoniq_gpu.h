@@ -71,9 +71,13 @@ typedef enum fq_precision {
 typedef enum fq_precond {
   FQ_PC_AUTO = 0,   /* FQ_PC_HX where it applies, else FQ_PC_JACOBI */
   FQ_PC_JACOBI = 1, /* diagonal of each block (Jacobi::new, iterative/src/precond.rs:62-64) */
-  FQ_PC_HX = 2      /* Hiptmair-Xu auxiliary-space blocks over a nodal multigrid V-cycle
+  FQ_PC_HX = 2,     /* Hiptmair-Xu auxiliary-space blocks over a nodal multigrid V-cycle
                        (formoniq/src/hx.rs, multigrid.rs): Kuhn cube meshes with positive
                        squared lengths; FQ_UNSUPPORTED elsewhere */
+  FQ_PC_DIRECT = 3, /* Dirac solves: the sparse direct factorization (fq_sparse_lu_*) of the
+                       system preconditioning FP64 GMRES; Kuhn cube meshes */
+  FQ_PC_COMPARISON = 4 /* Dirac solves: MINRES preconditioned by the inverse diagonal of the
+                       relative masses of the Euclidean comparison lattice; Kuhn cube meshes */
 } fq_precond;
 
 typedef struct fq_ctx fq_ctx;
@@ -386,21 +390,68 @@ fq_status fq_source_assemble(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, in
  * break the graph captures of the other lanes). */
 
 /* ---- the covariant Hodge-Dirac source problem ---------------------------- */
-/* dirac::solve_dirac_source (problems/dirac.rs:473-531) with MINRES in place of
- * the reference's sparse LU: S = A + m M of HodgeDirac::assemble_selfadjoint
- * (:205-260) on the relative complex, rhs = E^T (load - S lift). Preconditioner
- * (opts->preconditioner), on Kuhn cube meshes from the Euclidean comparison
- * lattice (the signed lengths' axis scales made positive): FQ_PC_AUTO the
- * inverse diagonal of its relative masses M_j, j = 0..n; FQ_PC_HX its relative
- * hdif_gram(j) blocks, each an HX multigrid. FQ_PC_JACOBI and other meshes:
- * |diag(S)|. load/lift/x are host,
- * flattened by grade (ambient offsets of HodgeDirac, :181-200). mass_term must
- * be nonzero. */
+/* dirac::solve_dirac_source (problems/dirac.rs:473-531): S = A + m M of
+ * HodgeDirac::assemble_selfadjoint (:205-260) on the relative complex,
+ * rhs = E^T (load - S lift). Solver (opts->preconditioner):
+ *   FQ_PC_AUTO / FQ_PC_DIRECT on fq_mesh_kuhn_cube meshes: the reference's
+ *     LU, here the sparse direct factorization (fq_sparse_lu_*) preconditioning
+ *     FP64 GMRES to opts->rtol on the true residual (report.refinements = 1
+ *     when the FP32 factors gave way to FP64 ones). At m = 0 the top-grade
+ *     harmonic (top_harmonic, :552-570) is tested against the kernel
+ *     (||S h|| <= 1e-8 ||h||) and, if it spans it, the system is bordered with
+ *     it (solve_bordered, :578-598): the solution orthogonal to the kernel.
+ *   FQ_PC_COMPARISON / FQ_PC_HX (Kuhn meshes): MINRES preconditioned from the
+ *     Euclidean comparison lattice (the signed lengths' axis scales made
+ *     positive): the inverse diagonal of its relative masses M_j, j = 0..n, or
+ *     its relative hdif_gram(j) blocks, each an HX multigrid.
+ *   FQ_PC_JACOBI, and FQ_PC_AUTO on other meshes: MINRES with |diag(S)|.
+ * The MINRES routes need m != 0. load/lift/x are host, flattened by grade
+ * (ambient offsets of HodgeDirac, :181-200). */
 fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* mesh, double mass_term, const double* load_host,
                                 const double* lift_host, double* x_host, const fq_solve_opts* opts,
                                 fq_report* report);
 /* The assembled relative Dirac system S (for parity tests); caller destroys. */
 fq_status fq_dirac_system(fq_ctx* ctx, fq_mesh* mesh, double mass_term, fq_matrix** out);
+
+/* ---- sparse direct solver ----------------------------------------------- */
+/* Stands in for FaerLu (formoniq/src/linalg/faer.rs:51-74) where the reference
+ * factors: solve_dirac_source (problems/dirac.rs:525-531) and the LU fallback of
+ * solve_source (problems/elliptic.rs:147-160). Multifrontal LU on a geometric
+ * nested-dissection ordering of the Kuhn vertex lattice: the fronts of each
+ * level of the elimination tree are assembled and partially factored together
+ * on the device (the system scaled to unit row maxima; the pivot rows of each
+ * tile chosen over all the front's fully summed rows by tournament pivoting;
+ * pivots below 1e-6 perturbed). The factors precondition a restarted GMRES in
+ * FP64 on the FP64 matrix, which stops on the true relative residual
+ * ||b - A x|| / ||b||. */
+typedef struct fq_sparse_lu fq_sparse_lu;
+/* Symbolic analysis of `a` (square, FP64 values, made by fq_assemble,
+ * fq_dirac_system or fq_mixed_system on `mesh`, a fq_mesh_kuhn_cube mesh):
+ * FQ_UNSUPPORTED on other meshes. */
+fq_status fq_sparse_lu_create(fq_ctx* ctx, fq_mesh* mesh, const fq_matrix* a, fq_sparse_lu** out);
+/* Numeric factorization of a's current values in FP32 (after every
+ * re-assembly). */
+fq_status fq_sparse_lu_factor(fq_sparse_lu* lu, const fq_matrix* a);
+/* x = A^-1 b (device vectors of a->nrows doubles) by GMRES to opts->rtol on the
+ * true FP64 residual, at most opts->max_iters iterations in all. GMRES runs on
+ * the FP32 factors for at most 60 iterations; if it has not converged by then,
+ * `a` is re-factored in FP64 (the factorization keeps FP64 afterwards, until
+ * the next fq_sparse_lu_factor) and GMRES starts again from zero: then
+ * report.refinements = 1. report.iters counts both. */
+fq_status fq_sparse_lu_solve(fq_sparse_lu* lu, const fq_matrix* a, const double* b_dev, double* x_dev,
+                             const fq_solve_opts* opts, fq_report* report);
+/* Fronts, levels, factorization flops, bytes of the current factors, pivots
+ * perturbed in the last factorization. */
+fq_status fq_sparse_lu_info(const fq_sparse_lu* lu, int64_t* fronts, int64_t* levels, double* flops,
+                            int64_t* factor_bytes, int64_t* perturbed_pivots);
+void fq_sparse_lu_destroy(fq_sparse_lu* lu);
+/* The symbolic analysis alone, on the host (no device, no context), for
+ * tests of the ordering: the pattern as host CSR, five vertex ids per unknown
+ * (-1 padded). stats[0..5] = fronts, levels, factorization flops, factor bytes
+ * (FP32), largest front, unknowns eliminated. Also checks every index the
+ * kernels will form against its buffer. */
+fq_status fq_sparse_lu_analyse_host(int dim, int nbox, int64_t n, const int32_t* rp, const int32_t* ci,
+                                    const int32_t* dof_vertices, double* stats);
 
 /* ---- batched assembly --------------------------------------------------- */
 /* No counterpart in the reference (one mesh per assemble_matrix call,

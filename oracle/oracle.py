@@ -705,9 +705,43 @@ def dirac_source_system(cx: Complex, lengths: np.ndarray, mass_term: float, load
     return s_rel, rhs, keep, offsets
 
 
+def top_harmonic(cx: Complex, lengths: np.ndarray) -> np.ndarray:
+    """top_harmonic (dirac.rs:552-570): zero below the top grade, M_n^-1 z on
+    the cells (relative top-grade mass, z the coherent orientation), in the flat
+    relative layout."""
+    rel = WhitneyComplex(cx, lengths, relative=True)
+    n = cx.dim
+    z = orientation_signs(cx).astype(np.float64)
+    h_n = direct_solve(rel.mass(n), z)
+    sizes = [len(cx.interior(k)) for k in range(n + 1)]
+    h = np.zeros(sum(sizes))
+    h[sum(sizes[:n]):] = h_n
+    return h
+
+
+def solve_bordered(s: sp.csr_matrix, rhs: np.ndarray, h: np.ndarray) -> np.ndarray:
+    """solve_bordered (dirac.rs:578-598): [[S, h], [h^T, 0]] [u; c] = [f; 0] by LU."""
+    n = len(rhs)
+    c = s.tocoo()
+    nzh = np.nonzero(h != 0.0)[0]
+    rows = np.concatenate([c.row, nzh, np.full(len(nzh), n)])
+    cols = np.concatenate([c.col, np.full(len(nzh), n), nzh])
+    vals = np.concatenate([c.data, h[nzh], h[nzh]])
+    b = coo_to_csr(rows, cols, vals, (n + 1, n + 1))
+    return direct_solve(b, np.concatenate([rhs, [0.0]]))[:n]
+
+
 def dirac_solve_source(cx, lengths, mass_term, load, lift):
+    """solve_dirac_source (dirac.rs:473-531): LU of the relative system, bordered
+    with the top harmonic at m = 0 when it spans the kernel."""
     s_rel, rhs, keep, offsets = dirac_source_system(cx, lengths, mass_term, load, lift)
-    interior = direct_solve(s_rel, rhs)
+    interior = None
+    if mass_term == 0.0:
+        h = top_harmonic(cx, lengths)
+        if np.linalg.norm(s_rel @ h) <= 1e-8 * np.linalg.norm(h):
+            interior = solve_bordered(s_rel, rhs, h)
+    if interior is None:
+        interior = direct_solve(s_rel, rhs)
     out = lift.copy()
     out[keep] += interior
     return out
