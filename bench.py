@@ -304,6 +304,17 @@ def run_ours(args):
         fq.Matrix.reassemble_many(mats)
         fq.Matrix.reassemble_many(mats_ieee)
         parity = {"fp64_float_float": parity_record(mats, omats), "fp64_ieee": parity_record(mats_ieee, omats)}
+    sub = {}
+    if world == 1 and not args.no_sub:
+        # compact forms of the batch, precision and serving workloads, in the
+        # same run as the headline so that one clock covers them
+        for name, fn in (("batch", batch_study), ("precision", precision_study), ("serve", serve_study)):
+            t0 = time.perf_counter()
+            try:
+                sub[name] = fn(args, compact=True)
+            except Exception as e:  # reported, not hidden: the line still prints
+                sub[name] = {"error": f"{type(e).__name__}: {e}"}
+            sub[name]["study_wall_s"] = time.perf_counter() - t0
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -320,6 +331,7 @@ def run_ours(args):
         "ieee_fp64": ieee_rec,
         "parity": parity,
         "solve": solve,
+        **sub,
     }
     if rank == 0:
         print(json.dumps(line))
@@ -462,11 +474,14 @@ def e2e_phase(ctx, mesh, mats, flush, args, ncells, world):
 # precision workload: 4D 12^4 Kuhn, k=2 mixed Hodge-Laplace
 # ---------------------------------------------------------------------------
 
-def run_precision(args):
-    """FP32 element matrices and SpMV with FP64 Gram inverse/determinant and FP64
-    iterative refinement, against the plain FP64 path; every result's relative
-    error is stated against an FP64 MINRES solve at rtol 1e-12 (the FP64 oracle at
-    this size, where a direct factorization does not fit the time budget)."""
+def precision_study(args, compact: bool):
+    """4D 12^4 Kuhn, k=2 mixed Hodge-Laplace (1,483,536 DOFs): FP32 element
+    matrices and SpMV with FP64 Gram inverse/determinant inside FP64 iterative
+    refinement, against the plain FP64 path. Each result's relative error is
+    stated against an FP64 solve at rtol 1e-12 on the device and, in the full
+    study, against the oracle's CPU MINRES at rtol 1e-12 on the oracle's own
+    KKT system. The KKT product's achieved HBM bandwidth (the system, 1.1 GB,
+    does not fit L2) is measured with L2 flushed before every product."""
     import torch
 
     import formoniq_gb300 as fq
@@ -479,9 +494,12 @@ def run_precision(args):
     mesh = fq.Mesh.kuhn_cube(ctx, dim, nbox)
     mesh.kuhn_lengths(jitter=JITTER, seed=SEED)
     rng = np.random.default_rng(SEED + 4)
-    src = torch.tensor(rng.standard_normal(mesh.nsimplices(grade)), device="cuda")
+    src_h = rng.standard_normal(mesh.nsimplices(grade))
+    src = torch.tensor(src_h, device="cuda")
     sig = torch.empty(mesh.nsimplices(grade - 1), dtype=torch.float64, device="cuda")
     u = torch.empty(mesh.nsimplices(grade), dtype=torch.float64, device="cuda")
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    nsolves = 3 if compact else args.solves
 
     def timed_solves(prob, opts, n):
         prob.solve_device(src.data_ptr(), sig.data_ptr(), u.data_ptr(), 0, opts)  # builds the preconditioner
@@ -495,29 +513,42 @@ def run_precision(args):
             lat.append(a.elapsed_time(b))
         return torch.cat([sig, u]).cpu().numpy(), sorted(lat), rep
 
-    def timed_assembly(prob, n=3):
-        prob.reassemble()
+    def timed(fn, n=3):
+        fn()
         torch.cuda.synchronize()
         t = []
         for _ in range(n):
+            flush.fill_(1.0)
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            prob.reassemble()
+            fn()
             b.record(stream)
             torch.cuda.synchronize()
             t.append(a.elapsed_time(b))
-        return min(t)
+        return statistics.median(t)
 
     out = {"metric": "solves/s @1e-8 rel err vs the FP64 oracle", "workload":
            f"kuhn {dim}D {nbox}^4 ({mesh.ncells()} cells), k={grade} mixed Hodge-Laplace, N(0,1) source seed {SEED + 4}",
-           "data": "synthetic", "n_solves": args.solves}
+           "data": "synthetic", "n_solves": nsolves}
     t0 = time.perf_counter()
     p64 = fq.MixedProblem(mesh, grade, fq.FQ_ABSOLUTE, fq.FQ_FP64)
     out["setup_fp64_s"] = time.perf_counter() - t0
     ns, nu, nh, nnz = p64.info()
     out["dofs"], out["kkt_nnz"] = ns + nu + nh, nnz
     ref, _, rref = timed_solves(p64, fq.SolveOpts.default(rtol=1e-12, max_iters=args.max_iters), 1)
-    out["oracle"] = {"rtol": 1e-12, "iters": rref.iters, "true_residual": rref.true_residual}
+    out["fp64_rtol_1e-12"] = {"iters": rref.iters, "true_residual": rref.true_residual}
+    # the KKT product on the device (SpMV roofline: nnz (8 + 4) + (n + 1) 4 + 2 n 8 bytes)
+    kkt = p64.system()
+    n = ns + nu + nh
+    xv = torch.tensor(rng.standard_normal(n), device="cuda")
+    yv = torch.empty_like(xv)
+    ms_spmv = timed(lambda: ctx.check(ctx.L.fq_spmv(ctx.h, kkt.h, fq._P(xv.data_ptr()), fq._P(yv.data_ptr()))), 5)
+    spmv_bytes = nnz * 12 + (n + 1) * 4 + 2 * n * 8
+    peak, peak_src = measured_peaks()
+    out["spmv"] = {"matrix": f"FP64 KKT, {n} rows, {nnz} nnz ({nnz * 12 / 1e9:.2f} GB of values and columns)",
+                   "ms": ms_spmv, "algorithmic_bytes": spmv_bytes, "achieved_GBps": spmv_bytes / (ms_spmv * 1e6),
+                   "peak_GBps": peak, "peak_source": peak_src, "frac": spmv_bytes / (ms_spmv * 1e6) / peak,
+                   "l2": "flushed before every product (256 MiB write)"}
     variants = [("fp64", p64, fq.SolveOpts.default(rtol=1e-10, max_iters=args.max_iters))]
     t0 = time.perf_counter()
     p32 = fq.MixedProblem(mesh, grade, fq.FQ_ABSOLUTE, fq.FQ_FP32)
@@ -525,18 +556,48 @@ def run_precision(args):
     variants.append(("fp32_refined", p32, fq.SolveOpts.default(rtol=1e-5, max_iters=args.max_iters,
                                                                 precision=fq.FQ_FP32, refine_rtol=1e-10,
                                                                 max_refinements=8)))
+    sols = {}
     for label, prob, opts in variants:
-        x, lat, rep = timed_solves(prob, opts, args.solves)
+        x, lat, rep = timed_solves(prob, opts, nsolves)
+        sols[label] = x
         mean = sum(lat) / len(lat)
         out[label] = {"solves_per_s": 1e3 / mean, "p50_ms": lat[(len(lat) - 1) // 2], "p99_ms": lat[-1],
                       "iters": rep.iters, "refinements": rep.refinements, "true_residual": rep.true_residual,
-                      "rel_err_vs_fp64_oracle": float(np.linalg.norm(x - ref) / np.linalg.norm(ref)),
-                      "kkt_assembly_ms": timed_assembly(prob)}
+                      "rel_err_vs_fp64_rtol_1e-12": float(np.linalg.norm(x - ref) / np.linalg.norm(ref)),
+                      "kkt_assembly_ms": timed(prob.reassemble)}
     p32.close()
     p64.close()
     mesh.close()
     ctx.close()
-    print(json.dumps(out))
+    if not compact:
+        # the oracle on the host: its own KKT system of the same mesh, lengths and
+        # source, MINRES at rtol 1e-12 (the solution does not depend on the
+        # preconditioner; the oracle uses its restatement of the HX blocks)
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import hx_oracle
+        import oracle
+
+        t0 = time.perf_counter()
+        cx, coords = oracle.cartesian_unit(dim, nbox)
+        coords = oracle.jitter_coords(coords, nbox, SEED, JITTER)
+        lengths = cx.edge_lengths_sq(coords)
+        wc = oracle.WhitneyComplex(cx, lengths)
+        a, rhs, ons, onu = oracle.assemble_mixed_kkt(wc, src_h, grade, oracle.harmonics(wc, grade))
+        hx = hx_oracle.HxPreconditioner(wc, cx, lengths, nbox, False)
+
+        def pc(r):
+            return np.concatenate([hx.apply(grade - 1, r[:ons]), hx.apply(grade, r[ons:ons + onu]), r[ons + onu:]])
+
+        xo, orep = oracle.minres(a, pc, rhs, rtol=1e-12)
+        out["cpu_oracle"] = {"rtol": 1e-12, "iters": orep.iters, "converged": orep.converged,
+                             "seconds": time.perf_counter() - t0, "cores": oracle.num_threads()}
+        for label, x in sols.items():
+            out[label]["rel_err_vs_cpu_oracle"] = float(np.linalg.norm(x - xo) / np.linalg.norm(xo))
+    return out
+
+
+def run_precision(args):
+    print(json.dumps(precision_study(args, compact=False)))
 
 
 # ---------------------------------------------------------------------------
@@ -566,75 +627,162 @@ def serve_stream(fq, n, seed, rate_per_s, max_cells_hodge=5e5, max_cells_dirac=3
     return reqs
 
 
-def run_stream(fq, reqs, lanes, cache, mixed_precision, dirac_iters):
+def run_stream(fq, reqs, lanes, cache, mixed_precision, dirac_iters, sols=None, inputs=None):
     """Submit the whole stream (the server releases each request at its
-    arrival time); returns per-request results in stream order."""
+    arrival time); returns per-request results in stream order. sols[i], when
+    given, receives request i's solution; inputs[i] = (lengths, source) pins a
+    request's inputs."""
     fp64 = fq.SolveOpts.default(rtol=1e-10)
     fp32 = fq.SolveOpts.default(rtol=1e-5, precision=fq.FQ_FP32, refine_rtol=1e-10, max_refinements=8)
     dirac = fq.SolveOpts.default(rtol=1e-10, max_iters=dirac_iters)
     with fq.Server(lanes=lanes, cache=cache) as srv:
         t0 = time.perf_counter()
         tickets = []
-        for r in reqs:
+        for i, r in enumerate(reqs):
             if r["kind"] == fq.FQ_REQ_DIRAC:
                 opts = dirac
             else:
                 opts = fp32 if mixed_precision else fp64
-            tickets.append(srv.submit(**r, opts=opts))
+            extra = {}
+            if sols is not None and sols[i] is not None:
+                extra["solution"] = sols[i]
+            if inputs is not None and inputs.get(i) is not None:
+                extra["lengths"], extra["source"] = inputs[i]
+            tickets.append(srv.submit(**r, opts=opts, **extra))
         res = [srv.wait(t) for t in tickets]
         wall = time.perf_counter() - t0
         stats = srv.stats()
     return res, wall, stats
 
 
+def pct(vals, p):
+    v = sorted(vals)
+    return v[min(len(v) - 1, max(0, int(math.ceil(p / 100 * len(v))) - 1))] if v else None
+
+
 def stream_summary(reqs, res, wall, kind=None):
     pairs = [(q, r) for q, r in zip(reqs, res) if kind is None or q["kind"] == kind]
     if not pairs:
         return None
-    lat = sorted(r["latency_ms"] for _, r in pairs)
+    lat = [r["latency_ms"] for _, r in pairs]
+    run = [r["run_ms"] for _, r in pairs]
+    que = [r["queue_ms"] for _, r in pairs]
     ok = [r for _, r in pairs if r["status"] == 0 and r["report"].converged]
     first = min(q["arrival_ms"] for q in reqs)
     span_ms = max(r["end_ms"] for r in res) - first
-
-    def pct(p):
-        return lat[min(len(lat) - 1, int(math.ceil(p / 100 * len(lat))) - 1)]
-
     statuses = collections.Counter(int(r["status"]) for _, r in pairs)
-    return {"solves_per_s": len(ok) / (span_ms * 1e-3), "p50_ms": pct(50), "p99_ms": pct(99),
-            "mean_run_ms": sum(r["run_ms"] for _, r in pairs) / len(pairs), "converged": len(ok), "n": len(pairs),
+    return {"solves_per_s": len(ok) / (span_ms * 1e-3), "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+            "service_p50_ms": pct(run, 50), "service_p99_ms": pct(run, 99), "mean_service_ms": sum(run) / len(run),
+            "queue_p50_ms": pct(que, 50), "queue_p99_ms": pct(que, 99), "converged": len(ok), "n": len(pairs),
             "wall_s": wall, "cache_hits": sum(r["cache_hit"] for _, r in pairs),
+            "fp64_factor_fallbacks": sum(1 for q, r in pairs if q["kind"] == 1 and r["report"].refinements > 0),
             "statuses": {str(k): v for k, v in sorted(statuses.items())},
             "unconverged": [{"dim": q.get("dim"), "nbox": q.get("nbox"), "grade": q.get("grade"),
-                             "status": int(r["status"]),
-                             "iters": int(r["report"].iters), "true_residual": float(r["report"].true_residual)}
+                             "status": int(r["status"]), "iters": int(r["report"].iters),
+                             "true_residual": float(r["report"].true_residual)}
                             for q, r in pairs if not (r["status"] == 0 and r["report"].converged)][:8]}
 
 
-def run_serve(args):
+def solution_sizes(fq, reqs):
+    """Length of each request's solution: (sigma, u) for Hodge, every grade for Dirac."""
+    ctx = fq.Context(0)
+    counts = {}
+    out = []
+    for q in reqs:
+        key = (q["dim"], q["nbox"])
+        if key not in counts:
+            m = fq.Mesh.kuhn_cube(ctx, *key)
+            counts[key] = [m.nsimplices(k) for k in range(key[0] + 1)]
+            m.close()
+        ns = counts[key]
+        if q["kind"] == fq.FQ_REQ_DIRAC:
+            out.append(sum(ns))
+        else:
+            k = q["grade"]
+            out.append((ns[k - 1] if k >= 1 else 0) + ns[k])
+    ctx.close()
+    return out
+
+
+def oracle_inputs(q):
+    """Host lengths and source of a request and its oracle solution
+    (solve_source / solve_dirac_source restated on the host)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    dim, nb = q["dim"], q["nbox"]
+    rng = np.random.default_rng(q["seed"])
+    if q.get("minkowski"):
+        cx, coords, signs = oracle.minkowski(dim, nb)
+        lengths = cx.edge_lengths_sq(coords, signs)
+        lengths = lengths * (1.0 + q["jitter"] * rng.uniform(-1.0, 1.0, len(lengths)))
+    else:
+        cx, coords = oracle.cartesian_unit(dim, nb)
+        lengths = cx.edge_lengths_sq(oracle.jitter_coords(coords, nb, q["seed"], q["jitter"]))
+    if q["kind"] == 1:  # Dirac
+        load = rng.standard_normal(sum(cx.nsimplices(k) for k in range(dim + 1)))
+        want = oracle.dirac_solve_source(cx, lengths, q["mass_term"], load, np.zeros(len(load)))
+        return lengths, load, want
+    k = q["grade"]
+    src = rng.standard_normal(cx.nsimplices(k))
+    wc = oracle.WhitneyComplex(cx, lengths, relative=bool(q["bc"]))
+    sigma, u, _, _ = oracle.solve_source(wc, src, k, rtol=1e-12)
+    return lengths, src, np.concatenate([sigma, u])
+
+
+def serve_study(args, compact: bool):
+    """The served form (lanes, residency, FP32-inner refinement for Hodge
+    requests) against the plain one (one lane, no residency, FP64) on the same
+    seeded Poisson stream; every sampled request's served solution against its
+    plain solution, and a few small requests against the oracle on the host."""
     import formoniq_gb300 as fq
 
-    reqs = serve_stream(fq, args.requests, SEED, args.rate)
-    served, wall_s, st = run_stream(fq, reqs, args.lanes, True, True, args.dirac_iters)
-    plain, wall_p, _ = run_stream(fq, reqs, 1, False, False, args.dirac_iters)
-    errs = []
-    for q, a, b in zip(reqs, served, plain):
-        if q["kind"] == fq.FQ_REQ_HODGE and a["status"] == 0 and b["status"] == 0 and b["checksum"] > 0:
-            # relative difference of the solution norms, served (FP32 inner) vs plain (FP64)
-            errs.append(abs(math.sqrt(a["checksum"]) - math.sqrt(b["checksum"])) / math.sqrt(b["checksum"]))
+    nreq = 40 if compact else args.requests
+    reqs = serve_stream(fq, nreq, SEED, args.rate)
+    sizes = solution_sizes(fq, reqs)
+    step = max(1, nreq // 200)
+    sample = [i for i in range(nreq) if i % step == 0]
+    sols_s = [np.zeros(sizes[i]) if i in sample else None for i in range(nreq)]
+    sols_p = [np.zeros(sizes[i]) if i in sample else None for i in range(nreq)]
+    # the smallest requests of each kind get host inputs, checked against the oracle
+    inputs, wants = {}, {}
+    if not compact:
+        for kind in (fq.FQ_REQ_HODGE, fq.FQ_REQ_DIRAC):
+            idx = sorted((i for i in sample if reqs[i]["kind"] == kind), key=lambda i: sizes[i])[:2]
+            for i in idx:
+                lengths, src, want = oracle_inputs(reqs[i])
+                inputs[i], wants[i] = (lengths, src), want
+    served, wall_s, st = run_stream(fq, reqs, args.lanes, True, True, args.dirac_iters, sols_s, inputs)
+    plain, wall_p, _ = run_stream(fq, reqs, 1, False, False, args.dirac_iters, sols_p, inputs)
+    errs = {"hodge": [], "dirac": []}
+    for i in sample:
+        if served[i]["status"] == 0 and plain[i]["status"] == 0:
+            kind = "hodge" if reqs[i]["kind"] == fq.FQ_REQ_HODGE else "dirac"
+            errs[kind].append(float(np.linalg.norm(sols_s[i] - sols_p[i]) / max(np.linalg.norm(sols_p[i]), 1e-300)))
+    oracle_errs = [{"kind": "hodge" if reqs[i]["kind"] == fq.FQ_REQ_HODGE else "dirac", "dim": reqs[i]["dim"],
+                    "nbox": reqs[i]["nbox"], "dofs": sizes[i],
+                    "served_rel_err": float(np.linalg.norm(sols_s[i] - w) / np.linalg.norm(w)),
+                    "plain_rel_err": float(np.linalg.norm(sols_p[i] - w) / np.linalg.norm(w))}
+                   for i, w in wants.items()]
     kinds = collections.Counter("hodge" if q["kind"] == fq.FQ_REQ_HODGE else "dirac" for q in reqs)
 
     def side(res, wall, **kw):
         return dict(all=stream_summary(reqs, res, wall), hodge=stream_summary(reqs, res, wall, fq.FQ_REQ_HODGE),
                     dirac=stream_summary(reqs, res, wall, fq.FQ_REQ_DIRAC), **kw)
 
-    out = {"metric": "solves/s and p50/p99 latency, served vs plain", "requests": len(reqs), "rate_per_s": args.rate,
-           "mix": dict(kinds), "data": "synthetic (seeded stream)", "dirac_max_iters": args.dirac_iters,
-           "served": side(served, wall_s, lanes=args.lanes, cache=True,
-                          precision="FP32 inner MINRES + FP64 refinement (Hodge), FP64 (Dirac)",
-                          peak_committed_gb=st["peak_committed_bytes"] / 1e9),
-           "plain": side(plain, wall_p, lanes=1, cache=False, precision="FP64"),
-           "hodge_max_rel_norm_diff_served_vs_plain": max(errs) if errs else None}
-    print(json.dumps(out))
+    return {"metric": "solves/s and p50/p99 latency, served vs plain", "requests": len(reqs), "rate_per_s": args.rate,
+            "mix": dict(kinds), "data": "synthetic (seeded Poisson stream)", "dirac_max_iters": args.dirac_iters,
+            "served": side(served, wall_s, lanes=args.lanes, cache=True,
+                           precision="FP32 inner MINRES + FP64 refinement (Hodge), FP64 GMRES on sparse LU (Dirac)",
+                           peak_committed_gb=st["peak_committed_bytes"] / 1e9),
+            "plain": side(plain, wall_p, lanes=1, cache=False, precision="FP64 (Hodge), FP64 GMRES on sparse LU (Dirac)"),
+            "served_vs_plain_rel_err": {k: {"n": len(v), "max": max(v) if v else None,
+                                            "median": statistics.median(v) if v else None} for k, v in errs.items()},
+            "sampled_requests": len(sample), "vs_cpu_oracle": oracle_errs}
+
+
+def run_serve(args):
+    print(json.dumps(serve_study(args, compact=False)))
 
 
 # ---------------------------------------------------------------------------
@@ -654,7 +802,7 @@ def batch_specs(n, seed):
     return specs
 
 
-def run_batch(args):
+def batch_study(args, compact: bool):
     import torch
 
     import formoniq_gb300 as fq
@@ -663,7 +811,7 @@ def run_batch(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     ctx = fq.Context(0, stream=stream.cuda_stream)
-    specs = batch_specs(args.meshes, SEED + 3)
+    specs = batch_specs(128 if compact else args.meshes, SEED + 3)
     t0 = time.perf_counter()
     meshes = []
     for i, (dim, nb, _) in enumerate(specs):
@@ -677,7 +825,7 @@ def run_batch(args):
     plan_s = time.perf_counter() - t0
     batch.assemble()
     t0 = time.perf_counter()
-    batch.tune(reps=2)
+    batch.tune(reps=1 if compact else 2)
     tune_s = time.perf_counter() - t0
     info = batch.info()
     batch.assemble()  # validates (status words) once with the tuned shape
@@ -697,18 +845,19 @@ def run_batch(args):
             ts.append(a.elapsed_time(b))
         return statistics.median(ts)
 
-    for _ in range(args.warmup):
+    for _ in range(max(3, args.warmup)):
         batch.assemble(check=False)
         batch.assemble_per_mesh(check=False)
     torch.cuda.synchronize()
-    ms_batched = timed(lambda: batch.assemble(check=False), args.steps)
-    ms_launches = timed(lambda: batch.assemble_per_mesh(check=False), args.steps)
+    reps = min(args.steps, 10) if compact else args.steps
+    ms_batched = timed(lambda: batch.assemble(check=False), reps)
+    ms_launches = timed(lambda: batch.assemble_per_mesh(check=False), reps)
 
     def dropin():
         for m, mat in zip(meshes, mats):
             mat.reassemble(m)
 
-    ms_dropin = timed(dropin, max(1, args.steps // 2))
+    ms_dropin = timed(dropin, max(1, reps // 2))
     cells = info["cells"]
     out = {"metric": "assembled cells/s (batched vs per-mesh launches)", "meshes": len(meshes),
            "form": "hdif_gram(k) = M_k + dif_both(k+1), FP64 values (float-float compute)",
@@ -729,7 +878,11 @@ def run_batch(args):
     for m in meshes:
         m.close()
     ctx.close()
-    print(json.dumps(out))
+    return out
+
+
+def run_batch(args):
+    print(json.dumps(batch_study(args, compact=False)))
 
 
 def run_next(args):
@@ -896,6 +1049,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-solve", action="store_true", help="skip the solve phase (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer phase (profiling runs)")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="skip the compact batch / precision / serving studies of the default run")
     ap.add_argument("--workload", default="assembly", choices=["assembly", "precision", "serve", "batch", "next"],
                     help="assembly: the headline line; precision: the 4D FP32-with-refinement study; "
                          "serve: the request stream, served vs plain; batch: many meshes in one launch set; "
@@ -904,8 +1059,8 @@ def main():
     ap.add_argument("--meshes", type=int, default=512, help="batch: number of meshes")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--lanes", type=int, default=4)
-    ap.add_argument("--dirac-iters", type=int, default=2000,
-                    help="serve: MINRES cap of the Lorentzian Dirac requests")
+    ap.add_argument("--dirac-iters", type=int, default=300,
+                    help="serve: iteration cap of the Lorentzian Dirac requests (GMRES on the sparse LU)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
