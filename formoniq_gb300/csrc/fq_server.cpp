@@ -58,7 +58,10 @@ int64_t kuhn_cells_count(int n, int nb) {
 }
 
 // Bytes a request may hold at its peak: the scatter-plan build sorts 24 bytes
-// per element triplet; plan, operator and Krylov vectors stay below that.
+// per element triplet; plan, operator and Krylov vectors stay below that. A
+// Dirac request adds the sparse direct solver's fronts: measured on Minkowski
+// Kuhn boxes of 1e3 to 3e5 cells, about 1,100 cells^(4/3) bytes in FP32, twice
+// that when the factors fall back to FP64.
 uint64_t estimate_bytes(const fq_request& r) {
   const int n = r.dim;
   int L = 0;
@@ -66,7 +69,10 @@ uint64_t estimate_bytes(const fq_request& r) {
     L = (1 << (n + 1)) - 1;
   else
     L = binom(n + 1, r.grade) + binom(n + 1, r.grade + 1);
-  return uint64_t(40) * uint64_t(kuhn_cells_count(n, r.nbox)) * uint64_t(L) * uint64_t(L) + (uint64_t(32) << 20);
+  const double cells = double(kuhn_cells_count(n, r.nbox));
+  uint64_t est = uint64_t(40) * uint64_t(cells) * uint64_t(L) * uint64_t(L) + (uint64_t(32) << 20);
+  if (r.kind == FQ_REQ_DIRAC) est += uint64_t(2.0 * 1100.0 * std::pow(cells, 4.0 / 3.0));
+  return est;
 }
 
 // Counter-based N(0,1) (Box-Muller on two splitmix64 uniforms).
