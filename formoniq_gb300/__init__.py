@@ -228,7 +228,7 @@ _SIGNATURES = {
                                              ctypes.POINTER(_Report)]),
     "fq_dirac_system": (ctypes.c_int, [_P, _P, ctypes.c_double, ctypes.POINTER(_P)]),
     "fq_sparse_lu_create": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(_P)]),
-    "fq_sparse_lu_factor": (ctypes.c_int, [_P, _P]),
+    "fq_sparse_lu_factor": (ctypes.c_int, [_P, _P, ctypes.c_int]),
     "fq_sparse_lu_solve": (ctypes.c_int, [_P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(_Report)]),
     "fq_sparse_lu_info": (ctypes.c_int, [_P, _I64P, _I64P, _DP, _I64P, _I64P]),
     "fq_sparse_lu_destroy": (None, [_P]),
@@ -847,8 +847,8 @@ class SparseLu:
         self.h = h
         self.ctx._adopt(self)
 
-    def factor(self):
-        self.ctx.check(self.ctx.L.fq_sparse_lu_factor(self.h, self.a.h), "fq_sparse_lu_factor")
+    def factor(self, precision: int = FQ_FP32):
+        self.ctx.check(self.ctx.L.fq_sparse_lu_factor(self.h, self.a.h, int(precision)), "fq_sparse_lu_factor")
         return self
 
     def solve_device(self, b_ptr: int, x_ptr: int, opts: Optional[SolveOpts] = None) -> "Report":

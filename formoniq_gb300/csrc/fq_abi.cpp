@@ -1411,7 +1411,7 @@ static fq_status dirac_direct(fq_ctx* ctx, fq_mesh* m, fq_matrix* sii, double ma
     cached = lu;
   }
   SparseLu& lu = *cached;
-  FQ_TRY(sparse_lu_factor(ctx, lu, rp, ci, val, FQ_FP32));
+  lu.factored = false;  // new values: the solve factors them (FP32 first)
   const fq_status gs = sparse_lu_solve(ctx, lu, rp, ci, val, bordered ? bb.as<double>() : rhs,
                                        bordered ? bx.as<double>() : x, o->rtol, o->max_iters, r);
   if (gs != FQ_OK && gs != FQ_NOT_CONVERGED) return gs;

@@ -627,8 +627,7 @@ __global__ void __launch_bounds__(256) scatter_sym_kernel(const int4* __restrict
   const int4 r = __ldcs(rec + u);
   const E v0 = r.z >= 0 ? elem[r.z] : E(0);  // every slot has a contribution; guarded all the same
   const E v1 = r.w >= 0 ? elem[r.w] : E(0);
-  E acc = E(0);
-  acc += v0;
+  E acc = v0;  // 0 + v0 is v0 (the element values are normalised float pairs)
   bool nz = nonzero_bits(v0);
   if (r.w >= 0) {
     acc += v1;
@@ -712,8 +711,7 @@ __global__ void __launch_bounds__(256) scatter_sym_multi_kernel(const int4* __re
 #pragma unroll
     for (int i = 0; i < U; ++i) {
       if (r[i].x < 0) continue;  // past the end
-      E acc = E(0);
-      acc += v0[i];
+      E acc = v0[i];
       bool nz = nonzero_bits(v0[i]);
       if (r[i].w >= 0) {
         acc += v1[i];

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "fq_sparse_lu.h"
@@ -317,6 +318,7 @@ __global__ void __launch_bounds__(kThreads) sl_tile_kernel(const FrontDesc* __re
     if (tid == 0) {
       T d = Tt[j * LD + j];
       if (!isfinite(d)) {
+        if (nbad == 0 && atomicCAS(status + 2, 0, list[blockIdx.x] + 1) == 0) status[3] = k + j;
         ++nbad;
         d = thresh;
       } else if (fabs(d) < thresh) {
@@ -785,7 +787,10 @@ fq_status factor_impl(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_
   // and a pivot below 1e-6 is perturbed
   sl_row_scale_kernel<<<grid_of(lu.n, 256), 256, 0, st>>>(rp, val, lu.n, lu.scale.as<double>());
   ctx->launches++;
-  const T thresh = T(1e-6);
+  // the pivot floor, relative to the scaled matrix's largest entry (1): about
+  // ten units in the last place of FP32; far below any pivot the near-resonant
+  // systems need in FP64
+  const T thresh = sizeof(T) == 4 ? T(1e-6) : T(1e-13);
   FQ_CUDA(ctx, cudaMemsetAsync(lu.status.p, 0, 4 * sizeof(int), st));
   FQ_CUDA(ctx, cudaMemsetAsync(lu.piv.p, 0, size_t(std::max<int64_t>(lu.n, 1)) * 4, st));
   const int tile_smem = 2 * C::TILE * (C::TILE + 1) * int(sizeof(T));
@@ -879,7 +884,18 @@ fq_status factor_impl(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_
   lu.perturbed = hs[0];
   lu.nonfinite = hs[1];
   lu.factored = hs[1] == 0;
-  if (hs[1] > 0) return set_error(ctx, FQ_BREAKDOWN, "sparse LU: non-finite pivot");
+  if (hs[1] > 0) {
+    const int x = hs[2] - 1;
+    int lev = -1;
+    for (int l = 0; l < lu.nlevels && x >= 0; ++l)
+      for (int32_t q = lu.level_ptr[l]; q < lu.level_ptr[l + 1]; ++q)
+        if (lu.level_fronts[q] == x) lev = l;
+    return set_error(ctx, FQ_BREAKDOWN,
+                     std::string("sparse LU: non-finite pivot (") + (sizeof(T) == 4 ? "FP32" : "FP64") + ", front " +
+                         std::to_string(x) + " of level " + std::to_string(lev) + "/" + std::to_string(lu.nlevels) +
+                         ", m " + std::to_string(x >= 0 ? lu.front_m[x] : -1) + ", f " +
+                         std::to_string(x >= 0 ? lu.front_f[x] : -1) + ", column " + std::to_string(hs[3]) + ")");
+  }
   return FQ_OK;
 }
 
@@ -1086,8 +1102,14 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
 fq_status sparse_lu_solve(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_t* ci, const double* val,
                           const double* b, double* x, double rtol, int64_t max_iters, fq_report* rep) {
   fq_report r{};
+  if (lu.factored && lu.precision == FQ_FP64) {
+    const fq_status s64 = sparse_lu_gmres(ctx, lu, rp, ci, val, b, x, rtol, max_iters, &r);
+    r.refinements = 1;
+    if (rep) *rep = r;
+    return s64;
+  }
   fq_status s = FQ_NOT_CONVERGED;
-  fq_status fs = (lu.factored && lu.precision == FQ_FP32) ? FQ_OK : sparse_lu_factor(ctx, lu, rp, ci, val, FQ_FP32);
+  fq_status fs = lu.factored ? FQ_OK : sparse_lu_factor(ctx, lu, rp, ci, val, FQ_FP32);
   if (fs == FQ_OK) {
     s = sparse_lu_gmres(ctx, lu, rp, ci, val, b, x, rtol, std::min<int64_t>(max_iters, kFp32Iterations), &r);
     if (s != FQ_OK && s != FQ_NOT_CONVERGED) return s;

@@ -58,12 +58,14 @@ fq_status fq_sparse_lu_create(fq_ctx* ctx, fq_mesh* mesh, const fq_matrix* a, fq
   FQ_GUARD_END(ctx)
 }
 
-fq_status fq_sparse_lu_factor(fq_sparse_lu* s, const fq_matrix* a) {
+fq_status fq_sparse_lu_factor(fq_sparse_lu* s, const fq_matrix* a, int precision) {
   if (!s || !a) return FQ_INVALID_ARG;
+  if (precision != FQ_FP32 && precision != FQ_FP64)
+    return set_error(s->ctx, FQ_INVALID_ARG, "sparse LU: factors in FQ_FP32 or FQ_FP64");
   if (a->nrows != s->lu.n || a->nnz != s->lu.nnz)
     return set_error(s->ctx, FQ_INVALID_ARG, "sparse LU: the matrix's pattern is not the analysed one");
   FQ_GUARD_BEGIN
-  return sparse_lu_factor(s->ctx, s->lu, a->rp, a->ci, a->values.as<double>(), FQ_FP32);
+  return sparse_lu_factor(s->ctx, s->lu, a->rp, a->ci, a->values.as<double>(), precision);
   FQ_GUARD_END(s->ctx)
 }
 

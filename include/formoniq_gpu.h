@@ -429,14 +429,14 @@ typedef struct fq_sparse_lu fq_sparse_lu;
  * fq_dirac_system or fq_mixed_system on `mesh`, a fq_mesh_kuhn_cube mesh):
  * FQ_UNSUPPORTED on other meshes. */
 fq_status fq_sparse_lu_create(fq_ctx* ctx, fq_mesh* mesh, const fq_matrix* a, fq_sparse_lu** out);
-/* Numeric factorization of a's current values in FP32 (after every
- * re-assembly). */
-fq_status fq_sparse_lu_factor(fq_sparse_lu* lu, const fq_matrix* a);
+/* Numeric factorization of a's current values (after every re-assembly), in
+ * precision FQ_FP32 (tiles of 128 columns on the FP32 pipe) or FQ_FP64. */
+fq_status fq_sparse_lu_factor(fq_sparse_lu* lu, const fq_matrix* a, int precision);
 /* x = A^-1 b (device vectors of a->nrows doubles) by GMRES to opts->rtol on the
- * true FP64 residual, at most opts->max_iters iterations in all. GMRES runs on
- * the FP32 factors for at most 60 iterations; if it has not converged by then,
- * `a` is re-factored in FP64 (the factorization keeps FP64 afterwards, until
- * the next fq_sparse_lu_factor) and GMRES starts again from zero: then
+ * true FP64 residual, at most opts->max_iters iterations in all. On FP32
+ * factors GMRES runs for at most 60 iterations; if it has not converged by
+ * then, `a` is re-factored in FP64 (the factorization keeps FP64 afterwards,
+ * until the next fq_sparse_lu_factor) and GMRES starts again from zero: then
  * report.refinements = 1. report.iters counts both. */
 fq_status fq_sparse_lu_solve(fq_sparse_lu* lu, const fq_matrix* a, const double* b_dev, double* x_dev,
                              const fq_solve_opts* opts, fq_report* report);
