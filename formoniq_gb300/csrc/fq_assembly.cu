@@ -945,10 +945,16 @@ fq_status compact_csr(fq_ctx* ctx, fq_matrix* m, int64_t nzero) {
 // ---------------------------------------------------------------------------
 // Element pass and assembly driver
 // ---------------------------------------------------------------------------
+// The type of the element buffer a program writes, as a precision mode: the 4D
+// Dirac program (all five grades coupled, 31 local dofs) runs in IEEE double
+// in FQ_FP64 too (no configuration needs it fast and its float-float build is
+// large), so its buffer holds doubles, and its scatter must read doubles.
+int element_buffer_mode(int n, int kind, int mode) {
+  return (n == 4 && kind == EK_DIRAC && mode == FQ_FP64) ? FQ_FP64_IEEE : mode;
+}
+
 template <int N>
 static int launch_dim(int grade, int kind, int mode, const ElemArgs& a, cudaStream_t st) {
-  // The 4D Dirac program (all five grades coupled, 31 local dofs) runs in IEEE
-  // double: no configuration needs it fast and its float-float build is large.
   if (kind == EK_METRIC || mode == 2 || (N == 4 && kind == EK_DIRAC)) return launch_typed<N, double>(grade, kind, a, st);
   if (mode == 1) return launch_typed<N, float>(grade, kind, a, st);
   return launch_typed<N, df64>(grade, kind, a, st);
@@ -1030,8 +1036,8 @@ static fq_status assemble_launch(fq_ctx* ctx, fq_matrix* m, cudaEvent_t* ev, boo
   if (p.nslots > 0 || p.ndiag_trip > 0) FQ_TRY(element_pass(ctx, mesh, m->kind, m->grade, mode, m->param, mesh->elem, p.nent));
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[1], ctx->stream));
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[2], ctx->stream));
-  launch_scatter(p, mesh->elem.p, m->full_values.p, with_flags ? m->zero_flags.as<uint8_t>() : nullptr, zc, mode,
-                 ctx->stream, ctx->scatter_shape);
+  launch_scatter(p, mesh->elem.p, m->full_values.p, with_flags ? m->zero_flags.as<uint8_t>() : nullptr, zc,
+                 element_buffer_mode(mesh->dim, m->kind, mode), ctx->stream, ctx->scatter_shape);
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[3], ctx->stream));
   if (p.nslots > 0) ctx->launches++;
   return FQ_OK;

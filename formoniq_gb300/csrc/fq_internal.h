@@ -228,6 +228,9 @@ fq_status build_plan(fq_ctx* ctx, fq_mesh* mesh, Plan& plan, const Layout& lay);
 // values[s] = sum of elem[perm[t]] over the slot's contributions; zero_flags[s]
 // = 1 when every contribution was exactly 0.0; status[1] += count of such
 // slots; status[0] |= 4 if a symmetric plan misses a mirror slot.
+// The element buffer's type (as a precision mode) of a program in a mode: the
+// 4D Dirac program writes doubles in FQ_FP64 too.
+int element_buffer_mode(int n, int kind, int mode);
 void launch_scatter(const Plan& plan, const void* elem, void* values, uint8_t* zero_flags, int* status, int mode,
                     cudaStream_t st, ScatterShape shape = ScatterShape());
 void launch_scatter_diag(const Plan& plan, const void* elem, double* out, int mode, cudaStream_t st);

@@ -84,7 +84,8 @@ extern "C" fq_status fq_reassemble_noalloc(fq_ctx* ctx, fq_mesh* mesh, const fq_
       return set_error(ctx, FQ_UNSUPPORTED, "no element program for this dimension/grade");
     ctx->launches++;
     FQ_CUDA(ctx, cudaGetLastError());
-    launch_scatter(p, base, values_out, nullptr, ctx->status.as<int>(), mode, st, ctx->scatter_shape);
+    launch_scatter(p, base, values_out, nullptr, ctx->status.as<int>(), element_buffer_mode(mesh->dim, pattern->kind, mode), st,
+                   ctx->scatter_shape);
     ctx->launches++;
     FQ_CUDA(ctx, cudaGetLastError());
   }

@@ -545,16 +545,24 @@ __global__ void __launch_bounds__(kThreads) sl_forward_kernel(const FrontDesc* _
     __syncthreads();
   }
   // the front's row interchanges, in the order the factorization made them
-  if (tid == 0)
-    for (int p = 0; p < f; ++p) {
-      const int t = piv[F.start + p];
-      if (t != p) {
-        const T a = r[p];
-        r[p] = r[t];
-        r[t] = a;
+  // (their targets staged through shared memory a chunk at a time, so that the
+  // one thread applying them does not wait on a global load per interchange)
+  __shared__ int pv[1024];
+  for (int p0 = 0; p0 < f; p0 += 1024) {
+    const int np = min(1024, f - p0);
+    for (int t = tid; t < np; t += nt) pv[t] = piv[F.start + p0 + t];
+    __syncthreads();
+    if (tid == 0)
+      for (int q = 0; q < np; ++q) {
+        const int p = p0 + q, t = pv[q];
+        if (t != p) {
+          const T a = r[p];
+          r[p] = r[t];
+          r[t] = a;
+        }
       }
-    }
-  __syncthreads();
+    __syncthreads();
+  }
   const T* P = pool + F.off;
   for (int k = 0; k < f; k += TL) {
     const int b = min(TL, f - k);
@@ -988,6 +996,14 @@ fq_status sparse_lu_apply(fq_ctx* ctx, SparseLu& lu, const double* r, double* z)
   return apply_impl<double>(ctx, lu, r, z);
 }
 
+// A solve ends when the relative residual meets rtol, or when the normwise
+// backward error ||b - A x|| / (||A||_F ||x|| + ||b||) has reached the rounding
+// level of FP64 (kBackwardFloor): what an LU solve of the same system
+// delivers. On a nearly singular system (the near-resonant Lorentzian boxes)
+// a residual of rtol may lie below that floor; GMRES then stops there instead
+// of iterating on rounding errors.
+constexpr double kBackwardFloor = 1e-14;
+
 fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_t* ci, const double* val,
                           const double* b, double* x, double rtol, int64_t max_iters, fq_report* rep) {
   const int64_t n = lu.n;
@@ -1005,9 +1021,10 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
   double* w = g.w.as<double>();
   const unsigned spmv_blocks = unsigned((n * 4 + 255) / 256);
   FQ_CUDA(ctx, cudaMemsetAsync(x, 0, size_t(n) * 8, st));
-  double bnorm2 = 0.0;
+  double bnorm2 = 0.0, anorm2 = 0.0;
   FQ_TRY(self_dot(ctx, g, n, b, &bnorm2));
-  const double bnorm = std::sqrt(bnorm2);
+  FQ_TRY(self_dot(ctx, g, lu.nnz, val, &anorm2));
+  const double bnorm = std::sqrt(bnorm2), anorm = std::sqrt(anorm2);
   fq_report r{};
   if (!(bnorm > 0.0)) {
     r.converged = 1;
@@ -1019,21 +1036,27 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
   bool done = false;
   std::vector<double> h, h2;
   while (!done && it < max_iters) {
-    // r = b - A x into V[0]
+    // r = b - A x into V[0]; the true residual and the backward error of x
     sl_spmv_kernel<<<spmv_blocks, 256, 0, st>>>(rp, ci, val, x, n, w);
     sl_residual_kernel<<<grid_of(n, 256), 256, 0, st>>>(b, w, n, V);
     ctx->launches += 2;
-    double beta2 = 0.0;
+    double beta2 = 0.0, x2 = 0.0;
     FQ_TRY(self_dot(ctx, g, n, V, &beta2));
+    FQ_TRY(self_dot(ctx, g, n, x, &x2));
     const double beta = std::sqrt(beta2);
     relres = beta / bnorm;
-    if (relres <= rtol) break;
+    if (relres <= rtol || (it > 0 && beta <= kBackwardFloor * (anorm * std::sqrt(x2) + bnorm))) {
+      done = true;
+      break;
+    }
     sl_scale_into_kernel<<<grid_of(n, 256), 256, 0, st>>>(V, 1.0 / beta, n, V);
     ctx->launches++;
     std::vector<std::vector<double>> H(restart + 1, std::vector<double>(restart, 0.0));
     std::vector<double> cs(restart, 0.0), sn(restart, 0.0), gv(restart + 1, 0.0);
     gv[0] = beta;
     int j = 0;
+    double best = relres;
+    int stale = 0;
     for (; j < restart && it < max_iters; ++j, ++it) {
       FQ_TRY(sparse_lu_apply(ctx, lu, V + int64_t(j) * n, Z + int64_t(j) * n));
       sl_spmv_kernel<<<spmv_blocks, 256, 0, st>>>(rp, ci, val, Z + int64_t(j) * n, n, w);
@@ -1066,6 +1089,16 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
       gv[j + 1] = -sn[j] * gv[j];
       gv[j] = cs[j] * gv[j];
       relres = std::fabs(gv[j + 1]) / bnorm;
+      // stagnation: five iterations without halving the residual estimate end
+      // the cycle early (the true residual then decides)
+      if (relres < 0.5 * best) {
+        best = relres;
+        stale = 0;
+      } else if (++stale >= 5) {
+        ++j;
+        ++it;
+        break;
+      }
       if (relres <= rtol || hn == 0.0) {
         ++j;
         ++it;
@@ -1080,21 +1113,39 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
       y[i] = H[i][i] != 0.0 ? s / H[i][i] : 0.0;
     }
     if (j > 0) FQ_TRY(axpy_h(ctx, g, Z, n, j, y, 1.0, x));
-    if (relres <= rtol) {
-      // confirm on the true residual
+    if (stale >= 5 && it < max_iters) {
+      // a stagnating cycle: accept x if it is at the rounding level, else the
+      // restart continues (and a stagnating FP32 preconditioner gives way to
+      // FP64 factors in sparse_lu_solve)
       sl_spmv_kernel<<<spmv_blocks, 256, 0, st>>>(rp, ci, val, x, n, w);
       sl_residual_kernel<<<grid_of(n, 256), 256, 0, st>>>(b, w, n, w);
       ctx->launches += 2;
-      double t2 = 0.0;
+      double t2 = 0.0, xx = 0.0;
       FQ_TRY(self_dot(ctx, g, n, w, &t2));
+      FQ_TRY(self_dot(ctx, g, n, x, &xx));
       relres = std::sqrt(t2) / bnorm;
-      done = relres <= rtol;
+      if (relres <= rtol || std::sqrt(t2) <= kBackwardFloor * (anorm * std::sqrt(xx) + bnorm)) {
+        done = true;
+        break;
+      }
+      if (lu.precision == FQ_FP32) break;  // the FP64 factors take over
     }
+  }
+  if (!done) {
+    // out of iterations: the last iterate's true residual and backward error
+    sl_spmv_kernel<<<spmv_blocks, 256, 0, st>>>(rp, ci, val, x, n, w);
+    sl_residual_kernel<<<grid_of(n, 256), 256, 0, st>>>(b, w, n, w);
+    ctx->launches += 2;
+    double t2 = 0.0, xx = 0.0;
+    FQ_TRY(self_dot(ctx, g, n, w, &t2));
+    FQ_TRY(self_dot(ctx, g, n, x, &xx));
+    relres = std::sqrt(t2) / bnorm;
+    done = relres <= rtol || std::sqrt(t2) <= kBackwardFloor * (anorm * std::sqrt(xx) + bnorm);
   }
   r.iters = it;
   r.residual = relres;
   r.true_residual = relres;
-  r.converged = relres <= rtol ? 1 : 0;
+  r.converged = done ? 1 : 0;
   if (rep) *rep = r;
   return r.converged ? FQ_OK : FQ_NOT_CONVERGED;
 }

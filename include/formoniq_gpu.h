@@ -433,7 +433,10 @@ fq_status fq_sparse_lu_create(fq_ctx* ctx, fq_mesh* mesh, const fq_matrix* a, fq
  * precision FQ_FP32 (tiles of 128 columns on the FP32 pipe) or FQ_FP64. */
 fq_status fq_sparse_lu_factor(fq_sparse_lu* lu, const fq_matrix* a, int precision);
 /* x = A^-1 b (device vectors of a->nrows doubles) by GMRES to opts->rtol on the
- * true FP64 residual, at most opts->max_iters iterations in all. On FP32
+ * true FP64 residual, or until the normwise backward error
+ * ||b - A x|| / (||A||_F ||x|| + ||b||) reaches 1e-14 (the rounding level an LU
+ * solve delivers; a nearly singular system may not allow rtol), at most
+ * opts->max_iters iterations in all. On FP32
  * factors GMRES runs for at most 60 iterations; if it has not converged by
  * then, `a` is re-factored in FP64 (the factorization keeps FP64 afterwards,
  * until the next fq_sparse_lu_factor) and GMRES starts again from zero: then

@@ -411,10 +411,10 @@ def test_mixed_precision_refinement_reaches_1e8(oracle, ctx):
 # Hodge-Dirac
 # ---------------------------------------------------------------------------
 
-@pytest.mark.parametrize("dim", [1, 2, 3])
+@pytest.mark.parametrize("dim", [1, 2, 3, 4])
 @pytest.mark.parametrize("mink", [False, True])
 def test_dirac_system_parity(oracle, ctx, dim, mink):
-    cx, mesh, lengths, _ = make_pair(oracle, ctx, dim, 3, jitter=0.0, minkowski=mink)
+    cx, mesh, lengths, _ = make_pair(oracle, ctx, dim, 2 if dim == 4 else 3, jitter=0.0, minkowski=mink)
     lengths = lengths * (1.0 + 0.05 * oracle.uniform_pm1(3, np.arange(len(lengths), dtype=np.uint64)))
     mesh.set_lengths_sq(lengths)
     s_rel, _, _, _ = oracle.dirac_source_system(cx, lengths, 1.5, np.zeros(sum(cx.nsimplices(k) for k in
