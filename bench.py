@@ -10,11 +10,12 @@ The same run times the mixed k=1 Hodge-Laplace solve by preconditioned MINRES to
 with host buffers.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-    python bench.py --workload precision|serve|batch|next
+    python bench.py --workload precision|serve|batch|next|dirac
 
 The other workloads: the 4D FP32-with-refinement study, the served request
-stream, many meshes assembled in one launch set, and the rows after the headline
-path (matrix-free operator, source load, de Rham map, leapfrog).
+stream, many meshes assembled in one launch set, the rows after the headline
+path (matrix-free operator, source load, de Rham map, leapfrog), and the direct
+Lorentzian Dirac solves by mesh size.
 
 Multi-GPU: the path does not shard (one mesh per solve), so N > 1 runs N
 independent replicas, one per rank, with no collective on the data path.
@@ -885,6 +886,97 @@ def run_batch(args):
     print(json.dumps(batch_study(args, compact=False)))
 
 
+# ---------------------------------------------------------------------------
+# Dirac workload: direct Lorentzian Dirac solves at the served stream's sizes
+# ---------------------------------------------------------------------------
+
+def run_dirac(args):
+    """The served stream's Lorentzian requests one size at a time: Minkowski
+    1+2 Kuhn boxes (time axis 0.7), squared lengths s (1 + U(-0.05, 0.05)),
+    the relative Hodge-Dirac source problem at m = 1.5 and at m = 0 (bordered
+    with the top harmonic) through fq.solve_dirac_source with host buffers.
+    Per size: the sparse direct solver's analysis, its FP32 and FP64
+    factorizations timed with CUDA events (TFLOP/s of the factor's flops),
+    and the end-to-end solve (wall clock, median of --solves after one
+    untimed call that builds the analysis). Sizes up to 8 boxes per axis are
+    checked against the oracle's LU solve on the same inputs, which is also
+    timed as the CPU baseline."""
+    import torch
+
+    import formoniq_gb300 as fq
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = fq.Context(0, stream=stream.cuda_stream)
+    sizes = [int(a) for a in args.dirac_sizes.split(",")]
+    side = np.array([0.7, 1.0, 1.0])
+    signs = np.array([-1.0, 1.0, 1.0])
+    out = {"metric": "Dirac solves/s (direct route) by mesh size", "data": "synthetic (seeded Minkowski 1+2 boxes)",
+           "rtol": 1e-10, "max_iters": args.dirac_iters, "sizes": []}
+    for nb in sizes:
+        mesh = fq.Mesh.kuhn_cube(ctx, 3, nb)
+        mesh.kuhn_lengths(side=side, ambient_signs=signs, jitter=0.0, seed=0)
+        rng = np.random.default_rng(SEED + nb)
+        lengths = mesh.lengths_sq() * (1.0 + 0.05 * rng.uniform(-1.0, 1.0, mesh.nsimplices(1)))
+        mesh.set_lengths_sq(lengths)
+        ntot = sum(mesh.nsimplices(k) for k in range(4))
+        load = rng.standard_normal(ntot)
+        rec = {"nbox": nb, "cells": mesh.ncells(), "unknowns_full": ntot}
+        # the factorizations of the m = 1.5 system
+        a = fq.dirac_system(mesh, 1.5)
+        t0 = time.perf_counter()
+        lu = fq.SparseLu(mesh, a)
+        torch.cuda.synchronize()
+        rec["analyse_s"] = time.perf_counter() - t0
+        info = lu.info()
+        rec.update(unknowns=int(a.shape[0]), fronts=int(info["fronts"]), levels=int(info["levels"]),
+                   factor_gflop=info["flops"] / 1e9, factor_gb=info["factor_bytes"] / 1e9)
+        for name, prec in (("fp32", fq.FQ_FP32), ("fp64", fq.FQ_FP64)):
+            lu.factor(prec)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lu.factor(prec)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            rec[f"factor_{name}_ms"] = ms
+            rec[f"factor_{name}_tflops"] = info["flops"] / (ms * 1e9)
+            rec[f"perturbed_{name}"] = int(lu.info()["perturbed_pivots"])
+        lu.close()
+        a.close()
+        for mass in (1.5, 0.0):
+            opts = fq.SolveOpts.default(rtol=1e-10, max_iters=args.dirac_iters)
+            x, rep = fq.solve_dirac_source(mesh, mass, load, None, opts)
+            ts = []
+            for _ in range(max(1, args.solves)):
+                t0 = time.perf_counter()
+                x, rep = fq.solve_dirac_source(mesh, mass, load, None, opts)
+                ts.append((time.perf_counter() - t0) * 1e3)
+            key = "m1.5" if mass else "m0"
+            r = {"e2e_ms": statistics.median(ts), "solves_per_s": 1e3 / statistics.median(ts),
+                 "gmres_iters": int(rep.iters), "fp64_factors": int(rep.refinements),
+                 "converged": bool(rep.converged), "true_residual": float(rep.true_residual)}
+            if nb <= 8 and not args.no_cpu:
+                sys.path.insert(0, os.path.join(ROOT, "oracle"))
+                import oracle
+
+                cx, _, _ = oracle.minkowski(3, nb)
+                t0 = time.perf_counter()
+                want = oracle.dirac_solve_source(cx, lengths, mass, load, np.zeros(ntot))
+                cpu_ms = (time.perf_counter() - t0) * 1e3
+                r["rel_err_vs_oracle"] = float(np.linalg.norm(x - want) / np.linalg.norm(want))
+                r["cpu_baseline"] = {"ms": cpu_ms, "kind": "port", "cores": 1,
+                                     "sample": "oracle.dirac_solve_source (SciPy SuperLU), same inputs"}
+            rec[key] = r
+        mesh.close()
+        out["sizes"].append(rec)
+        print(json.dumps(rec), file=sys.stderr, flush=True)
+    ctx.close()
+    print(json.dumps(out))
+
+
 def run_next(args):
     """The rows after the headline path on the 3D 32^3 mesh: the matrix-free
     operator against the assembled SpMV, the right-hand side (the source load
@@ -1051,16 +1143,20 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer phase (profiling runs)")
     ap.add_argument("--no-sub", action="store_true",
                     help="skip the compact batch / precision / serving studies of the default run")
-    ap.add_argument("--workload", default="assembly", choices=["assembly", "precision", "serve", "batch", "next"],
+    ap.add_argument("--workload", default="assembly",
+                    choices=["assembly", "precision", "serve", "batch", "next", "dirac"],
                     help="assembly: the headline line; precision: the 4D FP32-with-refinement study; "
                          "serve: the request stream, served vs plain; batch: many meshes in one launch set; "
-                         "next: matrix-free operator, source load, de Rham map, leapfrog")
+                         "next: matrix-free operator, source load, de Rham map, leapfrog; "
+                         "dirac: direct Lorentzian Dirac solves by mesh size")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--meshes", type=int, default=512, help="batch: number of meshes")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--lanes", type=int, default=4)
     ap.add_argument("--dirac-iters", type=int, default=300,
                     help="serve: iteration cap of the Lorentzian Dirac requests (GMRES on the sparse LU)")
+    ap.add_argument("--dirac-sizes", default="6,12,20,28,37",
+                    help="dirac: boxes per axis of the Minkowski meshes (6 N^3 cells each)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -1072,6 +1168,8 @@ def main():
         run_batch(args)
     elif args.workload == "next":
         run_next(args)
+    elif args.workload == "dirac":
+        run_dirac(args)
     else:
         run_ours(args)
 

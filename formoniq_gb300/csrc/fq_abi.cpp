@@ -1352,10 +1352,38 @@ static fq_status top_harmonic(fq_ctx* ctx, fq_mesh* m, int64_t nrel, DevBuf& h, 
   return FQ_OK;
 }
 
+// The mass term whose system is factored in place of a massless (or nearly
+// massless) one: 1e-3 over the mesh's diameter, estimated as nbox times the
+// root mean square edge length. The Hodge-Dirac operator pairs even and odd
+// grades only, so at m = 0 the fully summed block of every leaf front is
+// structurally singular (its even and odd counts differ); with the mass shift
+// every pivot is defined, and the eigenvalues (l + m) / (l + tau) of the
+// preconditioned system stay near 1 for the operator's nonzero spectrum
+// |l| >~ 1 / diameter, so GMRES on the exact system needs a handful of
+// iterations. The pivots of size tau grow the factors by about 1 / tau: they
+// are kept in FP64.
+static constexpr double kMasslessShift = 1e-3;
+static fq_status massless_shift(fq_ctx* ctx, const fq_mesh* m, double* tau) {
+  const int64_t ne = m->nsimp[1];
+  std::vector<double> l(static_cast<size_t>(std::max<int64_t>(ne, 1)));
+  FQ_CUDA(ctx, cudaMemcpyAsync(l.data(), m->lengths.p, ne * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  double acc = 0;
+  for (int64_t e = 0; e < ne; ++e) acc += std::fabs(l[e]);
+  const double rms = ne > 0 ? std::sqrt(acc / double(ne)) : 0.0;
+  const double diam = double(std::max(m->kuhn_nbox, 1)) * rms;
+  if (!(diam > 0) || !std::isfinite(diam))
+    return set_error(ctx, FQ_INVALID_ARG, "the massless Dirac solve needs finite nonzero edge lengths");
+  *tau = kMasslessShift / diam;
+  return FQ_OK;
+}
+
 // The direct route of the Dirac source problem: the relative system (bordered
 // with the top harmonic at m = 0 when it spans the kernel, as solve_bordered,
 // problems/dirac.rs:525-531, 578-598) factored by the sparse direct solver,
-// GMRES in FP64 to opts->rtol.
+// GMRES in FP64 to opts->rtol. When |m| is below the massless shift tau, the
+// factored matrix is the one with mass term tau (same sign as m), in FP64;
+// GMRES still runs on the system with mass term m.
 static fq_status dirac_direct(fq_ctx* ctx, fq_mesh* m, fq_matrix* sii, double mass_term, int64_t nrel,
                               const double* rhs, double* x, const fq_solve_opts* o, fq_report* r) {
   std::vector<int32_t> dofv;
@@ -1364,11 +1392,25 @@ static fq_status dirac_direct(fq_ctx* ctx, fq_mesh* m, fq_matrix* sii, double ma
   const int32_t* ci = sii->ci;
   const double* val = sii->values.as<double>();
   int64_t nsys = nrel;
-  DevBuf brp, bci, bval, bb, bx, h;
+  DevBuf brp, bci, bval, bb, bx, h, trp, tci, tval;
   bool bordered = false;
+  // the shifted system to factor, when the mass term is below the shift
+  double tau = 0;
+  FQ_TRY(massless_shift(ctx, m, &tau));
+  std::unique_ptr<fq_matrix> shifted;
+  if (std::fabs(mass_term) < tau && nrel > 0) {
+    fq_matrix* t = nullptr;
+    FQ_TRY(make_matrix(ctx, m, EK_DIRAC, 0, FQ_RELATIVE, FQ_FP64, mass_term < 0 ? -tau : tau, &t));
+    shifted.reset(t);
+  }
+  // the matrix factored: the system's own, or the shifted one, whose pattern
+  // holds the mass blocks that assembly drops as all-zero slots at m = 0
+  const int32_t* frp = shifted ? shifted->rp : rp;
+  const int32_t* fci = shifted ? shifted->ci : ci;
+  const double* fval = shifted ? shifted->values.as<double>() : nullptr;
+  int64_t off = 0;
   if (mass_term == 0.0 && nrel > 0) {
     DevBuf sh;
-    int64_t off = 0;
     FQ_TRY(top_harmonic(ctx, m, nrel, h, &off));
     FQ_TRY(sh.alloc(ctx, std::max<int64_t>(nrel, 1) * 8));
     launch_spmv(sii, h.p, sh.p, ctx->stream);
@@ -1388,6 +1430,16 @@ static fq_status dirac_direct(fq_ctx* ctx, fq_mesh* m, fq_matrix* sii, double ma
       rp = brp.as<int32_t>();
       ci = bci.as<int32_t>();
       val = bval.as<double>();
+      if (shifted) {
+        // the same border on the shifted matrix
+        FQ_TRY(border_csr(ctx, shifted.get(), h.as<double>() + off, off, m->ninterior[m->dim], trp, tci, tval));
+        frp = trp.as<int32_t>();
+        fci = tci.as<int32_t>();
+        fval = tval.as<double>();
+      } else {
+        frp = rp;
+        fci = ci;
+      }
       nsys = nrel + 1;
       dofv.resize(size_t(nsys) * 5, -1);
       FQ_TRY(bb.alloc(ctx, nsys * 8));
@@ -1401,17 +1453,19 @@ static fq_status dirac_direct(fq_ctx* ctx, fq_mesh* m, fq_matrix* sii, double ma
   // solve (new lengths or load), redone when the pattern changed
   std::shared_ptr<SparseLu>& cached = m->dirac_lu[bordered ? 1 : 0];
   int32_t nnz32 = 0;
-  FQ_CUDA(ctx, cudaMemcpyAsync(&nnz32, rp + nsys, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaMemcpyAsync(&nnz32, frp + nsys, 4, cudaMemcpyDeviceToHost, ctx->stream));
   FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   const int64_t nnz = nnz32;
   if (!cached || cached->n != nsys || cached->nnz != nnz) {
     cached.reset();
     auto lu = std::make_shared<SparseLu>();
-    FQ_TRY(sparse_lu_build(ctx, m, nsys, rp, ci, dofv, *lu));
+    FQ_TRY(sparse_lu_build(ctx, m, nsys, frp, fci, dofv, *lu));
     cached = lu;
   }
   SparseLu& lu = *cached;
   lu.factored = false;  // new values: the solve factors them (FP32 first)
+  // the shifted matrix in FP64; the solve then runs GMRES on the system alone
+  if (fval) FQ_TRY(sparse_lu_factor(ctx, lu, frp, fci, fval, FQ_FP64));
   const fq_status gs = sparse_lu_solve(ctx, lu, rp, ci, val, bordered ? bb.as<double>() : rhs,
                                        bordered ? bx.as<double>() : x, o->rtol, o->max_iters, r);
   if (gs != FQ_OK && gs != FQ_NOT_CONVERGED) return gs;

@@ -66,17 +66,37 @@ def test_dirac_direct_at_stream_sizes(oracle, ctx, nb):
     mesh.close()
 
 
-@pytest.mark.parametrize("dim,nb,mink", [(3, 4, True), (3, 4, False), (2, 8, True)])
+@pytest.mark.parametrize("dim,nb,mink", [(3, 4, True), (3, 4, False), (2, 8, True), (3, 8, True), (4, 3, True),
+                                         (4, 3, False)])
 def test_massless_dirac_bordered(oracle, ctx, dim, nb, mink):
     """m = 0: the relative system is singular with the top-grade harmonic as its
     kernel; both sides border it (solve_bordered, problems/dirac.rs:578-598) and
-    return the solution orthogonal to it."""
+    return the solution orthogonal to it. The device factors the bordered
+    system with a small mass shift (the unshifted one has structurally zero
+    pivots); GMRES on the exact system then needs few iterations."""
     cx, lengths, mesh = lattice_mesh(oracle, ctx, dim, nb, mink)
     ntot = sum(cx.nsimplices(k) for k in range(dim + 1))
     load = np.random.default_rng(3).standard_normal(ntot)
     want = oracle.dirac_solve_source(cx, lengths, 0.0, load, np.zeros(ntot))
     x, rep = fq.solve_dirac_source(mesh, 0.0, load, None, fq.SolveOpts.default(rtol=1e-12, max_iters=300))
     assert rep.converged, rep
+    assert rep.iters <= 40, rep
+    assert rel(x, want) < SOLVE_TOL
+    mesh.close()
+
+
+@pytest.mark.parametrize("mass", [1e-5, -1e-5])
+def test_nearly_massless_dirac(oracle, ctx, mass):
+    """0 < |m| below the shift: the system is regular (no border) but nearly
+    singular; the factored matrix carries the shift, GMRES the true mass."""
+    dim, nb = 3, 4
+    cx, lengths, mesh = lattice_mesh(oracle, ctx, dim, nb, True)
+    ntot = sum(cx.nsimplices(k) for k in range(dim + 1))
+    load = np.random.default_rng(4).standard_normal(ntot)
+    want = oracle.dirac_solve_source(cx, lengths, mass, load, np.zeros(ntot))
+    x, rep = fq.solve_dirac_source(mesh, mass, load, None, fq.SolveOpts.default(rtol=1e-12, max_iters=300))
+    assert rep.converged, rep
+    assert rep.iters <= 40, rep
     assert rel(x, want) < SOLVE_TOL
     mesh.close()
 
