@@ -944,6 +944,20 @@ def run_dirac(args):
             rec[f"factor_{name}_ms"] = ms
             rec[f"factor_{name}_tflops"] = info["flops"] / (ms * 1e9)
             rec[f"perturbed_{name}"] = int(lu.info()["perturbed_pivots"])
+        # the FP32 factors alone (no FP64 refactorization), GMRES to rtol or 500 iterations
+        # (the FP64 factors are still in place from the loop above; replace them first)
+        lu.factor(fq.FQ_FP32)
+        bvec = torch.tensor(rng.standard_normal(a.shape[0]), device="cuda")
+        xvec = torch.empty_like(bvec)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rep32 = lu.solve_device(bvec.data_ptr(), xvec.data_ptr(),
+                                fq.SolveOpts.default(rtol=1e-10, max_iters=500, max_refinements=0))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        rec["fp32_factors_only"] = {"gmres_iters": int(rep32.iters), "converged": bool(rep32.converged),
+                                    "true_residual": float(rep32.true_residual), "solve_ms": e0.elapsed_time(e1)}
         lu.close()
         a.close()
         for mass in (1.5, 0.0):

@@ -628,7 +628,9 @@ def solve_source(complex_: WhitneyComplex, source: np.ndarray, grade: int, opts:
 
 def solve_dirac_source(mesh: Mesh, mass_term: float, load_: np.ndarray, lift: Optional[np.ndarray] = None,
                        opts: Optional[SolveOpts] = None):
-    """dirac::solve_dirac_source (problems/dirac.rs:473-531) by MINRES."""
+    """dirac::solve_dirac_source (problems/dirac.rs:473-531): the sparse direct
+    route (FP64 GMRES on the system's LU, bordered at m = 0) on Kuhn cube
+    meshes, MINRES on other meshes or with the MINRES preconditioners."""
     ctx = mesh.ctx
     load_ = np.ascontiguousarray(load_, np.float64)
     lift_a = None if lift is None else np.ascontiguousarray(lift, np.float64)

@@ -44,6 +44,7 @@ void vec_fill(double* a, double v, int64_t n, cudaStream_t st);
 void vec_scale(double* a, double s, int64_t n, cudaStream_t st);
 fq_status border_csr(fq_ctx* ctx, const fq_matrix* a, const double* mh, int64_t ns, int64_t nu, DevBuf& nrp,
                      DevBuf& nci, DevBuf& nval);
+fq_status count_indefinite_cells(fq_ctx* ctx, const fq_mesh* m, int64_t* out);
 
 // ---- DevBuf -----------------------------------------------------------------
 DevBuf& DevBuf::operator=(DevBuf&& o) noexcept {
@@ -218,6 +219,11 @@ struct fq_mixed {
   // and rebuilt after a reassembly; hx_failed remembers an FQ_PC_AUTO fallback
   std::unique_ptr<HxPrecond> hx;
   bool hx_stale = true, hx_failed = false;
+  // the sparse direct route (Kuhn meshes): the LU carries the Lorentzian solve
+  // and finishes an unconverged MINRES (elliptic.rs:147-160); the analysis
+  // is kept while the pattern stays, the factors while the values stay
+  std::unique_ptr<SparseLu> lu;
+  int indefinite = -1;  // cells with an indefinite metric > 0: 1; none: 0; not yet counted: -1
   ~fq_mixed() {
     delete kkt;
     delete kkt32;
@@ -290,6 +296,8 @@ static fq_status mixed_assemble(fq_mixed* P) {
   fq_ctx* ctx = P->ctx;
   fq_mesh* m = P->mesh;
   P->hx_stale = true;
+  P->indefinite = -1;
+  if (P->lu) P->lu->factored = false;
   if (P->kkt) {
     FQ_TRY(assemble_into(ctx, P->kkt));
   } else {
@@ -394,18 +402,68 @@ static fq_status mixed_precond(fq_mixed* P, const fq_solve_opts* o, const HxPrec
   return FQ_OK;
 }
 
+// GMRES iterations the sparse LU may take when it finishes an unconverged
+// Krylov solve (whatever that solve's own cap was)
+static constexpr int64_t kLuFallbackIters = 300;
+
+// The whole KKT system by the sparse direct solver: GMRES in FP64 on the
+// system, preconditioned by its LU (FP32 factors first, FP64 when those do not
+// converge; report.refinements = 1 then). The factors stay for the next solve
+// on the same values.
+static fq_status mixed_direct(fq_mixed* P, const double* rhs, double* x, double rtol, int64_t max_iters,
+                              fq_report* rep) {
+  fq_ctx* ctx = P->ctx;
+  if (!P->lu || P->lu->n != P->n || P->lu->nnz != P->nnz) {
+    std::vector<int32_t> dofv;
+    FQ_TRY(layout_dof_vertices(ctx, P->mesh, EK_KKT, P->grade, P->bc, P->n, dofv));
+    auto lu = std::make_unique<SparseLu>();
+    FQ_TRY(sparse_lu_build(ctx, P->mesh, P->n, P->rp, P->ci, dofv, *lu));
+    P->lu = std::move(lu);
+  }
+  fq_report r{};
+  const fq_status s = sparse_lu_solve(ctx, *P->lu, P->rp, P->ci, P->val, rhs, x, rtol, max_iters, &r);
+  if (s != FQ_OK && s != FQ_NOT_CONVERGED) return s;
+  *rep = r;
+  return FQ_OK;
+}
+
+// The signature guard: whether a cell metric of the mesh is not positive
+// definite (then a block of the preconditioner is indefinite and the sparse
+// LU carries the solve, as FaerLu does in elliptic.rs:153-160).
+static fq_status mixed_indefinite(fq_mixed* P, bool* out) {
+  if (P->indefinite < 0) {
+    int64_t c = 0;
+    FQ_TRY(count_indefinite_cells(P->ctx, P->mesh, &c));
+    P->indefinite = c > 0 ? 1 : 0;
+  }
+  *out = P->indefinite == 1;
+  return FQ_OK;
+}
+
 static fq_status mixed_krylov(fq_mixed* P, const double* rhs, double* x, const fq_solve_opts* o, fq_report* rep) {
   fq_ctx* ctx = P->ctx;
   const int64_t n = P->n;
   rep->refinements = 0;
+  const bool kuhn = P->mesh->kuhn_nbox > 0;
+  if (o->preconditioner == FQ_PC_DIRECT && !kuhn)
+    return set_error(ctx, FQ_UNSUPPORTED, "the sparse direct solve needs a Kuhn cube mesh (fq_mesh_kuhn_cube)");
+  bool indefinite = false;
+  if (kuhn && o->preconditioner == FQ_PC_AUTO) FQ_TRY(mixed_indefinite(P, &indefinite));
+  if (kuhn && (o->preconditioner == FQ_PC_DIRECT || indefinite))
+    return mixed_direct(P, rhs, x, o->rtol, o->max_iters, rep);
   const HxPrecond* pc = nullptr;
   FQ_TRY(mixed_precond(P, o, &pc));
   if (P->precision != FQ_FP32 || !P->kkt32) {
     FQ_TRY(minres_run<double>(ctx, P->rp, P->ci, P->val, n, P->nnz, P->dinv.as<double>(), pc, rhs, x, o->rtol,
                               o->max_iters, rep));
-    // LU catches the rare non-convergence of the iterative path (elliptic.rs:147-159), here for
-    // systems small enough for a dense factorization
-    if (!rep->converged && ctx->dense_fallback && n <= kDenseMax && dense_fallback_available()) {
+    // LU catches the rare non-convergence of the iterative path (elliptic.rs:147-159): the
+    // sparse direct solver on Kuhn meshes (its GMRES is not held to the MINRES cap: FaerLu
+    // has none), a dense factorization for small other systems
+    if (!rep->converged && kuhn) {
+      const int64_t its = rep->iters;
+      FQ_TRY(mixed_direct(P, rhs, x, o->rtol, std::max<int64_t>(o->max_iters, kLuFallbackIters), rep));
+      rep->iters += its;
+    } else if (!rep->converged && ctx->dense_fallback && n <= kDenseMax && dense_fallback_available()) {
       FQ_TRY(dense_lu_solve(ctx, P->rp, P->ci, P->val, n, rhs, x));
       rep->converged = 1;
     }
@@ -439,7 +497,15 @@ static fq_status mixed_krylov(fq_mixed* P, const double* rhs, double* x, const f
   double rn = 0, bn = 0;
   FQ_TRY(residual64(ctx, P->rp, P->ci, P->val, n, x, rhs, r.as<double>(), &rn, &bn));
   rep->true_residual = bn > 0 ? rn / bn : 0.0;
-  if (P->precision == FQ_FP32) rep->converged = rep->true_residual <= o->refine_rtol;
+  if (P->precision == FQ_FP32) {
+    rep->converged = rep->true_residual <= o->refine_rtol;
+    // the refinement did not reach its tolerance: the sparse LU finishes it
+    if (!rep->converged && kuhn) {
+      const int64_t its = rep->iters;
+      FQ_TRY(mixed_direct(P, rhs, x, o->refine_rtol, std::max<int64_t>(o->max_iters, kLuFallbackIters), rep));
+      rep->iters += its;
+    }
+  }
   return FQ_OK;
 }
 
@@ -1385,7 +1451,7 @@ static fq_status massless_shift(fq_ctx* ctx, const fq_mesh* m, double* tau) {
 // factored matrix is the one with mass term tau (same sign as m), in FP64;
 // GMRES still runs on the system with mass term m.
 static fq_status dirac_direct(fq_ctx* ctx, fq_mesh* m, fq_matrix* sii, double mass_term, int64_t nrel,
-                              const double* rhs, double* x, const fq_solve_opts* o, fq_report* r) {
+                              const double* rhs, double* x, double rtol, int64_t max_iters, fq_report* r) {
   std::vector<int32_t> dofv;
   FQ_TRY(layout_dof_vertices(ctx, m, EK_DIRAC, 0, FQ_RELATIVE, nrel, dofv));
   const int32_t* rp = sii->rp;
@@ -1467,7 +1533,7 @@ static fq_status dirac_direct(fq_ctx* ctx, fq_mesh* m, fq_matrix* sii, double ma
   // the shifted matrix in FP64; the solve then runs GMRES on the system alone
   if (fval) FQ_TRY(sparse_lu_factor(ctx, lu, frp, fci, fval, FQ_FP64));
   const fq_status gs = sparse_lu_solve(ctx, lu, rp, ci, val, bordered ? bb.as<double>() : rhs,
-                                       bordered ? bx.as<double>() : x, o->rtol, o->max_iters, r);
+                                       bordered ? bx.as<double>() : x, rtol, max_iters, r);
   if (gs != FQ_OK && gs != FQ_NOT_CONVERGED) return gs;
   if (bordered) FQ_CUDA(ctx, cudaMemcpyAsync(x, bx.p, nrel * 8, cudaMemcpyDeviceToDevice, ctx->stream));
   return FQ_OK;
@@ -1546,7 +1612,7 @@ fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* m, double mass_term, const
   ctx->launches += 3;
   fq_report r{};
   if (direct) {
-    FQ_TRY(dirac_direct(ctx, m, sii, mass_term, nrel, rhs.as<double>(), x.as<double>(), o, &r));
+    FQ_TRY(dirac_direct(ctx, m, sii, mass_term, nrel, rhs.as<double>(), x.as<double>(), o->rtol, o->max_iters, &r));
   } else {
     vec_diag(sii, diag.as<double>(), st);
     vec_recip(diag.as<double>(), dinv.as<double>(), nullptr, nrel, 1, st);
@@ -1562,8 +1628,14 @@ fq_status fq_solve_dirac_source(fq_ctx* ctx, fq_mesh* m, double mass_term, const
     FQ_TRY(minres_run<double>(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, sii->nnz, pc_diag,
                               dp && dp->use_hx ? &dp->hx : nullptr, rhs.as<double>(), x.as<double>(), o->rtol,
                               o->max_iters, &r));
-    // the reference solves this system by LU: a small one MINRES left unconverged is finished that way
-    if (!r.converged && ctx->dense_fallback && nrel <= kDenseMax && dense_fallback_available()) {
+    // the reference solves this system by LU: one that MINRES left unconverged is finished
+    // that way, by the sparse direct route on Kuhn meshes, densely when small otherwise
+    if (!r.converged && kuhn) {
+      const int64_t its = r.iters;
+      FQ_TRY(dirac_direct(ctx, m, sii, mass_term, nrel, rhs.as<double>(), x.as<double>(), o->rtol,
+                          std::max<int64_t>(o->max_iters, kLuFallbackIters), &r));
+      r.iters += its;
+    } else if (!r.converged && ctx->dense_fallback && nrel <= kDenseMax && dense_fallback_available()) {
       FQ_TRY(dense_lu_solve(ctx, sii->rp, sii->ci, sii->values.as<double>(), nrel, rhs.as<double>(), x.as<double>()));
       r.converged = 1;
     }

@@ -1022,8 +1022,13 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
   const unsigned spmv_blocks = unsigned((n * 4 + 255) / 256);
   FQ_CUDA(ctx, cudaMemsetAsync(x, 0, size_t(n) * 8, st));
   double bnorm2 = 0.0, anorm2 = 0.0;
+  // the iterated matrix's own slot count: it may differ from the factored
+  // pattern's (a shifted matrix whose pattern holds more slots)
+  int32_t nnz_a = 0;
+  FQ_CUDA(ctx, cudaMemcpyAsync(&nnz_a, rp + n, 4, cudaMemcpyDeviceToHost, st));
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
   FQ_TRY(self_dot(ctx, g, n, b, &bnorm2));
-  FQ_TRY(self_dot(ctx, g, lu.nnz, val, &anorm2));
+  FQ_TRY(self_dot(ctx, g, nnz_a, val, &anorm2));
   const double bnorm = std::sqrt(bnorm2), anorm = std::sqrt(anorm2);
   fq_report r{};
   if (!(bnorm > 0.0)) {

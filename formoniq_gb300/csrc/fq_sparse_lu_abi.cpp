@@ -79,6 +79,14 @@ fq_status fq_sparse_lu_solve(fq_sparse_lu* s, const fq_matrix* a, const double* 
   fq_default_solve_opts(&d);
   if (!opts) opts = &d;
   FQ_GUARD_BEGIN
+  if (opts->max_refinements == 0) {
+    fq_report r{};
+    const fq_status st = sparse_lu_gmres(s->ctx, s->lu, a->rp, a->ci, a->values.as<double>(), b, x, opts->rtol,
+                                         opts->max_iters, &r);
+    r.refinements = 0;
+    if (rep) *rep = r;
+    return st;
+  }
   return sparse_lu_solve(s->ctx, s->lu, a->rp, a->ci, a->values.as<double>(), b, x, opts->rtol, opts->max_iters, rep);
   FQ_GUARD_END(s->ctx)
 }

@@ -150,4 +150,58 @@ fq_status border_csr(fq_ctx* ctx, const fq_matrix* a, const double* mh, int64_t 
   return FQ_OK;
 }
 
+// The signature guard of the mixed solve: the number of cells whose Regge
+// metric G_ij = (s_0i + s_0j - s_ij) / 2 (squared edge lengths s of the cell's
+// local edges) is not positive definite, by an FP64 Cholesky per cell. The
+// reference reads the same fact off the failing Cholesky of an indefinite
+// hdif_gram block (mixed_block_preconditioner, problems/elliptic.rs:25-47).
+__global__ void indefinite_cells_kernel(const double* lengths, const int32_t* cell_edges, int64_t nc, int n,
+                                        unsigned long long* count) {
+  unsigned long long local = 0;
+  const int ne = n * (n + 1) / 2;
+  GRID_STRIDE(c, nc) {
+    double s[10];
+    for (int e = 0; e < ne; ++e) s[e] = lengths[cell_edges[int64_t(e) * nc + c]];
+    auto ei = [](int a, int b) { return (b * (b - 1)) / 2 + a; };
+    double l[4][4] = {};
+    bool pd = true;
+    for (int j = 0; j < n && pd; ++j) {
+      for (int i = j; i < n; ++i) {
+        double g = i == j ? s[ei(0, j + 1)] : 0.5 * (s[ei(0, i + 1)] + s[ei(0, j + 1)] - s[ei(j + 1, i + 1)]);
+        for (int k = 0; k < j; ++k) g -= l[i][k] * l[j][k];
+        if (i == j) {
+          if (!(g > 0.0)) {
+            pd = false;
+            break;
+          }
+          l[j][j] = sqrt(g);
+        } else {
+          l[i][j] = g / l[j][j];
+        }
+      }
+    }
+    if (!pd) ++local;
+  }
+  if (local) atomicAdd(count, local);
+}
+
+fq_status count_indefinite_cells(fq_ctx* ctx, const fq_mesh* m, int64_t* out) {
+  *out = 0;
+  if (m->dim < 1 || m->ncells == 0) return FQ_OK;
+  if (!m->has_lengths) return set_error(ctx, FQ_INVALID_ARG, "mesh has no edge lengths");
+  DevBuf cnt;
+  FQ_TRY(cnt.alloc(ctx, 8));
+  FQ_CUDA(ctx, cudaMemsetAsync(cnt.p, 0, 8, ctx->stream));
+  indefinite_cells_kernel<<<g1(m->ncells), 256, 0, ctx->stream>>>(
+      m->lengths.as<double>(), m->cell_faces[1].as<int32_t>(), m->ncells, m->dim,
+      static_cast<unsigned long long*>(cnt.p));
+  ctx->launches++;
+  FQ_CUDA(ctx, cudaGetLastError());
+  unsigned long long h = 0;
+  FQ_CUDA(ctx, cudaMemcpyAsync(&h, cnt.p, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = int64_t(h);
+  return FQ_OK;
+}
+
 }  // namespace fq

@@ -74,8 +74,13 @@ typedef enum fq_precond {
   FQ_PC_HX = 2,     /* Hiptmair-Xu auxiliary-space blocks over a nodal multigrid V-cycle
                        (formoniq/src/hx.rs, multigrid.rs): Kuhn cube meshes with positive
                        squared lengths; FQ_UNSUPPORTED elsewhere */
-  FQ_PC_DIRECT = 3, /* Dirac solves: the sparse direct factorization (fq_sparse_lu_*) of the
-                       system preconditioning FP64 GMRES; Kuhn cube meshes */
+  FQ_PC_DIRECT = 3, /* Dirac and mixed solves: the sparse direct factorization
+                       (fq_sparse_lu_*) of the system preconditioning FP64 GMRES; Kuhn
+                       cube meshes. FQ_PC_AUTO takes it for a mixed solve on a mesh with a
+                       cell whose metric is not positive definite (Lorentzian: the
+                       reference's block preconditioner does not exist there and FaerLu
+                       carries the solve, elliptic.rs:153-160), and to finish a MINRES
+                       that did not converge (elliptic.rs:147-152) */
   FQ_PC_COMPARISON = 4 /* Dirac solves: MINRES preconditioned by the inverse diagonal of the
                        relative masses of the Euclidean comparison lattice; Kuhn cube meshes */
 } fq_precond;
@@ -284,7 +289,14 @@ fq_status fq_mixed_create(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, int p
 /* Re-assemble the KKT system after new lengths on the same mesh. */
 fq_status fq_mixed_reassemble(fq_mixed* prob);
 /* Solve with a host source GalerkinVector (ambient N_k doubles); outputs host
- * sigma (ambient N_{k-1}), u (ambient N_k), p (harmonic_dim); any may be NULL. */
+ * sigma (ambient N_{k-1}), u (ambient N_k), p (harmonic_dim); any may be NULL.
+ * Routes, as solve_source (elliptic.rs:140-160): block-preconditioned MINRES
+ * on Riemannian meshes; the sparse direct solver on Lorentzian Kuhn meshes (a
+ * cell metric not positive definite) or with FQ_PC_DIRECT; a MINRES (or FP32
+ * refinement) that does not converge is finished by the sparse direct solver
+ * on Kuhn meshes (its GMRES takes up to max(max_iters, 300) iterations; report
+ * iters count both, refinements is then the direct solve's: 1 = FP64 factors),
+ * by a dense LU on other meshes of at most 8192 unknowns. */
 fq_status fq_mixed_solve(fq_mixed* prob, const double* source_host, double* sigma_host, double* u_host,
                          double* p_host, const fq_solve_opts* opts, fq_report* report);
 /* Same on device pointers (source ambient N_k; outputs in the same layouts). */
@@ -381,13 +393,16 @@ fq_status fq_source_assemble(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, in
 
 /* Direct fallback: the reference finishes a MINRES that did not converge with a
  * sparse LU (problems/elliptic.rs:147-159) and solves the Dirac source problem by
- * LU. Here the mixed FP64 solve and the Dirac solve finish an unconverged MINRES
- * on a system of at most 8,192 unknowns by a dense LU with partial pivoting on
- * the device (cuSOLVER, loaded at run time); report.converged is then 1 with
- * report.iters the MINRES iterations spent, and report.true_residual that of the
- * direct solution. Larger systems keep the MINRES result (FQ_NOT_CONVERGED), and
- * so do the server's lanes (the factorization's synchronous allocations would
- * break the graph captures of the other lanes). */
+ * LU. Here the mixed solve and the Dirac solve finish an unconverged MINRES by
+ * the sparse direct solver (fq_sparse_lu_*, GMRES on its factors) on Kuhn cube
+ * meshes, at any size and in the server's lanes too (its allocations are
+ * stream-ordered). On other meshes, a system of at most 8,192 unknowns is
+ * finished by a dense LU with partial pivoting on the device (cuSOLVER, loaded
+ * at run time): report.converged is then 1 with report.iters the MINRES
+ * iterations spent, and report.true_residual that of the direct solution.
+ * Larger systems on such meshes keep the MINRES result (FQ_NOT_CONVERGED), and
+ * so do the server's lanes there (the dense factorization's synchronous
+ * allocations would break the graph captures of the other lanes). */
 
 /* ---- the covariant Hodge-Dirac source problem ---------------------------- */
 /* dirac::solve_dirac_source (problems/dirac.rs:473-531): S = A + m M of
@@ -440,7 +455,9 @@ fq_status fq_sparse_lu_factor(fq_sparse_lu* lu, const fq_matrix* a, int precisio
  * factors GMRES runs for at most 60 iterations; if it has not converged by
  * then, `a` is re-factored in FP64 (the factorization keeps FP64 afterwards,
  * until the next fq_sparse_lu_factor) and GMRES starts again from zero: then
- * report.refinements = 1. report.iters counts both. */
+ * report.refinements = 1. report.iters counts both. opts->max_refinements = 0
+ * keeps the current factors whatever their type: GMRES runs on them for up to
+ * opts->max_iters iterations and no FP64 factorization happens. */
 fq_status fq_sparse_lu_solve(fq_sparse_lu* lu, const fq_matrix* a, const double* b_dev, double* x_dev,
                              const fq_solve_opts* opts, fq_report* report);
 /* Fronts, levels, factorization flops, bytes of the current factors, pivots

@@ -535,36 +535,42 @@ def test_scatter_bytes_accounting(oracle, ctx):
     mesh.close()
 
 
+@pytest.mark.parametrize("kuhn", [True, False])
 @pytest.mark.parametrize("which", ["dirac", "mixed"])
-def test_dense_lu_finishes_an_unconverged_minres(oracle, ctx, which):
-    """The reference's LU fallback: a MINRES stopped after a few iterations on a
-    small system is finished by the dense direct solve."""
+def test_lu_finishes_an_unconverged_minres(oracle, ctx, which, kuhn):
+    """The reference's LU fallback (elliptic.rs:147-160): a MINRES stopped
+    after a few iterations is finished by a direct solve, the sparse LU
+    (GMRES on its factors) on a Kuhn cube mesh, the dense LU on a small mesh
+    given by its cells."""
+    def make_mesh(dim, nb, lengths):
+        m = fq.Mesh.kuhn_cube(ctx, dim, nb) if kuhn else fq.Mesh.from_cells(ctx, oracle.kuhn_cells(dim, nb))
+        m.set_lengths_sq(lengths)
+        return m
+
     if which == "dirac":
         cx, coords, signs = oracle.minkowski(3, 3)
         lengths = cx.edge_lengths_sq(coords, signs)
-        mesh = fq.Mesh.kuhn_cube(ctx, 3, 3)
-        mesh.set_lengths_sq(lengths)
+        mesh = make_mesh(3, 3, lengths)
         ntot = sum(cx.nsimplices(k) for k in range(4))
         load = np.random.default_rng(8).standard_normal(ntot)
         x_o = oracle.dirac_solve_source(cx, lengths, 1.5, load, np.zeros(ntot))
         x, rep = fq.solve_dirac_source(mesh, 1.5, load, None, fq.SolveOpts.default(rtol=1e-12, max_iters=5,
                                                                                    preconditioner=fq.FQ_PC_JACOBI))
-        assert rep.converged and rep.iters <= 6, rep
+        assert rep.converged and rep.iters <= (5 + 60 if kuhn else 6), rep
         assert np.linalg.norm(x - x_o) / np.linalg.norm(x_o) < 1e-9
         assert rep.true_residual < 1e-11
     else:
         cx, coords = oracle.cartesian_unit(2, 6)
         coords = oracle.jitter_coords(coords, 6, seed=2, amplitude=0.1)
         lengths = cx.edge_lengths_sq(coords)
-        mesh = fq.Mesh.kuhn_cube(ctx, 2, 6)
-        mesh.set_lengths_sq(lengths)
+        mesh = make_mesh(2, 6, lengths)
         owc = oracle.WhitneyComplex(cx, lengths)
         src = np.random.default_rng(3).standard_normal(cx.nsimplices(1))
         a, rhs, ns, nu = oracle.assemble_mixed_kkt(owc, src, 1, oracle.harmonics(owc, 1))
         x_o = oracle.direct_solve(a, rhs)
         sigma, u, p, rep = fq.solve_source(fq.WhitneyComplex(mesh), src, 1,
                                            fq.SolveOpts.default(rtol=1e-12, max_iters=3))
-        assert rep.converged and rep.iters <= 4, rep
+        assert rep.converged and rep.iters <= (3 + 60 if kuhn else 4), rep
         x = np.concatenate([sigma, u])
         assert np.linalg.norm(x - x_o[:ns + nu]) / np.linalg.norm(x_o) < 1e-9
     mesh.close()

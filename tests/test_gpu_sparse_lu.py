@@ -143,6 +143,11 @@ def test_sparse_lu_api_against_superlu(oracle, ctx, which):
     A2 = a.to_scipy()
     x, rep = lu.solve(b, fq.SolveOpts.default(rtol=1e-12, max_iters=300))
     assert rep.converged and rel(x, spla.spsolve(A2.tocsc(), b)) < SOLVE_TOL
+    # max_refinements = 0: GMRES on the FP32 factors only, no FP64 refactorization
+    lu.factor(fq.FQ_FP32)
+    x, rep = lu.solve(b, fq.SolveOpts.default(rtol=1e-12, max_iters=300, max_refinements=0))
+    assert rep.converged and rep.refinements == 0, rep
+    assert rel(x, spla.spsolve(A2.tocsc(), b)) < SOLVE_TOL
     lu.close()
 
 
@@ -154,3 +159,25 @@ def test_sparse_lu_rejects_non_lattice_meshes(oracle, ctx):
     with pytest.raises(fq.FqError) as e:
         fq.SparseLu(mesh, a)
     assert e.value.name == "FQ_UNSUPPORTED"
+
+
+@pytest.mark.parametrize("dim,nb,k,relative", [(3, 4, 1, False), (2, 8, 1, True), (3, 3, 2, False), (2, 6, 0, False)])
+def test_lorentzian_mixed_solve_by_sparse_lu(oracle, ctx, dim, nb, k, relative):
+    """solve_source on a Minkowski mesh: the hdif_gram blocks are indefinite,
+    so no block preconditioner exists and LU carries the solve
+    (elliptic.rs:153-160); the device counts the cells whose metric is not
+    positive definite and takes the sparse direct route."""
+    cx, lengths, mesh = lattice_mesh(oracle, ctx, dim, nb, True)
+    owc = oracle.WhitneyComplex(cx, lengths, relative=relative)
+    src = np.random.default_rng(21).standard_normal(cx.nsimplices(k))
+    harm = oracle.harmonics(owc, k)
+    a, rhs, ns, nu = oracle.assemble_mixed_kkt(owc, src, k, harm)
+    x_o = oracle.direct_solve(a, rhs)
+    want = np.concatenate(([owc.inclusion(k - 1) @ x_o[:ns]] if k > 0 else []) + [owc.inclusion(k) @ x_o[ns:ns + nu]])
+    gwc = fq.WhitneyComplex(mesh, relative=relative)
+    sigma, u, _, rep = fq.solve_source(gwc, src, k, fq.SolveOpts.default(rtol=1e-12, max_iters=300))
+    assert rep.converged, rep
+    assert rep.iters <= 60, rep
+    got = np.concatenate(([sigma] if k > 0 else []) + [u])
+    assert rel(got, want) < SOLVE_TOL
+    mesh.close()
