@@ -22,7 +22,6 @@ struct SlCfg<float> {
   static constexpr int ROWS = 256;    // rows of a tournament leaf or merge
   static constexpr int BM = 128;      // product tile (BM x BM outputs per CTA)
   static constexpr int TM = 8;        // outputs per thread and dimension
-  static constexpr int MAXM = 46000;  // front rows a solve CTA holds in shared memory
 };
 template <>
 struct SlCfg<double> {
@@ -30,12 +29,12 @@ struct SlCfg<double> {
   static constexpr int ROWS = 128;
   static constexpr int BM = 64;
   static constexpr int TM = 4;
-  static constexpr int MAXM = 26000;
 };
 static_assert(SlCfg<float>::TILE <= kTile && SlCfg<double>::TILE <= kTile, "tile store sized for kTile");
 
 constexpr int kBK = 32;  // K chunk of the products
 constexpr int kThreads = 256;
+constexpr int kMaxComposeRows = 46000;  // fully summed rows whose interchanges one CTA composes in shared memory
 
 // ---------------------------------------------------------------------------
 // assembly
@@ -519,35 +518,56 @@ __global__ void __launch_bounds__(kThreads) sl_gemm_kernel(const FrontDesc* __re
 // ---------------------------------------------------------------------------
 // solves: one CTA per front, the front's right-hand side in shared memory
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(kThreads) sl_forward_kernel(const FrontDesc* __restrict__ fd,
-                                                              const int32_t* __restrict__ list,
-                                                              const T* __restrict__ pool,
-                                                              const T* __restrict__ tiles,
-                                                              const int32_t* __restrict__ piv,
-                                                              const int32_t* __restrict__ ea, T* __restrict__ work,
-                                                              T* __restrict__ uvec) {
-  using C = SlCfg<T>;
-  constexpr int TL = C::TILE;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  T* r = reinterpret_cast<T*>(smraw);
-  __shared__ T y[TL];
-  const FrontDesc F = fd[list[blockIdx.x]];
-  const int m = F.m, f = F.f, tid = threadIdx.x, nt = blockDim.x;
-  for (int i = tid; i < m; i += nt) r[i] = i < f ? work[F.start + i] : T(0);
-  __syncthreads();
-  for (int which = 0; which < 2; ++which) {
-    const int c = which == 0 ? F.child0 : F.child1;
-    if (c < 0) continue;
-    const FrontDesc Cd = fd[c];
-    const int u = Cd.m - Cd.f;
-    for (int t = tid; t < u; t += nt) r[ea[Cd.ea_off + t]] += uvec[Cd.uvec_off + t];
-    __syncthreads();
+// ---------------------------------------------------------------------------
+// solve: one CTA per row block (the rows of one tile) of every front of a
+// level. Tile solutions are published through per-tile flags: the producer
+// writes its rows, fences, and stores the phase's target value; a consumer
+// acquires the flag before it reads them (L2, not L1). CTAs take their row
+// blocks by ticket, in list order, and a block waits only for blocks earlier
+// in the list, which already hold a CTA: every wait ends. A wait is bounded
+// all the same; one that runs out sets the solve status and goes on.
+// ---------------------------------------------------------------------------
+constexpr int kSolveThreads = 128;  // four warps; a lane holds TILE / 32 rows of the block
+constexpr int kWaitPolls = 1 << 20;  // about a second of polling
+
+__device__ __forceinline__ int load_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void store_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// thread 0 waits for the flag, then the block goes on
+// (once any wait has run out, the others give up at once: the solve is void)
+__device__ void wait_tile(const int* flag, int target, int* status) {
+  if (threadIdx.x == 0) {
+    bool ok = false;
+    for (int it = 0; it < kWaitPolls && !ok; ++it) {
+      ok = load_acquire(flag) == target;
+      if (!ok) {
+        if (load_acquire(status) != 0) break;
+        __nanosleep(64);
+      }
+    }
+    if (!ok) atomicOr(status, 1);
   }
-  // the front's row interchanges, in the order the factorization made them
-  // (their targets staged through shared memory a chunk at a time, so that the
-  // one thread applying them does not wait on a global load per interchange)
+  __syncthreads();
+}
+
+// The composed row interchanges of every front: the swaps p <-> piv[p], in
+// order of p, applied to the identity; fperm[start + i] names the front-local
+// row whose value ends at position i.
+__global__ void sl_compose_pivots_kernel(const FrontDesc* __restrict__ fd, const int32_t* __restrict__ piv,
+                                         int32_t* __restrict__ fperm) {
+  extern __shared__ int a[];
   __shared__ int pv[1024];
+  const FrontDesc F = fd[blockIdx.x];
+  const int f = F.f, tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < f; i += nt) a[i] = i;
+  __syncthreads();
   for (int p0 = 0; p0 < f; p0 += 1024) {
     const int np = min(1024, f - p0);
     for (int t = tid; t < np; t += nt) pv[t] = piv[F.start + p0 + t];
@@ -555,87 +575,189 @@ __global__ void __launch_bounds__(kThreads) sl_forward_kernel(const FrontDesc* _
     if (tid == 0)
       for (int q = 0; q < np; ++q) {
         const int p = p0 + q, t = pv[q];
-        if (t != p) {
-          const T a = r[p];
-          r[p] = r[t];
-          r[t] = a;
+        if (t != p && t >= 0 && t < f) {
+          const int v = a[p];
+          a[p] = a[t];
+          a[t] = v;
         }
       }
     __syncthreads();
   }
-  const T* P = pool + F.off;
-  for (int k = 0; k < f; k += TL) {
-    const int b = min(TL, f - k);
-    const T* iL = tiles + F.tile_off + int64_t(k / TL) * 2 * TL * TL;
-    if (tid < b) {
-      T s = T(0);
-      for (int l = 0; l <= tid; ++l) s += iL[l * TL + tid] * r[k + l];
-      y[tid] = s;
-    }
-    __syncthreads();
-    if (tid < b) r[k + tid] = y[tid];
-    for (int i = k + b + tid; i < m; i += nt) {
-      T s = T(0);
-      for (int l = 0; l < b; ++l) s += P[int64_t(k + l) * m + i] * y[l];
-      r[i] -= s;
-    }
-    __syncthreads();
-  }
-  for (int i = tid; i < m; i += nt) {
-    if (i < f)
-      work[F.start + i] = r[i];
-    else
-      uvec[F.uvec_off + (i - f)] = r[i];
-  }
+  for (int i = tid; i < f; i += nt) fperm[F.start + i] = a[i];
 }
 
+// Forward: row block w.y of front w.x. A block of the fully summed rows
+// (w.y < its tile count) takes rows of tile w.y and publishes that tile's y;
+// a later block takes update rows and writes the front's update vector.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) sl_backward_kernel(const FrontDesc* __restrict__ fd,
-                                                               const int32_t* __restrict__ list,
-                                                               const T* __restrict__ pool,
-                                                               const T* __restrict__ tiles,
-                                                               const int32_t* __restrict__ urows,
-                                                               T* __restrict__ work) {
+__global__ void __launch_bounds__(kSolveThreads) sl_forward_rows_kernel(
+    const int2* __restrict__ items, int nitems, int* __restrict__ ticket, const FrontDesc* __restrict__ fd,
+    const T* __restrict__ pool, const T* __restrict__ tiles, const int32_t* __restrict__ fperm,
+    const int32_t* __restrict__ rinv, const T* __restrict__ work, T* ybuf, T* uvec, int* flags, int target,
+    int* status) {
   using C = SlCfg<T>;
   constexpr int TL = C::TILE;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  T* x = reinterpret_cast<T*>(smraw);
-  __shared__ T z[TL];
-  __shared__ T part[kThreads / 32][TL];
-  const FrontDesc F = fd[list[blockIdx.x]];
-  const int m = F.m, f = F.f, tid = threadIdx.x, nt = blockDim.x;
-  for (int i = tid; i < m; i += nt) x[i] = i < f ? work[F.start + i] : work[urows[F.ea_off + (i - f)]];
+  constexpr int R = TL / 32;
+  __shared__ int s_item;
+  __shared__ T sy[TL];
+  __shared__ T part[kSolveThreads / 32][TL];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NW = kSolveThreads / 32;
+  if (tid == 0) s_item = atomicAdd(ticket, 1);
   __syncthreads();
+  const int it = s_item;
+  if (it >= nitems) return;
+  const int2 w = items[it];
+  const FrontDesc F = fd[w.x];
+  const int m = F.m, f = F.f, nF = (f + TL - 1) / TL;
+  const bool diag = w.y < nF;
+  const int r0 = diag ? w.y * TL : f + (w.y - nF) * TL;
+  const int nr = diag ? min(TL, f - r0) : min(TL, m - r0);
+  const int jmax = diag ? w.y : nF;
+  const int64_t ftile = F.tile_off / (2 * TL * TL);
   const T* P = pool + F.off;
-  const int ntiles = (f + TL - 1) / TL;
-  const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
-  for (int t = ntiles - 1; t >= 0; --t) {
-    const int k = t * TL, b = min(TL, f - k);
-    // z = y_t - U[t rows, columns after the tile] x: warps split the columns,
-    // lanes the tile rows
-    for (int i0 = 0; i0 < b; i0 += 32) {
-      const int i = i0 + lane;
-      T s = T(0);
-      if (i < b)
-        for (int c = k + b + warp; c < m; c += nw) s += P[int64_t(c) * m + k + i] * x[c];
-      if (i < TL) part[warp][i] = s;
-    }
+  T acc[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) acc[q] = T(0);
+  for (int j = 0; j < jmax; ++j) {
+    wait_tile(flags + ftile + j, target, status);
+    const int k = j * TL, b = min(TL, f - k);
+    if (tid < b) sy[tid] = __ldcg(ybuf + F.start + k + tid);
     __syncthreads();
-    if (tid < b) {
-      T s = x[k + tid];
-      for (int w = 0; w < nw; ++w) s -= part[w][tid];
-      z[tid] = s;
-    }
-    __syncthreads();
-    const T* iU = tiles + F.tile_off + int64_t(t) * 2 * TL * TL + TL * TL;
-    if (tid < b) {
-      T s = T(0);
-      for (int l = tid; l < b; ++l) s += iU[l * TL + tid] * z[l];
-      x[k + tid] = s;
+#pragma unroll 4
+    for (int l = warp; l < b; l += NW) {
+      const T yl = sy[l];
+      const T* col = P + int64_t(k + l) * m + r0;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        const int i = lane + 32 * q;
+        if (i < nr) acc[q] += col[i] * yl;
+      }
     }
     __syncthreads();
   }
-  for (int i = tid; i < f; i += nt) work[F.start + i] = x[i];
+#pragma unroll
+  for (int q = 0; q < R; ++q) part[warp][lane + 32 * q] = acc[q];
+  __syncthreads();
+  // the assembled, interchanged right-hand side of the block's rows, less the panel sums
+  if (tid < nr) {
+    const int row = r0 + tid;
+    const int src = row < f ? fperm[F.start + row] : row;
+    T v = src < f ? work[F.start + src] : T(0);
+    if (F.child0 >= 0) {
+      const int32_t q = rinv[2 * (F.roff + src)];
+      if (q >= 0) v += uvec[fd[F.child0].uvec_off + q];
+    }
+    if (F.child1 >= 0) {
+      const int32_t q = rinv[2 * (F.roff + src) + 1];
+      if (q >= 0) v += uvec[fd[F.child1].uvec_off + q];
+    }
+    T sum = T(0);
+#pragma unroll
+    for (int ww = 0; ww < NW; ++ww) sum += part[ww][tid];
+    v -= sum;
+    if (diag)
+      sy[tid] = v;
+    else
+      uvec[F.uvec_off + (row - f)] = v;
+  }
+  if (!diag) return;
+  __syncthreads();
+  // y = L_tt^-1 v, L_tt^-1 from the tile store (column-major, stride TL)
+  const T* iL = tiles + F.tile_off + int64_t(w.y) * 2 * TL * TL;
+  if (tid < nr) {
+    T y = T(0);
+    for (int l = 0; l <= tid; ++l) y += iL[l * TL + tid] * sy[l];
+    ybuf[F.start + r0 + tid] = y;
+    __threadfence();
+  }
+  __syncthreads();
+  if (tid == 0) store_release(flags + ftile + w.y, target);
+}
+
+// Backward: tile w.y of front w.x (the list takes a front's tiles last to
+// first). x_t = U_tt^-1 (y_t - U_t,later x_later - U_t,update x_update); the
+// update unknowns' x come from the ancestors, solved in earlier launches.
+template <typename T>
+__global__ void __launch_bounds__(kSolveThreads) sl_backward_rows_kernel(
+    const int2* __restrict__ items, int nitems, int* __restrict__ ticket, const FrontDesc* __restrict__ fd,
+    const T* __restrict__ pool, const T* __restrict__ tiles, const int32_t* __restrict__ urows,
+    const T* __restrict__ ybuf, T* work, int* flags, int target, int* status) {
+  using C = SlCfg<T>;
+  constexpr int TL = C::TILE;
+  constexpr int R = TL / 32;
+  constexpr int NW = kSolveThreads / 32;
+  __shared__ int s_item;
+  __shared__ T sx[TL];
+  __shared__ T part[NW][TL];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_item = atomicAdd(ticket, 1);
+  __syncthreads();
+  const int it = s_item;
+  if (it >= nitems) return;
+  const int2 w = items[it];
+  const FrontDesc F = fd[w.x];
+  const int m = F.m, f = F.f, nF = (f + TL - 1) / TL;
+  const int t = w.y, r0 = t * TL, nr = min(TL, f - r0);
+  const int64_t ftile = F.tile_off / (2 * TL * TL);
+  const T* P = pool + F.off;
+  T acc[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) acc[q] = T(0);
+  // the update columns, known before the level starts
+  for (int c0 = f; c0 < m; c0 += TL) {
+    const int b = min(TL, m - c0);
+    if (tid < b) sx[tid] = work[urows[F.ea_off + (c0 - f) + tid]];
+    __syncthreads();
+#pragma unroll 4
+    for (int l = warp; l < b; l += NW) {
+      const T xl = sx[l];
+      const T* col = P + int64_t(c0 + l) * m + r0;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        const int i = lane + 32 * q;
+        if (i < nr) acc[q] += col[i] * xl;
+      }
+    }
+    __syncthreads();
+  }
+  // the later tiles of the front, as they are published
+  for (int j = nF - 1; j > t; --j) {
+    wait_tile(flags + ftile + j, target, status);
+    const int k = j * TL, b = min(TL, f - k);
+    if (tid < b) sx[tid] = __ldcg(work + F.start + k + tid);
+    __syncthreads();
+#pragma unroll 4
+    for (int l = warp; l < b; l += NW) {
+      const T xl = sx[l];
+      const T* col = P + int64_t(k + l) * m + r0;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        const int i = lane + 32 * q;
+        if (i < nr) acc[q] += col[i] * xl;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q) part[warp][lane + 32 * q] = acc[q];
+  __syncthreads();
+  if (tid < nr) {
+    T z = ybuf[F.start + r0 + tid];
+#pragma unroll
+    for (int ww = 0; ww < NW; ++ww) z -= part[ww][tid];
+    sx[tid] = z;
+  }
+  __syncthreads();
+  const T* iU = tiles + F.tile_off + int64_t(t) * 2 * TL * TL + TL * TL;
+  if (tid < nr) {
+    T x = T(0);
+    for (int l = tid; l < nr; ++l) x += iU[l * TL + tid] * sx[l];
+    work[F.start + r0 + tid] = x;
+    __threadfence();
+  }
+  __syncthreads();
+  if (tid == 0) store_release(flags + ftile + t, target);
 }
 
 // (D A D)^-1 = D^-1 A^-1 D^-1, so A^-1 r = D (D A D)^-1 D r
@@ -751,12 +873,11 @@ fq_status set_attributes(fq_ctx* ctx) {
   using C = SlCfg<T>;
   const int tile_smem = 2 * C::TILE * (C::TILE + 1) * int(sizeof(T));
   const int blk_smem = C::TILE * (C::ROWS + 1) * int(sizeof(T));
-  const int solve_smem = C::MAXM * int(sizeof(T));
   FQ_CUDA(ctx, cudaFuncSetAttribute(sl_tile_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem));
   FQ_CUDA(ctx, cudaFuncSetAttribute(sl_tourn_leaf_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, blk_smem));
   FQ_CUDA(ctx, cudaFuncSetAttribute(sl_tourn_merge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, blk_smem));
-  FQ_CUDA(ctx, cudaFuncSetAttribute(sl_forward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, solve_smem));
-  FQ_CUDA(ctx, cudaFuncSetAttribute(sl_backward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, solve_smem));
+  FQ_CUDA(ctx, cudaFuncSetAttribute(sl_compose_pivots_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kMaxComposeRows * 4));
   return FQ_OK;
 }
 
@@ -764,10 +885,10 @@ template <typename T>
 fq_status factor_impl(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_t* ci, const double* val) {
   using C = SlCfg<T>;
   cudaStream_t st = ctx->stream;
-  int64_t maxm_all = 0;
-  for (int x = 0; x < lu.nfronts; ++x) maxm_all = std::max<int64_t>(maxm_all, lu.front_m[x]);
-  if (maxm_all > C::MAXM)
-    return set_error(ctx, FQ_UNSUPPORTED, "sparse LU: a front too large for this precision's solve");
+  int64_t maxf_all = 0;
+  for (int x = 0; x < lu.nfronts; ++x) maxf_all = std::max<int64_t>(maxf_all, lu.front_f[x]);
+  if (maxf_all > kMaxComposeRows)
+    return set_error(ctx, FQ_UNSUPPORTED, "sparse LU: a front with more fully summed rows than the solve holds");
   const int prec = sizeof(T) == 4 ? FQ_FP32 : FQ_FP64;
   if (lu.precision != prec) {
     lu.pool.release();
@@ -785,6 +906,15 @@ fq_status factor_impl(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_
   const int64_t half_sets = std::max<int64_t>(lu.tourn_sets, 1) * 2;  // FP64 leaves are half as tall
   if (!lu.piv.p) {
     FQ_TRY(lu.piv.alloc(ctx, size_t(std::max<int64_t>(lu.n, 1)) * 4));
+    FQ_TRY(lu.fperm.alloc(ctx, size_t(std::max<int64_t>(lu.n, 1)) * 4));
+    FQ_TRY(lu.ybuf.alloc(ctx, size_t(std::max<int64_t>(lu.n, 1)) * 8));
+    // one flag per tile of the narrowest tiles (FP64), zero: no phase published
+    const size_t nflags = size_t(lu.tile_elems / (2 * SlCfg<double>::TILE * SlCfg<double>::TILE) + 1);
+    FQ_TRY(lu.flags.alloc(ctx, nflags * 4));
+    FQ_CUDA(ctx, cudaMemsetAsync(lu.flags.p, 0, nflags * 4, st));
+    FQ_TRY(lu.tickets.alloc(ctx, size_t(2 * std::max(lu.nlevels, 1)) * 4));
+    FQ_TRY(lu.solve_status.alloc(ctx, 4));
+    FQ_CUDA(ctx, cudaMemsetAsync(lu.solve_status.p, 0, 4, st));
     FQ_TRY(lu.status.alloc(ctx, 4 * sizeof(int)));
     FQ_TRY(lu.scale.alloc(ctx, size_t(std::max<int64_t>(lu.n, 1)) * 8));
     FQ_TRY(lu.tourn_cand.alloc(ctx, size_t(half_sets) * 2 * kTile * 4));
@@ -885,6 +1015,10 @@ fq_status factor_impl(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_
       }
     }
   }
+  // the composed interchanges of every front, for the solve
+  sl_compose_pivots_kernel<<<unsigned(lu.nfronts), 256, size_t(maxf_all) * 4, st>>>(fd, lu.piv.as<int32_t>(),
+                                                                                   lu.fperm.as<int32_t>());
+  ctx->launches++;
   FQ_CUDA(ctx, cudaGetLastError());
   int hs[4] = {0, 0, 0, 0};
   FQ_CUDA(ctx, cudaMemcpyAsync(hs, lu.status.p, sizeof hs, cudaMemcpyDeviceToHost, st));
@@ -907,34 +1041,75 @@ fq_status factor_impl(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_
   return FQ_OK;
 }
 
+// The solve's row blocks, level by level, for tiles of width tl: forward, every
+// front's fully summed tiles in order, then its update rows; backward, its
+// tiles last to first.
+fq_status make_items(fq_ctx* ctx, SparseLu& lu, int tl) {
+  std::vector<int2> fw, bw;
+  lu.fwd_ptr.assign(size_t(lu.nlevels) + 1, 0);
+  lu.bwd_ptr.assign(size_t(lu.nlevels) + 1, 0);
+  for (int l = 0; l < lu.nlevels; ++l) {
+    for (int32_t q = lu.level_ptr[l]; q < lu.level_ptr[l + 1]; ++q) {
+      const int x = lu.level_fronts[q];
+      const int f = lu.front_f[x], u = lu.front_m[x] - f;
+      const int nF = (f + tl - 1) / tl, nU = (u + tl - 1) / tl;
+      for (int b = 0; b < nF + nU; ++b) fw.push_back(make_int2(x, b));
+      for (int b = nF - 1; b >= 0; --b) bw.push_back(make_int2(x, b));
+    }
+    lu.fwd_ptr[l + 1] = int64_t(fw.size());
+    lu.bwd_ptr[l + 1] = int64_t(bw.size());
+  }
+  for (int l = 0; l < lu.nlevels; ++l)
+    if (lu.fwd_ptr[l + 1] - lu.fwd_ptr[l] > 0x7fffffff)
+      return set_error(ctx, FQ_UNSUPPORTED, "sparse LU: a level with more row blocks than one launch takes");
+  FQ_TRY(lu.fwd_items.alloc(ctx, std::max<size_t>(fw.size(), 1) * sizeof(int2)));
+  FQ_TRY(lu.bwd_items.alloc(ctx, std::max<size_t>(bw.size(), 1) * sizeof(int2)));
+  if (!fw.empty())
+    FQ_CUDA(ctx, cudaMemcpyAsync(lu.fwd_items.p, fw.data(), fw.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  if (!bw.empty())
+    FQ_CUDA(ctx, cudaMemcpyAsync(lu.bwd_items.p, bw.data(), bw.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the host lists go out of scope
+  return FQ_OK;
+}
+
 template <typename T>
 fq_status apply_impl(fq_ctx* ctx, SparseLu& lu, const double* r, double* z) {
+  using C = SlCfg<T>;
   cudaStream_t st = ctx->stream;
+  if (lu.items_precision != lu.precision) {
+    FQ_TRY(make_items(ctx, lu, C::TILE));
+    lu.items_precision = lu.precision;
+  }
   const FrontDesc* fd = lu.fronts.as<FrontDesc>();
-  const int32_t* lists = lu.level_list.as<int32_t>();
   T* work = lu.work.as<T>();
+  T* ybuf = lu.ybuf.as<T>();
+  int* tickets = lu.tickets.as<int>();
+  int* flags = lu.flags.as<int>();
+  int* status = lu.solve_status.as<int>();
+  ++lu.epoch;
+  const int fwd_target = int(2u * lu.epoch + 1u), bwd_target = int(2u * lu.epoch + 2u);
+  FQ_CUDA(ctx, cudaMemsetAsync(tickets, 0, size_t(2 * std::max(lu.nlevels, 1)) * 4, st));
   sl_permute_in_kernel<T><<<grid_of(lu.n, 256), 256, 0, st>>>(r, lu.perm.as<int32_t>(), lu.scale.as<double>(), lu.n,
                                                               work);
   ctx->launches++;
+  const int2* fwi = lu.fwd_items.as<int2>();
+  const int2* bwi = lu.bwd_items.as<int2>();
   for (int l = 0; l < lu.nlevels; ++l) {
-    const int32_t q0 = lu.level_ptr[l], q1 = lu.level_ptr[l + 1];
-    if (q1 <= q0) continue;
-    int64_t maxm = 0;
-    for (int32_t q = q0; q < q1; ++q) maxm = std::max<int64_t>(maxm, lu.front_m[lu.level_fronts[q]]);
-    const size_t smem = size_t(std::max<int64_t>(maxm, 1)) * sizeof(T);
-    sl_forward_kernel<T><<<unsigned(q1 - q0), kThreads, smem, st>>>(fd, lists + q0, lu.pool.as<T>(), lu.tiles.as<T>(),
-                                                                    lu.piv.as<int32_t>(), lu.ea_map.as<int32_t>(), work,
-                                                                    lu.uvec.as<T>());
+    const int64_t b = lu.fwd_ptr[l], e = lu.fwd_ptr[l + 1];
+    if (e <= b) continue;
+    sl_forward_rows_kernel<T><<<unsigned(e - b), kSolveThreads, 0, st>>>(
+        fwi + b, int(e - b), tickets + l, fd, lu.pool.as<T>(), lu.tiles.as<T>(), lu.fperm.as<int32_t>(),
+        lu.rinv.as<int32_t>(), work, ybuf, lu.uvec.as<T>(), flags, fwd_target, status);
     ctx->launches++;
   }
   for (int l = lu.nlevels - 1; l >= 0; --l) {
-    const int32_t q0 = lu.level_ptr[l], q1 = lu.level_ptr[l + 1];
-    if (q1 <= q0) continue;
-    int64_t maxm = 0;
-    for (int32_t q = q0; q < q1; ++q) maxm = std::max<int64_t>(maxm, lu.front_m[lu.level_fronts[q]]);
-    const size_t smem = size_t(std::max<int64_t>(maxm, 1)) * sizeof(T);
-    sl_backward_kernel<T><<<unsigned(q1 - q0), kThreads, smem, st>>>(fd, lists + q0, lu.pool.as<T>(), lu.tiles.as<T>(),
-                                                                     lu.urows.as<int32_t>(), work);
+    const int64_t b = lu.bwd_ptr[l], e = lu.bwd_ptr[l + 1];
+    if (e <= b) continue;
+    sl_backward_rows_kernel<T><<<unsigned(e - b), kSolveThreads, 0, st>>>(
+        bwi + b, int(e - b), tickets + lu.nlevels + l, fd, lu.pool.as<T>(), lu.tiles.as<T>(),
+        lu.urows.as<int32_t>(), ybuf, work, flags, bwd_target, status);
     ctx->launches++;
   }
   sl_permute_out_kernel<T><<<grid_of(lu.n, 256), 256, 0, st>>>(work, lu.perm.as<int32_t>(), lu.scale.as<double>(),
@@ -1039,6 +1214,7 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
   int64_t it = 0;
   double relres = 1.0;
   bool done = false;
+  const int stale_limit = lu.precision == FQ_FP32 ? 3 : 5;
   std::vector<double> h, h2;
   while (!done && it < max_iters) {
     // r = b - A x into V[0]; the true residual and the backward error of x
@@ -1094,12 +1270,13 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
       gv[j + 1] = -sn[j] * gv[j];
       gv[j] = cs[j] * gv[j];
       relres = std::fabs(gv[j + 1]) / bnorm;
-      // stagnation: five iterations without halving the residual estimate end
-      // the cycle early (the true residual then decides)
+      // stagnation: five iterations without halving the residual estimate (three
+      // on FP32 factors, which then give way to FP64 ones) end the cycle early
+      // (the true residual then decides)
       if (relres < 0.5 * best) {
         best = relres;
         stale = 0;
-      } else if (++stale >= 5) {
+      } else if (++stale >= stale_limit) {
         ++j;
         ++it;
         break;
@@ -1118,7 +1295,7 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
       y[i] = H[i][i] != 0.0 ? s / H[i][i] : 0.0;
     }
     if (j > 0) FQ_TRY(axpy_h(ctx, g, Z, n, j, y, 1.0, x));
-    if (stale >= 5 && it < max_iters) {
+    if (stale >= stale_limit && it < max_iters) {
       // a stagnating cycle: accept x if it is at the rounding level, else the
       // restart continues (and a stagnating FP32 preconditioner gives way to
       // FP64 factors in sparse_lu_solve)
@@ -1152,6 +1329,14 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
   r.true_residual = relres;
   r.converged = done ? 1 : 0;
   if (rep) *rep = r;
+  // a wait of the triangular solves that ran out (none should) voids the result
+  int waits = 0;
+  FQ_CUDA(ctx, cudaMemcpyAsync(&waits, lu.solve_status.p, 4, cudaMemcpyDeviceToHost, st));
+  FQ_CUDA(ctx, cudaStreamSynchronize(st));
+  if (waits) {
+    FQ_CUDA(ctx, cudaMemsetAsync(lu.solve_status.p, 0, 4, st));
+    return set_error(ctx, FQ_CUDA_ERROR, "sparse LU solve: a wait for a tile's solution ran out");
+  }
   return r.converged ? FQ_OK : FQ_NOT_CONVERGED;
 }
 
@@ -1165,6 +1350,14 @@ fq_status sparse_lu_solve(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
     return s64;
   }
   fq_status s = FQ_NOT_CONVERGED;
+  if (!lu.factored && lu.prefer_fp64) {
+    // FP32 factors of this pattern did not converge before: FP64 ones at once
+    FQ_TRY(sparse_lu_factor(ctx, lu, rp, ci, val, FQ_FP64));
+    const fq_status s64 = sparse_lu_gmres(ctx, lu, rp, ci, val, b, x, rtol, max_iters, &r);
+    r.refinements = 1;
+    if (rep) *rep = r;
+    return s64;
+  }
   fq_status fs = lu.factored ? FQ_OK : sparse_lu_factor(ctx, lu, rp, ci, val, FQ_FP32);
   if (fs == FQ_OK) {
     s = sparse_lu_gmres(ctx, lu, rp, ci, val, b, x, rtol, std::min<int64_t>(max_iters, kFp32Iterations), &r);
@@ -1177,7 +1370,9 @@ fq_status sparse_lu_solve(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
     if (rep) *rep = r;
     return FQ_OK;
   }
-  // the FP32 factors were not enough: FP64 factors, GMRES from zero
+  // the FP32 factors were not enough: FP64 factors, GMRES from zero (and FP64
+  // at once for the next values of this pattern)
+  lu.prefer_fp64 = true;
   fs = sparse_lu_factor(ctx, lu, rp, ci, val, FQ_FP64);
   if (fs == FQ_UNSUPPORTED || fs == FQ_BREAKDOWN) {
     if (rep) *rep = r;

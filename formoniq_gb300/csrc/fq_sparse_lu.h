@@ -29,9 +29,13 @@
 //     the L and U panels by products with those inverses, and the trailing
 //     Schur update, each a batched product (FP32: tiles of 128 columns on the
 //     FP32 pipe; FP64: tiles of 64 columns).
-//   - Solve: forward and backward substitution front by front (one CTA per
-//     front), the unknowns in elimination order; update vectors passed to the
-//     parent like the Schur complements.
+//   - Solve: forward and backward substitution level by level, one launch per
+//     level and direction, one CTA per row block (a tile's rows) of every
+//     front of the level: a block streams its rows of the L (U) panel against
+//     the tile solutions before it (after it), waiting for each on a flag its
+//     producer publishes, then applies the tile's triangular inverse. CTAs take
+//     row blocks by ticket, so a block only waits for blocks already running.
+//     Update vectors go to the parent like the Schur complements.
 //   - Accuracy: the factors precondition a restarted GMRES in FP64 on the FP64
 //     matrix (GMRES-based iterative refinement), which stops on the true FP64
 //     relative residual; FP32 factors first, FP64 ones when those do not
@@ -54,6 +58,7 @@ struct FrontDesc {
   int64_t start;     // elimination position of its first fully summed unknown
   int64_t ea_off;    // offset of its update unknowns in ea_map / urows
   int64_t uvec_off;  // offset of its forward update vector
+  int64_t roff;      // offset of its rows in the per-row maps (rinv)
   int32_t m, f;      // front size, fully summed count
   int32_t parent;    // parent front or -1
   int32_t child0, child1;  // children or -1
@@ -75,6 +80,7 @@ struct SparseLu {
   int64_t pool_elems = 0;
   int64_t tile_elems = 0;  // entries of the tiles' triangular inverses (two kTile^2 blocks per 128 columns)
   int64_t uvec_elems = 0;  // entries of the forward update vectors (u per front)
+  int64_t row_elems = 0;   // rows of all fronts (m per front)
   double flops = 0.0;      // of the numeric factorization
   int64_t tourn_sets = 0;  // candidate sets of the widest level: fronts x ceil(max f / 256)
   // device data
@@ -87,6 +93,8 @@ struct SparseLu {
   std::vector<int64_t> asm_ptr_h;  // [nlevels + 1]
   DevBuf ea_map;      // int32: per front, the parent-local index of each of its update unknowns
   DevBuf urows;       // int32: per front, the elimination positions of its update unknowns
+  DevBuf rinv;        // int32 [2 x row_elems]: per front row, its index among child 0's and
+                      // child 1's update unknowns (-1: none), the extend-add maps inverted
   int precision = -1; // FQ_FP32 or FQ_FP64: the type of the factors below
   DevBuf pool;        // the fronts
   DevBuf tiles;       // per tile, inverse of unit L then inverse of U (tile x tile each)
@@ -98,13 +106,25 @@ struct SparseLu {
   DevBuf status;      // int [4]: perturbed pivots, non-finite pivots
   DevBuf tourn_cand;  // int32: tournament candidates (ping-pong)
   DevBuf tourn_count; // int32: their counts
+  // the solve: row blocks of the fronts, one CTA each, level by level
+  DevBuf fperm;       // int32 [n]: per fully summed position, the front-local row whose value
+                      // the composed interchanges move there
+  DevBuf ybuf;        // [n]: forward solution of the fully summed rows
+  DevBuf flags;       // int32: per tile, the solve phase whose solution is published
+  DevBuf tickets;     // int32 [2 x nlevels]: row-block tickets of the level launches
+  DevBuf solve_status;  // int32: waits that ran out
+  int items_precision = -1;  // the tile width the item lists below were made for
+  DevBuf fwd_items, bwd_items;  // int2 (front, row block), by level
+  std::vector<int64_t> fwd_ptr, bwd_ptr;  // [nlevels + 1]
+  uint32_t epoch = 0;   // solves so far (flags carry 2 epoch + 1 forward, 2 epoch + 2 backward)
   int perturbed = 0, nonfinite = 0;
   bool factored = false;
+  bool prefer_fp64 = false;  // an FP32 factorization of this pattern did not converge: later solves factor in FP64
 };
 
 // The host maps of a symbolic analysis (uploaded by sparse_lu_analyse).
 struct SparseLuMaps {
-  std::vector<int32_t> pos, aslot, arow, ea, ur;
+  std::vector<int32_t> pos, aslot, arow, ea, ur, rinv;
   std::vector<int64_t> aoff;
   std::vector<FrontDesc> fd;
 };
@@ -136,7 +156,9 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
 // The solve with precision adaptation: GMRES on FP32 factors (factored here if
 // the current ones are not FP32) for at most kFp32Iterations iterations; if it
 // has not converged, the system is factored in FP64 and GMRES starts again from
-// zero (report.refinements = 1 then; iterations of both counted).
+// zero (report.refinements = 1 then; iterations of both counted). After such a
+// fallback the analysis remembers it, and the next unfactored solve of the
+// pattern factors in FP64 at once.
 constexpr int64_t kFp32Iterations = 60;
 fq_status sparse_lu_solve(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_t* ci, const double* val,
                           const double* b, double* x, double rtol, int64_t max_iters, fq_report* rep);

@@ -254,7 +254,7 @@ fq_status sparse_lu_analyse_host(fq_ctx* ctx, SparseLu& lu, int dim, int nbox, i
     for (int x : post) lu.level_fronts[fill[level[x]]++] = x;
   }
   std::vector<FrontDesc> fd(nn);
-  int64_t off = 0, toff = 0, eoff = 0, uoff = 0;
+  int64_t off = 0, toff = 0, eoff = 0, uoff = 0, roff = 0;
   double flops = 0.0;
   for (int l = 0; l < nlev; ++l) {
     for (int32_t q = lu.level_ptr[l]; q < lu.level_ptr[l + 1]; ++q) {
@@ -272,6 +272,7 @@ fq_status sparse_lu_analyse_host(fq_ctx* ctx, SparseLu& lu, int dim, int nbox, i
       d.start = start[x];
       d.ea_off = eoff;
       d.uvec_off = uoff;
+      d.roff = roff;
       d.m = int32_t(m);
       d.f = int32_t(f);
       d.parent = nodes[x].parent;
@@ -283,6 +284,7 @@ fq_status sparse_lu_analyse_host(fq_ctx* ctx, SparseLu& lu, int dim, int nbox, i
       toff += tiles * 2 * int64_t(kTile) * kTile;
       eoff += u;
       uoff += u;
+      roff += m;
       const double df = double(f), du = double(u);
       flops += 2.0 / 3.0 * df * df * df + 2.0 * df * df * du + 2.0 * df * du * du;
     }
@@ -298,6 +300,7 @@ fq_status sparse_lu_analyse_host(fq_ctx* ctx, SparseLu& lu, int dim, int nbox, i
   lu.pool_elems = std::max<int64_t>(off, 1);
   lu.tile_elems = std::max<int64_t>(toff, 1);
   lu.uvec_elems = std::max<int64_t>(uoff, 1);
+  lu.row_elems = std::max<int64_t>(roff, 1);
   lu.flops = flops;
   // front-local index of an elimination position
   auto local = [&](int x, int32_t p) -> int64_t {
@@ -318,6 +321,21 @@ fq_status sparse_lu_analyse_host(fq_ctx* ctx, SparseLu& lu, int dim, int nbox, i
       ea[fd[x].ea_off + t] = int32_t(li);
     }
   }
+  // the extend-add maps inverted: per front row, its index among each child's
+  // update unknowns (a child's map is one to one)
+  std::vector<int32_t> rinv(static_cast<size_t>(2 * std::max<int64_t>(roff, 1)), -1);
+  for (int x = 0; x < nn; ++x)
+    for (int which = 0; which < 2; ++which) {
+      const int c = nodes[x].child[which];
+      if (c < 0) continue;
+      for (int64_t t = 0; t < int64_t(U[c].size()); ++t) {
+        const int64_t li = ea[fd[c].ea_off + t];
+        if (li < 0 || li >= fd[x].m) return set_error(ctx, FQ_CUDA_ERROR, "sparse LU: an update row outside its parent");
+        int32_t& slot = rinv[size_t(2 * (fd[x].roff + li) + which)];
+        if (slot != -1) return set_error(ctx, FQ_CUDA_ERROR, "sparse LU: two update rows of a child on one parent row");
+        slot = int32_t(t);
+      }
+    }
   // assembly map, grouped by level
   const int64_t nz = rp[n];
   std::vector<int64_t> aptr(nlev + 1, 0);
@@ -353,8 +371,18 @@ fq_status sparse_lu_analyse_host(fq_ctx* ctx, SparseLu& lu, int dim, int nbox, i
     if (d.f > d.m || d.m < 0 || d.off + int64_t(d.m) * d.m > lu.pool_elems ||
         d.tile_off + ((int64_t(d.f) + kTile - 1) / kTile) * 2 * kTile * kTile > lu.tile_elems ||
         d.start + d.f > n || d.ea_off + (d.m - d.f) > std::max<int64_t>(eoff, 1) ||
-        d.uvec_off + (d.m - d.f) > lu.uvec_elems)
+        d.uvec_off + (d.m - d.f) > lu.uvec_elems || d.roff < 0 || d.roff + d.m > lu.row_elems)
       return set_error(ctx, FQ_CUDA_ERROR, "sparse LU: a front's ranges overrun their stores");
+    for (int which = 0; which < 2; ++which) {
+      const int c = which == 0 ? d.child0 : d.child1;
+      if (c >= 0 && (c >= nn || fd[c].parent != x))
+        return set_error(ctx, FQ_CUDA_ERROR, "sparse LU: a child that does not name its parent");
+      for (int64_t i = 0; i < d.m; ++i) {
+        const int32_t t = rinv[size_t(2 * (d.roff + i) + which)];
+        if (t != -1 && (c < 0 || t < 0 || t >= fd[c].m - fd[c].f))
+          return set_error(ctx, FQ_CUDA_ERROR, "sparse LU: an inverted update map entry outside its child");
+      }
+    }
     const int p = d.parent;
     if (d.m > d.f && p < 0) return set_error(ctx, FQ_CUDA_ERROR, "sparse LU: the root has update unknowns");
     for (int64_t t = 0; t < d.m - d.f; ++t)
@@ -371,6 +399,7 @@ fq_status sparse_lu_analyse_host(fq_ctx* ctx, SparseLu& lu, int dim, int nbox, i
   mp.aoff = std::move(aoff);
   mp.ea = std::move(ea);
   mp.ur = std::move(ur);
+  mp.rinv = std::move(rinv);
   return FQ_OK;
 }
 
@@ -388,6 +417,7 @@ fq_status sparse_lu_analyse(fq_ctx* ctx, SparseLu& lu, int dim, int nbox, int64_
   FQ_TRY(lu.asm_row.alloc(ctx, mp.arow.size() * 4));
   FQ_TRY(lu.ea_map.alloc(ctx, mp.ea.size() * 4));
   FQ_TRY(lu.urows.alloc(ctx, mp.ur.size() * 4));
+  FQ_TRY(lu.rinv.alloc(ctx, mp.rinv.size() * 4));
   FQ_CUDA(ctx, cudaMemcpyAsync(lu.perm.p, mp.pos.data(), size_t(n) * 4, cudaMemcpyHostToDevice, st));
   FQ_CUDA(ctx, cudaMemcpyAsync(lu.fronts.p, mp.fd.data(), sizeof(FrontDesc) * nn, cudaMemcpyHostToDevice, st));
   FQ_CUDA(ctx, cudaMemcpyAsync(lu.level_list.p, lu.level_fronts.data(), size_t(nn) * 4, cudaMemcpyHostToDevice, st));
@@ -396,6 +426,7 @@ fq_status sparse_lu_analyse(fq_ctx* ctx, SparseLu& lu, int dim, int nbox, int64_
   FQ_CUDA(ctx, cudaMemcpyAsync(lu.asm_row.p, mp.arow.data(), mp.arow.size() * 4, cudaMemcpyHostToDevice, st));
   FQ_CUDA(ctx, cudaMemcpyAsync(lu.ea_map.p, mp.ea.data(), mp.ea.size() * 4, cudaMemcpyHostToDevice, st));
   FQ_CUDA(ctx, cudaMemcpyAsync(lu.urows.p, mp.ur.data(), mp.ur.size() * 4, cudaMemcpyHostToDevice, st));
+  FQ_CUDA(ctx, cudaMemcpyAsync(lu.rinv.p, mp.rinv.data(), mp.rinv.size() * 4, cudaMemcpyHostToDevice, st));
   FQ_CUDA(ctx, cudaStreamSynchronize(st));  // the host maps go out of scope
   return FQ_OK;
 }
