@@ -895,8 +895,9 @@ def run_dirac(args):
     1+2 Kuhn boxes (time axis 0.7), squared lengths s (1 + U(-0.05, 0.05)),
     the relative Hodge-Dirac source problem at m = 1.5 and at m = 0 (bordered
     with the top harmonic) through fq.solve_dirac_source with host buffers.
-    Per size: the sparse direct solver's analysis, its FP32 and FP64
-    factorizations timed with CUDA events (TFLOP/s of the factor's flops),
+    Per size: the sparse direct solver's analysis, its FP32, float-float
+    (FQ_FP64, the default for FP64 factors) and IEEE FP64 factorizations timed
+    with CUDA events (TFLOP/s of the factor's flops),
     and the end-to-end solve (wall clock, median of --solves after one
     untimed call that builds the analysis). Sizes up to 8 boxes per axis are
     checked against the oracle's LU solve on the same inputs, which is also
@@ -932,7 +933,7 @@ def run_dirac(args):
         info = lu.info()
         rec.update(unknowns=int(a.shape[0]), fronts=int(info["fronts"]), levels=int(info["levels"]),
                    factor_gflop=info["flops"] / 1e9, factor_gb=info["factor_bytes"] / 1e9)
-        for name, prec in (("fp32", fq.FQ_FP32), ("fp64", fq.FQ_FP64)):
+        for name, prec in (("fp32", fq.FQ_FP32), ("fp64", fq.FQ_FP64), ("fp64_ieee", fq.FQ_FP64_IEEE)):
             lu.factor(prec)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

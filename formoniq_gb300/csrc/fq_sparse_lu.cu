@@ -8,11 +8,85 @@
 #include <string>
 #include <vector>
 
+#include "fq_df64.cuh"
 #include "fq_sparse_lu.h"
 
 namespace fq {
 
 namespace {
+
+// Arithmetic of the three factor types: FP32, IEEE FP64, and float-float
+// (df64: a value as the unevaluated sum of two floats, 48-bit significand, all
+// arithmetic on the FP32 pipe, which on this GPU runs many times faster than
+// the FP64 one). mag() is a magnitude for pivot comparisons (the leading part
+// of a float-float).
+template <typename T>
+struct Num;
+template <>
+struct Num<float> {
+  static constexpr int kPrecision = FQ_FP32;
+  static __device__ __forceinline__ float mag(float a) { return fabsf(a); }
+  static __device__ __forceinline__ bool finite(float a) { return isfinite(a); }
+  static __device__ __forceinline__ bool nonzero(float a) { return a != 0.f; }
+  static __device__ __forceinline__ bool negative(float a) { return a < 0.f; }
+  static __device__ __forceinline__ float fma(float a, float b, float c) { return fmaf(a, b, c); }
+  static __device__ __forceinline__ float recip(float a) { return 1.f / a; }
+  static __device__ __forceinline__ float div(float a, float b) { return a / b; }
+  static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+  static __device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
+  static __host__ __device__ __forceinline__ float from_double(double d) { return float(d); }
+  static __device__ __forceinline__ double to_double(float a) { return double(a); }
+};
+template <>
+struct Num<double> {
+  static constexpr int kPrecision = FQ_FP64_IEEE;
+  static __device__ __forceinline__ double mag(double a) { return fabs(a); }
+  static __device__ __forceinline__ bool finite(double a) { return isfinite(a); }
+  static __device__ __forceinline__ bool nonzero(double a) { return a != 0.0; }
+  static __device__ __forceinline__ bool negative(double a) { return a < 0.0; }
+  static __device__ __forceinline__ double fma(double a, double b, double c) { return ::fma(a, b, c); }
+  static __device__ __forceinline__ double recip(double a) { return 1.0 / a; }
+  static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+  static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
+  static __device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
+  static __host__ __device__ __forceinline__ double from_double(double d) { return d; }
+  static __device__ __forceinline__ double to_double(double a) { return a; }
+};
+template <>
+struct Num<df64> {
+  static constexpr int kPrecision = FQ_FP64;
+  static __device__ __forceinline__ float mag(df64 a) { return fabsf(a.hi); }
+  static __device__ __forceinline__ bool finite(df64 a) { return isfinite(a.hi) && isfinite(a.lo); }
+  static __device__ __forceinline__ bool nonzero(df64 a) { return a.hi != 0.f || a.lo != 0.f; }
+  static __device__ __forceinline__ bool negative(df64 a) { return a.hi < 0.f; }
+  // c + a b: the product's leading part and its error (exact by FMA, plus the
+  // cross terms), TwoSum of the leading parts, the trailing parts in FP32,
+  // one renormalisation (15 FP32 operations; error about 2^-46 of the terms)
+  static __device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c) {
+    const float p = f_mul(a.hi, b.hi);
+    float e = f_fma(a.hi, b.hi, -p);
+    e = f_fma(a.hi, b.lo, e);
+    e = f_fma(a.lo, b.hi, e);
+    const df64 s = two_sum(c.hi, p);
+    const float t = f_add(c.lo, f_add(e, s.lo));
+    return fast_two_sum(s.hi, t);
+  }
+  // 1 / a: the FP32 reciprocal refined by one Newton step in float-float
+  // (the division of Bailey's double-double arithmetic)
+  static __device__ __forceinline__ df64 recip(df64 a) {
+    const df64 q(__frcp_rn(a.hi), 0.f);
+    const df64 e = df64(1.f, 0.f) - a * q;
+    return q + q * e;
+  }
+  static __device__ __forceinline__ df64 div(df64 a, df64 b) { return a * recip(b); }
+  static __device__ __forceinline__ df64 mul(df64 a, df64 b) { return a * b; }
+  static __device__ __forceinline__ df64 ldcg(const df64* p) {
+    const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+    return df64(v.x, v.y);
+  }
+  static __host__ __device__ __forceinline__ df64 from_double(double d) { return df64(d); }
+  static __device__ __forceinline__ double to_double(df64 a) { return a.to_double(); }
+};
 
 template <typename T>
 struct SlCfg;
@@ -25,6 +99,13 @@ struct SlCfg<float> {
 };
 template <>
 struct SlCfg<double> {
+  static constexpr int TILE = 64;
+  static constexpr int ROWS = 128;
+  static constexpr int BM = 64;
+  static constexpr int TM = 4;
+};
+template <>
+struct SlCfg<df64> {
   static constexpr int TILE = 64;
   static constexpr int ROWS = 128;
   static constexpr int BM = 64;
@@ -46,7 +127,7 @@ __global__ void sl_assemble_kernel(const int32_t* __restrict__ slot, const int32
                                    const double* __restrict__ d, T* __restrict__ pool) {
   for (int64_t q = b + int64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < e; q += int64_t(gridDim.x) * blockDim.x) {
     const int32_t s = slot[q];
-    pool[off[q]] = T(d[row[q]] * val[s] * d[ci[s]]);
+    pool[off[q]] = Num<T>::from_double(d[row[q]] * val[s] * d[ci[s]]);
   }
 }
 
@@ -101,17 +182,18 @@ __device__ void gepp_select(T* blk, int ld, int* idx, int rows, int b) {
   const int steps = min(rows, b);
   for (int j = 0; j < steps; ++j) {
     if (tid < 32) {
-      T best = T(-1);
+      using M = decltype(Num<T>::mag(T()));
+      M best = M(-1);
       int bi = j;
       for (int i = j + tid; i < rows; i += 32) {
-        const T a = fabs(blk[j * ld + i]);
+        const M a = Num<T>::mag(blk[j * ld + i]);
         if (a > best || (a == best && i < bi)) {
           best = a;
           bi = i;
         }
       }
       for (int o = 16; o > 0; o >>= 1) {
-        const T ob = __shfl_down_sync(0xffffffffu, best, o);
+        const M ob = __shfl_down_sync(0xffffffffu, best, o);
         const int oi = __shfl_down_sync(0xffffffffu, bi, o);
         if (ob > best || (ob == best && oi < bi)) {
           best = ob;
@@ -136,9 +218,9 @@ __device__ void gepp_select(T* blk, int ld, int* idx, int rows, int b) {
     }
     __syncthreads();
     const T d = blk[j * ld + j];
-    if (d != T(0) && isfinite(d)) {
-      const T rinv = T(1) / d;
-      for (int i = j + 1 + tid; i < rows; i += nt) blk[j * ld + i] *= rinv;
+    if (Num<T>::nonzero(d) && Num<T>::finite(d)) {
+      const T rinv = Num<T>::recip(d);
+      for (int i = j + 1 + tid; i < rows; i += nt) blk[j * ld + i] = Num<T>::mul(blk[j * ld + i], rinv);
       __syncthreads();
       const int w = rows - j - 1, c = b - j - 1;
       for (int t = tid; t < w * c; t += nt) {
@@ -316,20 +398,20 @@ __global__ void __launch_bounds__(kThreads) sl_tile_kernel(const FrontDesc* __re
   for (int j = 0; j < b; ++j) {
     if (tid == 0) {
       T d = Tt[j * LD + j];
-      if (!isfinite(d)) {
+      if (!Num<T>::finite(d)) {
         if (nbad == 0 && atomicCAS(status + 2, 0, list[blockIdx.x] + 1) == 0) status[3] = k + j;
         ++nbad;
         d = thresh;
-      } else if (fabs(d) < thresh) {
+      } else if (Num<T>::mag(d) < Num<T>::mag(thresh)) {
         ++npert;
-        d = d < T(0) ? -thresh : thresh;
+        d = Num<T>::negative(d) ? -thresh : thresh;
       }
       Tt[j * LD + j] = d;
-      s_val = T(1) / d;
+      s_val = Num<T>::recip(d);
     }
     __syncthreads();
     const T rinv = s_val;
-    for (int i = j + 1 + tid; i < b; i += nt) Tt[j * LD + i] *= rinv;
+    for (int i = j + 1 + tid; i < b; i += nt) Tt[j * LD + i] = Num<T>::mul(Tt[j * LD + i], rinv);
     __syncthreads();
     const int w = b - j - 1;
     for (int t = tid; t < w * w; t += nt) {
@@ -367,11 +449,11 @@ __global__ void __launch_bounds__(kThreads) sl_tile_kernel(const FrontDesc* __re
   if (tid < b) {
     const int j = tid;
     for (int i = 0; i < b; ++i) Xs[j * LD + i] = T(0);
-    Xs[j * LD + j] = T(1) / Tt[j * LD + j];
+    Xs[j * LD + j] = Num<T>::recip(Tt[j * LD + j]);
     for (int i = j - 1; i >= 0; --i) {
       T s = T(0);
       for (int l = i + 1; l <= j; ++l) s += Tt[l * LD + i] * Xs[j * LD + l];
-      Xs[j * LD + i] = -s / Tt[i * LD + i];
+      Xs[j * LD + i] = Num<T>::div(-s, Tt[i * LD + i]);
     }
   }
   __syncthreads();
@@ -408,6 +490,14 @@ struct Vec16<double> {
     const double2 v = *reinterpret_cast<const double2*>(p);
     o[0] = v.x;
     o[1] = v.y;
+  }
+};
+template <>
+struct Vec16<df64> {
+  static __device__ __forceinline__ void load(const df64* p, df64* o) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    o[0] = df64(v.x, v.y);
+    o[1] = df64(v.z, v.w);
   }
 };
 
@@ -494,7 +584,7 @@ __global__ void __launch_bounds__(kThreads) sl_gemm_kernel(const FrontDesc* __re
 #pragma unroll
       for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < TM; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+        for (int j = 0; j < TM; ++j) acc[i][j] = Num<T>::fma(av[i], bv[j], acc[i][j]);
     }
     __syncthreads();
   }
@@ -622,7 +712,7 @@ __global__ void __launch_bounds__(kSolveThreads) sl_forward_rows_kernel(
   for (int j = 0; j < jmax; ++j) {
     wait_tile(flags + ftile + j, target, status);
     const int k = j * TL, b = min(TL, f - k);
-    if (tid < b) sy[tid] = __ldcg(ybuf + F.start + k + tid);
+    if (tid < b) sy[tid] = Num<T>::ldcg(ybuf + F.start + k + tid);
     __syncthreads();
 #pragma unroll 4
     for (int l = warp; l < b; l += NW) {
@@ -631,7 +721,7 @@ __global__ void __launch_bounds__(kSolveThreads) sl_forward_rows_kernel(
 #pragma unroll
       for (int q = 0; q < R; ++q) {
         const int i = lane + 32 * q;
-        if (i < nr) acc[q] += col[i] * yl;
+        if (i < nr) acc[q] = Num<T>::fma(col[i], yl, acc[q]);
       }
     }
     __syncthreads();
@@ -667,7 +757,7 @@ __global__ void __launch_bounds__(kSolveThreads) sl_forward_rows_kernel(
   const T* iL = tiles + F.tile_off + int64_t(w.y) * 2 * TL * TL;
   if (tid < nr) {
     T y = T(0);
-    for (int l = 0; l <= tid; ++l) y += iL[l * TL + tid] * sy[l];
+    for (int l = 0; l <= tid; ++l) y = Num<T>::fma(iL[l * TL + tid], sy[l], y);
     ybuf[F.start + r0 + tid] = y;
     __threadfence();
   }
@@ -716,7 +806,7 @@ __global__ void __launch_bounds__(kSolveThreads) sl_backward_rows_kernel(
 #pragma unroll
       for (int q = 0; q < R; ++q) {
         const int i = lane + 32 * q;
-        if (i < nr) acc[q] += col[i] * xl;
+        if (i < nr) acc[q] = Num<T>::fma(col[i], xl, acc[q]);
       }
     }
     __syncthreads();
@@ -725,7 +815,7 @@ __global__ void __launch_bounds__(kSolveThreads) sl_backward_rows_kernel(
   for (int j = nF - 1; j > t; --j) {
     wait_tile(flags + ftile + j, target, status);
     const int k = j * TL, b = min(TL, f - k);
-    if (tid < b) sx[tid] = __ldcg(work + F.start + k + tid);
+    if (tid < b) sx[tid] = Num<T>::ldcg(work + F.start + k + tid);
     __syncthreads();
 #pragma unroll 4
     for (int l = warp; l < b; l += NW) {
@@ -734,7 +824,7 @@ __global__ void __launch_bounds__(kSolveThreads) sl_backward_rows_kernel(
 #pragma unroll
       for (int q = 0; q < R; ++q) {
         const int i = lane + 32 * q;
-        if (i < nr) acc[q] += col[i] * xl;
+        if (i < nr) acc[q] = Num<T>::fma(col[i], xl, acc[q]);
       }
     }
     __syncthreads();
@@ -752,7 +842,7 @@ __global__ void __launch_bounds__(kSolveThreads) sl_backward_rows_kernel(
   const T* iU = tiles + F.tile_off + int64_t(t) * 2 * TL * TL + TL * TL;
   if (tid < nr) {
     T x = T(0);
-    for (int l = tid; l < nr; ++l) x += iU[l * TL + tid] * sx[l];
+    for (int l = tid; l < nr; ++l) x = Num<T>::fma(iU[l * TL + tid], sx[l], x);
     work[F.start + r0 + tid] = x;
     __threadfence();
   }
@@ -765,14 +855,14 @@ template <typename T>
 __global__ void sl_permute_in_kernel(const double* __restrict__ r, const int32_t* __restrict__ perm,
                                      const double* __restrict__ d, int64_t n, T* __restrict__ w) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
-    w[perm[i]] = T(d[i] * r[i]);
+    w[perm[i]] = Num<T>::from_double(d[i] * r[i]);
 }
 
 template <typename T>
 __global__ void sl_permute_out_kernel(const T* __restrict__ w, const int32_t* __restrict__ perm,
                                       const double* __restrict__ d, int64_t n, double* __restrict__ z) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
-    z[i] = d[i] * double(w[perm[i]]);
+    z[i] = d[i] * Num<T>::to_double(w[perm[i]]);
 }
 
 // ---------------------------------------------------------------------------
@@ -889,7 +979,7 @@ fq_status factor_impl(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_
   for (int x = 0; x < lu.nfronts; ++x) maxf_all = std::max<int64_t>(maxf_all, lu.front_f[x]);
   if (maxf_all > kMaxComposeRows)
     return set_error(ctx, FQ_UNSUPPORTED, "sparse LU: a front with more fully summed rows than the solve holds");
-  const int prec = sizeof(T) == 4 ? FQ_FP32 : FQ_FP64;
+  const int prec = Num<T>::kPrecision;
   if (lu.precision != prec) {
     lu.pool.release();
     lu.tiles.release();
@@ -927,8 +1017,8 @@ fq_status factor_impl(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_
   ctx->launches++;
   // the pivot floor, relative to the scaled matrix's largest entry (1): about
   // ten units in the last place of FP32; far below any pivot the near-resonant
-  // systems need in FP64
-  const T thresh = sizeof(T) == 4 ? T(1e-6) : T(1e-13);
+  // systems need in float-float (48-bit) and FP64
+  const T thresh = Num<T>::from_double(prec == FQ_FP32 ? 1e-6 : prec == FQ_FP64 ? 1e-12 : 1e-13);
   FQ_CUDA(ctx, cudaMemsetAsync(lu.status.p, 0, 4 * sizeof(int), st));
   FQ_CUDA(ctx, cudaMemsetAsync(lu.piv.p, 0, size_t(std::max<int64_t>(lu.n, 1)) * 4, st));
   const int tile_smem = 2 * C::TILE * (C::TILE + 1) * int(sizeof(T));
@@ -1033,7 +1123,8 @@ fq_status factor_impl(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_
       for (int32_t q = lu.level_ptr[l]; q < lu.level_ptr[l + 1]; ++q)
         if (lu.level_fronts[q] == x) lev = l;
     return set_error(ctx, FQ_BREAKDOWN,
-                     std::string("sparse LU: non-finite pivot (") + (sizeof(T) == 4 ? "FP32" : "FP64") + ", front " +
+                     std::string("sparse LU: non-finite pivot (") +
+                         (prec == FQ_FP32 ? "FP32" : prec == FQ_FP64 ? "float-float" : "FP64") + ", front " +
                          std::to_string(x) + " of level " + std::to_string(lev) + "/" + std::to_string(lu.nlevels) +
                          ", m " + std::to_string(x >= 0 ? lu.front_m[x] : -1) + ", f " +
                          std::to_string(x >= 0 ? lu.front_f[x] : -1) + ", column " + std::to_string(hs[3]) + ")");
@@ -1162,13 +1253,15 @@ fq_status sparse_lu_factor(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const i
                            int precision) {
   lu.factored = false;
   if (precision == FQ_FP32) return factor_impl<float>(ctx, lu, rp, ci, val);
-  return factor_impl<double>(ctx, lu, rp, ci, val);
+  if (precision == FQ_FP64_IEEE) return factor_impl<double>(ctx, lu, rp, ci, val);
+  return factor_impl<df64>(ctx, lu, rp, ci, val);
 }
 
 fq_status sparse_lu_apply(fq_ctx* ctx, SparseLu& lu, const double* r, double* z) {
   if (!lu.factored) return set_error(ctx, FQ_INVALID_ARG, "sparse LU: not factored");
   if (lu.precision == FQ_FP32) return apply_impl<float>(ctx, lu, r, z);
-  return apply_impl<double>(ctx, lu, r, z);
+  if (lu.precision == FQ_FP64_IEEE) return apply_impl<double>(ctx, lu, r, z);
+  return apply_impl<df64>(ctx, lu, r, z);
 }
 
 // A solve ends when the relative residual meets rtol, or when the normwise
@@ -1343,7 +1436,7 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
 fq_status sparse_lu_solve(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_t* ci, const double* val,
                           const double* b, double* x, double rtol, int64_t max_iters, fq_report* rep) {
   fq_report r{};
-  if (lu.factored && lu.precision == FQ_FP64) {
+  if (lu.factored && lu.precision != FQ_FP32) {
     const fq_status s64 = sparse_lu_gmres(ctx, lu, rp, ci, val, b, x, rtol, max_iters, &r);
     r.refinements = 1;
     if (rep) *rep = r;

@@ -38,8 +38,10 @@
 //     Update vectors go to the parent like the Schur complements.
 //   - Accuracy: the factors precondition a restarted GMRES in FP64 on the FP64
 //     matrix (GMRES-based iterative refinement), which stops on the true FP64
-//     relative residual; FP32 factors first, FP64 ones when those do not
-//     converge (the near-resonant Lorentzian systems).
+//     relative residual; FP32 factors first, float-float ones (FQ_FP64) when
+//     those do not converge (the near-resonant Lorentzian systems). Float-float
+//     arithmetic runs on the FP32 pipe, which this GPU has many times the
+//     throughput of its FP64 pipe; IEEE FP64 factors remain on request.
 #pragma once
 
 #include <cstdint>
@@ -95,7 +97,7 @@ struct SparseLu {
   DevBuf urows;       // int32: per front, the elimination positions of its update unknowns
   DevBuf rinv;        // int32 [2 x row_elems]: per front row, its index among child 0's and
                       // child 1's update unknowns (-1: none), the extend-add maps inverted
-  int precision = -1; // FQ_FP32 or FQ_FP64: the type of the factors below
+  int precision = -1; // the type of the factors below: FQ_FP32, FQ_FP64 (float-float) or FQ_FP64_IEEE
   DevBuf pool;        // the fronts
   DevBuf tiles;       // per tile, inverse of unit L then inverse of U (tile x tile each)
   DevBuf piv;         // int32 [n]: per fully summed position p, the front-local row
@@ -144,7 +146,8 @@ fq_status sparse_lu_analyse(fq_ctx* ctx, SparseLu& lu, int dim, int nbox, int64_
 fq_status sparse_lu_build(fq_ctx* ctx, const fq_mesh* m, int64_t n, const int32_t* rp, const int32_t* ci,
                           const std::vector<int32_t>& dofv, SparseLu& lu);
 // Numeric factorization from the device CSR values (FP64) of the analysed
-// pattern, in FQ_FP32 or FQ_FP64.
+// pattern, in FQ_FP32, FQ_FP64 (float-float: pairs of floats, 48-bit
+// significand, on the FP32 pipe) or FQ_FP64_IEEE (IEEE double).
 fq_status sparse_lu_factor(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_t* ci, const double* val,
                            int precision);
 // z = (LU)^-1 r on the device (FP64 in and out, the factors' type inside).

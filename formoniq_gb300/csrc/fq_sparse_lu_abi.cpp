@@ -60,8 +60,8 @@ fq_status fq_sparse_lu_create(fq_ctx* ctx, fq_mesh* mesh, const fq_matrix* a, fq
 
 fq_status fq_sparse_lu_factor(fq_sparse_lu* s, const fq_matrix* a, int precision) {
   if (!s || !a) return FQ_INVALID_ARG;
-  if (precision != FQ_FP32 && precision != FQ_FP64)
-    return set_error(s->ctx, FQ_INVALID_ARG, "sparse LU: factors in FQ_FP32 or FQ_FP64");
+  if (precision != FQ_FP32 && precision != FQ_FP64 && precision != FQ_FP64_IEEE)
+    return set_error(s->ctx, FQ_INVALID_ARG, "sparse LU: factors in FQ_FP32, FQ_FP64 or FQ_FP64_IEEE");
   if (a->nrows != s->lu.n || a->nnz != s->lu.nnz)
     return set_error(s->ctx, FQ_INVALID_ARG, "sparse LU: the matrix's pattern is not the analysed one");
   FQ_GUARD_BEGIN
@@ -97,7 +97,7 @@ fq_status fq_sparse_lu_info(const fq_sparse_lu* s, int64_t* fronts, int64_t* lev
   if (fronts) *fronts = s->lu.nfronts;
   if (levels) *levels = s->lu.nlevels;
   if (flops) *flops = s->lu.flops;
-  if (factor_bytes) *factor_bytes = (s->lu.pool_elems + s->lu.tile_elems) * (s->lu.precision == FQ_FP64 ? 8 : 4);
+  if (factor_bytes) *factor_bytes = (s->lu.pool_elems + s->lu.tile_elems) * (s->lu.precision == FQ_FP32 ? 4 : 8);
   if (perturbed_pivots) *perturbed_pivots = s->lu.perturbed;
   return FQ_OK;
 }

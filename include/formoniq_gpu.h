@@ -445,7 +445,10 @@ typedef struct fq_sparse_lu fq_sparse_lu;
  * FQ_UNSUPPORTED on other meshes. */
 fq_status fq_sparse_lu_create(fq_ctx* ctx, fq_mesh* mesh, const fq_matrix* a, fq_sparse_lu** out);
 /* Numeric factorization of a's current values (after every re-assembly), in
- * precision FQ_FP32 (tiles of 128 columns on the FP32 pipe) or FQ_FP64. */
+ * precision FQ_FP32 (tiles of 128 columns on the FP32 pipe), FQ_FP64 (float-
+ * float: each value a pair of floats, 48-bit significand, computed on the
+ * FP32 pipe; tiles of 64 columns) or FQ_FP64_IEEE (IEEE double on the FP64
+ * pipe, which runs at a small fraction of the FP32 pipe's rate on GB300). */
 fq_status fq_sparse_lu_factor(fq_sparse_lu* lu, const fq_matrix* a, int precision);
 /* x = A^-1 b (device vectors of a->nrows doubles) by GMRES to opts->rtol on the
  * true FP64 residual, or until the normwise backward error

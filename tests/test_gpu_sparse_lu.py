@@ -143,11 +143,18 @@ def test_sparse_lu_api_against_superlu(oracle, ctx, which):
     A2 = a.to_scipy()
     x, rep = lu.solve(b, fq.SolveOpts.default(rtol=1e-12, max_iters=300))
     assert rep.converged and rel(x, spla.spsolve(A2.tocsc(), b)) < SOLVE_TOL
-    # max_refinements = 0: GMRES on the FP32 factors only, no FP64 refactorization
-    lu.factor(fq.FQ_FP32)
-    x, rep = lu.solve(b, fq.SolveOpts.default(rtol=1e-12, max_iters=300, max_refinements=0))
-    assert rep.converged and rep.refinements == 0, rep
-    assert rel(x, spla.spsolve(A2.tocsc(), b)) < SOLVE_TOL
+    # max_refinements = 0: GMRES on the given factors only, no refactorization: FP32,
+    # float-float (FQ_FP64) and IEEE FP64 factors each precondition to the same solution
+    want2 = spla.spsolve(A2.tocsc(), b)
+    iters = {}
+    for prec in (fq.FQ_FP32, fq.FQ_FP64, fq.FQ_FP64_IEEE):
+        lu.factor(prec)
+        x, rep = lu.solve(b, fq.SolveOpts.default(rtol=1e-12, max_iters=300, max_refinements=0))
+        assert rep.converged and rep.refinements == 0, (prec, rep)
+        assert rel(x, want2) < SOLVE_TOL, prec
+        iters[prec] = rep.iters
+    # the 48-bit factors are as good a preconditioner as the 53-bit ones
+    assert iters[fq.FQ_FP64] <= iters[fq.FQ_FP64_IEEE] + 1, iters
     lu.close()
 
 
