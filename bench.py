@@ -628,14 +628,15 @@ def serve_stream(fq, n, seed, rate_per_s, max_cells_hodge=5e5, max_cells_dirac=3
     return reqs
 
 
-def run_stream(fq, reqs, lanes, cache, mixed_precision, dirac_iters, sols=None, inputs=None):
+def run_stream(fq, reqs, lanes, cache, mixed_precision, dirac_iters, sols=None, inputs=None, tight=False):
     """Submit the whole stream (the server releases each request at its
     arrival time); returns per-request results in stream order. sols[i], when
     given, receives request i's solution; inputs[i] = (lengths, source) pins a
-    request's inputs."""
-    fp64 = fq.SolveOpts.default(rtol=1e-10)
+    request's inputs. tight: FP64 solves to rtol 1e-13 (the accuracy reference
+    of the sampled requests)."""
+    fp64 = fq.SolveOpts.default(rtol=1e-13 if tight else 1e-10, max_iters=40_000 if tight else 10_000)
     fp32 = fq.SolveOpts.default(rtol=1e-5, precision=fq.FQ_FP32, refine_rtol=1e-10, max_refinements=8)
-    dirac = fq.SolveOpts.default(rtol=1e-10, max_iters=dirac_iters)
+    dirac = fq.SolveOpts.default(rtol=1e-13 if tight else 1e-10, max_iters=dirac_iters)
     with fq.Server(lanes=lanes, cache=cache) as srv:
         t0 = time.perf_counter()
         tickets = []
@@ -741,7 +742,7 @@ def serve_study(args, compact: bool):
     nreq = 40 if compact else args.requests
     reqs = serve_stream(fq, nreq, SEED, args.rate)
     sizes = solution_sizes(fq, reqs)
-    step = max(1, nreq // 200)
+    step = max(1, nreq // 100)
     sample = [i for i in range(nreq) if i % step == 0]
     sols_s = [np.zeros(sizes[i]) if i in sample else None for i in range(nreq)]
     sols_p = [np.zeros(sizes[i]) if i in sample else None for i in range(nreq)]
@@ -755,11 +756,23 @@ def serve_study(args, compact: bool):
                 inputs[i], wants[i] = (lengths, src), want
     served, wall_s, st = run_stream(fq, reqs, args.lanes, True, True, args.dirac_iters, sols_s, inputs)
     plain, wall_p, _ = run_stream(fq, reqs, 1, False, False, args.dirac_iters, sols_p, inputs)
+    # the sampled requests again, one lane, solved to rtol 1e-13: the accuracy
+    # reference both sides are measured against
+    sub = [dict(reqs[i], arrival_ms=0.0) for i in sample]
+    sols_t = [np.zeros(sizes[i]) for i in sample]
+    tight, _, _ = run_stream(fq, sub, 1, False, False, args.dirac_iters, sols_t,
+                             {j: inputs[i] for j, i in enumerate(sample) if i in inputs}, tight=True)
     errs = {"hodge": [], "dirac": []}
-    for i in sample:
+    acc = {side: {"hodge": [], "dirac": []} for side in ("served", "plain")}
+    for j, i in enumerate(sample):
+        kind = "hodge" if reqs[i]["kind"] == fq.FQ_REQ_HODGE else "dirac"
         if served[i]["status"] == 0 and plain[i]["status"] == 0:
-            kind = "hodge" if reqs[i]["kind"] == fq.FQ_REQ_HODGE else "dirac"
             errs[kind].append(float(np.linalg.norm(sols_s[i] - sols_p[i]) / max(np.linalg.norm(sols_p[i]), 1e-300)))
+        if tight[j]["status"] == 0:
+            ref = max(np.linalg.norm(sols_t[j]), 1e-300)
+            for side, sol, res in (("served", sols_s[i], served[i]), ("plain", sols_p[i], plain[i])):
+                if res["status"] == 0:
+                    acc[side][kind].append(float(np.linalg.norm(sol - sols_t[j]) / ref))
     oracle_errs = [{"kind": "hodge" if reqs[i]["kind"] == fq.FQ_REQ_HODGE else "dirac", "dim": reqs[i]["dim"],
                     "nbox": reqs[i]["nbox"], "dofs": sizes[i],
                     "served_rel_err": float(np.linalg.norm(sols_s[i] - w) / np.linalg.norm(w)),
@@ -779,6 +792,12 @@ def serve_study(args, compact: bool):
             "plain": side(plain, wall_p, lanes=1, cache=False, precision="FP64 (Hodge), FP64 GMRES on sparse LU (Dirac)"),
             "served_vs_plain_rel_err": {k: {"n": len(v), "max": max(v) if v else None,
                                             "median": statistics.median(v) if v else None} for k, v in errs.items()},
+            "rel_err_vs_tight_solve": {side: {k: {"n": len(v), "max": max(v) if v else None,
+                                                  "median": statistics.median(v) if v else None,
+                                                  "over_1e-8": sum(1 for e in v if e > 1e-8)}
+                                              for k, v in d.items()} for side, d in acc.items()},
+            "tight_solve": "the sampled requests re-solved on one lane in FP64 to rtol 1e-13 (MINRES; GMRES on the "
+                           "sparse LU for Dirac, stopping at its backward-error floor)",
             "sampled_requests": len(sample), "vs_cpu_oracle": oracle_errs}
 
 

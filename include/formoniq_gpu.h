@@ -409,12 +409,15 @@ fq_status fq_source_assemble(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, in
  * HodgeDirac::assemble_selfadjoint (:205-260) on the relative complex,
  * rhs = E^T (load - S lift). Solver (opts->preconditioner):
  *   FQ_PC_AUTO / FQ_PC_DIRECT on fq_mesh_kuhn_cube meshes: the reference's
- *     LU, here the sparse direct factorization (fq_sparse_lu_*) preconditioning
- *     FP64 GMRES to opts->rtol on the true residual (report.refinements = 1
- *     when the FP32 factors gave way to FP64 ones). At m = 0 the top-grade
- *     harmonic (top_harmonic, :552-570) is tested against the kernel
- *     (||S h|| <= 1e-8 ||h||) and, if it spans it, the system is bordered with
- *     it (solve_bordered, :578-598): the solution orthogonal to the kernel.
+ *     LU, here the sparse direct factorization (fq_sparse_lu_*, float-float
+ *     factors) preconditioning FP64 GMRES to opts->rtol on the true residual
+ *     (report.refinements = 1). At m = 0 the top-grade harmonic (top_harmonic,
+ *     :552-570) is tested against the kernel (||S h|| <= 1e-8 ||h||) and, if
+ *     it spans it, the system is bordered with it (solve_bordered, :578-598):
+ *     the solution orthogonal to the kernel. When |m| is below a shift tau =
+ *     1e-3 / (mesh diameter), the factored matrix carries mass term tau (the
+ *     massless system's fronts have structurally zero pivots); GMRES runs on
+ *     the system itself.
  *   FQ_PC_COMPARISON / FQ_PC_HX (Kuhn meshes): MINRES preconditioned from the
  *     Euclidean comparison lattice (the signed lengths' axis scales made
  *     positive): the inverse diagonal of its relative masses M_j, j = 0..n, or
