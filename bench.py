@@ -10,7 +10,7 @@ The same run times the mixed k=1 Hodge-Laplace solve by preconditioned MINRES to
 with host buffers.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-    python bench.py --workload precision|serve|batch|next|dirac
+    python bench.py --workload precision|serve|batch|next|dirac|shapes
 
 The other workloads: the 4D FP32-with-refinement study, the served request
 stream, many meshes assembled in one launch set, the rows after the headline
@@ -906,6 +906,46 @@ def run_batch(args):
 
 
 # ---------------------------------------------------------------------------
+# scatter launch shapes on the headline step
+# ---------------------------------------------------------------------------
+
+def run_shapes(args):
+    """The headline step (3D 32^3, the four forms) with every launch shape of
+    the symmetric scatter (fq_ctx_set_scatter_shape: slots per thread 0 = one
+    thread per upper slot, 1-8 on a persistent grid; CTAs per SM 0 = as many as
+    are resident) in each precision mode; --steps timed steps after --warmup,
+    L2 flushed before each, per-kernel split from the profiled pass."""
+    import torch
+
+    import formoniq_gb300 as fq
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = fq.Context(0, stream=stream.cuda_stream)
+    mesh = fq.Mesh.kuhn_cube(ctx, DIM, NBOX)
+    mesh.kuhn_lengths(jitter=JITTER, seed=SEED)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    out = {"metric": "ms per assembly step by scatter launch shape", "workload": workload_name(mesh.ncells()),
+           "shapes": []}
+    for prec, label in ((fq.FQ_FP64, "fp64 float-float"), (fq.FQ_FP64_IEEE, "fp64 ieee"), (fq.FQ_FP32, "fp32")):
+        mats = [getattr(fq.WhitneyComplex(mesh, precision=prec), name)(k) for name, k in FORMS]
+        for spt in (-1, 0, 1, 2, 4, 8):
+            for bps in ((0,) if spt <= 0 else (0, 2, 4, 8)):
+                ctx.set_scatter_shape(spt, bps)
+                t = timed_assembly(ctx, mats, flush, stream, args.steps, args.warmup, 1)
+                out["shapes"].append({"precision": label, "slots_per_thread": spt, "blocks_per_sm": bps,
+                                      "ms_per_step": t["ms"], "element_ms": t["el_ms"] / max(t["el_n"], 1) * len(FORMS),
+                                      "scatter_ms": t["sc_ms"] / max(t["sc_n"], 1) * len(FORMS)})
+        ctx.set_scatter_shape(-1, 0)
+        for m in mats:
+            m.close()
+    mesh.close()
+    ctx.close()
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------
 # Dirac workload: direct Lorentzian Dirac solves at the served stream's sizes
 # ---------------------------------------------------------------------------
 
@@ -1178,11 +1218,12 @@ def main():
     ap.add_argument("--no-sub", action="store_true",
                     help="skip the compact batch / precision / serving studies of the default run")
     ap.add_argument("--workload", default="assembly",
-                    choices=["assembly", "precision", "serve", "batch", "next", "dirac"],
+                    choices=["assembly", "precision", "serve", "batch", "next", "dirac", "shapes"],
                     help="assembly: the headline line; precision: the 4D FP32-with-refinement study; "
                          "serve: the request stream, served vs plain; batch: many meshes in one launch set; "
                          "next: matrix-free operator, source load, de Rham map, leapfrog; "
-                         "dirac: direct Lorentzian Dirac solves by mesh size")
+                         "dirac: direct Lorentzian Dirac solves by mesh size; "
+                         "shapes: the headline step by scatter launch shape")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--meshes", type=int, default=512, help="batch: number of meshes")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate (requests/s)")
@@ -1204,6 +1245,8 @@ def main():
         run_next(args)
     elif args.workload == "dirac":
         run_dirac(args)
+    elif args.workload == "shapes":
+        run_shapes(args)
     else:
         run_ours(args)
 

@@ -26,7 +26,9 @@ namespace fq {
 // rounding, 2e-13 relative at 3D on 0.15h-jittered cells, which leaves the
 // 1e-12 element tolerance a margin. At 4D the same loss reaches 9e-13, and a
 // Lorentzian cell may be near null, so for those, as in the other modes, they
-// stay IEEE double.
+// stay IEEE double. FP32 programs take the float-float inverse of every
+// Riemannian cell, 4D included (far inside their 1e-5 tolerance), rounded to
+// FP32.
 template <int N, typename T>
 FQ_HD T cell_bary(const double* s, Bary<N, T>& B, bool& bad) {
   constexpr int NE = cbinom(N + 1, 2);
@@ -49,6 +51,30 @@ FQ_HD T cell_bary(const double* s, Bary<N, T>& B, bool& bad) {
       bad = !(det.hi != 0.f) || !isfinite(det.hi);
       // vol = sqrt|det| / n!  (regge/src/lib.rs:26-28)
       return dd_sqrt(dd_abs(det)) * df64(1.0 / double(cfact(N)));
+    }
+  }
+  // FP32 programs on the same cells: the float-float metric and inverse (on the
+  // FP32 pipe, where IEEE double would bind the FP64 pipe), rounded to FP32
+  if (std::is_same<T, float>::value && riemannian) {
+    if constexpr (std::is_same<T, float>::value) {
+      df64 sd[NE > 0 ? NE : 1];
+#pragma unroll
+      for (int e = 0; e < NE; ++e) sd[e] = df64(s[e]);
+      df64 g[N > 0 ? N : 1][N > 0 ? N : 1];
+      df64 gi[N > 0 ? N : 1][N > 0 ? N : 1];
+      regge_metric_t<N, df64>(sd, g);
+      const df64 det = sym_inverse_t<N, df64>(g, gi);
+      float gf[N > 0 ? N : 1][N > 0 ? N : 1];
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = 0; j < N; ++j) gf[i][j] = f_add(gi[i][j].hi, gi[i][j].lo);
+      bary_gramian_t<N, float>(gf, B);
+      const df64 rd = recip(det);
+      B.rdet = f_add(rd.hi, rd.lo);
+      bad = !(det.hi != 0.f) || !isfinite(det.hi);
+      const df64 v = dd_sqrt(dd_abs(det)) * df64(1.0 / double(cfact(N)));
+      return f_add(v.hi, v.lo);
     }
   }
   double g[N > 0 ? N : 1][N > 0 ? N : 1];

@@ -117,6 +117,12 @@ constexpr int kBK = 32;  // K chunk of the products
 constexpr int kThreads = 256;
 constexpr int kMaxComposeRows = 46000;  // fully summed rows whose interchanges one CTA composes in shared memory
 
+// A shared-memory array of n values of T, declared as raw storage (float-float
+// has a constructor, which shared memory cannot run)
+#define SL_SHARED_ARRAY(T, name, n)                                     \
+  __shared__ __align__(16) unsigned char name##_raw[sizeof(T) * (n)]; \
+  T* name = reinterpret_cast<T*>(name##_raw)
+
 // ---------------------------------------------------------------------------
 // assembly
 // ---------------------------------------------------------------------------
@@ -382,7 +388,7 @@ __global__ void __launch_bounds__(kThreads) sl_tile_kernel(const FrontDesc* __re
   extern __shared__ __align__(16) unsigned char smraw[];
   T* Tt = reinterpret_cast<T*>(smraw);  // [TL][LD], column-major Tt[col * LD + row]
   T* Xs = Tt + TL * LD;                 // inverse under construction
-  __shared__ T s_val;
+  SL_SHARED_ARRAY(T, s_val, 1);
   const FrontDesc F = fd[list[blockIdx.x]];
   if (F.f <= k) return;
   const int b = min(TL, F.f - k);
@@ -407,10 +413,10 @@ __global__ void __launch_bounds__(kThreads) sl_tile_kernel(const FrontDesc* __re
         d = Num<T>::negative(d) ? -thresh : thresh;
       }
       Tt[j * LD + j] = d;
-      s_val = Num<T>::recip(d);
+      s_val[0] = Num<T>::recip(d);
     }
     __syncthreads();
-    const T rinv = s_val;
+    const T rinv = s_val[0];
     for (int i = j + 1 + tid; i < b; i += nt) Tt[j * LD + i] = Num<T>::mul(Tt[j * LD + i], rinv);
     __syncthreads();
     const int w = b - j - 1;
@@ -501,17 +507,25 @@ struct Vec16<df64> {
   }
 };
 
+// The operands of a tile step's product for one BM x BM output tile (mode as
+// above); false when the CTA has no tile.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) sl_gemm_kernel(const FrontDesc* __restrict__ fd,
-                                                           const int32_t* __restrict__ list, int k, int mode,
-                                                           T* __restrict__ pool, const T* __restrict__ tiles) {
+struct GemmTile {
+  const T* Xp;
+  int64_t ldx;
+  const T* Yp;
+  int64_t ldy;
+  T* Cp;
+  int64_t m, rlim, clim;
+  int b;
+};
+
+template <typename T>
+__device__ __forceinline__ bool gemm_tile(const FrontDesc& F, int k, int mode, T* pool, const T* tiles,
+                                          GemmTile<T>& g) {
   using C = SlCfg<T>;
-  constexpr int BM = C::BM, TM = C::TM, H = TM / 2, TL = C::TILE;
-  constexpr int BP = BM + 16 / int(sizeof(T));  // padded row of the B chunk, 16-byte aligned
-  __shared__ __align__(16) T As[kBK][BM];
-  __shared__ __align__(16) T Bs[kBK][BP];
-  const FrontDesc F = fd[list[blockIdx.y]];
-  if (F.f <= k) return;
+  constexpr int BM = C::BM, TL = C::TILE;
+  if (F.f <= k) return false;
   const int b = min(TL, F.f - k);
   const int64_t m = F.m;
   const int64_t rest = m - k - b;
@@ -526,52 +540,86 @@ __global__ void __launch_bounds__(kThreads) sl_gemm_kernel(const FrontDesc* __re
     rows = rest;
     cols = rest;
   }
-  if (rows <= 0 || cols <= 0) return;
+  if (rows <= 0 || cols <= 0) return false;
   const int64_t tr = (rows + BM - 1) / BM, tc = (cols + BM - 1) / BM;
   const int64_t tile = blockIdx.x;
-  if (tile >= tr * tc) return;
+  if (tile >= tr * tc) return false;
   const int64_t r0 = (tile % tr) * BM, c0 = (tile / tr) * BM;
   T* P = pool + F.off;
   const T* inv = tiles + F.tile_off + int64_t(k / TL) * 2 * TL * TL;
-  const T* Xp;
-  int64_t ldx;
-  const T* Yp;
-  int64_t ldy;
-  T* Cp;
   if (mode == 0) {
-    Xp = P + int64_t(k) * m + (k + b + r0);
-    ldx = m;
-    Yp = inv + TL * TL + c0 * TL;  // invU, ld TL
-    ldy = TL;
-    Cp = P + int64_t(k + c0) * m + (k + b + r0);
+    g.Xp = P + int64_t(k) * m + (k + b + r0);
+    g.ldx = m;
+    g.Yp = inv + TL * TL + c0 * TL;  // invU, ld TL
+    g.ldy = TL;
+    g.Cp = P + int64_t(k + c0) * m + (k + b + r0);
   } else if (mode == 1) {
-    Xp = inv + r0;  // invL, ld TL
-    ldx = TL;
-    Yp = P + (k + b + c0) * m + k;
-    ldy = m;
-    Cp = P + (k + b + c0) * m + (k + r0);
+    g.Xp = inv + r0;  // invL, ld TL
+    g.ldx = TL;
+    g.Yp = P + (k + b + c0) * m + k;
+    g.ldy = m;
+    g.Cp = P + (k + b + c0) * m + (k + r0);
   } else {
-    Xp = P + int64_t(k) * m + (k + b + r0);
-    ldx = m;
-    Yp = P + (k + b + c0) * m + k;
-    ldy = m;
-    Cp = P + (k + b + c0) * m + (k + b + r0);
+    g.Xp = P + int64_t(k) * m + (k + b + r0);
+    g.ldx = m;
+    g.Yp = P + (k + b + c0) * m + k;
+    g.ldy = m;
+    g.Cp = P + (k + b + c0) * m + (k + b + r0);
   }
+  g.m = m;
+  g.rlim = rows - r0;
+  g.clim = cols - c0;
+  g.b = b;
+  return true;
+}
+
+// TM x TM outputs of a thread written back (mode 2: subtracted)
+template <typename T, int BM, int TM>
+__device__ __forceinline__ void gemm_store(const GemmTile<T>& g, int mode, int tx, int ty, const T (&acc)[TM][TM]) {
+  constexpr int H = TM / 2;
+#pragma unroll
+  for (int j = 0; j < TM; ++j) {
+    const int c = (j < H ? tx * H + j : BM / 2 + tx * H + (j - H));
+    if (c >= g.clim) continue;
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      const int r = (i < H ? ty * H + i : BM / 2 + ty * H + (i - H));
+      if (r >= g.rlim) continue;
+      T* dst = g.Cp + int64_t(c) * g.m + r;
+      if (mode == 2)
+        *dst -= acc[i][j];
+      else
+        *dst = acc[i][j];
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) sl_gemm_kernel(const FrontDesc* __restrict__ fd,
+                                                           const int32_t* __restrict__ list, int k, int mode,
+                                                           T* __restrict__ pool, const T* __restrict__ tiles) {
+  using C = SlCfg<T>;
+  constexpr int BM = C::BM, TM = C::TM, H = TM / 2;
+  constexpr int BP = BM + 16 / int(sizeof(T));  // padded row of the B chunk, 16-byte aligned
+  __shared__ __align__(16) T As[kBK][BM];
+  __shared__ __align__(16) T Bs[kBK][BP];
+  GemmTile<T> g;
+  if (!gemm_tile<T>(fd[list[blockIdx.y]], k, mode, pool, tiles, g)) return;
+  const int b = g.b;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   T acc[TM][TM];
 #pragma unroll
   for (int i = 0; i < TM; ++i)
 #pragma unroll
     for (int j = 0; j < TM; ++j) acc[i][j] = T(0);
-  const int64_t rlim = rows - r0, clim = cols - c0;
   for (int q0 = 0; q0 < b; q0 += kBK) {
     for (int t = tid; t < BM * kBK; t += kThreads) {
       const int q = t / BM, r = t - q * BM;
-      As[q][r] = (r < rlim && q0 + q < b) ? Xp[int64_t(q0 + q) * ldx + r] : T(0);
+      As[q][r] = (r < g.rlim && q0 + q < b) ? g.Xp[int64_t(q0 + q) * g.ldx + r] : T(0);
     }
     for (int t = tid; t < BM * kBK; t += kThreads) {
       const int c = t / kBK, q = t - c * kBK;
-      Bs[q][c] = (c < clim && q0 + q < b) ? Yp[int64_t(c) * ldy + q0 + q] : T(0);
+      Bs[q][c] = (c < g.clim && q0 + q < b) ? g.Yp[int64_t(c) * g.ldy + q0 + q] : T(0);
     }
     __syncthreads();
 #pragma unroll 8
@@ -588,26 +636,9 @@ __global__ void __launch_bounds__(kThreads) sl_gemm_kernel(const FrontDesc* __re
     }
     __syncthreads();
   }
-#pragma unroll
-  for (int j = 0; j < TM; ++j) {
-    const int c = (j < H ? tx * H + j : BM / 2 + tx * H + (j - H));
-    if (c >= clim) continue;
-#pragma unroll
-    for (int i = 0; i < TM; ++i) {
-      const int r = (i < H ? ty * H + i : BM / 2 + ty * H + (i - H));
-      if (r >= rlim) continue;
-      T* dst = Cp + int64_t(c) * m + r;
-      if (mode == 2)
-        *dst -= acc[i][j];
-      else
-        *dst = acc[i][j];
-    }
-  }
+  gemm_store<T, BM, TM>(g, mode, tx, ty, acc);
 }
 
-// ---------------------------------------------------------------------------
-// solves: one CTA per front, the front's right-hand side in shared memory
-// ---------------------------------------------------------------------------
 // ---------------------------------------------------------------------------
 // solve: one CTA per row block (the rows of one tile) of every front of a
 // level. Tile solutions are published through per-tile flags: the producer
@@ -688,11 +719,11 @@ __global__ void __launch_bounds__(kSolveThreads) sl_forward_rows_kernel(
   using C = SlCfg<T>;
   constexpr int TL = C::TILE;
   constexpr int R = TL / 32;
-  __shared__ int s_item;
-  __shared__ T sy[TL];
-  __shared__ T part[kSolveThreads / 32][TL];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = kSolveThreads / 32;
+  __shared__ int s_item;
+  SL_SHARED_ARRAY(T, sy, TL);
+  SL_SHARED_ARRAY(T, part, NW * TL);  // [warp][row]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) s_item = atomicAdd(ticket, 1);
   __syncthreads();
   const int it = s_item;
@@ -727,7 +758,7 @@ __global__ void __launch_bounds__(kSolveThreads) sl_forward_rows_kernel(
     __syncthreads();
   }
 #pragma unroll
-  for (int q = 0; q < R; ++q) part[warp][lane + 32 * q] = acc[q];
+  for (int q = 0; q < R; ++q) part[warp * TL + lane + 32 * q] = acc[q];
   __syncthreads();
   // the assembled, interchanged right-hand side of the block's rows, less the panel sums
   if (tid < nr) {
@@ -744,7 +775,7 @@ __global__ void __launch_bounds__(kSolveThreads) sl_forward_rows_kernel(
     }
     T sum = T(0);
 #pragma unroll
-    for (int ww = 0; ww < NW; ++ww) sum += part[ww][tid];
+    for (int ww = 0; ww < NW; ++ww) sum += part[ww * TL + tid];
     v -= sum;
     if (diag)
       sy[tid] = v;
@@ -778,8 +809,8 @@ __global__ void __launch_bounds__(kSolveThreads) sl_backward_rows_kernel(
   constexpr int R = TL / 32;
   constexpr int NW = kSolveThreads / 32;
   __shared__ int s_item;
-  __shared__ T sx[TL];
-  __shared__ T part[NW][TL];
+  SL_SHARED_ARRAY(T, sx, TL);
+  SL_SHARED_ARRAY(T, part, NW * TL);  // [warp][row]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) s_item = atomicAdd(ticket, 1);
   __syncthreads();
@@ -830,12 +861,12 @@ __global__ void __launch_bounds__(kSolveThreads) sl_backward_rows_kernel(
     __syncthreads();
   }
 #pragma unroll
-  for (int q = 0; q < R; ++q) part[warp][lane + 32 * q] = acc[q];
+  for (int q = 0; q < R; ++q) part[warp * TL + lane + 32 * q] = acc[q];
   __syncthreads();
   if (tid < nr) {
     T z = ybuf[F.start + r0 + tid];
 #pragma unroll
-    for (int ww = 0; ww < NW; ++ww) z -= part[ww][tid];
+    for (int ww = 0; ww < NW; ++ww) z -= part[ww * TL + tid];
     sx[tid] = z;
   }
   __syncthreads();
@@ -1098,9 +1129,9 @@ fq_status factor_impl(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_
       const int64_t rest = std::max<int64_t>(0, maxm - k);
       const int64_t tl = (rest + C::BM - 1) / C::BM;
       if (tl > 0) {
-        sl_gemm_kernel<T><<<dim3(unsigned(tl), unsigned(nl)), kThreads, 0, st>>>(fd, list, k, 0, pool, tiles);
-        sl_gemm_kernel<T><<<dim3(unsigned(tl), unsigned(nl)), kThreads, 0, st>>>(fd, list, k, 1, pool, tiles);
-        sl_gemm_kernel<T><<<dim3(unsigned(tl * tl), unsigned(nl)), kThreads, 0, st>>>(fd, list, k, 2, pool, tiles);
+        const unsigned grids[3] = {unsigned(tl), unsigned(tl), unsigned(tl * tl)};
+        for (int mode = 0; mode < 3; ++mode)
+          sl_gemm_kernel<T><<<dim3(grids[mode], unsigned(nl)), kThreads, 0, st>>>(fd, list, k, mode, pool, tiles);
         ctx->launches += 3;
       }
     }
