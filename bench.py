@@ -878,6 +878,19 @@ def batch_study(args, compact: bool):
             mat.reassemble(m)
 
     ms_dropin = timed(dropin, max(1, reps // 2))
+    # the element pass as one fused launch over every class (same values), at
+    # each grid, against the tuned per-class launches above
+    fused = {"registers_per_thread": batch.fused_registers(), "ms_by_grid": {}}
+    for per_sm in (0, 2, 4, 8):
+        batch.set_element_launch(True, per_sm * 152)
+        for _ in range(3):
+            batch.assemble(check=False)
+        fused["ms_by_grid"][f"{per_sm}_per_sm" if per_sm else "one_thread_per_cell"] = timed(
+            lambda: batch.assemble(check=False), reps)
+    batch.set_element_launch(False)
+    fused["best_ms"] = min(fused["ms_by_grid"].values())
+    fused["cells_per_s"] = info["cells"] / (fused["best_ms"] * 1e-3)
+    fused["launches"] = 2
     cells = info["cells"]
     out = {"metric": "assembled cells/s (batched vs per-mesh launches)", "meshes": len(meshes),
            "form": "hdif_gram(k) = M_k + dif_both(k+1), FP64 values (float-float compute)",
@@ -890,6 +903,7 @@ def batch_study(args, compact: bool):
            "batched": {"ms": ms_batched, "cells_per_s": cells / (ms_batched * 1e-3)},
            "per_mesh_launches": {"ms": ms_launches, "cells_per_s": cells / (ms_launches * 1e-3)},
            "per_mesh_dropin_reassemble": {"ms": ms_dropin, "cells_per_s": cells / (ms_dropin * 1e-3)},
+           "fused_single_element_launch": fused,
            "setup_s": {"meshes": mesh_s, "plans": plan_s, "tune": tune_s},
            "l2": "flushed before every timed assembly (256 MiB write)"}
     for m in mats:

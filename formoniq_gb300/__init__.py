@@ -200,6 +200,8 @@ _SIGNATURES = {
     "fq_batch_create": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_P), _I32P, ctypes.c_int, ctypes.POINTER(_P)]),
     "fq_batch_tune": (ctypes.c_int, [_P, ctypes.c_int]),
     "fq_batch_set_launch": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "fq_batch_set_element_launch": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
+    "fq_batch_fused_registers": (ctypes.c_int, []),
     "fq_batch_assemble": (ctypes.c_int, [_P, ctypes.c_int]),
     "fq_batch_assemble_per_mesh": (ctypes.c_int, [_P, ctypes.c_int]),
     "fq_batch_info": (ctypes.c_int, [_P, _I64P, _I64P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
@@ -1015,6 +1017,15 @@ class Batch:
     def set_launch(self, element_grid: int = 0, scatter_tps: int = 1, scatter_grid: int = 0):
         self.ctx.check(self.ctx.L.fq_batch_set_launch(self.h, element_grid, scatter_tps, scatter_grid),
                        "fq_batch_set_launch")
+
+    def set_element_launch(self, fused: bool, grid: int = 0):
+        """The element pass as one fused launch over every class, or one per class
+        (fq_batch_set_element_launch)."""
+        self.ctx.check(self.ctx.L.fq_batch_set_element_launch(self.h, int(bool(fused)), int(grid)),
+                       "fq_batch_set_element_launch")
+
+    def fused_registers(self) -> int:
+        return int(self.ctx.L.fq_batch_fused_registers())
 
     def assemble(self, check: bool = True):
         self.ctx.check(self.ctx.L.fq_batch_assemble(self.h, int(check)), "fq_batch_assemble")

@@ -31,6 +31,10 @@
 namespace fq {
 
 fq_status get_plan(fq_ctx* ctx, fq_mesh* m, int kind, int grade, int row_bc, int col_bc, Plan** out);
+bool batch_fused_supported(int kind, int dim, int grade);
+void launch_batch_fused_hdif(const ElemFusedEntry* ent, int n, int64_t total, int grid, int* status,
+                             cudaStream_t st);
+int batch_fused_registers();
 
 struct ScatterBatchEntry {
   int64_t begin, nslots;
@@ -279,6 +283,10 @@ struct fq_batch {
   int64_t real_slots = 0;
   int64_t total_up = 0;  // padded upper-slot index space (0: some plan is not symmetric)
   int tps = 1, sgrid = 0;  // tps 0: warp-staged scatter, -1: symmetric
+  // the element pass as one fused launch over every class (fq_batch_fused.cu)
+  bool fused = false;
+  int fgrid = 0;
+  DevBuf ftable;  // ElemFusedEntry[], members in order
   cudaGraphExec_t graph = nullptr;
   ~fq_batch() {
     if (graph) cudaGraphExecDestroy(graph);
@@ -290,7 +298,11 @@ namespace {
 fq_status enqueue_batch(fq_batch* B) {
   fq_ctx* ctx = B->ctx;
   cudaStream_t st = ctx->stream;
+  if (B->fused)
+    launch_batch_fused_hdif(B->ftable.as<ElemFusedEntry>(), int(B->members.size()), B->total_cells, B->fgrid,
+                            ctx->status.as<int>(), st);
   for (auto& c : B->classes) {
+    if (B->fused) break;
     ElemArgs a;
     a.ncells = 0;
     a.lengths = nullptr;
@@ -534,6 +546,43 @@ fq_status fq_batch_set_launch(fq_batch* B, int element_grid, int scatter_tps, in
   B->sgrid = scatter_grid;
   return capture(B);
 }
+
+fq_status fq_batch_set_element_launch(fq_batch* B, int fused, int grid) {
+  if (!B || grid < 0) return FQ_INVALID_ARG;
+  fq_ctx* ctx = B->ctx;
+  if (fused) {
+    for (auto& mb : B->members)
+      if (!batch_fused_supported(B->kind, mb.mesh->dim, mb.grade))
+        return set_error(ctx, FQ_UNSUPPORTED, "the fused element launch covers hdif_gram batches of dimensions 2-4");
+    if (!B->ftable.p) {
+      std::vector<ElemFusedEntry> tab;
+      int64_t begin = 0;
+      for (auto& mb : B->members) {
+        ElemFusedEntry e{};
+        e.begin = begin;
+        e.ncells = mb.mesh->ncells;
+        e.lengths = mb.mesh->lengths.as<double>();
+        e.cell_edges = mb.mesh->cell_faces[1].as<int32_t>();
+        e.out = B->elem.as<df64>() + mb.elem_off;
+        e.nent = int(mb.plan->nent);
+        e.dim = mb.mesh->dim;
+        e.grade = mb.grade;
+        tab.push_back(e);
+        begin += e.ncells;
+      }
+      FQ_TRY(B->ftable.alloc(ctx, std::max<size_t>(tab.size(), 1) * sizeof(ElemFusedEntry)));
+      if (!tab.empty())
+        FQ_CUDA(ctx, cudaMemcpyAsync(B->ftable.p, tab.data(), tab.size() * sizeof(ElemFusedEntry),
+                                     cudaMemcpyHostToDevice, ctx->stream));
+      FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+  }
+  B->fused = fused != 0;
+  B->fgrid = grid;
+  return capture(B);
+}
+
+int fq_batch_fused_registers(void) { return batch_fused_registers(); }
 
 fq_status fq_batch_assemble(fq_batch* B, int check) {
   if (!B) return FQ_INVALID_ARG;

@@ -234,6 +234,28 @@ FQ_HD void element_entries(const Bary<N, T>& B, T vol, double param, Put&& put) 
   }
 }
 
+// One cell of an element program: squared lengths in, the packed entries out
+// ([nent][nc] layout of its mesh's buffer).
+template <int N, int K, int KIND, typename T>
+__device__ __forceinline__ void element_cell(const double* lengths, const int32_t* cell_edges, int64_t nc,
+                                             int64_t cell, void* outp, int nent, double param, int* status) {
+  constexpr int NE = cbinom(N + 1, 2);
+  double s[NE > 0 ? NE : 1];
+#pragma unroll
+  for (int e = 0; e < NE; ++e) s[e] = __ldg(lengths + __ldg(cell_edges + int64_t(e) * nc + cell));
+  Bary<N, T> B;
+  bool bad = false;
+  const T vol = cell_bary<N, T>(s, B, bad);
+  if (bad) atomicOr(status, 1);
+  T* out = static_cast<T*>(outp);
+  element_entries<N, K, KIND, T>(B, vol, param, [&](int e, T v) {
+    if (e < nent)
+      out[int64_t(e) * nc + cell] = v;
+    else
+      atomicOr(status, 2);
+  });
+}
+
 template <int N, int K, int KIND, typename T>
 __global__ void __launch_bounds__(128) element_kernel(ElemArgs a) {
   const int64_t total = a.batch ? a.total : a.ncells;
@@ -259,11 +281,11 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs a) {
       cell_edges = b.cell_edges;
       outp = b.out;
     }
-    constexpr int NE = cbinom(N + 1, 2);
-    double s[NE > 0 ? NE : 1];
-#pragma unroll
-    for (int e = 0; e < NE; ++e) s[e] = __ldg(lengths + __ldg(cell_edges + int64_t(e) * nc + cell));
     if constexpr (KIND == EK_METRIC) {
+      constexpr int NE = cbinom(N + 1, 2);
+      double s[NE > 0 ? NE : 1];
+#pragma unroll
+      for (int e = 0; e < NE; ++e) s[e] = __ldg(lengths + __ldg(cell_edges + int64_t(e) * nc + cell));
       double gm[N > 0 ? N : 1][N > 0 ? N : 1];
       double ginv[N > 0 ? N : 1][N > 0 ? N : 1];
       regge_metric<N>(s, gm);
@@ -279,18 +301,7 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs a) {
       if (a.det_out) a.det_out[cell] = det;
       if (a.vol_out) a.vol_out[cell] = vol;
     } else {
-      Bary<N, T> B;
-      bool bad = false;
-      const T vol = cell_bary<N, T>(s, B, bad);
-      if (bad) atomicOr(a.status, 1);
-      T* out = static_cast<T*>(outp);
-      const int nent = a.nent;
-      element_entries<N, K, KIND, T>(B, vol, a.param, [&](int e, T v) {
-        if (e < nent)
-          out[int64_t(e) * nc + cell] = v;
-        else
-          atomicOr(a.status, 2);
-      });
+      element_cell<N, K, KIND, T>(lengths, cell_edges, nc, cell, outp, a.nent, a.param, a.status);
     }
   }
 }

@@ -39,6 +39,17 @@ struct ElemBatchEntry {
   void* out;
 };
 
+// One mesh of the fused batch element launch (every class in one launch): as
+// ElemBatchEntry, plus the mesh's program (dimension, grade) and its entries
+// per cell.
+struct ElemFusedEntry {
+  int64_t begin, ncells;
+  const double* lengths;
+  const int32_t* cell_edges;
+  void* out;
+  int nent, dim, grade, pad;
+};
+
 // Arguments of the per-cell kernel (device pointers).
 struct ElemArgs {
   int64_t ncells;

@@ -506,6 +506,15 @@ fq_status fq_batch_set_launch(fq_batch* batch, int element_grid, int scatter_tps
 /* One assembly of the whole batch (one graph launch). check != 0 waits and
  * checks the status words (degenerate cells; a slot that summed exact zeros
  * only, which the reference would drop: FQ_UNSUPPORTED). */
+/* The element pass as one fused launch over every (dimension, grade) class
+ * (fused = 1; a grid-stride grid of `grid` CTAs, 0 = one thread per cell) or
+ * one launch per class (fused = 0, the default). The fused kernel covers
+ * hdif_gram batches of dimensions 2-4 (FQ_UNSUPPORTED otherwise); it runs every
+ * class at the register allocation of the heaviest program. Values are the
+ * same bit for bit either way. */
+fq_status fq_batch_set_element_launch(fq_batch* batch, int fused, int grid);
+/* Registers per thread of the fused element kernel (-1 if unknown). */
+int fq_batch_fused_registers(void);
 fq_status fq_batch_assemble(fq_batch* batch, int check);
 /* The same assembly as two launches per mesh (the per-mesh baseline). */
 fq_status fq_batch_assemble_per_mesh(fq_batch* batch, int check);

@@ -88,3 +88,30 @@ def test_batch_matches_the_oracle(oracle, ctx):
     batch.close()
     for m in meshes:
         m.close()
+
+
+def test_fused_element_launch_equals_per_class_launches(ctx):
+    """One fused element launch over every (dimension, grade) class gives the
+    per-class launches' values bit for bit (the same programs on the same
+    cells); other forms are refused."""
+    specs = SPECS + [(4, 2)]
+    grades = GRADES + [4]
+    meshes = meshes_of(ctx, specs)
+    batch = fq.Batch(ctx, meshes, grades, fq.FQ_BATCH_HDIF)
+    batch.assemble()
+    ref = [batch.to_scipy(i).data.copy() for i in range(len(meshes))]
+    assert batch.fused_registers() > 0
+    for grid in (0, 2 * 152):
+        batch.set_element_launch(True, grid)
+        batch.assemble()
+        for i in range(len(meshes)):
+            np.testing.assert_array_equal(batch.to_scipy(i).data, ref[i])
+    batch.set_element_launch(False)
+    batch.close()
+    mass = fq.Batch(ctx, meshes, grades, fq.FQ_BATCH_MASS)
+    with pytest.raises(fq.FqError) as e:
+        mass.set_element_launch(True)
+    assert e.value.name == "FQ_UNSUPPORTED"
+    mass.close()
+    for m in meshes:
+        m.close()
