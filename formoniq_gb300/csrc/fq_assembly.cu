@@ -977,6 +977,25 @@ int launch_element(int n, int grade, int kind, int mode, const ElemArgs& a, cuda
   }
 }
 
+int launch_element_multi(int n, int mode, const ElemMultiArgs& a, cudaStream_t st) {
+  auto typed = [&](auto tag) -> int {
+    using T = decltype(tag);
+    switch (n) {
+      case 1:
+        return launch_multi_typed<1, T>(a, st);
+      case 2:
+        return launch_multi_typed<2, T>(a, st);
+      case 3:
+        return launch_multi_typed<3, T>(a, st);
+      default:
+        return -1;
+    }
+  };
+  if (mode == FQ_FP32) return typed(float());
+  if (mode == FQ_FP64_IEEE) return typed(double());
+  return typed(df64());
+}
+
 fq_status element_pass(fq_ctx* ctx, fq_mesh* m, int kind, int grade, int mode, double param, DevBuf& buf,
                        int nent) {
   if (!m->has_lengths) return set_error(ctx, FQ_INVALID_ARG, "mesh has no edge lengths");
@@ -1038,6 +1057,72 @@ static fq_status assemble_launch(fq_ctx* ctx, fq_matrix* m, cudaEvent_t* ev, boo
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[2], ctx->stream));
   launch_scatter(p, mesh->elem.p, m->full_values.p, with_flags ? m->zero_flags.as<uint8_t>() : nullptr, zc,
                  element_buffer_mode(mesh->dim, m->kind, mode), ctx->stream, ctx->scatter_shape);
+  if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[3], ctx->stream));
+  if (p.nslots > 0) ctx->launches++;
+  return FQ_OK;
+}
+
+// Matrices per multi-program element pass of a device multi-matrix assembly
+// (measured on the 3D 32^3 step: passes of two matrices lose to single-matrix
+// passes, since each runs the multi-program kernel's register allocation).
+constexpr int kMultiChunk = kMultiPrograms;
+
+// Whether the matrices can share one multi-program element pass: 2 to
+// kMultiPrograms mass / dif_both matrices of one mesh of dimension 1-3 in one
+// precision, each with slots.
+static bool multi_fusable(fq_matrix* const* mats, int count) {
+  if (count < 2 || count > kMultiPrograms || !mats[0]->plan) return false;
+  const fq_mesh* mesh = mats[0]->mesh;
+  const int mode = mats[0]->precision;
+  if (mesh->dim < 1 || mesh->dim > 3 || !mesh->has_lengths) return false;
+  for (int i = 0; i < count; ++i) {
+    const fq_matrix* m = mats[i];
+    if (!m->plan || m->mesh != mesh || m->precision != mode || m->plan->nslots <= 0) return false;
+    if (!(m->kind == EK_MASS || (m->kind == EK_DIF_BOTH && m->grade >= 1)) || m->grade > mesh->dim) return false;
+    if (element_buffer_mode(mesh->dim, m->kind, mode) != mode) return false;
+  }
+  return true;
+}
+
+// The multi-program element pass of fusable matrices into their own buffers.
+static fq_status multi_element_pass(fq_ctx* ctx, fq_matrix* const* mats, int count) {
+  fq_mesh* mesh = mats[0]->mesh;
+  const int mode = mats[0]->precision;
+  const size_t w = mode == FQ_FP32 ? 4 : 8;
+  ElemMultiArgs a{};
+  a.ncells = mesh->ncells;
+  a.lengths = mesh->lengths.as<double>();
+  a.cell_edges = mesh->cell_faces[1].as<int32_t>();
+  a.status = ctx->status.as<int>();
+  a.nprog = count;
+  for (int i = 0; i < count; ++i) {
+    fq_matrix* m = mats[i];
+    const size_t need = size_t(std::max(m->plan->nent, 1)) * size_t(std::max<int64_t>(mesh->ncells, 1)) * w;
+    if (m->elem.bytes < need) FQ_TRY(m->elem.alloc(ctx, need));
+    a.kind[i] = m->kind;
+    a.grade[i] = m->grade;
+    a.nent[i] = m->plan->nent;
+    a.out[i] = m->elem.p;
+  }
+  if (launch_element_multi(mesh->dim, mode, a, ctx->stream) != 0)
+    return set_error(ctx, FQ_UNSUPPORTED, "no multi-program element pass for this dimension");
+  ctx->launches++;
+  FQ_CUDA(ctx, cudaGetLastError());
+  return FQ_OK;
+}
+
+// The scatter of a matrix whose element pass has run into `elem`.
+static fq_status scatter_launch(fq_ctx* ctx, fq_matrix* m, const void* elem, cudaEvent_t* ev) {
+  Plan& p = *m->plan;
+  const int mode = m->precision;
+  const size_t w = mode == FQ_FP32 ? 4 : 8;
+  if (m->full_values.bytes < size_t(std::max<int64_t>(p.nslots, 1)) * w)
+    FQ_TRY(m->full_values.alloc(ctx, std::max<int64_t>(p.nslots, 1) * w));
+  if (m->zero_flags.bytes < size_t(std::max<int64_t>(p.nslots, 1)))
+    FQ_TRY(m->zero_flags.alloc(ctx, std::max<int64_t>(p.nslots, 1)));
+  if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[2], ctx->stream));
+  launch_scatter(p, elem, m->full_values.p, nullptr, ctx->status.as<int>(),
+                 element_buffer_mode(m->mesh->dim, m->kind, mode), ctx->stream, ctx->scatter_shape);
   if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[3], ctx->stream));
   if (p.nslots > 0) ctx->launches++;
   return FQ_OK;
@@ -1117,8 +1202,28 @@ fq_status assemble_many(fq_ctx* ctx, fq_matrix* const* mats, int count) {
     }
   }
   FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), ctx->stream));
-  for (int i = 0; i < count; ++i)
-    if (mats[i]->plan) FQ_TRY(assemble_launch(ctx, mats[i], prof ? ctx->prof_events.data() + 4 * i : nullptr));
+  for (int i0 = 0; i0 < count; i0 += kMultiChunk) {
+    const int nc = std::min(kMultiChunk, count - i0);
+    if (multi_fusable(mats + i0, nc)) {
+      // one element pass for the chunk (the metric once per cell), then its scatters;
+      // the pass's time is the chunk's first matrix's element time, the others' zero
+      cudaEvent_t* ev = prof ? ctx->prof_events.data() + 4 * i0 : nullptr;
+      if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[0], ctx->stream));
+      FQ_TRY(multi_element_pass(ctx, mats + i0, nc));
+      if (ev) FQ_CUDA(ctx, cudaEventRecord(ev[1], ctx->stream));
+      for (int i = i0; i < i0 + nc; ++i) {
+        cudaEvent_t* e = prof ? ctx->prof_events.data() + 4 * i : nullptr;
+        if (e && i > i0) {
+          FQ_CUDA(ctx, cudaEventRecord(e[0], ctx->stream));
+          FQ_CUDA(ctx, cudaEventRecord(e[1], ctx->stream));
+        }
+        FQ_TRY(scatter_launch(ctx, mats[i], mats[i]->elem.p, e));
+      }
+    } else {
+      for (int i = i0; i < i0 + nc; ++i)
+        if (mats[i]->plan) FQ_TRY(assemble_launch(ctx, mats[i], prof ? ctx->prof_events.data() + 4 * i : nullptr));
+    }
+  }
   FQ_CUDA(ctx, cudaMemcpyAsync(ctx->host_status, ctx->status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost,
                                ctx->stream));
   FQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1158,6 +1263,8 @@ fq_status assemble_host_many(fq_ctx* ctx, fq_mesh* mesh, const double* lengths, 
   mesh->has_lengths = true;
   FQ_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, 8 * sizeof(int), st));
   std::vector<char> streamed(size_t(count), 0);
+  // per matrix (no multi-program pass): the first download starts after the
+  // first matrix's scatter, not after one pass over every program
   for (int i = 0; i < count; ++i) {
     fq_matrix* m = mats[i];
     if (!m->plan) continue;

@@ -12,6 +12,8 @@
 
 namespace fq {
 
+constexpr int kElemMultiThreads = 128;
+
 template <int N, int K, int KIND, typename T>
 int launch_one_t(const ElemArgs& a, cudaStream_t st) {
   constexpr int threads = 128;
@@ -68,6 +70,14 @@ int launch_k_t(int kind, const ElemArgs& a, cudaStream_t st) {
       break;
   }
   return -1;
+}
+
+template <int N, typename T>
+int launch_multi_typed(const ElemMultiArgs& a, cudaStream_t st) {
+  if (a.ncells <= 0) return 0;
+  const unsigned blocks = unsigned((a.ncells + kElemMultiThreads - 1) / kElemMultiThreads);
+  element_multi_kernel<N, T><<<blocks, kElemMultiThreads, 0, st>>>(a);
+  return 0;
 }
 
 template <int N, typename T>

@@ -306,8 +306,58 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs a) {
   }
 }
 
+// The multi-program pass (ElemMultiArgs): one thread per cell, the cell's
+// barycentric Gramian once, then each program's entries into its buffer.
+// The Gramian and volume wait in shared memory between programs, so that they
+// do not hold registers through every program.
+template <int N, typename T>
+__global__ void __launch_bounds__(128) element_multi_kernel(ElemMultiArgs a) {
+  __shared__ __align__(16) unsigned char stage_raw[sizeof(Bary<N, T>) * 128];
+  __shared__ __align__(16) unsigned char vol_raw[sizeof(T) * 128];
+  Bary<N, T>& Bsh = reinterpret_cast<Bary<N, T>*>(stage_raw)[threadIdx.x];
+  T& vsh = reinterpret_cast<T*>(vol_raw)[threadIdx.x];
+  const int64_t nc = a.ncells;
+  for (int64_t cell = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; cell < nc;
+       cell += int64_t(gridDim.x) * blockDim.x) {
+    {
+      constexpr int NE = cbinom(N + 1, 2);
+      double s[NE > 0 ? NE : 1];
+#pragma unroll
+      for (int e = 0; e < NE; ++e) s[e] = __ldg(a.lengths + __ldg(a.cell_edges + int64_t(e) * nc + cell));
+      Bary<N, T> B;
+      bool bad = false;
+      vsh = cell_bary<N, T>(s, B, bad);
+      Bsh = B;
+      if (bad) atomicOr(a.status, 1);
+    }
+    for (int p = 0; p < a.nprog; ++p) {
+      // reloaded per program: the programs' stores go through generic pointers,
+      // which the compiler cannot tell from this shared-memory copy
+      const Bary<N, T> B = Bsh;
+      const T vol = vsh;
+      T* out = static_cast<T*>(a.out[p]);
+      const int nent = a.nent[p];
+      auto put = [&](int e, T v) {
+        if (e < nent)
+          out[int64_t(e) * nc + cell] = v;
+        else
+          atomicOr(a.status, 2);
+      };
+      const int key = a.kind[p] * 8 + a.grade[p];
+      static_for<N + 1>([&](auto KK) {
+        constexpr int K = decltype(KK)::value;
+        if (key == EK_MASS * 8 + K) element_entries<N, K, EK_MASS, T>(B, vol, 0.0, put);
+        if constexpr (K >= 1)
+          if (key == EK_DIF_BOTH * 8 + K) element_entries<N, K, EK_DIF_BOTH, T>(B, vol, 0.0, put);
+      });
+    }
+  }
+}
+
 // Launch helper for one dimension and arithmetic type, every program and grade.
 template <int N, typename T>
 int launch_typed(int K, int kind, const ElemArgs& a, cudaStream_t st);
+template <int N, typename T>
+int launch_multi_typed(const ElemMultiArgs& a, cudaStream_t st);
 
 }  // namespace fq

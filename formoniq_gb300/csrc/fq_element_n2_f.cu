@@ -3,4 +3,5 @@
 
 namespace fq {
 template int launch_typed<2, float>(int K, int kind, const ElemArgs& a, cudaStream_t st);
+template int launch_multi_typed<2, float>(const ElemMultiArgs& a, cudaStream_t st);
 }  // namespace fq

@@ -147,6 +147,8 @@ struct fq_matrix {
   fq::DevBuf row_ptr, col_idx, values;
   // topological-pattern values and flags before compaction
   fq::DevBuf full_values, zero_flags;
+  // own element buffer, for the multi-program pass of a multi-matrix assembly
+  fq::DevBuf elem;
 };
 
 struct fq_ctx {

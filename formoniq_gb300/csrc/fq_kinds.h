@@ -50,6 +50,20 @@ struct ElemFusedEntry {
   int nent, dim, grade, pad;
 };
 
+// Several element programs of one mesh in one pass: each cell's metric,
+// inverse and barycentric Gramian computed once for all of them. Programs:
+// EK_MASS or EK_DIF_BOTH at their grades, each into its own buffer.
+constexpr int kMultiPrograms = 4;
+struct ElemMultiArgs {
+  int64_t ncells;
+  const double* lengths;
+  const int32_t* cell_edges;
+  int* status;
+  int nprog;
+  int kind[kMultiPrograms], grade[kMultiPrograms], nent[kMultiPrograms];
+  void* out[kMultiPrograms];
+};
+
 // Arguments of the per-cell kernel (device pointers).
 struct ElemArgs {
   int64_t ncells;
