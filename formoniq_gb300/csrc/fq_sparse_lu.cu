@@ -96,6 +96,7 @@ struct SlCfg<float> {
   static constexpr int ROWS = 256;    // rows of a tournament leaf or merge
   static constexpr int BM = 128;      // product tile (BM x BM outputs per CTA)
   static constexpr int TM = 8;        // outputs per thread and dimension
+  static constexpr int MINB = 2;      // resident product CTAs per SM the registers allow
 };
 template <>
 struct SlCfg<double> {
@@ -103,6 +104,7 @@ struct SlCfg<double> {
   static constexpr int ROWS = 128;
   static constexpr int BM = 64;
   static constexpr int TM = 4;
+  static constexpr int MINB = 4;
 };
 template <>
 struct SlCfg<df64> {
@@ -110,6 +112,7 @@ struct SlCfg<df64> {
   static constexpr int ROWS = 128;
   static constexpr int BM = 64;
   static constexpr int TM = 4;
+  static constexpr int MINB = 4;
 };
 static_assert(SlCfg<float>::TILE <= kTile && SlCfg<double>::TILE <= kTile, "tile store sized for kTile");
 
@@ -595,14 +598,14 @@ __device__ __forceinline__ void gemm_store(const GemmTile<T>& g, int mode, int t
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) sl_gemm_kernel(const FrontDesc* __restrict__ fd,
+__global__ void __launch_bounds__(kThreads, SlCfg<T>::MINB) sl_gemm_kernel(const FrontDesc* __restrict__ fd,
                                                            const int32_t* __restrict__ list, int k, int mode,
                                                            T* __restrict__ pool, const T* __restrict__ tiles) {
   using C = SlCfg<T>;
   constexpr int BM = C::BM, TM = C::TM, H = TM / 2;
   constexpr int BP = BM + 16 / int(sizeof(T));  // padded row of the B chunk, 16-byte aligned
-  __shared__ __align__(16) T As[kBK][BM];
-  __shared__ __align__(16) T Bs[kBK][BP];
+  SL_SHARED_ARRAY(T, As, kBK * BM);  // [q][row]
+  SL_SHARED_ARRAY(T, Bs, kBK * BP);  // [q][col], padded rows
   GemmTile<T> g;
   if (!gemm_tile<T>(fd[list[blockIdx.y]], k, mode, pool, tiles, g)) return;
   const int b = g.b;
@@ -615,20 +618,20 @@ __global__ void __launch_bounds__(kThreads) sl_gemm_kernel(const FrontDesc* __re
   for (int q0 = 0; q0 < b; q0 += kBK) {
     for (int t = tid; t < BM * kBK; t += kThreads) {
       const int q = t / BM, r = t - q * BM;
-      As[q][r] = (r < g.rlim && q0 + q < b) ? g.Xp[int64_t(q0 + q) * g.ldx + r] : T(0);
+      As[q * BM + r] = (r < g.rlim && q0 + q < b) ? g.Xp[int64_t(q0 + q) * g.ldx + r] : T(0);
     }
     for (int t = tid; t < BM * kBK; t += kThreads) {
       const int c = t / kBK, q = t - c * kBK;
-      Bs[q][c] = (c < g.clim && q0 + q < b) ? g.Yp[int64_t(c) * g.ldy + q0 + q] : T(0);
+      Bs[q * BP + c] = (c < g.clim && q0 + q < b) ? g.Yp[int64_t(c) * g.ldy + q0 + q] : T(0);
     }
     __syncthreads();
 #pragma unroll 8
     for (int q = 0; q < kBK; ++q) {
       T av[TM], bv[TM];
-      Vec16<T>::load(&As[q][ty * H], av);
-      Vec16<T>::load(&As[q][BM / 2 + ty * H], av + H);
-      Vec16<T>::load(&Bs[q][tx * H], bv);
-      Vec16<T>::load(&Bs[q][BM / 2 + tx * H], bv + H);
+      Vec16<T>::load(As + q * BM + ty * H, av);
+      Vec16<T>::load(As + q * BM + BM / 2 + ty * H, av + H);
+      Vec16<T>::load(Bs + q * BP + tx * H, bv);
+      Vec16<T>::load(Bs + q * BP + BM / 2 + tx * H, bv + H);
 #pragma unroll
       for (int i = 0; i < TM; ++i)
 #pragma unroll
