@@ -252,7 +252,7 @@ __device__ void gepp_select(T* blk, int ld, int* idx, int rows, int b) {
       const int w = rows - j - 1, c = b - j - 1;
       for (int t = tid; t < w * c; t += nt) {
         const int l = j + 1 + t / w, i = j + 1 + t % w;
-        blk[l * ld + i] -= blk[j * ld + i] * blk[l * ld + j];
+        blk[l * ld + i] = Num<T>::fma(-blk[j * ld + i], blk[l * ld + j], blk[l * ld + i]);
       }
     }
     __syncthreads();
@@ -443,7 +443,7 @@ __global__ void __launch_bounds__(kThreads) sl_tile_kernel(const FrontDesc* __re
     const int w = b - j - 1;
     for (int t = tid; t < w * w; t += nt) {
       const int l = j + 1 + t / w, i = j + 1 + t % w;
-      Tt[l * LD + i] -= Tt[j * LD + i] * Tt[l * LD + j];
+      Tt[l * LD + i] = Num<T>::fma(-Tt[j * LD + i], Tt[l * LD + j], Tt[l * LD + i]);
     }
     __syncthreads();
   }
@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(kThreads) sl_tile_kernel(const FrontDesc* __re
     Xs[j * LD + j] = T(1);
     for (int i = j + 1; i < b; ++i) {
       T s = T(0);
-      for (int l = j; l < i; ++l) s += Tt[l * LD + i] * Xs[j * LD + l];
+      for (int l = j; l < i; ++l) s = Num<T>::fma(Tt[l * LD + i], Xs[j * LD + l], s);
       Xs[j * LD + i] = -s;
     }
   }
@@ -479,7 +479,7 @@ __global__ void __launch_bounds__(kThreads) sl_tile_kernel(const FrontDesc* __re
     Xs[j * LD + j] = Num<T>::recip(Tt[j * LD + j]);
     for (int i = j - 1; i >= 0; --i) {
       T s = T(0);
-      for (int l = i + 1; l <= j; ++l) s += Tt[l * LD + i] * Xs[j * LD + l];
+      for (int l = i + 1; l <= j; ++l) s = Num<T>::fma(Tt[l * LD + i], Xs[j * LD + l], s);
       Xs[j * LD + i] = Num<T>::div(-s, Tt[i * LD + i]);
     }
   }
