@@ -574,3 +574,32 @@ def test_lu_finishes_an_unconverged_minres(oracle, ctx, which, kuhn):
         x = np.concatenate([sigma, u])
         assert np.linalg.norm(x - x_o[:ns + nu]) / np.linalg.norm(x_o) < 1e-9
     mesh.close()
+
+
+@pytest.mark.parametrize("precision", [fq.FQ_FP64, fq.FQ_FP64_IEEE, fq.FQ_FP32])
+@pytest.mark.parametrize("dim,nb", [(1, 9), (2, 6), (3, 4)])
+def test_multi_matrix_assembly_shares_one_element_pass(oracle, ctx, precision, dim, nb):
+    """fq_reassemble_many of up to four mass / dif_both matrices of one mesh
+    runs one element pass for all of them (the cell's metric once). Its
+    matrices equal the per-matrix assembly (bit for bit in float-float, whose
+    operations are never contracted; to rounding otherwise) and the oracle."""
+    cx, mesh, lengths, _ = make_pair(oracle, ctx, dim, nb)
+    forms = [("mass", 1), ("mass", min(2, dim)), ("dif_both", 1), ("dif_both", dim)][:4]
+    gwc = fq.WhitneyComplex(mesh, precision=precision)
+    owc = oracle.WhitneyComplex(cx, lengths)
+    many = [getattr(gwc, name)(k) for name, k in forms]
+    fq.Matrix.reassemble_many(many)
+    tol = FP32_TOL if precision == fq.FQ_FP32 else FP64_TOL
+    for (name, k), m in zip(forms, many):
+        single = getattr(fq.WhitneyComplex(mesh, precision=precision), name)(k)
+        single.reassemble(mesh)
+        a, b = m.to_scipy(), single.to_scipy()
+        csr_equal_pattern(a, b)
+        if precision == fq.FQ_FP64:
+            np.testing.assert_array_equal(a.data, b.data)
+        else:
+            assert rel_frob(a, b) < (1e-6 if precision == fq.FQ_FP32 else 1e-15)
+        assert rel_frob(a, getattr(owc, name)(k)) < tol
+        single.close()
+        m.close()
+    mesh.close()
