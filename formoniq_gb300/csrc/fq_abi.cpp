@@ -411,7 +411,7 @@ static constexpr int64_t kLuFallbackIters = 300;
 // converge; report.refinements = 1 then). The factors stay for the next solve
 // on the same values.
 static fq_status mixed_direct(fq_mixed* P, const double* rhs, double* x, double rtol, int64_t max_iters,
-                              fq_report* rep) {
+                              fq_report* rep, bool float_float_first = false) {
   fq_ctx* ctx = P->ctx;
   if (!P->lu || P->lu->n != P->n || P->lu->nnz != P->nnz) {
     std::vector<int32_t> dofv;
@@ -420,6 +420,9 @@ static fq_status mixed_direct(fq_mixed* P, const double* rhs, double* x, double 
     FQ_TRY(sparse_lu_build(ctx, P->mesh, P->n, P->rp, P->ci, dofv, *lu));
     P->lu = std::move(lu);
   }
+  // Lorentzian systems: float-float factors at once (FP32 factors of the
+  // Minkowski KKT systems stop converging from about 1.5e4 unknowns)
+  if (float_float_first && !P->lu->factored) FQ_TRY(sparse_lu_factor(ctx, *P->lu, P->rp, P->ci, P->val, FQ_FP64));
   fq_report r{};
   const fq_status s = sparse_lu_solve(ctx, *P->lu, P->rp, P->ci, P->val, rhs, x, rtol, max_iters, &r);
   if (s != FQ_OK && s != FQ_NOT_CONVERGED) return s;
@@ -450,7 +453,7 @@ static fq_status mixed_krylov(fq_mixed* P, const double* rhs, double* x, const f
   bool indefinite = false;
   if (kuhn && o->preconditioner == FQ_PC_AUTO) FQ_TRY(mixed_indefinite(P, &indefinite));
   if (kuhn && (o->preconditioner == FQ_PC_DIRECT || indefinite))
-    return mixed_direct(P, rhs, x, o->rtol, o->max_iters, rep);
+    return mixed_direct(P, rhs, x, o->rtol, o->max_iters, rep, indefinite);
   const HxPrecond* pc = nullptr;
   FQ_TRY(mixed_precond(P, o, &pc));
   if (P->precision != FQ_FP32 || !P->kkt32) {
