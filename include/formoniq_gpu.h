@@ -292,7 +292,9 @@ fq_status fq_mixed_reassemble(fq_mixed* prob);
  * sigma (ambient N_{k-1}), u (ambient N_k), p (harmonic_dim); any may be NULL.
  * Routes, as solve_source (elliptic.rs:140-160): block-preconditioned MINRES
  * on Riemannian meshes; the sparse direct solver on Lorentzian Kuhn meshes (a
- * cell metric not positive definite) or with FQ_PC_DIRECT; a MINRES (or FP32
+ * cell metric not positive definite; float-float factors) or with FQ_PC_DIRECT
+ * (FP32 factors first); the factors stay with the problem for later solves
+ * until fq_mixed_reassemble; a MINRES (or FP32
  * refinement) that does not converge is finished by the sparse direct solver
  * on Kuhn meshes (its GMRES takes up to max(max_iters, 300) iterations; report
  * iters count both, refinements is then the direct solve's: 1 = FP64 factors),
