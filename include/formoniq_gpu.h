@@ -208,7 +208,11 @@ fq_status fq_reassemble(fq_ctx* ctx, fq_mesh* mesh, fq_matrix* mat);
  * 130-183, each a BilinearForm::assemble, galerkin.rs:52-57): the element passes
  * and scatters of all matrices (any meshes of this context) are queued back to
  * back on the context's stream and the status is read once at the end. Same
- * results and errors as calling fq_reassemble on each in order. */
+ * results and errors as calling fq_reassemble on each in order. Each run of up
+ * to four consecutive mass / dif_both matrices of one mesh of dimension 1-3 in
+ * one precision shares a single element pass (each cell's metric and Gramian
+ * computed once), into element buffers the matrices then keep; the values are
+ * the per-matrix assembly's (bit for bit in FQ_FP64). */
 fq_status fq_reassemble_many(fq_ctx* ctx, fq_matrix* const* mats, int count);
 /* HilbertComplex::hdif_gram (whitney_complex.rs:180-183): M_k + dif_both(k+1). */
 fq_status fq_hdif_gram(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, fq_matrix** out);
