@@ -208,8 +208,9 @@ fq_status fq_reassemble(fq_ctx* ctx, fq_mesh* mesh, fq_matrix* mat);
  * 130-183, each a BilinearForm::assemble, galerkin.rs:52-57): the element passes
  * and scatters of all matrices (any meshes of this context) are queued back to
  * back on the context's stream and the status is read once at the end. Same
- * results and errors as calling fq_reassemble on each in order. Each run of up
- * to four consecutive mass / dif_both matrices of one mesh of dimension 1-3 in
+ * results and errors as calling fq_reassemble on each in order. The matrices
+ * are taken in groups of four (the last may be shorter); a group of two or
+ * more that are all mass / dif_both matrices of one mesh of dimension 1-3 in
  * one precision shares a single element pass (each cell's metric and Gramian
  * computed once), into element buffers the matrices then keep; the values are
  * the per-matrix assembly's (bit for bit in FQ_FP64). */
