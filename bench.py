@@ -340,6 +340,14 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+# DRAM bytes (read + write) of the step's four scatter launches in FQ_FP64 on
+# the 3D 32^3 workload, from one ncu capture of this build (--metrics
+# dram__bytes_read.sum,dram__bytes_write.sum --cache-control none; summary in
+# profiles/assembly_3d32_fp64_launches.md): the bench cannot run ncu itself, so
+# the line carries the captured figure and says so.
+SCATTER_TRAFFIC_3D32_FP64 = 251_345_920 + 116_041_984
+
+
 def roofline_record(ctx, mesh, mats, ncells, ms, t):
     """Algorithmic bytes per launch of each kernel (per form, summed over the
     step's forms) over its CUDA-event time on the launching stream."""
@@ -367,8 +375,14 @@ def roofline_record(ctx, mesh, mats, ncells, ms, t):
     dom_bytes, dom_ms = (el_bytes, el_avg) if dominant == "element" else (sc_bytes, sc_avg)
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     fused_gbps = fused_bytes / (ms * 1e-3) / 1e9
+    fp64 = all(m.info()[3] == 0 for m in mats)
+    traffic = SCATTER_TRAFFIC_3D32_FP64 if (dominant == "scatter" and fp64 and n == 3 and ncells == 6 * NBOX ** 3) \
+        else None
     return {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+            "frac": achieved / hbm_peak, "traffic": traffic,
+            "traffic_source": "ncu capture of the four scatter launches of one step (per step, like achieved)"
+            if traffic else None,
+            "traffic_over_algorithmic": traffic / dom_bytes if traffic else None, "peak_source": peak_src,
             "algorithmic_bytes_per_step": dom_bytes, "kernel_ms_per_step": dom_ms,
             "element_ms_per_step": el_avg, "scatter_ms_per_step": sc_avg,
             "element_bytes_per_step": el_bytes, "scatter_bytes_per_step": sc_bytes,
