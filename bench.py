@@ -691,7 +691,7 @@ def stream_summary(reqs, res, wall, kind=None):
             "service_p50_ms": pct(run, 50), "service_p99_ms": pct(run, 99), "mean_service_ms": sum(run) / len(run),
             "queue_p50_ms": pct(que, 50), "queue_p99_ms": pct(que, 99), "converged": len(ok), "n": len(pairs),
             "wall_s": wall, "cache_hits": sum(r["cache_hit"] for _, r in pairs),
-            "fp64_factor_fallbacks": sum(1 for q, r in pairs if q["kind"] == 1 and r["report"].refinements > 0),
+            "dirac_on_fp64_class_factors": sum(1 for q, r in pairs if q["kind"] == 1 and r["report"].refinements > 0),
             "statuses": {str(k): v for k, v in sorted(statuses.items())},
             "unconverged": [{"dim": q.get("dim"), "nbox": q.get("nbox"), "grade": q.get("grade"),
                              "status": int(r["status"]), "iters": int(r["report"].iters),
