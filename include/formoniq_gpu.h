@@ -302,7 +302,8 @@ fq_status fq_mixed_reassemble(fq_mixed* prob);
  * until fq_mixed_reassemble; a MINRES (or FP32
  * refinement) that does not converge is finished by the sparse direct solver
  * on Kuhn meshes (its GMRES takes up to max(max_iters, 300) iterations; report
- * iters count both, refinements is then the direct solve's: 1 = FP64 factors),
+ * iters count both, refinements is then the direct solve's: 1 = float-float or
+ * IEEE FP64 factors),
  * by a dense LU on other meshes of at most 8192 unknowns. */
 fq_status fq_mixed_solve(fq_mixed* prob, const double* source_host, double* sigma_host, double* u_host,
                          double* p_host, const fq_solve_opts* opts, fq_report* report);
@@ -465,12 +466,14 @@ fq_status fq_sparse_lu_factor(fq_sparse_lu* lu, const fq_matrix* a, int precisio
  * ||b - A x|| / (||A||_F ||x|| + ||b||) reaches 1e-14 (the rounding level an LU
  * solve delivers; a nearly singular system may not allow rtol), at most
  * opts->max_iters iterations in all. On FP32
- * factors GMRES runs for at most 60 iterations; if it has not converged by
- * then, `a` is re-factored in FP64 (the factorization keeps FP64 afterwards,
- * until the next fq_sparse_lu_factor) and GMRES starts again from zero: then
- * report.refinements = 1. report.iters counts both. opts->max_refinements = 0
+ * factors GMRES runs for at most 60 iterations (stopping earlier when three
+ * iterations do not halve the residual); if it has not converged by then, `a`
+ * is re-factored in FQ_FP64 (float-float; the factorization keeps that type
+ * afterwards, until the next fq_sparse_lu_factor) and GMRES starts again from
+ * zero: then report.refinements = 1. report.iters counts both. On FQ_FP64 or
+ * FQ_FP64_IEEE factors report.refinements is 1. opts->max_refinements = 0
  * keeps the current factors whatever their type: GMRES runs on them for up to
- * opts->max_iters iterations and no FP64 factorization happens. */
+ * opts->max_iters iterations and no re-factorization happens. */
 fq_status fq_sparse_lu_solve(fq_sparse_lu* lu, const fq_matrix* a, const double* b_dev, double* x_dev,
                              const fq_solve_opts* opts, fq_report* report);
 /* Fronts, levels, factorization flops, bytes of the current factors, pivots
