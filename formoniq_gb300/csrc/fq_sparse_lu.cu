@@ -1447,7 +1447,7 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
     if (stale >= stale_limit && it < max_iters) {
       // a stagnating cycle: accept x if it is at the rounding level, else the
       // restart continues (and a stagnating FP32 preconditioner gives way to
-      // FP64 factors in sparse_lu_solve)
+      // float-float factors in sparse_lu_solve)
       sl_spmv_kernel<<<spmv_blocks, 256, 0, st>>>(rp, ci, val, x, n, w);
       sl_residual_kernel<<<grid_of(n, 256), 256, 0, st>>>(b, w, n, w);
       ctx->launches += 2;
@@ -1459,7 +1459,7 @@ fq_status sparse_lu_gmres(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
         done = true;
         break;
       }
-      if (lu.precision == FQ_FP32) break;  // the FP64 factors take over
+      if (lu.precision == FQ_FP32) break;  // the float-float factors take over
     }
   }
   if (!done) {
@@ -1519,7 +1519,7 @@ fq_status sparse_lu_solve(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const in
     if (rep) *rep = r;
     return FQ_OK;
   }
-  // the FP32 factors were not enough: FP64 factors, GMRES from zero (and FP64
+  // the FP32 factors were not enough: float-float factors, GMRES from zero (and those
   // at once for the next values of this pattern)
   lu.prefer_fp64 = true;
   fs = sparse_lu_factor(ctx, lu, rp, ci, val, FQ_FP64);
