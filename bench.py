@@ -341,10 +341,10 @@ def run_ours(args):
 
 
 # DRAM bytes (read + write) of the step's four scatter launches in FQ_FP64 on
-# the 3D 32^3 workload, from one ncu capture of this build (--metrics
-# dram__bytes_read.sum,dram__bytes_write.sum --cache-control none; summary in
-# profiles/assembly_3d32_fp64_launches.md): the bench cannot run ncu itself, so
-# the line carries the captured figure and says so.
+# the 3D 32^3 workload, from one ncu capture of the current kernels (--metrics
+# dram__bytes_read.sum,dram__bytes_write.sum --cache-control none; its summary
+# is kept under profiles/): the bench cannot run ncu itself, so the line
+# carries the captured figure and says so.
 SCATTER_TRAFFIC_3D32_FP64 = 251_345_920 + 116_041_984
 
 

@@ -1,6 +1,6 @@
 // Instrumentation: the sustained FMA rate of the FP64 and FP32 pipes, the
-// denominators for the element kernels' compute roofline (the driver-measured
-// peaks cover HBM and bf16 tensor throughput only).
+// denominators for the element kernels' compute roofline (the measured peaks
+// file covers HBM copy and bf16 tensor throughput only).
 #include <cuda_runtime.h>
 
 #include "fq_internal.h"

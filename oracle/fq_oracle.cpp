@@ -1,7 +1,7 @@
 // fq_oracle.cpp -- TEST INFRASTRUCTURE, NOT PRODUCT CODE.
 //
 // A plain C++17 (OpenMP) restatement of formoniq's Galerkin assembly path, used
-// only as the checker: by the tests under tests/, by __graft_entry__.smoke() and
+// only as the test oracle: by the tests under tests/, by __graft_entry__.smoke() and
 // by bench.py's CPU-baseline / reference arm. Nothing in formoniq_gb300/ links,
 // loads or calls this file.
 //

@@ -1,6 +1,6 @@
 """CPU restatement of the HX-multigrid preconditioner (test infrastructure only).
 
-This is the checker of the device preconditioner behind fq_hx_apply / fq_hx_cg and
+This is the test oracle of the device preconditioner behind fq_hx_apply / fq_hx_cg and
 of the mixed solve's HX blocks; nothing in the product imports it.
 
 What it restates, and from where:

@@ -1,7 +1,7 @@
 """TEST INFRASTRUCTURE, NOT PRODUCT CODE: the CPU oracle of formoniq's Galerkin path.
 
 Only tests/, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline and
-reference arms may import this module, and only as the checker. It wraps the C++
+reference arms may import this module, and only as the oracle. It wraps the C++
 restatement in ``oracle/fq_oracle.cpp`` (built into ``oracle/_build``) and adds
 the parts the reference writes on top of assembled sparse matrices:
 
