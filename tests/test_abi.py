@@ -62,6 +62,18 @@ def test_context_without_device_fails_loudly(native):
     assert e.value.name == "FQ_NO_DEVICE"
 
 
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """No CPU fallback: without the CUDA library every entry point raises."""
+    import formoniq_gb300 as fq
+
+    monkeypatch.setattr(fq, "_lib", None)
+    monkeypatch.setattr(fq, "lib_path", lambda: str(tmp_path / "libformoniq_gb300.so"))
+    with pytest.raises(fq.FqUnavailable):
+        fq.load()
+    with pytest.raises(fq.FqUnavailable):
+        fq.Context(0)
+
+
 def test_kernels_are_blackwell_native():
     """The hot kernels are built for sm_103a only (one -gencode)."""
     from formoniq_gb300 import _build
