@@ -480,9 +480,42 @@ def e2e_phase(ctx, mesh, mats, flush, args, ncells, world):
         e2e_step()
         e_ms.append((time.perf_counter() - t) * 1e3)
     e2e_ms = sum(e_ms) / len(e_ms)
+    h2d = lengths_h.numel() * 8
+    d2h = sum(o.numel() * 8 for o in outs)
     return {"value": world * ncells / (e2e_ms * 1e-3), "unit": "cells/s",
-            "h2d_bytes_per_step": lengths_h.numel() * 8,
-            "d2h_bytes_per_step": sum(o.numel() * 8 for o in outs), "ms_per_step": e2e_ms}
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+            "link": link_floor(h2d, d2h, e2e_ms)}
+
+
+def link_floor(h2d: int, d2h: int, e2e_ms: float) -> dict:
+    """The host link's bound on the end-to-end step: plain pinned copies of the
+    step's byte counts (one copy each way, CUDA events on the current stream).
+    Splitting a download over several streams, or storing into the pinned
+    buffer from the SMs, moves no more bytes per second than one copy-engine
+    copy, so the sum of the two copy times is the step's floor."""
+    import torch
+
+    hd = torch.empty(max(h2d // 8, 1), dtype=torch.float64).pin_memory()
+    dd = torch.empty(max(h2d // 8, 1), dtype=torch.float64, device="cuda")
+    ds = torch.empty(max(d2h // 8, 1), dtype=torch.float64, device="cuda")
+    hs = torch.empty(max(d2h // 8, 1), dtype=torch.float64).pin_memory()
+
+    def copy_ms(dst, src, reps=10):
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            dst.copy_(src, non_blocking=True)
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    up_ms, down_ms = copy_ms(dd, hd), copy_ms(hs, ds)
+    floor_ms = up_ms + down_ms
+    return {"h2d_GBps": hd.numel() * 8 / up_ms / 1e6, "d2h_GBps": hs.numel() * 8 / down_ms / 1e6,
+            "floor_ms": floor_ms, "frac": floor_ms / e2e_ms}
 
 
 # ---------------------------------------------------------------------------
