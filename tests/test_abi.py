@@ -44,6 +44,32 @@ def test_binding_covers_the_header():
     assert sorted(fq.exported_symbols()) == declared_functions()
 
 
+def header_arities():
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = {}
+    for name, args in re.findall(r"\b(fq_[a-z0-9_]+)\s*\(([^;{()]*)\)\s*;", text):
+        args = args.strip()
+        out[name] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_rust_binding_covers_the_header():
+    """The extern blocks a formoniq maintainer adds bind every entry point,
+    each with the header's number of arguments."""
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    blocks = "\n".join(re.findall(r"```rust\n(.*?)```", doc, flags=re.S))
+    bound = {}
+    for name, args in re.findall(r"\bfn (fq_[a-z0-9_]+)\s*\(([^)]*)\)", blocks):
+        args = args.strip().rstrip(",")
+        bound[name] = 0 if not args else args.count(",") + 1
+    want = header_arities()
+    assert sorted(want) == declared_functions()
+    assert sorted(bound) == sorted(want), (sorted(set(want) - set(bound)), sorted(set(bound) - set(want)))
+    wrong = {n: (bound[n], want[n]) for n in want if bound[n] != want[n]}
+    assert not wrong, wrong
+
+
 def test_status_names(native):
     native.fq_status_name.restype = ctypes.c_char_p
     assert native.fq_status_name(0) == b"FQ_OK"
