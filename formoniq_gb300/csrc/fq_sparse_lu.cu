@@ -1067,8 +1067,8 @@ fq_status factor_impl(fq_ctx* ctx, SparseLu& lu, const int32_t* rp, const int32_
     FQ_TRY(lu.tourn_count.alloc(ctx, size_t(half_sets) * 2 * 4));
   }
   FQ_TRY(set_attributes<T>(ctx));
-  // the symmetric scaling; every entry of D A D is then at most 1 in magnitude,
-  // and a pivot below 1e-6 is perturbed
+  // the symmetric scaling D A D, d_i = 1 / sqrt(max_j |a_ij|): on a symmetric
+  // matrix every entry is then at most 1 in magnitude
   sl_row_scale_kernel<<<grid_of(lu.n, 256), 256, 0, st>>>(rp, val, lu.n, lu.scale.as<double>());
   ctx->launches++;
   // the pivot floor, relative to the scaled matrix's largest entry (1): about

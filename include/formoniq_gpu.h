@@ -110,6 +110,10 @@ typedef struct fq_report {
 } fq_report;
 
 /* ---- context ------------------------------------------------------------ */
+/* No counterpart in the reference (a CPU crate on rayon's global pool): a
+ * context holds the device, its CUDA stream, an optional HBM budget (0 = none)
+ * and the last error message. fq_default_solve_opts fills the reference's
+ * StopCriterion defaults (iterative/src/lib.rs:193-208) and FQ_PC_AUTO. */
 fq_status fq_ctx_create(int device, void* cuda_stream, uint64_t hbm_budget_bytes, fq_ctx** out);
 /* Destroy every mesh, matrix and mixed problem made on a context first. */
 void fq_ctx_destroy(fq_ctx* ctx);
@@ -151,11 +155,11 @@ fq_status fq_mesh_from_cells(fq_ctx* ctx, int dim, int64_t ncells, const int32_t
 fq_status fq_mesh_kuhn_cube(fq_ctx* ctx, int dim, int nboxes_per_axis, fq_mesh** out);
 void fq_mesh_destroy(fq_mesh* mesh);
 int fq_mesh_dim(const fq_mesh* mesh);
-/* Complex::nsimplices; 0 off 0..dim. */
+/* Complex::nsimplices (simplicial/src/topology/complex.rs:58-60); 0 off 0..dim. */
 int64_t fq_mesh_nsimplices(const fq_mesh* mesh, int grade);
 /* HilbertComplex::ndofs (whitney_complex.rs:376-383 / :588-595). */
 int64_t fq_mesh_ndofs(const fq_mesh* mesh, int grade, fq_bc bc);
-/* The grade-k skeleton, host int32 [N_k][k+1], colex order. */
+/* Complex::skeleton(k) (complex.rs:48-50): host int32 [N_k][k+1], colex order. */
 fq_status fq_mesh_simplices(const fq_mesh* mesh, int grade, int32_t* out);
 /* Kept (interior) kidx of the relative complex, increasing (whitney_complex.rs:548-566). */
 fq_status fq_mesh_interior(const fq_mesh* mesh, int grade, int64_t* out);
@@ -200,8 +204,9 @@ fq_status fq_element_matrices(fq_ctx* ctx, fq_mesh* mesh, fq_form form, int grad
  * (form, grade, bc) and cached on the mesh. */
 fq_status fq_assemble(fq_ctx* ctx, fq_mesh* mesh, fq_form form, int grade, fq_bc bc, fq_precision prec,
                       fq_matrix** out);
-/* Re-assemble into an existing matrix (same mesh, form, grade, bc, precision)
- * after new lengths: the hot loop of a geometry sweep. */
+/* BilinearForm::assemble again (galerkin.rs:52-57) into an existing matrix
+ * (same mesh, form, grade, bc, precision) after new lengths: the hot loop of a
+ * geometry sweep. */
 fq_status fq_reassemble(fq_ctx* ctx, fq_mesh* mesh, fq_matrix* mat);
 /* Several fq_reassemble calls in one (a geometry sweep that refreshes a set of
  * operators, e.g. the HilbertComplex masses and stiffnesses, whitney_complex.rs:
@@ -220,9 +225,10 @@ fq_status fq_hdif_gram(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, fq_matri
 /* HilbertComplex::dif (whitney_complex.rs:417-423, relative :640-643): the
  * coboundary N_{k+1} x N_k, entries +-1. */
 fq_status fq_coboundary(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, fq_matrix** out);
-/* The end-to-end assembly call with host buffers: uploads lengths_sq (N_1
- * doubles), assembles, downloads the CSR values (nnz doubles or floats) into
- * values_out. The pattern comes from fq_matrix_copy_to_host of a prior fq_assemble. */
+/* BilinearForm::assemble (galerkin.rs:52-57) from host lengths into host
+ * values, the end-to-end call: uploads lengths_sq (N_1 doubles), assembles,
+ * downloads the CSR values (nnz doubles or floats) into values_out. The
+ * pattern comes from fq_matrix_copy_to_host of a prior fq_assemble. */
 fq_status fq_assemble_host(fq_ctx* ctx, fq_mesh* mesh, fq_matrix* mat, const double* lengths_sq_host,
                            void* values_out_host);
 /* fq_assemble_host for several matrices of one mesh (the operators a geometry
@@ -249,6 +255,9 @@ fq_status fq_assemble_host_many(fq_ctx* ctx, fq_mesh* mesh, const double* length
  * whose work overlaps on the GPU race. */
 fq_status fq_reassemble_noalloc(fq_ctx* ctx, fq_mesh* mesh, const fq_matrix* pattern, void* values_out);
 
+/* The assembled matrix stands in for the reference's GalerkinMatrix, a CSR
+ * matrix built from the COO triplets of assemble_matrix (galerkin.rs:138-188):
+ * its shape, nnz, arrays (device or host copies) and release. */
 fq_status fq_matrix_info(const fq_matrix* m, int64_t* nrows, int64_t* ncols, int64_t* nnz, int* precision);
 /* The bytes one re-assembly's scatter reads and writes for this matrix: every
  * element value once, the plan's records and the indices it still reads, every
@@ -316,7 +325,7 @@ fq_status fq_mixed_info(const fq_mixed* prob, int64_t* n_sigma, int64_t* n_u, in
 /* The assembled KKT matrix (owned by the problem; do not destroy). */
 const fq_matrix* fq_mixed_system(const fq_mixed* prob);
 void fq_mixed_destroy(fq_mixed* prob);
-/* One-shot elliptic::solve_source with host buffers. */
+/* One-shot elliptic::solve_source (problems/elliptic.rs:132-182) with host buffers. */
 fq_status fq_solve_source(fq_ctx* ctx, fq_mesh* mesh, int grade, fq_bc bc, const double* source_host,
                           double* sigma_host, double* u_host, double* p_host, const fq_solve_opts* opts,
                           fq_report* report);
@@ -445,9 +454,11 @@ fq_status fq_dirac_system(fq_ctx* ctx, fq_mesh* mesh, double mass_term, fq_matri
  * solve_source (problems/elliptic.rs:147-160). Multifrontal LU on a geometric
  * nested-dissection ordering of the Kuhn vertex lattice: the fronts of each
  * level of the elimination tree are assembled and partially factored together
- * on the device (the system scaled to unit row maxima; the pivot rows of each
- * tile chosen over all the front's fully summed rows by tournament pivoting;
- * pivots below 1e-6 perturbed). The factors precondition a restarted GMRES in
+ * on the device (the system scaled symmetrically, D A D with d_i the inverse
+ * square root of row i's largest magnitude; the pivot rows of each tile chosen
+ * over all the front's fully summed rows by tournament pivoting; pivots below
+ * 1e-6 (FQ_FP32 factors), 1e-12 (float-float) or 1e-13 (IEEE FP64) of the
+ * scaled matrix perturbed). The factors precondition a restarted GMRES in
  * FP64 on the FP64 matrix, which stops on the true relative residual
  * ||b - A x|| / ||b||. */
 typedef struct fq_sparse_lu fq_sparse_lu;
