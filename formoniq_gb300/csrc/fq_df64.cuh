@@ -137,7 +137,9 @@ FQ_HDI double widen(float f) {
                    (uint64_t(u & 0x7fffffu) << 29));
 }
 
-struct df64 {
+// 8-byte aligned like float2: one 64-bit load or store moves a value, where a
+// 4-byte-aligned pair takes two 32-bit accesses.
+struct alignas(8) df64 {
   float hi, lo;
 
   FQ_HDI df64() : hi(0.f), lo(0.f) {}
@@ -247,7 +249,8 @@ FQ_HDI df64 dd_sqrt(df64 a) {
   return fast_two_sum(q, res.hi / (q + q));
 }
 
-// Storage: a df64 occupies the same 8 bytes as a double.
+// Storage: a df64 occupies the same 8 bytes as a double, with its alignment.
 static_assert(sizeof(df64) == 8, "df64 must pack into 8 bytes");
+static_assert(alignof(df64) == 8, "df64 must be 8-byte aligned");
 
 }  // namespace fq
