@@ -152,6 +152,66 @@ def test_minkowski_regge_volume(oracle, dim):
     assert abs(vol[0] - 1 / math.factorial(dim)) < 1e-12
 
 
+def lengths_from_cell_gramians(cx, gramian_of_cell):
+    """Per-cell Gram matrices G (edge vectors from the cell's first vertex) read
+    back as edge lengths, l_ij = G_ii + G_jj - 2 G_ij with G_0. = 0: the
+    reference's metric -> lengths conversion (CellGramians::to_edge_lengths_sq).
+    Every cell sharing an edge must read back the same length."""
+    index = {tuple(e): i for i, e in enumerate(cx.simplices(1))}
+    out = np.full(len(index), np.nan)
+    for c in cx.simplices(cx.dim):
+        g = np.zeros((len(c), len(c)))
+        g[1:, 1:] = gramian_of_cell(c)
+        for i in range(len(c)):
+            for j in range(i + 1, len(c)):
+                ln = g[i, i] + g[j, j] - 2 * g[i, j]
+                e = index[(c[i], c[j])]
+                if np.isnan(out[e]):
+                    out[e] = ln
+                else:
+                    assert abs(out[e] - ln) <= 1e-12 * max(1.0, abs(ln))
+    assert not np.isnan(out).any()
+    return out
+
+
+def masses_agree(oracle, cx, a_lengths, b_lengths):
+    wa, wb = oracle.WhitneyComplex(cx, a_lengths), oracle.WhitneyComplex(cx, b_lengths)
+    for k in range(cx.dim + 1):
+        a, b = wa.mass(k).toarray(), wb.mass(k).toarray()
+        assert np.abs(a - b).max() <= 1e-12 * max(1.0, np.abs(a).max()), k
+
+
+def test_cell_gramians_round_trip_assembles_identically(oracle):
+    """galerkin.rs:380-392: lengths -> per-cell metrics -> lengths on the unit
+    3D box N = 2 gives the same masses (1e-12)."""
+    cx, coords = oracle.cartesian_unit(3, 2)
+    lengths = cx.edge_lengths_sq(coords)
+    index = {tuple(e): i for i, e in enumerate(cx.simplices(1))}
+
+    def from_lengths(c):  # G_ij = (l_0i + l_0j - l_ij) / 2
+        l0 = [lengths[index[(c[0], v)]] for v in c[1:]]
+        n = len(c) - 1
+        lij = lambda i, j: lengths[index[(c[min(i, j) + 1], c[max(i, j) + 1])]]
+        return np.array([[l0[i] if i == j else (l0[i] + l0[j] - lij(i, j)) / 2 for j in range(n)] for i in range(n)])
+
+    masses_agree(oracle, cx, lengths, lengths_from_cell_gramians(cx, from_lengths))
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_lorentzian_sources_reduce_to_the_same_regge_data(oracle, dim):
+    """galerkin.rs:394-421: on the Minkowski box (time axis scaled 0.7) the
+    lengths of the embedding and the lengths read back from the per-cell
+    Gramians E^T eta E it induces assemble the same masses (1e-12)."""
+    cx, coords, signs = oracle.minkowski(dim, 2)
+    eta = np.diag(signs)
+
+    def from_coords(c):
+        e = (coords[c[1:]] - coords[c[0]]).T
+        return e.T @ eta @ e
+
+    masses_agree(oracle, cx, cx.edge_lengths_sq(coords, signs), lengths_from_cell_gramians(cx, from_coords))
+
+
 # ---- global operators (tests/fem3d.rs, tests/fdm.rs, whitney_complex.rs tests) ----
 
 def _fem3d(n):
