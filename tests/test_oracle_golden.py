@@ -386,6 +386,30 @@ def test_minres_agrees_with_cg_on_spd(oracle):
     assert np.linalg.norm(xm - xc) < 1e-7
 
 
+def test_block_diagonal_of_exact_blocks_is_exact(oracle):
+    """precond.rs:217-240: on a block-diagonal operator (blocks of 3, 4 and 2
+    distinct diagonal entries) the block-Jacobi preconditioner is the exact
+    inverse, so preconditioned CG converges in one step (the oracle's MINRES
+    too); precond.rs:242-255: the block preconditioner is self-adjoint."""
+    sizes = [3, 4, 2]
+    offs = np.cumsum([0] + sizes)
+    d = 1.0 + (np.arange(offs[-1]) % 6)
+    a = sp.diags(d).tocsr()
+    blocks = [1.0 / d[offs[i]:offs[i + 1]] for i in range(len(sizes))]
+
+    def precond(r):
+        return np.concatenate([blocks[i] * r[offs[i]:offs[i + 1]] for i in range(len(sizes))])
+
+    b = np.cos(np.arange(offs[-1]) - 4.0)
+    for solve in (oracle.cg, oracle.minres):
+        x, rep = solve(a, precond, b, rtol=1e-12)
+        assert rep.converged and rep.iters <= 1, (solve.__name__, rep)
+        assert np.linalg.norm(x - b / d) < 1e-9
+    r = np.log(np.arange(1.0, offs[-1] + 1))
+    s = np.cos(2.0 * np.arange(offs[-1]))
+    assert abs(precond(r) @ s - r @ precond(s)) < 1e-12
+
+
 # ---- the mixed problem (problems/elliptic.rs:259-367) ----
 
 @pytest.mark.parametrize("dim", [1, 2, 3])
