@@ -152,6 +152,22 @@ def test_minkowski_regge_volume(oracle, dim):
     assert abs(vol[0] - 1 / math.factorial(dim)) < 1e-12
 
 
+@pytest.mark.parametrize("dim", [2, 3, 4])
+def test_degeneracy_is_scale_invariant(oracle, dim):
+    """simplex.rs:378-390: the unit simplex scaled by s^2 (s = 1e-4, 1, 1e4) is
+    not degenerate; with edge (1, 2) collapsed to 0 it is, at every scale (the
+    oracle flags the cell whose metric has no inverse, where Metric::dual
+    would panic)."""
+    edges = [(a, b) for b in range(dim + 1) for a in range(b)]
+    unit = np.array([1.0 if a == 0 else 2.0 for a, b in edges])
+    cx = oracle.Complex.from_cells(np.arange(dim + 1, dtype=np.int32)[None, :])
+    for s in (1e-4, 1.0, 1e4):
+        lengths = unit * s * s
+        assert cx.cell_metrics(lengths)[4] == 0
+        lengths[edges.index((1, 2))] = 0.0
+        assert cx.cell_metrics(lengths)[4] == 1
+
+
 def lengths_from_cell_gramians(cx, gramian_of_cell):
     """Per-cell Gram matrices G (edge vectors from the cell's first vertex) read
     back as edge lengths, l_ij = G_ii + G_jj - 2 G_ij with G_0. = 0: the
