@@ -329,6 +329,25 @@ def test_dif_both_and_dif_test_local_and_global_routes_agree(oracle, dim):
 
 
 @pytest.mark.parametrize("dim", [1, 2, 3])
+def test_hdif_norm_and_gram_agree(oracle, dim):
+    """whitney_complex.rs:866-891: the quadratic form of hdif_gram(k) is the
+    squared L2 norm plus the squared dif seminorm (by the global product
+    D_k u against M_{k+1}), on the unit boxes N = 2, every grade (1e-10)."""
+    cx, coords = oracle.cartesian_unit(dim, 2)
+    wc = oracle.WhitneyComplex(cx, cx.edge_lengths_sq(coords))
+    for k in range(dim + 1):
+        u = (np.arange(cx.nsimplices(k)) % 5) - 2.0
+        l2 = u @ (wc.mass(k) @ u)
+        semi = 0.0
+        if k < dim:
+            du = wc.dif(k) @ u
+            semi = du @ (wc.mass(k + 1) @ du)
+        gram = u @ (wc.hdif_gram(k) @ u)
+        assert semi >= -1e-12
+        assert abs(math.sqrt(gram) - math.sqrt(l2 + semi)) < 1e-10, (k, gram, l2 + semi)
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
 def test_the_relative_stiffness_is_the_restriction_of_the_full_one(oracle, dim):
     """whitney_complex.rs:825-861."""
     cx, coords = oracle.cartesian_unit(dim, 2)
@@ -400,6 +419,21 @@ def test_minres_agrees_with_cg_on_spd(oracle):
     assert rm.converged
     assert np.linalg.norm(xm - x_true) < 1e-8
     assert np.linalg.norm(xm - xc) < 1e-7
+
+
+def test_preconditioning_preserves_the_solution(oracle):
+    """krylov.rs:247-262: Jacobi-preconditioned CG and plain CG reach the same
+    solution of tridiag(20; 1, 4, 1) (1e-9)."""
+    n = 20
+    a = sp.diags([np.ones(n - 1), 4.0 * np.ones(n), np.ones(n - 1)], [-1, 0, 1]).tocsr()
+    x_true = np.cos(np.arange(n) ** 2.0)
+    b = a @ x_true
+    x_plain, r1 = oracle.cg(a, lambda r: r, b, rtol=1e-12)
+    x_jacobi, r2 = oracle.cg(a, lambda r: r / a.diagonal(), b, rtol=1e-12)
+    assert r1.converged and r2.converged
+    assert np.linalg.norm(x_plain - x_true) < 1e-9
+    assert np.linalg.norm(x_jacobi - x_true) < 1e-9
+    assert np.linalg.norm(x_plain - x_jacobi) < 1e-9
 
 
 def test_block_diagonal_of_exact_blocks_is_exact(oracle):
