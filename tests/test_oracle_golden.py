@@ -118,6 +118,72 @@ def test_skeletons_are_colex_sorted(oracle):
         assert keys == sorted(keys) and len(set(keys)) == len(keys)
 
 
+# ---- topology (simplicial/src/topology/{complex,orientation}.rs) ----
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_coboundary_squares_to_zero(oracle, dim):
+    """complex.rs:394-408: dif(k+1) dif(k) = 0 exactly on cube(dim, 2), on the
+    full and on the relative complex."""
+    cx, coords = oracle.cartesian_unit(dim, 2)
+    lengths = cx.edge_lengths_sq(coords)
+    for relative in (False, True):
+        wc = oracle.WhitneyComplex(cx, lengths, relative=relative)
+        for k in range(dim - 1):
+            dd = (wc.dif(k + 1) @ wc.dif(k)).tocsr()
+            assert np.all(dd.data == 0.0), (relative, k)
+
+
+def coherent(cx, sgn):
+    """Adjacent cells induce opposite orientations on their shared facet: the
+    facet that drops vertex position p of a cell with sign s gets s (-1)^p."""
+    facets = {}
+    for c, cell in enumerate(cx.simplices(cx.dim)):
+        for p in range(cx.dim + 1):
+            f = tuple(np.delete(cell, p).tolist())
+            induced = sgn[c] * (-1.0) ** p
+            if f in facets:
+                if facets.pop(f) != -induced:
+                    return False
+            else:
+                facets[f] = induced
+    return True
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3, 4])
+def test_kuhn_boxes_are_coherently_oriented(oracle, dim):
+    """orientation.rs:240-275: the orientation the top harmonic is built on
+    (z = M_n h) is coherent on the Kuhn boxes N = 2, every sign +-1."""
+    cx = oracle.Complex.from_cells(oracle.kuhn_cells(dim, 2))
+    sgn = oracle.orientation_signs(cx)
+    assert np.all(np.abs(sgn) == 1.0)
+    assert coherent(cx, sgn)
+
+
+def test_sphere_is_orientable_and_not_trivially_signed(oracle):
+    """orientation.rs:327-343: the boundary of a tetrahedron is coherently
+    oriented, and not by all-positive signs (its colex frames disagree)."""
+    cx = oracle.Complex.from_cells(np.array([[0, 1, 2], [0, 1, 3], [0, 2, 3], [1, 2, 3]], np.int32))
+    sgn = oracle.orientation_signs(cx)
+    assert np.all(np.abs(sgn) == 1.0) and coherent(cx, sgn)
+    assert (sgn < 0).any()
+    assert not coherent(cx, np.ones(4))
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_boundary_facets_are_the_facets_of_one_cell(oracle, dim):
+    """complex.rs:410-424: the (n-1)-simplices the relative complex drops are
+    exactly the facets that belong to a single cell."""
+    cx = oracle.Complex.from_cells(oracle.kuhn_cells(dim, 2))
+    count = {}
+    for cell in cx.simplices(dim):
+        for p in range(dim + 1):
+            f = tuple(np.delete(cell, p).tolist())
+            count[f] = count.get(f, 0) + 1
+    facets = cx.simplices(dim - 1)
+    single = {i for i, f in enumerate(facets) if count[tuple(f.tolist())] == 1}
+    assert set(range(len(facets))) - set(cx.interior(dim - 1).tolist()) == single
+
+
 # ---- geometry (regge/src/lengths/simplex.rs:350-436) ----
 
 @pytest.mark.parametrize("dim", [1, 2, 3, 4])
