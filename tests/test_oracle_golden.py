@@ -234,6 +234,49 @@ def test_degeneracy_is_scale_invariant(oracle, dim):
         assert cx.cell_metrics(lengths)[4] == 1
 
 
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_edge_length_is_endpoint_distance(oracle, dim):
+    """coord/mesh.rs:327-342: an edge's squared length is the squared distance
+    of its endpoints, exactly (unit boxes N = 2)."""
+    cx, coords = oracle.cartesian_unit(dim, 2)
+    e = cx.simplices(1)
+    d = coords[e[:, 1]] - coords[e[:, 0]]
+    want = np.zeros(len(e))
+    for a in range(coords.shape[1]):
+        want = want + d[:, a] * d[:, a]
+    np.testing.assert_array_equal(cx.edge_lengths_sq(coords), want)
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_minkowski_ambient_induces_lorentzian_cell_metrics(oracle, dim):
+    """coord/mesh.rs:344-363: the unit box N = 2 in Minkowski ambient space
+    (its diagonal edges null) has every cell metric of signature (n-1, 1)."""
+    cx, coords = oracle.cartesian_unit(dim, 2)
+    signs = np.ones(dim)
+    signs[0] = -1.0
+    g, _, det, _, bad = cx.cell_metrics(cx.edge_lengths_sq(coords, signs))
+    assert bad == 0 and np.all(det < 0)
+    for gc in g:
+        ev = np.linalg.eigvalsh(gc)
+        assert (ev < 0).sum() == 1 and (ev > 0).sum() == dim - 1
+
+
+def test_lorentzian_ambient_realizes_lorentzian_regge_data(oracle):
+    """coord/mesh.rs:365-398: the 2D box N = 1 with time scaled 0.7 has both
+    timelike and spacelike edges, and each cell metric rebuilt from the signed
+    lengths is the embedding's E^T eta E (1e-12), signature (1, 1)."""
+    cx, coords, signs = oracle.minkowski(2, 1)
+    lengths = cx.edge_lengths_sq(coords, signs)
+    assert (lengths < 0).any() and (lengths > 0).any()
+    g = cx.cell_metrics(lengths)[0]
+    eta = np.diag(signs)
+    for c, cell in enumerate(cx.simplices(2)):
+        e = (coords[cell[1:]] - coords[cell[0]]).T
+        np.testing.assert_allclose(g[c], e.T @ eta @ e, rtol=0, atol=1e-12)
+        ev = np.linalg.eigvalsh(g[c])
+        assert (ev < 0).sum() == 1 and (ev > 0).sum() == 1
+
+
 def lengths_from_cell_gramians(cx, gramian_of_cell):
     """Per-cell Gram matrices G (edge vectors from the cell's first vertex) read
     back as edge lengths, l_ij = G_ii + G_jj - 2 G_ij with G_0. = 0: the
