@@ -17,10 +17,13 @@ import pytest
 
 
 @pytest.mark.parametrize("k", [0, 1, 2, 3, 4])
-@pytest.mark.parametrize("degree", [1, 3, 5, 7])
+@pytest.mark.parametrize("degree", [0, 1, 2, 3, 4, 5, 7])
 def test_gm_rule_is_exact_to_its_degree(oracle, k, degree):
+    """quadrature.rs:184-235: exact on every barycentric monomial up to the
+    degree asked for; weights and each node's barycentric coordinates sum to 1."""
     bary, w = oracle.gm_rule(k, degree)
     assert abs(w.sum() - 1.0) < 1e-14
+    assert np.abs(bary.sum(axis=1) - 1.0).max() < 1e-12
     for total in range(degree + 1):
         for a in itertools.product(range(total + 1), repeat=k + 1):
             if sum(a) != total:
