@@ -3,7 +3,8 @@
 Mirrors the reference's own checks of the structure: formoniq/src/hx.rs tests
 (hx_cg_matches_the_direct_solve, hx_multigrid_matches_the_direct_solve),
 formoniq/src/multigrid.rs tests (mg_cg_matches_the_direct_solve,
-mg_cg_iterations_are_mesh_independent), iterative/src/aux_space.rs
+mg_cg_iterations_are_mesh_independent, galerkin_coarse_matches_reassembly), the
+definition of vector_nodal_prolongation (hx.rs:89-125), iterative/src/aux_space.rs
 (combiner_is_self_adjoint) and iterative/src/multigrid.rs
 (vcycle_contracts_uniformly_in_h).
 """
@@ -71,6 +72,58 @@ def test_prolongation_reproduces_linear_functions(dim, nf, relative):
     else:
         assert P.shape == (max(nf - 1, 0) ** dim, max(nc - 1, 0) ** dim)
         assert (P.data > 0).all() and (np.asarray(P.sum(axis=1)).ravel() <= 1 + 1e-14).all()
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_vector_nodal_is_the_references_on_the_unit_box(oracle, dim):
+    """hx.rs:89-125 restated from the mesh's true coordinates: entry
+    (sigma, I * nvertices + a) = <e_I, tau_sigma> / (k+1)! for every vertex a of
+    the k-simplex sigma, tau_sigma the ambient tangent blade (colex minors of
+    the edge vectors from sigma's first vertex). On the unjittered unit box N = 2
+    the lattice frame (per-axis RMS axis-edge length) is the true one, and the
+    oracle's Pi_k equals it up to its node-major column order."""
+    nbox = 2
+    cx, coords = oracle.cartesian_unit(dim, nbox)
+    lengths = cx.edge_lengths_sq(coords)
+    h = hxo.lattice_spacing(cx, lengths, dim, nbox)
+    np.testing.assert_allclose(h, 1.0 / nbox, rtol=1e-15)
+    nv = cx.nsimplices(0)
+    for k in range(1, dim + 1):
+        subsets = hxo.colex_subsets(dim, k)
+        simp = cx.simplices(k)
+        want = np.zeros((len(simp), len(subsets) * nv))
+        for row, s in enumerate(simp):
+            e = (coords[s[1:]] - coords[s[0]]).T  # ambient x k
+            for comp, sub in enumerate(subsets):
+                value = np.linalg.det(e[sub, :]) / math.factorial(k + 1)
+                for a in s:
+                    want[row, comp * nv + a] = value
+        got = hxo.vector_nodal(cx, k, dim, nbox, False, h).toarray()
+        ncomp = len(subsets)
+        perm = [(c % ncomp) * nv + c // ncomp for c in range(got.shape[1])]  # node-major -> I-major
+        reordered = np.zeros_like(want)
+        reordered[:, perm] = got
+        np.testing.assert_allclose(reordered, want, rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("relative", [False, True])
+def test_galerkin_coarse_matches_reassembly(oracle, dim, relative):
+    """multigrid.rs:250-281 on the lattice levels: on the unjittered unit box
+    the Kuhn mesh of 2N refines the one of N, so the reference's refinement
+    tower and this lattice coarsening give the same levels there, and P^T A_f P
+    of the grade-0 hdif_gram equals the operator reassembled on the coarse mesh
+    (relative Frobenius 1e-10)."""
+    nc, nf = 2, 4
+
+    def hdif0(nbox):
+        cx, coords = oracle.cartesian_unit(dim, nbox)
+        return oracle.WhitneyComplex(cx, cx.edge_lengths_sq(coords), relative=relative).hdif_gram(0).toarray()
+
+    P = hxo.lattice_prolongation(dim, nf, nc, relative)
+    galerkin = P.T @ hdif0(nf) @ P
+    want = hdif0(nc)
+    assert np.linalg.norm(galerkin - want) < 1e-10 * np.linalg.norm(want)
 
 
 @pytest.mark.parametrize("dim", [2, 3])
