@@ -44,26 +44,72 @@ def test_binding_covers_the_header():
     assert sorted(fq.exported_symbols()) == declared_functions()
 
 
-def header_arities():
+C_BASE = {"int": "c_int", "fq_status": "c_int", "fq_form": "c_int", "fq_bc": "c_int", "fq_precision": "c_int",
+          "int32_t": "i32", "int64_t": "i64", "uint64_t": "u64", "int8_t": "i8", "double": "f64", "void": "c_void",
+          "char": "c_char", "size_t": "usize"}
+
+
+def c_to_rust(ctype):
+    """A C parameter or return type in Rust FFI spelling: the base renamed
+    (fq_x -> FqX, enums -> c_int), each pointer level *const or *mut by the
+    constness of what it points to (const T* -> *const T; T* const* -> *const *mut T)."""
+    toks = re.findall(r"const|\*|[A-Za-z_][A-Za-z0-9_]*", ctype)
+    base_const, base, levels = False, None, []  # levels: constness of each pointer itself
+    for t in toks:
+        if t == "const":
+            if base is None:
+                base_const = True
+            elif levels:
+                levels[-1] = True
+            else:
+                base_const = True
+        elif t == "*":
+            levels.append(False)
+        else:
+            base = t
+    name = C_BASE.get(base) or "".join(w.capitalize() for w in base.split("_"))
+    pointee_const = [base_const] + levels[:-1]
+    return "".join("*const " if c else "*mut " for c in reversed(pointee_const)) + name if levels else name
+
+
+def header_prototypes():
+    """name -> (return type, [parameter types]) in Rust spelling."""
     text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
     text = re.sub(r"//[^\n]*", "", text)
     out = {}
-    for name, args in re.findall(r"\b(fq_[a-z0-9_]+)\s*\(([^;{()]*)\)\s*;", text):
-        args = args.strip()
-        out[name] = 0 if args in ("", "void") else args.count(",") + 1
+    for ret, name, args in re.findall(r"([A-Za-z_][A-Za-z0-9_ \*]*?)\s*\b(fq_[a-z0-9_]+)\s*\(([^;{()]*)\)\s*;", text):
+        ret = ret.split()[-2:] if ret.split()[-1:] == ["*"] else ret
+        ret = " ".join(ret) if isinstance(ret, list) else ret
+        params = [] if args.strip() in ("", "void") else [a.strip() for a in args.split(",")]
+        ptypes = [c_to_rust(re.sub(r"\b[A-Za-z_][A-Za-z0-9_]*\s*$", "", a)) for a in params]
+        rt = c_to_rust(ret.strip())
+        out[name] = (None if rt == "c_void" else rt, ptypes)
     return out
 
 
-def test_rust_binding_covers_the_header():
-    """The extern blocks a formoniq maintainer adds bind every entry point,
-    each with the header's number of arguments."""
+def rust_prototypes():
     doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
     blocks = "\n".join(re.findall(r"```rust\n(.*?)```", doc, flags=re.S))
-    bound = {}
-    for name, args in re.findall(r"\bfn (fq_[a-z0-9_]+)\s*\(([^)]*)\)", blocks):
-        args = args.strip().rstrip(",")
-        bound[name] = 0 if not args else args.count(",") + 1
-    want = header_arities()
+    out = {}
+    for name, args, ret in re.findall(r"\bfn (fq_[a-z0-9_]+)\s*\(([^)]*)\)\s*(?:->\s*([^;]+))?;", blocks):
+        params = [a for a in (x.strip() for x in args.split(",")) if a]
+        ptypes = [re.sub(r"\s+", " ", a.split(":", 1)[1].strip()).replace("c_double", "f64") for a in params]
+        out[name] = (re.sub(r"\s+", " ", ret.strip()).replace("c_double", "f64") if ret else None, ptypes)
+    return out
+
+
+def test_c_types_spell_in_rust():
+    assert c_to_rust("const fq_matrix* const* mats".rsplit(" ", 1)[0]) == "*const *const FqMatrix"
+    assert c_to_rust("fq_matrix* const*") == "*const *mut FqMatrix"
+    assert c_to_rust("const int32_t**") == "*mut *const i32"
+    assert c_to_rust("fq_bc") == "c_int"
+    assert c_to_rust("const fq_solve_opts*") == "*const FqSolveOpts"
+
+
+def test_rust_binding_covers_the_header():
+    """The extern blocks a formoniq maintainer adds bind every entry point with
+    the header's parameter and return types (pointer mutability included)."""
+    want, bound = header_prototypes(), rust_prototypes()
     assert sorted(want) == declared_functions()
     assert sorted(bound) == sorted(want), (sorted(set(want) - set(bound)), sorted(set(bound) - set(want)))
     wrong = {n: (bound[n], want[n]) for n in want if bound[n] != want[n]}
