@@ -3,6 +3,8 @@ exports every function include/formoniq_gpu.h declares; no compute is called."""
 import ctypes
 import os
 import re
+import shutil
+import subprocess
 
 import pytest
 
@@ -114,6 +116,103 @@ def test_rust_binding_covers_the_header():
     assert sorted(bound) == sorted(want), (sorted(set(want) - set(bound)), sorted(set(bound) - set(want)))
     wrong = {n: (bound[n], want[n]) for n in want if bound[n] != want[n]}
     assert not wrong, wrong
+
+
+C_SCALAR = {"int": "i4", "fq_status": "i4", "fq_form": "i4", "fq_bc": "i4", "fq_precision": "i4", "int32_t": "i4",
+            "int64_t": "i8", "uint64_t": "u8", "int8_t": "i1", "double": "f8", "char": "i1", "size_t": "u8"}
+C_STRUCTS = {"fq_solve_opts": "SolveOpts", "fq_report": "_Report", "fq_request": "_Request", "fq_result": "_Result",
+             "fq_server_stats": "_ServerStats"}
+
+
+def c_kind(ctype):
+    """A C type as a kind: scalars by class and width, pointers by pointee,
+    the header's structs by their ctypes mirror, handles opaque."""
+    toks = [t for t in re.findall(r"\*|[A-Za-z_][A-Za-z0-9_]*", ctype) if t != "const"]
+    base = next(t for t in toks if t != "*")
+    kind = C_SCALAR.get(base) or ("struct:" + C_STRUCTS[base] if base in C_STRUCTS else
+                                  "void" if base == "void" else "opaque")
+    for _ in range(toks.count("*")):
+        kind = "ptr:" + kind
+    return kind
+
+
+def ctypes_kind(t):
+    if t is None:
+        return "void"
+    if t is ctypes.c_void_p:
+        return "ptr:any"
+    if t is ctypes.c_char_p:
+        return "ptr:i1"
+    if issubclass(t, ctypes._Pointer):
+        return "ptr:" + ctypes_kind(t._type_)
+    if issubclass(t, ctypes.Structure):
+        return "struct:" + t.__name__
+    code = t._type_
+    cls = "f" if code in "fd" else ("u" if code.isupper() else "i")
+    return f"{cls}{ctypes.sizeof(t)}"
+
+
+def kinds_match(c, py):
+    if py == "ptr:any":
+        return c.startswith("ptr:")
+    if c.startswith("ptr:") and py.startswith("ptr:"):
+        return kinds_match(c[4:], py[4:]) or (c[4:] == "opaque" and py[4:] == "any")
+    return c == py
+
+
+def header_c_prototypes():
+    """name -> (return type, [parameter types]) as written in the header."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = {}
+    for ret, name, args in re.findall(r"([A-Za-z_][A-Za-z0-9_ \*]*?)\s*\b(fq_[a-z0-9_]+)\s*\(([^;{()]*)\)\s*;", text):
+        params = [] if args.strip() in ("", "void") else [a.strip() for a in args.split(",")]
+        out[name] = (ret.strip(), [re.sub(r"\b[A-Za-z_][A-Za-z0-9_]*\s*$", "", a) for a in params])
+    return out
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every ctypes argtype and restype of the binding has the header's class
+    and width (c_void_p standing for any pointer): a wrong integer width here
+    would pass truncated sizes to the device."""
+    import formoniq_gb300 as fq
+
+    want = header_c_prototypes()
+    wrong = {}
+    for name, (res, args) in fq._SIGNATURES.items():
+        cret, cargs = want[name]
+        if len(args) != len(cargs) or not kinds_match(c_kind(cret), ctypes_kind(res)) or not all(
+                kinds_match(c_kind(c), ctypes_kind(a)) for c, a in zip(cargs, args)):
+            wrong[name] = ([c_kind(c) for c in [cret] + cargs], [ctypes_kind(a) for a in [res] + args])
+    assert not wrong, wrong
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of the header's structs have its field offsets and
+    sizes, as a C compiler lays them out (gcc on the header itself)."""
+    import formoniq_gb300 as fq
+
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("no C compiler")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "formoniq_gpu.h"', "int main(void) {"]
+    for cname, pyname in C_STRUCTS.items():
+        lines.append(f'printf("{cname} __size__ %zu\\n", sizeof({cname}));')
+        for fname, _ in getattr(fq, pyname)._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(lines))
+    subprocess.run([gcc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        struct, field, value = line.split()
+        got[(struct, field)] = int(value)
+    for cname, pyname in C_STRUCTS.items():
+        cls = getattr(fq, pyname)
+        assert got[(cname, "__size__")] == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
 
 
 def test_status_names(native):
