@@ -22,3 +22,23 @@ def test_reference_arm_prints_one_contract_line():
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert "kuhn 3D 32^3" in d["config"]["workload"]
+
+
+def test_device_arm_line_carries_every_contract_key():
+    """The device arm's JSON line (built where it prints, checked here without a
+    GPU by reading bench.py): every key of the bench contract, the roofline,
+    CPU-baseline, end-to-end and clock records, and the workload name in config."""
+    import ast
+
+    tree = ast.parse(open(os.path.join(ROOT, "bench.py")).read())
+    lines = [n.value for n in ast.walk(tree) if isinstance(n, ast.Assign) and isinstance(n.value, ast.Dict)
+             and any(isinstance(t, ast.Name) and t.id == "line" for t in n.targets)
+             and "roofline" in {k.value for k in n.value.keys if isinstance(k, ast.Constant)}]
+    assert len(lines) == 1  # the device arm's line; the reference arm's is run above
+    keys = {k.value for k in lines[0].keys if isinstance(k, ast.Constant)}
+    for want in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                 "scaling", "vs_baseline", "dtype", "data", "config", "roofline", "e2e", "cpu_baseline",
+                 "gpu_launches", "clocks", "parity"):
+        assert want in keys, want
+    config = lines[0].values[[k.value if isinstance(k, ast.Constant) else None for k in lines[0].keys].index("config")]
+    assert "workload" in {k.value for k in config.keys if isinstance(k, ast.Constant)}
