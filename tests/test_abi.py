@@ -100,6 +100,32 @@ def rust_prototypes():
     return out
 
 
+def header_struct_fields(name):
+    """(field, type) of a header typedef struct, in order (comma lists split)."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    body = re.search(r"typedef struct " + name + r" \{(.*?)\} " + name + ";", text, flags=re.S).group(1)
+    out = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        m = re.match(r"(.*?)([A-Za-z_][A-Za-z0-9_]*(?:\s*,\s*[A-Za-z_][A-Za-z0-9_]*)*)$", decl, flags=re.S)
+        ctype, names = m.group(1), [x.strip() for x in m.group(2).split(",")]
+        out += [(n, c_to_rust(ctype)) for n in names]
+    return out
+
+
+def test_rust_structs_mirror_the_header():
+    """FqSolveOpts and FqReport in the binding have the header's fields, in
+    order, with the header's types (repr(C) then lays them out alike)."""
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    for rust, c in (("FqSolveOpts", "fq_solve_opts"), ("FqReport", "fq_report")):
+        body = re.search(r"pub struct " + rust + r" \{(.*?)\}", doc, flags=re.S).group(1)
+        got = [(m.group(1), m.group(2).strip()) for m in re.finditer(r"pub (\w+): ([\w* ]+)", body)]
+        want = header_struct_fields(c)
+        assert got == want, (rust, got, want)
+
+
 def test_c_types_spell_in_rust():
     assert c_to_rust("const fq_matrix* const* mats".rsplit(" ", 1)[0]) == "*const *const FqMatrix"
     assert c_to_rust("fq_matrix* const*") == "*const *mut FqMatrix"
